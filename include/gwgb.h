@@ -1,0 +1,209 @@
+/*
+ * gwgb.h — C ABI of the GB300 symmetry-adapted GW engine.
+ *
+ * The engine replaces the GPU half of SymmetryMBPT's cuGW solver for one GW
+ * iteration over the irrep-blocked ("flat block") layout:
+ *
+ *   P0 contraction -> P~ = (1 - P~0)^-1 P~0 solve -> Sigma contraction -> Dyson,
+ *   with the tau <-> i omega sparse-grid (IR) transforms in between.
+ *
+ * Every entry point takes plain pointers and sizes; complex numbers are
+ * interleaved (re, im) doubles, i.e. the memory layout of
+ * std::complex<double>.  Every call returns 0 on success or a GWGB_E* code;
+ * gwgb_last_error() returns the message of the last failure on the calling
+ * thread.  A handle owns one CUDA device context slice (its device buffers,
+ * one stream, its CUDA graphs); calls on one handle are serialised by an
+ * internal mutex and distinct handles are independent.
+ *
+ * Host layouts are exactly the reference's host layouts:
+ *   G(tau), Sigma(tau):  [nts][ns][flat_ao]      (irreducible k slices)
+ *   P0(tau), P~(tau):    [ink][nts][qslice]      (irreducible q slices)
+ *   F, S, H:             [ns][flat_ao]
+ *   V:                   flat block-sparse, pair k1*nk+k2 slices
+ */
+#ifndef GWGB_H
+#define GWGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GWGB_OK              0
+#define GWGB_E_INVALID       1  /* bad argument, inconsistent layout, odd nts */
+#define GWGB_E_NOMEM         2  /* device or host allocation failed */
+#define GWGB_E_CUDA          3  /* CUDA runtime error */
+#define GWGB_E_TIMEOUT       4  /* a bounded device-side wait ran out */
+#define GWGB_E_NUMERIC       5  /* singular block in Dyson or W~ solve */
+#define GWGB_E_STATE         6  /* call order violated (e.g. solve before upload) */
+#define GWGB_E_UNSUPPORTED   7  /* shape beyond the limits of the built kernels */
+
+/* ---- contraction precision -------------------------------------------- */
+#define GWGB_PREC_FP64       0  /* complex128 everywhere: the drop-in path */
+#define GWGB_PREC_TF32X3     1  /* P0/Sigma on tcgen05 kind::tf32, 3-pass split, FP32 accumulate */
+#define GWGB_PREC_BF16X3     2  /* P0/Sigma on tcgen05 kind::f16 (bf16), 3-way split */
+
+typedef struct gwgb_handle_s *gwgb_handle;
+
+/* Solver parameters; the subset of params_t the GW solver reads
+ * (SymmetryMBPT/include/common/params_t.h:20-74, cugw_solver_block.h:117-142). */
+typedef struct gwgb_params {
+  int32_t ns;        /* spins, 1 or 2 */
+  int32_t nts;       /* tau points including 0 and beta (= ni + 2); must be even */
+  int32_t nw;        /* fermionic Matsubara sampling points */
+  int32_t nw_b;      /* bosonic Matsubara sampling points */
+  double  beta;      /* inverse temperature */
+  int32_t precision; /* GWGB_PREC_* */
+  int32_t device;    /* CUDA device ordinal */
+  int32_t nt_batch;  /* accepted for params_t compatibility; the kernels choose their own tau tiles */
+  int32_t flags;     /* reserved, 0 */
+} gwgb_params;
+
+/* Block layout: the arrays symmetry_utils_t reads from symmetry_info.h5,
+ * symmetry_rot.h5 and df_int/meta.h5
+ * (SymmetryMBPT/src/common/symmetry_utils.cpp:6-218).  Lists per k point are
+ * passed CSR style: entries [ptr[k], ptr[k+1]).  Offsets are derived inside
+ * the library with the reference's packing rule (blocks in list order, each
+ * b*b row-major; V blocks [q_b][k1_b][k2_b] with q = k2 - k1). */
+typedef struct gwgb_layout {
+  int32_t nk;                       /* k points in the full BZ */
+  int32_t ink;                      /* stored (irreducible) k points */
+  const int32_t *irre_list;         /* [ink]  full-BZ index of stored k      (irre_conj_list_) */
+  const int32_t *index;             /* [nk]   full-BZ index of the representative (index_) */
+  const int32_t *irre_index;        /* [nk]   position of the representative in irre_list */
+  const int32_t *conj_index;        /* [nk]   time-reversal partner used for rotation */
+  const int32_t *q_ind;             /* [nk*nk] q_ind_(j, q), row-major */
+  const int32_t *q_ind2;            /* [nk*nk] q_ind2_(i, j), row-major */
+  const int32_t *ao_block_ptr;      /* [nk+1] */
+  const int32_t *ao_sizes;          /* AO irrep block sizes per k */
+  const int32_t *aux_block_ptr;     /* [nk+1] */
+  const int32_t *aux_sizes;         /* aux irrep block sizes per q */
+  const int32_t *kpair_block_ptr;   /* [nk*nk+1] */
+  const int32_t *tensor_irreps;     /* 3 ints per V block: (iq, ik1, ik2) */
+  const int32_t *orep_block_ptr;    /* [nk+1] */
+  const int32_t *orep_irreps;       /* 2 ints per block: (block at k, block at irreducible k) */
+  const int32_t *auxrep_block_ptr;  /* [nk+1] */
+  const int32_t *auxrep_irreps;     /* 2 ints per block */
+} gwgb_layout;
+
+/* Per-stage device times of the last solve, milliseconds (CUDA events).
+ * Names follow the reference's execution_statistic_t events
+ * (SymmetryMBPT/include/solver/cugw_solver_block.h:248-262). */
+typedef struct gwgb_stats {
+  double rotate_G_ms;     /* "Copy data": iBZ -> BZ rotation of G */
+  double p0_ms;           /* "P0_contraction" */
+  double pq_ms;           /* "Compute P": tau->Omega, W~ solve, Omega->tau */
+  double rotate_P_ms;     /* P~(q_irr) -> P~(q) */
+  double sigma_ms;        /* "Sigma_contraction" */
+  double dyson_ms;        /* Dyson: tau->omega, block inverses, omega->tau */
+  double total_ms;
+  double p0_flops;        /* algorithmic FLOPs (8MNK per complex GEMM) of the P0 stage */
+  double sigma_flops;     /* algorithmic FLOPs of the Sigma stage */
+  double leakage;         /* max|c_{n-1}| / max|c_0| of G after the last Dyson */
+  int64_t kernel_launches;/* kernels launched by the last solve/iteration */
+} gwgb_stats;
+
+/* Library version string. */
+const char *gwgb_version(void);
+
+/* Message of the last failed call on this thread (never NULL). */
+const char *gwgb_last_error(void);
+
+/* Create a handle: validates the layout, builds the (q,k) / (k,q) work lists
+ * and allocates the device buffers.  Replaces solver_factory_t::construct_solver
+ * with scf_type == cuGW (SymmetryMBPT/include/solver/solver_factory_t.h:34-55)
+ * and the cugw_routine_block constructor
+ * (SymmetryMBPT/src/cuda/cugw_routines_block.cu:6-44). */
+int gwgb_create(const gwgb_params *params, const gwgb_layout *layout, gwgb_handle *out);
+
+/* Release every device buffer of the handle. */
+int gwgb_destroy(gwgb_handle h);
+
+/* Select the contraction precision for subsequent solves. Replaces
+ * solver_block_t::single_prec_run (SymmetryMBPT/include/solver/solver_block_t.h:48). */
+int gwgb_set_precision(gwgb_handle h, int32_t precision);
+
+/* Upload V (flat_V_size complex) into HBM; the host buffer is only read
+ * during the call.  Replaces set_shared_Coulomb/read_entire_Coulomb_integrals
+ * (SymmetryMBPT/include/solver/cuhf_solver_block.h:43-53, 106-118) and the
+ * per-pair reader callback (SymmetryMBPT/include/cuda/cugw_routines_block.h:17-20). */
+int gwgb_upload_V(gwgb_handle h, const double *V_flat, int64_t n_complex);
+
+/* Upload the rotation matrices orep / auxrep (flat block form, all nk).
+ * Replaces copy_ORep_host_to_device / copy_AuxRep_host_to_device
+ * (SymmetryMBPT/src/cuda/cugw_routines_block.cu:214-234). */
+int gwgb_set_reps(gwgb_handle h, const double *orep, int64_t n_orep,
+                  const double *auxrep, int64_t n_auxrep);
+
+/* IR transform matrices built on the host in FP64 (transformer_t,
+ * SymmetryMBPT/src/common/transformer_t.cpp:48-82), row-major complex:
+ *   Tnt [nw][nts-2], Ttn [nts][nw], Tnt_BF [nw_b][nts-2], Ttn_FB [nts][nw_b];
+ * wsample_fermi [nw] Matsubara indices n (omega_n = (2n+1) pi / beta);
+ * tct_first / tct_last: rows 0 and nts-3 of the real Tct matrix (leakage check,
+ * SymmetryMBPT/src/scmbpt/sc_type_block.cpp:66-71); may be NULL. */
+int gwgb_set_transforms(gwgb_handle h, const double *Tnt, const double *Ttn,
+                        const double *Tnt_BF, const double *Ttn_FB,
+                        const int64_t *wsample_fermi,
+                        const double *tct_first, const double *tct_last);
+
+/* One-electron inputs F, S [ns][flat_ao] (already Bz-shifted and
+ * Hermitised as sc_loop_block_t::read_input_data does,
+ * SymmetryMBPT/src/scmbpt/sc_loop_block_t.cpp:64-109). */
+int gwgb_set_fock(gwgb_handle h, const double *F, const double *S);
+
+/* G(tau) host <-> device, layout [nts][ns][flat_ao].  Replaces
+ * copy_G_host_to_device (SymmetryMBPT/src/cuda/cugw_routines_block.cu:100-201);
+ * the iBZ -> BZ rotation and the G(-tau) view happen on the device. */
+int gwgb_set_G(gwgb_handle h, const double *G_ts_kij);
+int gwgb_get_G(gwgb_handle h, double *G_ts_kij);
+
+/* Sigma(tau) host <-> device, layout [nts][ns][flat_ao].  get overwrites the
+ * host buffer (the reference's D2H copy adds into a zeroed buffer,
+ * SymmetryMBPT/src/cuda/cugw_routines_block.cu:249-274). */
+int gwgb_set_sigma(gwgb_handle h, const double *Sigma_ts_kij);
+int gwgb_get_sigma(gwgb_handle h, double *Sigma_ts_kij);
+
+/* P0 / P~ host <-> device, layout [ink][nts][qslice]
+ * (cugw_solver_block_t::P0_q_t_QP, SymmetryMBPT/include/solver/cugw_solver_block.h:180). */
+int gwgb_set_P0(gwgb_handle h, const double *P_q_t_QP);
+int gwgb_get_P0(gwgb_handle h, double *P_q_t_QP);
+
+/* P0 only: after the call the P0 buffer holds c/nk * sum for t < nts/2 and
+ * zeros above, as cugw_solver_block_t::solve_P0 leaves it
+ * (SymmetryMBPT/src/solver/cugw_solver_block.cpp:67-84, 139-190). */
+int gwgb_solve_P0(gwgb_handle h);
+
+/* P~ = (1 - P~0)^-1 P~0 from the P0 buffer, in place, all nts.  Replaces
+ * cugw_solver_block_t::compute_Pq_from_P0q (cugw_solver_block.cpp:385-439). */
+int gwgb_solve_Pq(gwgb_handle h);
+
+/* Sigma from P0 (test hook): mirrors P0 in tau, then the Sigma contraction.
+ * Replaces cugw_solver_block_t::solve_sigma (cugw_solver_block.cpp:86-112, 192-252). */
+int gwgb_solve_sigma(gwgb_handle h);
+
+/* Full GW self-energy: P0 -> P~ -> Sigma.  Replaces
+ * cugw_solver_block_t::solve (cugw_solver_block.cpp:34-65, 254-315). */
+int gwgb_solve(gwgb_handle h);
+
+/* Dyson: G(tau) from Sigma(tau), F, S at chemical potential mu.  Replaces
+ * dyson_sc_block_t::compute_G (SymmetryMBPT/src/scmbpt/sc_type_block.cpp:6-87). */
+int gwgb_dyson(gwgb_handle h, double mu);
+
+/* One GW iteration on resident data: solve() then Dyson at mu; captured as
+ * one CUDA graph on first use and replayed afterwards. */
+int gwgb_iteration(gwgb_handle h, double mu);
+
+/* Per-stage timings and algorithmic FLOPs of the last solve/iteration. */
+int gwgb_get_stats(gwgb_handle h, gwgb_stats *out);
+
+/* Block until all work of the handle is done. */
+int gwgb_synchronize(gwgb_handle h);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* GWGB_H */
