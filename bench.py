@@ -1,0 +1,307 @@
+"""Benchmark: seconds per symmetry-adapted GW iteration on one GB300.
+
+Workload: the C2 crystal (Fm-3m, 3x3x3 k mesh = 27 k / 4 irreducible,
+nao=26, naux=120, nts=100, beta=100, ns=1, V stored for all 729 k pairs),
+synthetic seeded data (see mbsymmetry_gb300/crystal.py).  One step = one GW
+iteration P0 -> P~ (W~ solve) -> Sigma -> Dyson with all tau <-> i omega
+transforms, FP64 (the drop-in path), replayed as one CUDA graph.
+
+  value  device time of the iteration (CUDA events recorded on the engine's
+         stream), inputs resident in HBM, L2 flushed before every iteration.
+  e2e    the same iteration through the public C ABI with host buffers:
+         gwgb_set_G (H2D) + gwgb_iteration + gwgb_get_sigma + gwgb_get_G (D2H).
+
+--impl reference times the FP64 CPU oracle (the restatement of the
+reference's CPU algorithm) on the host cores on a bounded sample of the same
+workload, extrapolated to a full iteration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+CONFIG = "C2"
+WORKLOAD = ("C2: Fm-3m 3x3x3 k mesh (27 k, 4 irreducible), nao=26, naux=120, nts=100, beta=100, "
+            "ns=1, V stored for all 729 k pairs, irrep blocks 1-8 (AO) / 2-40 (aux)")
+METRIC = "s/GW iteration (FP64 drop-in, P0 -> W~ -> Sigma -> Dyson)"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _rank_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def _load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def _setup():
+    from mbsymmetry_gb300.crystal import CONFIGS, load_ir, make_crystal
+    from mbsymmetry_gb300.transformer import build_transforms
+    spec = CONFIGS[CONFIG]
+    cr = make_crystal(spec)
+    tr = build_transforms(load_ir(spec.nts), spec.beta)
+    return cr, tr
+
+
+def _cpu_reference(cr, tr, steps, threads=0):
+    """Time the FP64 CPU oracle on a bounded sample: G rotation, P0 and Sigma
+    for a subset of tau points, the full W~ solve and the full Dyson step;
+    contraction times are scaled to all tau points."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle  # the CPU baseline (restatement of the reference's CPU path)
+    L, nts, ns = cr.layout, tr.nts, cr.ns
+    orc = Oracle(L, ns, nts, threads=threads)
+    zero = np.zeros(nts * ns * L.flat_ao_size, np.complex128)
+    G, _ = orc.dyson(zero, cr.F, cr.S, tr, cr.mu)
+    nt_p0, nt_sig = 2, 2
+    per_step = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        Gf = orc.rotate_G(G)
+        t1 = time.perf_counter()
+        P0 = orc.p0(Gf, cr.V, nt_max=nt_p0)
+        t2 = time.perf_counter()
+        P = orc.p_tilde(P0, tr)
+        t3 = time.perf_counter()
+        Pf = orc.rotate_P(P)
+        t4 = time.perf_counter()
+        orc.sigma(Gf, Pf, cr.V, nt_max=nt_sig)
+        t5 = time.perf_counter()
+        orc.dyson(zero, cr.F, cr.S, tr, cr.mu)
+        t6 = time.perf_counter()
+        full = ((t1 - t0) + (t2 - t1) * (nts // 2) / nt_p0 + (t3 - t2) + (t4 - t3)
+                + (t5 - t4) * nts / nt_sig + (t6 - t5))
+        per_step.append(full)
+    sample = (f"{CONFIG}: P0 for {nt_p0} of {nts // 2} tau points and Sigma for {nt_sig} of {nts} "
+              f"(scaled linearly in tau), rotations, W~ solve and Dyson in full; per step")
+    return float(np.mean(per_step)), orc.threads(), sample
+
+
+def run_reference(args):
+    rank, world, _ = _rank_info()
+    if rank != 0:
+        return
+    cr, tr = _setup()
+    for _ in range(max(0, min(args.warmup, 1))):
+        _cpu_reference(cr, tr, 1)
+    v, cores, sample = _cpu_reference(cr, tr, args.steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "precision": "fp64"},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    rank, world, local = _rank_info()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = local
+    torch.cuda.set_device(dev)
+    from mbsymmetry_gb300.solver import GWSolver
+    from mbsymmetry_gb300 import _abi
+    import ctypes
+
+    cr, tr = _setup()
+    L = cr.layout
+    s = GWSolver(L, cr.ns, tr, device=dev)
+    s.set_shared_Coulomb(cr.V)
+    s.set_fock(cr.F, cr.S)
+    s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+    s.dyson(cr.mu)                          # G0: the input of every timed iteration
+    G0 = s.G_tau()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        s.set_G(G0)
+        s.iteration(cr.mu)
+    stage_tot = {}
+    times = []
+    with ClockSampler(dev) as clocks:
+        barrier()
+        for _ in range(args.steps):
+            s.set_G(G0)                     # same input each step (not timed)
+            flush.zero_()                   # L2 flush between timed iterations
+            torch.cuda.synchronize()
+            s.iteration(cr.mu)              # events inside the engine's graph
+            st = s.stats()
+            times.append(st["total_ms"])
+            for k in ("rotate_G_ms", "p0_ms", "pq_ms", "rotate_P_ms", "sigma_ms", "dyson_ms"):
+                stage_tot[k] = stage_tot.get(k, 0.0) + st[k]
+        barrier()
+    launches = int(st["kernel_launches"]) * args.steps
+    ms = float(np.mean(times))
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    stages = {k: v / args.steps for k, v in stage_tot.items()}
+
+    # ---- e2e through the C ABI with pinned host buffers ------------------
+    g_host = torch.from_numpy(G0.view(np.float64)).pin_memory()
+    sig_host = torch.empty(2 * s.g_size, dtype=torch.float64).pin_memory()
+    g_out = torch.empty(2 * s.g_size, dtype=torch.float64).pin_memory()
+    lib = _abi.load()
+    h = s.h
+    vp = ctypes.c_void_p
+    for _ in range(2):
+        _abi.check(lib.gwgb_set_G(h, vp(g_host.data_ptr())))
+        _abi.check(lib.gwgb_iteration(h, cr.mu))
+    e2e = []
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _abi.check(lib.gwgb_set_G(h, vp(g_host.data_ptr())))
+        _abi.check(lib.gwgb_iteration(h, cr.mu))
+        _abi.check(lib.gwgb_get_sigma(h, vp(sig_host.data_ptr())))
+        _abi.check(lib.gwgb_get_G(h, vp(g_out.data_ptr())))
+        e2e.append(time.perf_counter() - t0)
+    barrier()
+    e2e_s = float(np.mean(e2e))
+    if world > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    gbytes = s.g_size * 16
+
+    # ---- roofline of the dominant kernel ---------------------------------
+    peaks = _load_peaks()
+    probe = ctypes.CDLL(os.path.join(ROOT, "mbsymmetry_gb300", "csrc", "probe", "libgwgb_probe.so"))
+    probe.gwgb_probe_fp64_tflops.restype = ctypes.c_double
+    probe.gwgb_probe_fp64_tflops.argtypes = [ctypes.c_int]
+    fp64_peak = probe.gwgb_probe_fp64_tflops(dev)
+    dom = "sigma" if stages["sigma_ms"] >= stages["p0_ms"] else "p0"
+    flops = st[f"{dom}_flops"]
+    dom_ms = stages[f"{dom}_ms"]
+    achieved = flops / (dom_ms * 1e-3) / 1e12
+    roofline = {"bound": "tensor", "kernel": f"{dom}_fp64_kernel", "achieved": achieved, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": None,
+                "peak_source": "FP64 FMA microbenchmark measured in this run (MEASURED_PEAKS.json has no FP64 "
+                               "figure); contraction FLOPs = 8MNK per complex GEMM of the block layout",
+                "flop_alg_per_launch": flops, "kernel_ms": dom_ms}
+
+    line = {
+        "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "precision": "fp64", "l2": "flushed (256 MiB write) before each step",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": gbytes, "d2h_bytes_per_step": 2 * gbytes},
+        "gpu_launches": launches,
+        "stages_ms": stages,
+        "contraction_tflops": {"p0": st["p0_flops"] / (stages["p0_ms"] * 1e-3) / 1e12,
+                               "sigma": st["sigma_flops"] / (stages["sigma_ms"] * 1e-3) / 1e12},
+        "roofline": roofline,
+        "clocks": clocks.summary(),
+        "peaks": {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops"),
+                  "fp64_tflops_measured": fp64_peak},
+    }
+    s.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        v, cores, sample = _cpu_reference(cr, tr, 1)
+        line["cpu_baseline"] = {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,945 @@
+// GB300 GW engine: host orchestration behind the C ABI of include/gwgb.h.
+//
+// One handle = one GPU, one stream.  All tensors of a GW iteration are
+// resident in HBM for the handle's lifetime: V (all stored k pairs), G(tau)
+// for the irreducible k plus the rotated copies of the other k, P0/P~(tau),
+// Sigma(tau), the frequency-domain work buffers and the work lists of the
+// kernels.  An iteration is a fixed sequence of kernel launches over static
+// work lists, so it is captured once as a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "kernels.h"
+
+namespace gwgb {
+
+static thread_local std::string g_last_error = "";
+
+// ---------------------------------------------------------------------------
+// Host copy of the layout with every derived offset (the arrays of
+// symmetry_utils_t, SymmetryMBPT/src/common/symmetry_utils.cpp:96-307).
+// ---------------------------------------------------------------------------
+struct Lay {
+  int nk = 0, ink = 0;
+  std::vector<int> irre_list, index, irre_index, conj_index, q_ind, q_ind2;
+  std::vector<int> ao_ptr, ao_sz, aux_ptr, aux_sz;
+  std::vector<int64_t> ao_off, aux_off;
+  std::vector<int64_t> kao_off, kao_sz, qaux_off, qaux_sz;    // full BZ
+  std::vector<int64_t> kao_off_irre, qaux_off_irre;           // iBZ
+  int64_t flat_ao = 0, flat_aux = 0, flat_ao_full = 0, flat_aux_full = 0;
+  std::vector<int> kp_ptr, ti;
+  std::vector<int64_t> t_off, kp_off;
+  int64_t flat_V = 0;
+  std::vector<int> or_ptr, or_ir, ar_ptr, ar_ir;
+  std::vector<int64_t> or_off, kor_off, ar_off, kar_off;
+  int64_t flat_orep = 0, flat_auxrep = 0;
+  int max_ao = 0, max_aux = 0;
+
+  int mom_cons(int i, int j, int k) const { return q_ind[k * nk + q_ind2[i * nk + j]]; }
+  int aosz(int k, int b) const { return ao_sz[ao_ptr[k] + b]; }
+  int auxsz(int k, int b) const { return aux_sz[aux_ptr[k] + b]; }
+  int64_t aooff(int k, int b) const { return ao_off[ao_ptr[k] + b]; }
+  int64_t auxoff(int k, int b) const { return aux_off[aux_ptr[k] + b]; }
+  int nao_blocks(int k) const { return ao_ptr[k + 1] - ao_ptr[k]; }
+  int naux_blocks(int k) const { return aux_ptr[k + 1] - aux_ptr[k]; }
+};
+
+template <typename T>
+static std::vector<T> copy_vec(const int32_t *p, size_t n, const char *what) {
+  GWGB_REQUIRE(p != nullptr || n == 0, GWGB_E_INVALID, std::string("layout field ") + what + " is NULL");
+  std::vector<T> v(n);
+  for (size_t i = 0; i < n; ++i) v[i] = (T)p[i];
+  return v;
+}
+
+static Lay derive_layout(const gwgb_layout &L) {
+  Lay l;
+  const int nk = L.nk, ink = L.ink;
+  GWGB_REQUIRE(nk > 0 && ink > 0 && ink <= nk, GWGB_E_INVALID, "nk/ink out of range");
+  l.nk = nk; l.ink = ink;
+  l.irre_list = copy_vec<int>(L.irre_list, ink, "irre_list");
+  l.index = copy_vec<int>(L.index, nk, "index");
+  l.irre_index = copy_vec<int>(L.irre_index, nk, "irre_index");
+  l.conj_index = copy_vec<int>(L.conj_index, nk, "conj_index");
+  l.q_ind = copy_vec<int>(L.q_ind, (size_t)nk * nk, "q_ind");
+  l.q_ind2 = copy_vec<int>(L.q_ind2, (size_t)nk * nk, "q_ind2");
+  for (int v : l.irre_list) GWGB_REQUIRE(v >= 0 && v < nk, GWGB_E_INVALID, "irre_list entry out of range");
+  for (int v : l.index) GWGB_REQUIRE(v >= 0 && v < nk, GWGB_E_INVALID, "index entry out of range");
+  for (int v : l.irre_index) GWGB_REQUIRE(v >= 0 && v < ink, GWGB_E_INVALID, "irre_index entry out of range");
+  for (int v : l.conj_index) GWGB_REQUIRE(v >= 0 && v < nk, GWGB_E_INVALID, "conj_index entry out of range");
+  for (int v : l.q_ind) GWGB_REQUIRE(v >= 0 && v < nk, GWGB_E_INVALID, "q_ind entry out of range");
+  for (int v : l.q_ind2) GWGB_REQUIRE(v >= 0 && v < nk, GWGB_E_INVALID, "q_ind2 entry out of range");
+  l.ao_ptr = copy_vec<int>(L.ao_block_ptr, nk + 1, "ao_block_ptr");
+  l.aux_ptr = copy_vec<int>(L.aux_block_ptr, nk + 1, "aux_block_ptr");
+  GWGB_REQUIRE(l.ao_ptr[0] == 0 && l.aux_ptr[0] == 0, GWGB_E_INVALID, "block pointer arrays must start at 0");
+  for (int k = 0; k < nk; ++k)
+    GWGB_REQUIRE(l.ao_ptr[k + 1] > l.ao_ptr[k] && l.aux_ptr[k + 1] > l.aux_ptr[k], GWGB_E_INVALID,
+                 "every k point needs at least one AO and one aux block");
+  l.ao_sz = copy_vec<int>(L.ao_sizes, l.ao_ptr[nk], "ao_sizes");
+  l.aux_sz = copy_vec<int>(L.aux_sizes, l.aux_ptr[nk], "aux_sizes");
+  for (int v : l.ao_sz) GWGB_REQUIRE(v > 0 && v <= MAX_BLOCK, GWGB_E_UNSUPPORTED, "AO block size outside 1..64");
+  for (int v : l.aux_sz) GWGB_REQUIRE(v > 0 && v <= MAX_BLOCK, GWGB_E_UNSUPPORTED, "aux block size outside 1..64");
+  l.max_ao = *std::max_element(l.ao_sz.begin(), l.ao_sz.end());
+  l.max_aux = *std::max_element(l.aux_sz.begin(), l.aux_sz.end());
+  l.ao_off.resize(l.ao_sz.size());
+  l.aux_off.resize(l.aux_sz.size());
+  l.kao_off.resize(nk); l.kao_sz.resize(nk); l.qaux_off.resize(nk); l.qaux_sz.resize(nk);
+  int64_t ka = 0, qa = 0;
+  int nao0 = -1, naux0 = -1;
+  for (int k = 0; k < nk; ++k) {
+    int64_t acc = 0;
+    int nao = 0, naux = 0;
+    for (int b = l.ao_ptr[k]; b < l.ao_ptr[k + 1]; ++b) { l.ao_off[b] = acc; acc += (int64_t)l.ao_sz[b] * l.ao_sz[b]; nao += l.ao_sz[b]; }
+    l.kao_sz[k] = acc; l.kao_off[k] = ka; ka += acc;
+    acc = 0;
+    for (int b = l.aux_ptr[k]; b < l.aux_ptr[k + 1]; ++b) { l.aux_off[b] = acc; acc += (int64_t)l.aux_sz[b] * l.aux_sz[b]; naux += l.aux_sz[b]; }
+    l.qaux_sz[k] = acc; l.qaux_off[k] = qa; qa += acc;
+    if (k == 0) { nao0 = nao; naux0 = naux; }
+    GWGB_REQUIRE(nao == nao0 && naux == naux0, GWGB_E_INVALID, "block sizes of every k must add up to the same nao/naux");
+  }
+  l.flat_ao_full = ka; l.flat_aux_full = qa;
+  l.kao_off_irre.resize(ink); l.qaux_off_irre.resize(ink);
+  ka = 0; qa = 0;
+  for (int ik = 0; ik < ink; ++ik) {
+    int k = l.irre_list[ik];
+    l.kao_off_irre[ik] = ka; ka += l.kao_sz[k];
+    l.qaux_off_irre[ik] = qa; qa += l.qaux_sz[k];
+  }
+  l.flat_ao = ka; l.flat_aux = qa;
+  // aux blocks of q and -q must agree: V(k1, k2) is read with aux_sizes(k2-k1)
+  // in P0 and aux_sizes(k1-k2) in Sigma (gw_block.cpp:23-24 vs 101-102).
+  for (int q = 0; q < nk; ++q) {
+    int mq = l.mom_cons(0, q, 0);
+    GWGB_REQUIRE(l.naux_blocks(q) == l.naux_blocks(mq), GWGB_E_INVALID, "aux blocks of q and -q differ");
+    for (int b = 0; b < l.naux_blocks(q); ++b)
+      GWGB_REQUIRE(l.auxsz(q, b) == l.auxsz(mq, b), GWGB_E_INVALID, "aux blocks of q and -q differ");
+  }
+  // V blocks
+  const int np = nk * nk;
+  l.kp_ptr = copy_vec<int>(L.kpair_block_ptr, np + 1, "kpair_block_ptr");
+  GWGB_REQUIRE(l.kp_ptr[0] == 0, GWGB_E_INVALID, "kpair_block_ptr must start at 0");
+  for (int p = 0; p < np; ++p) GWGB_REQUIRE(l.kp_ptr[p + 1] >= l.kp_ptr[p], GWGB_E_INVALID, "kpair_block_ptr not monotone");
+  l.ti = copy_vec<int>(L.tensor_irreps, 3 * (size_t)l.kp_ptr[np], "tensor_irreps");
+  l.t_off.resize(l.kp_ptr[np]);
+  l.kp_off.resize(np);
+  int64_t va = 0;
+  for (int p = 0; p < np; ++p) {
+    int k1 = p / nk, k2 = p % nk;
+    int q = l.mom_cons(k2, k1, 0);
+    int64_t acc = 0;
+    l.kp_off[p] = va;
+    for (int b = l.kp_ptr[p]; b < l.kp_ptr[p + 1]; ++b) {
+      int iq = l.ti[3 * b], i1 = l.ti[3 * b + 1], i2 = l.ti[3 * b + 2];
+      GWGB_REQUIRE(iq >= 0 && iq < l.naux_blocks(q) && i1 >= 0 && i1 < l.nao_blocks(k1) && i2 >= 0 &&
+                       i2 < l.nao_blocks(k2),
+                   GWGB_E_INVALID, "tensor_irreps entry out of range");
+      l.t_off[b] = acc;
+      acc += (int64_t)l.auxsz(q, iq) * l.aosz(k1, i1) * l.aosz(k2, i2);
+    }
+    va += acc;
+  }
+  l.flat_V = va;
+  // rotation blocks
+  l.or_ptr = copy_vec<int>(L.orep_block_ptr, nk + 1, "orep_block_ptr");
+  l.ar_ptr = copy_vec<int>(L.auxrep_block_ptr, nk + 1, "auxrep_block_ptr");
+  l.or_ir = copy_vec<int>(L.orep_irreps, 2 * (size_t)l.or_ptr[nk], "orep_irreps");
+  l.ar_ir = copy_vec<int>(L.auxrep_irreps, 2 * (size_t)l.ar_ptr[nk], "auxrep_irreps");
+  l.or_off.resize(l.or_ptr[nk]); l.ar_off.resize(l.ar_ptr[nk]);
+  l.kor_off.resize(nk); l.kar_off.resize(nk);
+  int64_t oa = 0, aa = 0;
+  for (int k = 0; k < nk; ++k) {
+    int ck = l.conj_index[k];
+    int kk = l.irre_list[l.irre_index[ck]];
+    l.kor_off[k] = oa;
+    for (int b = l.or_ptr[k]; b < l.or_ptr[k + 1]; ++b) {
+      int i1 = l.or_ir[2 * b], i2 = l.or_ir[2 * b + 1];
+      GWGB_REQUIRE(i1 >= 0 && i1 < l.nao_blocks(ck) && i2 >= 0 && i2 < l.nao_blocks(kk), GWGB_E_INVALID,
+                   "orep_irreps entry out of range");
+      l.or_off[b] = oa - l.kor_off[k];
+      oa += (int64_t)l.aosz(ck, i1) * l.aosz(kk, i2);
+    }
+    l.kar_off[k] = aa;
+    for (int b = l.ar_ptr[k]; b < l.ar_ptr[k + 1]; ++b) {
+      int i1 = l.ar_ir[2 * b], i2 = l.ar_ir[2 * b + 1];
+      GWGB_REQUIRE(i1 >= 0 && i1 < l.naux_blocks(ck) && i2 >= 0 && i2 < l.naux_blocks(kk), GWGB_E_INVALID,
+                   "auxrep_irreps entry out of range");
+      l.ar_off[b] = aa - l.kar_off[k];
+      aa += (int64_t)l.auxsz(ck, i1) * l.auxsz(kk, i2);
+    }
+  }
+  l.flat_orep = oa; l.flat_auxrep = aa;
+  return l;
+}
+
+// ---------------------------------------------------------------------------
+// device buffer helper
+// ---------------------------------------------------------------------------
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  void alloc(size_t count) {
+    free();
+    n = count;
+    if (count) GWGB_CUDA(cudaMalloc(&p, count * sizeof(T)));
+  }
+  void upload(const std::vector<T> &v, cudaStream_t st) {
+    alloc(v.size());
+    if (n) GWGB_CUDA(cudaMemcpyAsync(p, v.data(), n * sizeof(T), cudaMemcpyHostToDevice, st));
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct GRef {
+  int64_t base;
+  int32_t stride;
+};
+
+class Engine {
+ public:
+  Engine(const gwgb_params &p, const gwgb_layout &L);
+  ~Engine();
+
+  void set_precision(int prec) {
+    GWGB_REQUIRE(prec == GWGB_PREC_FP64, GWGB_E_UNSUPPORTED,
+                 "this build implements the FP64 contraction path only");
+    prec_ = prec;
+  }
+  void upload_V(const double *V, int64_t n);
+  void set_reps(const double *orep, int64_t no, const double *auxrep, int64_t na);
+  void set_transforms(const double *Tnt, const double *Ttn, const double *TntBF, const double *TtnFB,
+                      const int64_t *ws, const double *tf, const double *tl);
+  void set_fock(const double *F, const double *S);
+  void set_G(const double *G);
+  void get_G(double *G);
+  void set_sigma(const double *S);
+  void get_sigma(double *S);
+  void set_P0(const double *P);
+  void get_P0(double *P);
+  void solve_P0();
+  void solve_Pq();
+  void solve_sigma();
+  void solve();
+  void dyson(double mu);
+  void iteration(double mu);
+  void stats(gwgb_stats *out) const { *out = stats_; }
+  void synchronize() { GWGB_CUDA(cudaStreamSynchronize(st_)); check_device_flags(); }
+  int device() const { return dev_; }
+  std::mutex mu_lock;
+
+ private:
+  // parameters
+  int ns_, nts_, nw_, nw_b_, ncheb_, prec_, dev_;
+  double beta_;
+  Lay l_;
+  cudaStream_t st_ = nullptr;
+  int smem_bytes_ = 0;
+  bool have_V_ = false, have_T_ = false, have_F_ = false, have_reps_ = false;
+
+  // device data
+  DBuf<double2> V_, Gall_, Pall_, Sig_, Pw_, Ww_, F_, S_, orep_, auxrep_;
+  DBuf<double2> Tnt_, Ttn_, TntBF_, TtnFB_;
+  DBuf<double> tct_f_, tct_l_, mu_dev_;
+  DBuf<int64_t> ws_;
+  DBuf<int> bad_;
+  DBuf<unsigned long long> leak_;
+  DBuf<int64_t> qoff_irr_;
+  DBuf<int32_t> qsz_irr_;
+  // work lists
+  DBuf<P0Tile> p0_tiles_;
+  DBuf<P0Contrib> p0_contribs_;
+  DBuf<SigTile> sig_tiles_;
+  DBuf<SigContrib> sig_contribs_;
+  DBuf<RotTask> rotG_, rotP_;
+  DBuf<TSlab> slab_p_fwd_, slab_p_bwd_, slab_s_fwd_, slab_g_bwd_;
+  DBuf<InvTask> inv_w_, inv_d_;
+  int p0_maxo_ = 8, sig_maxo_ = 8, rot_smem_ = 0;
+  int max_cols_p_ = 0, max_cols_g_ = 0;
+  int64_t g_rot_off_ = 0, p_rot_off_ = 0;  // start of the rotated parts
+  double p0_flops_ = 0, sig_flops_ = 0;
+  bool has_tct_ = false;
+  // graph
+  cudaGraphExec_t graph_exec_ = nullptr;
+  cudaEvent_t ev_[8];
+  double *mu_host_ = nullptr;
+  gwgb_stats stats_{};
+
+  void build_work_lists();
+  void require_ready(bool need_T) const {
+    GWGB_REQUIRE(have_V_, GWGB_E_STATE, "V has not been uploaded");
+    GWGB_REQUIRE(have_reps_, GWGB_E_STATE, "rotation matrices have not been set");
+    GWGB_REQUIRE(!need_T || have_T_, GWGB_E_STATE, "transform matrices have not been set");
+  }
+  // stage launchers (no synchronisation)
+  void k_rotate_G();
+  void k_p0(int mirror);
+  void k_pq(bool mirror_first);
+  void k_rotate_P();
+  void k_sigma();
+  void k_dyson();
+  void record(int i) { GWGB_CUDA(cudaEventRecord(ev_[i], st_)); }
+  float elapsed(int a, int b) {
+    float ms = 0;
+    GWGB_CUDA(cudaEventElapsedTime(&ms, ev_[a], ev_[b]));
+    return ms;
+  }
+  void check_device_flags();
+  void finish_stats(bool with_dyson, bool with_gw);
+};
+
+Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
+  GWGB_REQUIRE(p.ns == 1 || p.ns == 2, GWGB_E_INVALID, "ns must be 1 or 2");
+  GWGB_REQUIRE(p.nts >= 4 && p.nts % 2 == 0, GWGB_E_INVALID, "Number of tau points should be even number");
+  GWGB_REQUIRE(p.nts <= 160 && p.nw > 0 && p.nw <= 160 && p.nw_b > 0 && p.nw_b <= 160, GWGB_E_UNSUPPORTED,
+               "tau/frequency grids are limited to 160 points");
+  GWGB_REQUIRE(p.beta > 0.0, GWGB_E_INVALID, "beta must be positive");
+  ns_ = p.ns; nts_ = p.nts; nw_ = p.nw; nw_b_ = p.nw_b; ncheb_ = p.nts - 2;
+  beta_ = p.beta; prec_ = GWGB_PREC_FP64; dev_ = p.device;
+  l_ = derive_layout(L);
+  GWGB_CUDA(cudaSetDevice(dev_));
+  GWGB_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+  for (auto &e : ev_) GWGB_CUDA(cudaEventCreate(&e));
+  int optin = 0;
+  GWGB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev_));
+  smem_bytes_ = std::min(optin, 200 * 1024);
+  set_fp64_kernel_attributes(smem_bytes_);
+  if (p.precision != GWGB_PREC_FP64) set_precision(p.precision);
+  GWGB_CUDA(cudaMallocHost(&mu_host_, sizeof(double)));
+  build_work_lists();
+  // buffers
+  const int64_t fa = l_.flat_ao, fq = l_.flat_aux;
+  V_.alloc(l_.flat_V);
+  Sig_.alloc((size_t)nts_ * ns_ * fa);
+  Pw_.alloc((size_t)nw_b_ * fq);
+  Ww_.alloc((size_t)nw_ * ns_ * fa);
+  F_.alloc((size_t)ns_ * fa);
+  S_.alloc((size_t)ns_ * fa);
+  orep_.alloc(l_.flat_orep);
+  auxrep_.alloc(l_.flat_auxrep);
+  mu_dev_.alloc(1);
+  bad_.alloc(2);
+  leak_.alloc(2);
+  GWGB_CUDA(cudaMemsetAsync(Gall_.p, 0, Gall_.n * sizeof(double2), st_));
+  GWGB_CUDA(cudaMemsetAsync(Pall_.p, 0, Pall_.n * sizeof(double2), st_));
+  GWGB_CUDA(cudaMemsetAsync(Sig_.p, 0, Sig_.n * sizeof(double2), st_));
+  GWGB_CUDA(cudaMemsetAsync(bad_.p, 0, 2 * sizeof(int), st_));
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+
+Engine::~Engine() {
+  if (st_) cudaStreamSynchronize(st_);
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  for (auto &e : ev_) if (e) cudaEventDestroy(e);
+  if (mu_host_) cudaFreeHost(mu_host_);
+  DBuf<double2> *bufs[] = {&V_, &Gall_, &Pall_, &Sig_, &Pw_, &Ww_, &F_, &S_, &orep_, &auxrep_,
+                           &Tnt_, &Ttn_, &TntBF_, &TtnFB_};
+  for (auto *b : bufs) b->free();
+  tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
+  qoff_irr_.free(); qsz_irr_.free();
+  p0_tiles_.free(); p0_contribs_.free(); sig_tiles_.free(); sig_contribs_.free();
+  rotG_.free(); rotP_.free(); slab_p_fwd_.free(); slab_p_bwd_.free(); slab_s_fwd_.free(); slab_g_bwd_.free();
+  inv_w_.free(); inv_d_.free();
+  if (st_) cudaStreamDestroy(st_);
+}
+
+// ---------------------------------------------------------------------------
+// work lists
+// ---------------------------------------------------------------------------
+void Engine::build_work_lists() {
+  const Lay &l = l_;
+  const int nk = l.nk, ink = l.ink;
+  const int64_t fa = l.flat_ao, fq = l.flat_aux;
+  const int cap = smem_bytes_ / (int)sizeof(double2);
+
+  // --- G references: irreducible k read in place from the host-layout
+  //     buffer, every other k from its rotated copy [k'][t][s][kslice].
+  std::vector<GRef> gref(nk);
+  std::vector<RotTask> rg;
+  g_rot_off_ = (int64_t)nts_ * ns_ * fa;
+  int64_t go = g_rot_off_;
+  rot_smem_ = 0;
+  for (int k = 0; k < nk; ++k) {
+    const int ck = l.conj_index[k];
+    const int ick = l.irre_index[ck];
+    const int kk = l.irre_list[ick];
+    if (l.index[ck] == ck && k == ck && kk == k) {
+      gref[k] = {l.kao_off_irre[ick], (int32_t)fa};
+      continue;
+    }
+    gref[k] = {go, (int32_t)l.kao_sz[k]};
+    if (l.index[ck] == ck) {
+      GWGB_REQUIRE(l.kao_sz[k] == l.kao_sz[kk], GWGB_E_INVALID, "k slice size differs from its representative");
+      rg.push_back({go, l.kao_off_irre[ick], 0, (int32_t)l.kao_sz[k], (int32_t)fa, (int32_t)l.kao_sz[k], 0, 0,
+                    (int32_t)(k != ck)});
+    } else {
+      std::vector<int> covered(l.nao_blocks(ck), 0);
+      for (int b = l.or_ptr[ck]; b < l.or_ptr[ck + 1]; ++b) {
+        int i1 = l.or_ir[2 * b], i2 = l.or_ir[2 * b + 1];
+        int m = l.aosz(ck, i1), n = l.aosz(kk, i2);
+        GWGB_REQUIRE(m == n, GWGB_E_INVALID, "orep block must be square");
+        covered[i1]++;
+        rg.push_back({go + l.aooff(ck, i1), l.kao_off_irre[ick] + l.aooff(kk, i2), l.kor_off[ck] + l.or_off[b],
+                      (int32_t)l.kao_sz[k], (int32_t)fa, m, n, 1, (int32_t)(k != ck)});
+        rot_smem_ = std::max(rot_smem_, (int)((2 * m * n + n * n) * sizeof(double2)));
+      }
+      for (int c : covered) GWGB_REQUIRE(c == 1, GWGB_E_INVALID, "orep must map every block of k exactly once");
+    }
+    go += (int64_t)nts_ * ns_ * l.kao_sz[k];
+  }
+  Gall_.alloc((size_t)go);
+
+  // --- P references: irreducible q in place, others rotated [q'][t][qslice]
+  std::vector<GRef> pref(nk);
+  std::vector<RotTask> rp;
+  p_rot_off_ = (int64_t)nts_ * fq;
+  int64_t po = p_rot_off_;
+  for (int q = 0; q < nk; ++q) {
+    const int cq = l.conj_index[q];
+    const int q_ir = l.irre_index[q];  // cugw_qkpt_block.cu:147
+    const int qq = l.irre_list[q_ir];
+    if (l.index[cq] == cq && q == cq && qq == q) {
+      pref[q] = {(int64_t)nts_ * l.qaux_off_irre[q_ir], (int32_t)l.qaux_sz[q]};
+      continue;
+    }
+    pref[q] = {po, (int32_t)l.qaux_sz[q]};
+    const int64_t src = (int64_t)nts_ * l.qaux_off_irre[q_ir];
+    if (l.index[cq] == cq) {
+      GWGB_REQUIRE(l.qaux_sz[q] == l.qaux_sz[qq], GWGB_E_INVALID, "q slice size differs from its representative");
+      rp.push_back({po, src, 0, (int32_t)l.qaux_sz[q], (int32_t)l.qaux_sz[qq], (int32_t)l.qaux_sz[q], 0, 0,
+                    (int32_t)(q != cq)});
+    } else {
+      std::vector<int> covered(l.naux_blocks(cq), 0);
+      for (int b = l.ar_ptr[cq]; b < l.ar_ptr[cq + 1]; ++b) {
+        int i1 = l.ar_ir[2 * b], i2 = l.ar_ir[2 * b + 1];
+        int m = l.auxsz(cq, i1), n = l.auxsz(qq, i2);
+        GWGB_REQUIRE(m == n, GWGB_E_INVALID, "auxrep block must be square");
+        covered[i1]++;
+        rp.push_back({po + l.auxoff(cq, i1), src + l.auxoff(qq, i2), l.kar_off[cq] + l.ar_off[b],
+                      (int32_t)l.qaux_sz[q], (int32_t)l.qaux_sz[qq], m, n, 1, (int32_t)(q != cq)});
+        rot_smem_ = std::max(rot_smem_, (int)((2 * m * n + n * n) * sizeof(double2)));
+      }
+      for (int c : covered) GWGB_REQUIRE(c == 1, GWGB_E_INVALID, "auxrep must map every block of q exactly once");
+    }
+    po += (int64_t)nts_ * l.qaux_sz[q];
+  }
+  Pall_.alloc((size_t)po);
+  rotG_.upload(rg, st_);
+  rotP_.upload(rp, st_);
+
+  // --- P0 tiles: owner = (q_irr, aux block iq, tau range)
+  std::vector<P0Tile> pt;
+  std::vector<P0Contrib> pc;
+  p0_flops_ = 0;
+  int maxo = 1;
+  const int half = nts_ / 2;
+  for (int iqr = 0; iqr < ink; ++iqr) {
+    const int q = l.irre_list[iqr];
+    for (int iq = 0; iq < l.naux_blocks(q); ++iq) {
+      const int qb = l.auxsz(q, iq);
+      const int c0 = (int)pc.size();
+      double flop = 0;
+      int b2max = 1;
+      for (int k1 = 0; k1 < nk; ++k1) {
+        const int k2 = l.mom_cons(k1, 0, q);  // k2 = k1 + q (cugw_routines_block.cu:283)
+        const int p = k1 * nk + k2;
+        for (int b = l.kp_ptr[p]; b < l.kp_ptr[p + 1]; ++b) {
+          if (l.ti[3 * b] != iq) continue;
+          const int i1 = l.ti[3 * b + 1], i2 = l.ti[3 * b + 2];
+          const int b1 = l.aosz(k1, i1), b2 = l.aosz(k2, i2);
+          pc.push_back({l.kp_off[p] + l.t_off[b], gref[k1].base + l.aooff(k1, i1), gref[k2].base + l.aooff(k2, i2),
+                        gref[k1].stride, gref[k2].stride, b1, b2});
+          flop += 8.0 * ((double)b2 * qb * b1 * b1 + (double)qb * b1 * b2 * b2 + (double)qb * qb * b1 * b2);
+          b2max = std::max(b2max, b2);
+        }
+      }
+      const int c1 = (int)pc.size();
+      p0_flops_ += flop * ns_ * half;
+      int nt = std::max(1, std::min(half, (256 + qb * qb - 1) / (qb * qb)));
+      while (nt > 1 && nt * qb * qb > 2048) --nt;
+      while (nt > 1 && 2 * qb * b2max * nt > cap) --nt;
+      GWGB_REQUIRE(2 * qb * b2max * nt <= cap, GWGB_E_UNSUPPORTED, "P0 block too large for shared memory");
+      maxo = std::max(maxo, (nt * qb * qb + 255) / 256);
+      for (int t0 = 0; t0 < half; t0 += nt) {
+        const int n = std::min(nt, half - t0);
+        const double cost = flop * n * ns_;
+        pt.push_back({(int64_t)nts_ * l.qaux_off_irre[iqr] + l.auxoff(q, iq), (int32_t)l.qaux_sz[q], qb, c0, c1,
+                      t0, n, (int32_t)std::min(cost / 1e3, 2e9), 0});
+      }
+    }
+  }
+  GWGB_REQUIRE(maxo <= 16, GWGB_E_UNSUPPORTED, "P0 output tile too large");
+  p0_maxo_ = maxo;
+  std::stable_sort(pt.begin(), pt.end(), [](const P0Tile &a, const P0Tile &b) { return a.cost > b.cost; });
+  p0_tiles_.upload(pt, st_);
+  p0_contribs_.upload(pc, st_);
+
+  // --- Sigma tiles: owner = (k_irr, AO block i1, spin, tau range)
+  std::vector<SigTile> stl;
+  std::vector<SigContrib> sc;
+  sig_flops_ = 0;
+  maxo = 1;
+  for (int ik = 0; ik < ink; ++ik) {
+    const int k1 = l.irre_list[ik];
+    for (int i1 = 0; i1 < l.nao_blocks(k1); ++i1) {
+      const int b1 = l.aosz(k1, i1);
+      const int c0 = (int)sc.size();
+      double flop = 0;
+      int qbmax = 1;
+      for (int q = 0; q < nk; ++q) {
+        const int k2 = l.mom_cons(k1, q, 0);  // k2 = k1 - q (cugw_routines_block.cu:307)
+        const int p = k1 * nk + k2;
+        for (int b = l.kp_ptr[p]; b < l.kp_ptr[p + 1]; ++b) {
+          if (l.ti[3 * b + 1] != i1) continue;
+          const int iq = l.ti[3 * b], i2 = l.ti[3 * b + 2];
+          const int qb = l.auxsz(q, iq), b2 = l.aosz(k2, i2);
+          sc.push_back({l.kp_off[p] + l.t_off[b], gref[k2].base + l.aooff(k2, i2), pref[q].base + l.auxoff(q, iq),
+                        gref[k2].stride, pref[q].stride, b2, qb});
+          flop += 8.0 * ((double)qb * b1 * b2 * b2 + (double)b1 * b2 * qb * qb + (double)b1 * b1 * b2 * qb);
+          qbmax = std::max(qbmax, qb);
+        }
+      }
+      const int c1 = (int)sc.size();
+      sig_flops_ += flop * ns_ * nts_;
+      int nt = std::max(1, std::min(nts_, (256 + b1 * b1 - 1) / (b1 * b1)));
+      while (nt > 1 && nt * b1 * b1 > 2048) --nt;
+      while (nt > 1 && 2 * qbmax * b1 * nt > cap) --nt;
+      GWGB_REQUIRE(2 * qbmax * b1 * nt <= cap, GWGB_E_UNSUPPORTED, "Sigma block too large for shared memory");
+      maxo = std::max(maxo, (nt * b1 * b1 + 255) / 256);
+      for (int s = 0; s < ns_; ++s)
+        for (int t0 = 0; t0 < nts_; t0 += nt) {
+          const int n = std::min(nt, nts_ - t0);
+          const double cost = flop * n;
+          stl.push_back({(int64_t)s * fa + l.kao_off_irre[ik] + l.aooff(k1, i1), (int32_t)(ns_ * fa), b1, c0, c1, t0,
+                         n, s, (int32_t)std::min(cost / 1e3, 2e9)});
+        }
+    }
+  }
+  GWGB_REQUIRE(maxo <= 16, GWGB_E_UNSUPPORTED, "Sigma output tile too large");
+  sig_maxo_ = maxo;
+  std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
+  sig_tiles_.upload(stl, st_);
+  sig_contribs_.upload(sc, st_);
+
+  // --- transforms and block inverses
+  std::vector<TSlab> pf, pb, sf, gb;
+  std::vector<InvTask> iw, id;
+  std::vector<int64_t> qo(ink);
+  std::vector<int32_t> qs(ink);
+  max_cols_p_ = max_cols_g_ = 0;
+  for (int iqr = 0; iqr < ink; ++iqr) {
+    const int q = l.irre_list[iqr];
+    const int64_t off = l.qaux_off_irre[iqr];
+    const int32_t sz = (int32_t)l.qaux_sz[q];
+    qo[iqr] = off;
+    qs[iqr] = sz;
+    pf.push_back({(int64_t)nts_ * off, (int64_t)nw_b_ * off, sz, sz, sz, 0});
+    pb.push_back({(int64_t)nw_b_ * off, (int64_t)nts_ * off, sz, sz, sz, 0});
+    max_cols_p_ = std::max(max_cols_p_, (int)sz);
+    for (int n = 0; n < nw_b_; ++n)
+      for (int b = 0; b < l.naux_blocks(q); ++b)
+        iw.push_back({(int64_t)nw_b_ * off + (int64_t)n * sz + l.auxoff(q, b), 0, 0, l.auxsz(q, b), -1});
+  }
+  for (int s = 0; s < ns_; ++s)
+    for (int ik = 0; ik < ink; ++ik) {
+      const int k = l.irre_list[ik];
+      const int64_t koff = l.kao_off_irre[ik];
+      const int32_t ksz = (int32_t)l.kao_sz[k];
+      const int64_t wbase = (int64_t)nw_ * (s * fa + koff);
+      sf.push_back({s * fa + koff, wbase, (int32_t)(ns_ * fa), ksz, ksz, 0});
+      gb.push_back({wbase, s * fa + koff, ksz, (int32_t)(ns_ * fa), ksz, 0});
+      max_cols_g_ = std::max(max_cols_g_, (int)ksz);
+      for (int w = 0; w < nw_; ++w)
+        for (int b = 0; b < l.nao_blocks(k); ++b)
+          id.push_back({wbase + (int64_t)w * ksz + l.aooff(k, b), s * fa + koff + l.aooff(k, b),
+                        s * fa + koff + l.aooff(k, b), l.aosz(k, b), w});
+    }
+  slab_p_fwd_.upload(pf, st_);
+  slab_p_bwd_.upload(pb, st_);
+  slab_s_fwd_.upload(sf, st_);
+  slab_g_bwd_.upload(gb, st_);
+  inv_w_.upload(iw, st_);
+  inv_d_.upload(id, st_);
+  qoff_irr_.upload(qo, st_);
+  qsz_irr_.upload(qs, st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+
+// ---------------------------------------------------------------------------
+// uploads / downloads
+// ---------------------------------------------------------------------------
+static void h2d(void *d, const void *h, size_t bytes, cudaStream_t st) {
+  GWGB_REQUIRE(h != nullptr || bytes == 0, GWGB_E_INVALID, "NULL host pointer");
+  GWGB_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st));
+}
+static void d2h(void *h, const void *d, size_t bytes, cudaStream_t st) {
+  GWGB_REQUIRE(h != nullptr || bytes == 0, GWGB_E_INVALID, "NULL host pointer");
+  GWGB_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, st));
+}
+
+void Engine::upload_V(const double *V, int64_t n) {
+  GWGB_REQUIRE(n == l_.flat_V, GWGB_E_INVALID,
+               "V size " + std::to_string(n) + " does not match the layout (" + std::to_string(l_.flat_V) + ")");
+  h2d(V_.p, V, (size_t)n * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  have_V_ = true;
+}
+
+void Engine::set_reps(const double *orep, int64_t no, const double *auxrep, int64_t na) {
+  GWGB_REQUIRE(no == l_.flat_orep && na == l_.flat_auxrep, GWGB_E_INVALID, "rotation matrix sizes do not match the layout");
+  h2d(orep_.p, orep, (size_t)no * sizeof(double2), st_);
+  h2d(auxrep_.p, auxrep, (size_t)na * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  have_reps_ = true;
+}
+
+void Engine::set_transforms(const double *Tnt, const double *Ttn, const double *TntBF, const double *TtnFB,
+                            const int64_t *ws, const double *tf, const double *tl) {
+  GWGB_REQUIRE(Tnt && Ttn && TntBF && TtnFB && ws, GWGB_E_INVALID, "transform matrices must not be NULL");
+  Tnt_.alloc((size_t)nw_ * ncheb_);
+  Ttn_.alloc((size_t)nts_ * nw_);
+  TntBF_.alloc((size_t)nw_b_ * ncheb_);
+  TtnFB_.alloc((size_t)nts_ * nw_b_);
+  ws_.alloc(nw_);
+  h2d(Tnt_.p, Tnt, Tnt_.n * sizeof(double2), st_);
+  h2d(Ttn_.p, Ttn, Ttn_.n * sizeof(double2), st_);
+  h2d(TntBF_.p, TntBF, TntBF_.n * sizeof(double2), st_);
+  h2d(TtnFB_.p, TtnFB, TtnFB_.n * sizeof(double2), st_);
+  h2d(ws_.p, ws, nw_ * sizeof(int64_t), st_);
+  has_tct_ = tf && tl;
+  if (has_tct_) {
+    tct_f_.alloc(ncheb_);
+    tct_l_.alloc(ncheb_);
+    h2d(tct_f_.p, tf, ncheb_ * sizeof(double), st_);
+    h2d(tct_l_.p, tl, ncheb_ * sizeof(double), st_);
+  }
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  have_T_ = true;
+}
+
+void Engine::set_fock(const double *F, const double *S) {
+  h2d(F_.p, F, F_.n * sizeof(double2), st_);
+  h2d(S_.p, S, S_.n * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  have_F_ = true;
+}
+
+void Engine::set_G(const double *G) {
+  h2d(Gall_.p, G, (size_t)nts_ * ns_ * l_.flat_ao * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+void Engine::get_G(double *G) {
+  d2h(G, Gall_.p, (size_t)nts_ * ns_ * l_.flat_ao * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+void Engine::set_sigma(const double *S) {
+  h2d(Sig_.p, S, Sig_.n * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+void Engine::get_sigma(double *S) {
+  d2h(S, Sig_.p, Sig_.n * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+void Engine::set_P0(const double *P) {
+  h2d(Pall_.p, P, (size_t)nts_ * l_.flat_aux * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+void Engine::get_P0(double *P) {
+  d2h(P, Pall_.p, (size_t)nts_ * l_.flat_aux * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+
+// ---------------------------------------------------------------------------
+// stages
+// ---------------------------------------------------------------------------
+void Engine::k_rotate_G() {
+  launch_rotate(rotG_.p, (int)rotG_.n, nts_ * ns_, rot_smem_, Gall_.p, orep_.p, Gall_.p, st_);
+}
+
+void Engine::k_p0(int mirror) {
+  const double pref = -1.0 / l_.nk * (ns_ == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
+  launch_p0_fp64(p0_tiles_.p, (int)p0_tiles_.n, p0_maxo_, p0_contribs_.p, V_.p, Gall_.p, Pall_.p, ns_, nts_, pref,
+                 mirror, smem_bytes_, st_);
+}
+
+void Engine::k_pq(bool mirror_first) {
+  if (mirror_first) launch_mirror(Pall_.p, qoff_irr_.p, qsz_irr_.p, l_.ink, nts_, st_);
+  launch_transform(slab_p_fwd_.p, (int)slab_p_fwd_.n, max_cols_p_, TntBF_.p, nw_b_, ncheb_, 1, Pall_.p, Pw_.p, st_);
+  launch_inverse(inv_w_.p, (int)inv_w_.n, l_.max_aux, Pw_.p, nullptr, nullptr, nullptr, beta_, 0.0, 0, bad_.p, st_);
+  launch_transform(slab_p_bwd_.p, (int)slab_p_bwd_.n, max_cols_p_, TtnFB_.p, nts_, nw_b_, 0, Pw_.p, Pall_.p, st_);
+}
+
+void Engine::k_rotate_P() {
+  launch_rotate(rotP_.p, (int)rotP_.n, nts_, rot_smem_, Pall_.p, auxrep_.p, Pall_.p, st_);
+}
+
+void Engine::k_sigma() {
+  launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Sig_.p, ns_,
+                    -1.0 / l_.nk, smem_bytes_, st_);
+}
+
+void Engine::k_dyson() {
+  launch_transform(slab_s_fwd_.p, (int)slab_s_fwd_.n, max_cols_g_, Tnt_.p, nw_, ncheb_, 1, Sig_.p, Ww_.p, st_);
+  launch_inverse(inv_d_.p, (int)inv_d_.n, l_.max_ao, Ww_.p, S_.p, F_.p, ws_.p, beta_, 0.0, 1, bad_.p + 1, st_);
+  launch_transform(slab_g_bwd_.p, (int)slab_g_bwd_.n, max_cols_g_, Ttn_.p, nts_, nw_, 0, Ww_.p, Gall_.p, st_);
+  if (has_tct_) {
+    GWGB_CUDA(cudaMemsetAsync(leak_.p, 0, 2 * sizeof(unsigned long long), st_));
+    launch_leakage(slab_g_bwd_.p, (int)slab_g_bwd_.n, Gall_.p, tct_f_.p, tct_l_.p, ncheb_, leak_.p, st_);
+  }
+}
+
+void Engine::check_device_flags() {
+  int bad[2] = {0, 0};
+  GWGB_CUDA(cudaMemcpy(bad, bad_.p, sizeof(bad), cudaMemcpyDeviceToHost));
+  if (bad[0] || bad[1]) {
+    GWGB_CUDA(cudaMemset(bad_.p, 0, sizeof(bad)));
+    throw Error(GWGB_E_NUMERIC, bad[0] ? "singular block in the W~ solve (1 - P~0)" : "singular block in Dyson");
+  }
+}
+
+void Engine::finish_stats(bool with_dyson, bool with_gw) {
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  check_device_flags();
+  gwgb_stats s{};
+  if (with_gw) {
+    s.rotate_G_ms = elapsed(0, 1);
+    s.p0_ms = elapsed(1, 2);
+    s.pq_ms = elapsed(2, 3);
+    s.rotate_P_ms = elapsed(3, 4);
+    s.sigma_ms = elapsed(4, 5);
+    s.p0_flops = p0_flops_;
+    s.sigma_flops = sig_flops_;
+  }
+  if (with_dyson) {
+    s.dyson_ms = elapsed(5, 6);
+    if (has_tct_) {
+      unsigned long long lk[2];
+      GWGB_CUDA(cudaMemcpy(lk, leak_.p, sizeof(lk), cudaMemcpyDeviceToHost));
+      double f, la;
+      std::memcpy(&f, &lk[0], 8);
+      std::memcpy(&la, &lk[1], 8);
+      s.leakage = f > 0 ? la / f : 0.0;
+    }
+  }
+  s.total_ms = elapsed(with_gw ? 0 : 5, with_dyson ? 6 : 5);
+  int64_t launches = 0;
+  if (with_gw) launches += (rotG_.n ? 1 : 0) + (p0_tiles_.n ? 1 : 0) + 3 + (rotP_.n ? 1 : 0) + (sig_tiles_.n ? 1 : 0);
+  if (with_dyson) launches += 3 + (has_tct_ ? 1 : 0);
+  s.kernel_launches = launches;
+  stats_ = s;
+}
+
+void Engine::solve_P0() {
+  require_ready(false);
+  record(0);
+  k_rotate_G();
+  record(1);
+  k_p0(0);
+  launch_zero_upper(Pall_.p, qoff_irr_.p, qsz_irr_.p, l_.ink, nts_, st_);
+  for (int i = 2; i <= 6; ++i) record(i);
+  finish_stats(false, true);
+}
+
+void Engine::solve_Pq() {
+  require_ready(true);
+  record(0); record(1); record(2);
+  k_pq(true);
+  for (int i = 3; i <= 6; ++i) record(i);
+  finish_stats(false, true);
+}
+
+void Engine::solve_sigma() {
+  require_ready(false);
+  record(0);
+  k_rotate_G();
+  record(1);
+  k_p0(1);
+  record(2);
+  record(3);
+  k_rotate_P();
+  record(4);
+  k_sigma();
+  record(5);
+  record(6);
+  finish_stats(false, true);
+}
+
+void Engine::solve() {
+  require_ready(true);
+  record(0);
+  k_rotate_G();
+  record(1);
+  k_p0(1);
+  record(2);
+  k_pq(false);
+  record(3);
+  k_rotate_P();
+  record(4);
+  k_sigma();
+  record(5);
+  record(6);
+  finish_stats(false, true);
+}
+
+void Engine::dyson(double mu) {
+  GWGB_REQUIRE(have_T_, GWGB_E_STATE, "transform matrices have not been set");
+  GWGB_REQUIRE(have_F_, GWGB_E_STATE, "F and S have not been set");
+  // mu enters the inverse kernel by value here (no graph)
+  record(5);
+  launch_transform(slab_s_fwd_.p, (int)slab_s_fwd_.n, max_cols_g_, Tnt_.p, nw_, ncheb_, 1, Sig_.p, Ww_.p, st_);
+  launch_inverse(inv_d_.p, (int)inv_d_.n, l_.max_ao, Ww_.p, S_.p, F_.p, ws_.p, beta_, mu, 1, bad_.p + 1, st_);
+  launch_transform(slab_g_bwd_.p, (int)slab_g_bwd_.n, max_cols_g_, Ttn_.p, nts_, nw_, 0, Ww_.p, Gall_.p, st_);
+  if (has_tct_) {
+    GWGB_CUDA(cudaMemsetAsync(leak_.p, 0, 2 * sizeof(unsigned long long), st_));
+    launch_leakage(slab_g_bwd_.p, (int)slab_g_bwd_.n, Gall_.p, tct_f_.p, tct_l_.p, ncheb_, leak_.p, st_);
+  }
+  record(6);
+  finish_stats(true, false);
+}
+
+void Engine::iteration(double mu) {
+  require_ready(true);
+  GWGB_REQUIRE(have_F_, GWGB_E_STATE, "F and S have not been set");
+  // The graph holds mu by value; rebuild when it changes.
+  if (!graph_exec_ || *mu_host_ != mu) {
+    if (graph_exec_) {
+      cudaGraphExecDestroy(graph_exec_);
+      graph_exec_ = nullptr;
+    }
+    *mu_host_ = mu;
+    cudaGraph_t g;
+    GWGB_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+    record(0);
+    k_rotate_G();
+    record(1);
+    k_p0(1);
+    record(2);
+    k_pq(false);
+    record(3);
+    k_rotate_P();
+    record(4);
+    k_sigma();
+    record(5);
+    launch_transform(slab_s_fwd_.p, (int)slab_s_fwd_.n, max_cols_g_, Tnt_.p, nw_, ncheb_, 1, Sig_.p, Ww_.p, st_);
+    launch_inverse(inv_d_.p, (int)inv_d_.n, l_.max_ao, Ww_.p, S_.p, F_.p, ws_.p, beta_, mu, 1, bad_.p + 1, st_);
+    launch_transform(slab_g_bwd_.p, (int)slab_g_bwd_.n, max_cols_g_, Ttn_.p, nts_, nw_, 0, Ww_.p, Gall_.p, st_);
+    if (has_tct_) {
+      GWGB_CUDA(cudaMemsetAsync(leak_.p, 0, 2 * sizeof(unsigned long long), st_));
+      launch_leakage(slab_g_bwd_.p, (int)slab_g_bwd_.n, Gall_.p, tct_f_.p, tct_l_.p, ncheb_, leak_.p, st_);
+    }
+    record(6);
+    cudaError_t e = cudaStreamEndCapture(st_, &g);
+    GWGB_CUDA(e);
+    GWGB_CUDA(cudaGraphInstantiate(&graph_exec_, g, 0));
+    cudaGraphDestroy(g);
+  }
+  GWGB_CUDA(cudaGraphLaunch(graph_exec_, st_));
+  finish_stats(true, true);
+}
+
+}  // namespace gwgb
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using gwgb::Engine;
+
+struct gwgb_handle_s {
+  Engine *e;
+};
+
+template <typename F>
+static int guarded(F &&f) {
+  try {
+    f();
+    return GWGB_OK;
+  } catch (const gwgb::Error &e) {
+    gwgb::g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    gwgb::g_last_error = "host allocation failed";
+    return GWGB_E_NOMEM;
+  } catch (const std::exception &e) {
+    gwgb::g_last_error = e.what();
+    return GWGB_E_INVALID;
+  }
+}
+
+template <typename F>
+static int on_handle(gwgb_handle h, F &&f) {
+  if (!h || !h->e) {
+    gwgb::g_last_error = "NULL handle";
+    return GWGB_E_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(h->e->mu_lock);
+  return guarded([&] {
+    GWGB_CUDA(cudaSetDevice(h->e->device()));
+    f(*h->e);
+  });
+}
+
+extern "C" {
+
+const char *gwgb_version(void) { return "gwgb 0.1 (sm_103a, FP64 contraction path)"; }
+
+const char *gwgb_last_error(void) { return gwgb::g_last_error.c_str(); }
+
+int gwgb_create(const gwgb_params *params, const gwgb_layout *layout, gwgb_handle *out) {
+  return guarded([&] {
+    GWGB_REQUIRE(params && layout && out, GWGB_E_INVALID, "NULL argument to gwgb_create");
+    *out = nullptr;
+    auto *h = new gwgb_handle_s{nullptr};
+    try {
+      h->e = new Engine(*params, *layout);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int gwgb_destroy(gwgb_handle h) {
+  if (!h) return GWGB_OK;
+  int rc = guarded([&] { delete h->e; });
+  delete h;
+  return rc;
+}
+
+#define GWGB_FORWARD(name, sig_args, call)                                       \
+  int name sig_args { return on_handle(h, [&](Engine &e) { call; }); }
+
+GWGB_FORWARD(gwgb_set_precision, (gwgb_handle h, int32_t precision), e.set_precision(precision))
+GWGB_FORWARD(gwgb_upload_V, (gwgb_handle h, const double *V, int64_t n), e.upload_V(V, n))
+GWGB_FORWARD(gwgb_set_reps, (gwgb_handle h, const double *o, int64_t no, const double *a, int64_t na),
+             e.set_reps(o, no, a, na))
+GWGB_FORWARD(gwgb_set_transforms,
+             (gwgb_handle h, const double *Tnt, const double *Ttn, const double *TntBF, const double *TtnFB,
+              const int64_t *ws, const double *tf, const double *tl),
+             e.set_transforms(Tnt, Ttn, TntBF, TtnFB, ws, tf, tl))
+GWGB_FORWARD(gwgb_set_fock, (gwgb_handle h, const double *F, const double *S), e.set_fock(F, S))
+GWGB_FORWARD(gwgb_set_G, (gwgb_handle h, const double *G), e.set_G(G))
+GWGB_FORWARD(gwgb_get_G, (gwgb_handle h, double *G), e.get_G(G))
+GWGB_FORWARD(gwgb_set_sigma, (gwgb_handle h, const double *S), e.set_sigma(S))
+GWGB_FORWARD(gwgb_get_sigma, (gwgb_handle h, double *S), e.get_sigma(S))
+GWGB_FORWARD(gwgb_set_P0, (gwgb_handle h, const double *P), e.set_P0(P))
+GWGB_FORWARD(gwgb_get_P0, (gwgb_handle h, double *P), e.get_P0(P))
+GWGB_FORWARD(gwgb_solve_P0, (gwgb_handle h), e.solve_P0())
+GWGB_FORWARD(gwgb_solve_Pq, (gwgb_handle h), e.solve_Pq())
+GWGB_FORWARD(gwgb_solve_sigma, (gwgb_handle h), e.solve_sigma())
+GWGB_FORWARD(gwgb_solve, (gwgb_handle h), e.solve())
+GWGB_FORWARD(gwgb_dyson, (gwgb_handle h, double mu), e.dyson(mu))
+GWGB_FORWARD(gwgb_iteration, (gwgb_handle h, double mu), e.iteration(mu))
+GWGB_FORWARD(gwgb_get_stats, (gwgb_handle h, gwgb_stats *out), GWGB_REQUIRE(out, GWGB_E_INVALID, "NULL stats"); e.stats(out))
+GWGB_FORWARD(gwgb_synchronize, (gwgb_handle h), e.synchronize())
+
+}  // extern "C"

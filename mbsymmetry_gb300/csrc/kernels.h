@@ -1,0 +1,45 @@
+// Launchers of the GW engine kernels (host side).
+#pragma once
+
+#include "common.h"
+
+namespace gwgb {
+
+// Largest irrep block (AO or aux) the FP64 kernels accept.
+constexpr int MAX_BLOCK = 64;
+
+__host__ __device__ constexpr int inv_warps_per_block(int nmax) {
+  return nmax <= 16 ? 4 : (nmax <= 32 ? 2 : 1);
+}
+__host__ __device__ constexpr int inv_smem_bytes(int nmax) {
+  return inv_warps_per_block(nmax) * (2 * nmax * nmax * 16 + nmax * 4);
+}
+__host__ __device__ constexpr int rotate_smem_bytes(int nmax) { return 3 * nmax * nmax * 16; }
+
+void set_fp64_kernel_attributes(int smem_bytes);
+
+void launch_p0_fp64(const P0Tile *tiles, int ntiles, int maxo, const P0Contrib *contribs,
+                    const double2 *V, const double2 *G, double2 *P0, int ns, int nts, double pref,
+                    int mirror, int smem_bytes, cudaStream_t st);
+
+void launch_sigma_fp64(const SigTile *tiles, int ntiles, int maxo, const SigContrib *contribs,
+                       const double2 *V, const double2 *G, const double2 *P, double2 *Sig, int ns,
+                       double scale, int smem_bytes, cudaStream_t st);
+
+void launch_rotate(const RotTask *tasks, int ntasks, int nbatch, int smem_bytes, const double2 *src,
+                   const double2 *O, double2 *dst, cudaStream_t st);
+
+void launch_mirror(double2 *P, const int64_t *qoff, const int32_t *qsz, int nq, int nts, cudaStream_t st);
+void launch_zero_upper(double2 *P, const int64_t *qoff, const int32_t *qsz, int nq, int nts, cudaStream_t st);
+
+void launch_transform(const TSlab *slabs, int nslabs, int max_cols, const double2 *T, int nout, int nin,
+                      int row0, const double2 *X, double2 *Y, cudaStream_t st);
+
+void launch_inverse(const InvTask *tasks, int ntasks, int nmax, double2 *W, const double2 *S,
+                    const double2 *F, const int64_t *wsample, double beta, double mu, int mode, int *bad,
+                    cudaStream_t st);
+
+void launch_leakage(const TSlab *slabs, int nslabs, const double2 *G, const double *tf, const double *tl,
+                    int ncheb, unsigned long long *out, cudaStream_t st);
+
+}  // namespace gwgb

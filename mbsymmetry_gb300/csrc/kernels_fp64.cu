@@ -1,0 +1,568 @@
+// FP64 kernels of the GW engine: block rotations, the P0 and Sigma
+// contractions, the tau <-> omega transforms and the batched block inverses.
+//
+// GB300's FP64 rate is a small fraction of its tensor rate, so these kernels
+// are FP64-pipe bound: they keep the reference's three-GEMM contraction
+// order (no redundant flops), keep every SM busy with owner-computes tiles
+// (one CTA owns an output block for a tau range and sums all its (k, q, s)
+// contributions, so no atomics and bitwise run-to-run reproducibility), and
+// stage the per-contribution intermediates in shared memory.
+#include "common.h"
+#include "kernels.h"
+
+namespace gwgb {
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// c + a * b
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {
+  c.x = fma(a.x, b.x, c.x);
+  c.x = fma(-a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y);
+  c.y = fma(a.y, b.x, c.y);
+  return c;
+}
+// c + conj(a) * b
+__device__ __forceinline__ double2 cfma_conja(double2 a, double2 b, double2 c) {
+  c.x = fma(a.x, b.x, c.x);
+  c.x = fma(a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y);
+  c.y = fma(-a.y, b.x, c.y);
+  return c;
+}
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+
+// ---------------------------------------------------------------------------
+// P0 contraction (restates gw_block.cpp:52-75 / cugw_qkpt_block.cu:195-267):
+//   X1[t,m][Q] = sum_p G^{k1}(beta - tau)[t][p] V[Q][p][m]
+//   X2[P][t,m] = sum_n conj(V[P][t][n]) G^{k2}(tau)[m][n]
+//   P0(tau)[Q][P] += sum_{t,m} X1[t,m][Q] X2[P][t,m]
+// The t (row of the k1 block) range is processed in chunks so the
+// intermediates of any block size fit in shared memory.
+// ---------------------------------------------------------------------------
+template <int MAXO>
+__global__ void __launch_bounds__(256) p0_fp64_kernel(const P0Tile *__restrict__ tiles,
+                                                      const P0Contrib *__restrict__ contribs,
+                                                      const double2 *__restrict__ V,
+                                                      const double2 *__restrict__ G,
+                                                      double2 *__restrict__ P0, int ns, int nts,
+                                                      double pref, int mirror, int smem_cap) {
+  extern __shared__ double2 sm[];
+  const P0Tile tile = tiles[blockIdx.x];
+  const int qb = tile.qb, nt = tile.nt;
+  const int nout = nt * qb * qb;
+  double2 acc[MAXO];
+#pragma unroll
+  for (int i = 0; i < MAXO; ++i) acc[i] = make_double2(0.0, 0.0);
+
+  for (int c = tile.c0; c < tile.c1; ++c) {
+    const P0Contrib cb = contribs[c];
+    const int b1 = cb.b1, b2 = cb.b2;
+    const double2 *Vb = V + cb.v;
+    int TT = smem_cap / (2 * qb * b2 * nt);
+    TT = TT < b1 ? TT : b1;
+    for (int s = 0; s < ns; ++s) {
+      for (int r0 = 0; r0 < b1; r0 += TT) {
+        const int tn = (b1 - r0) < TT ? (b1 - r0) : TT;
+        const int K = tn * b2;
+        double2 *X1 = sm;
+        double2 *X2 = sm + (size_t)nt * qb * K;
+        __syncthreads();
+        for (int e = threadIdx.x; e < nt * qb * K; e += blockDim.x) {
+          const int it = e / (qb * K);
+          const int rem = e - it * qb * K;
+          const int Q = rem / K, k = rem - Q * K;
+          const int tt = k / b2, m = k - tt * b2;
+          const int tau = tile.t0 + it;
+          const double2 *Gm = G + cb.ga + ((size_t)(nts - 1 - tau) * ns + s) * cb.sa + (size_t)(r0 + tt) * b1;
+          const double2 *Vq = Vb + (size_t)Q * b1 * b2 + m;
+          double2 a = make_double2(0.0, 0.0);
+          for (int p = 0; p < b1; ++p) a = cfma(Gm[p], Vq[(size_t)p * b2], a);
+          X1[(size_t)(it * qb + Q) * K + k] = a;
+        }
+        for (int e = threadIdx.x; e < nt * qb * K; e += blockDim.x) {
+          const int it = e / (qb * K);
+          const int rem = e - it * qb * K;
+          const int P = rem / K, k = rem - P * K;
+          const int tt = k / b2, m = k - tt * b2;
+          const int tau = tile.t0 + it;
+          const double2 *G2 = G + cb.gb + ((size_t)tau * ns + s) * cb.sb + (size_t)m * b2;
+          const double2 *Vr = Vb + ((size_t)P * b1 + r0 + tt) * b2;
+          double2 a = make_double2(0.0, 0.0);
+          for (int n = 0; n < b2; ++n) a = cfma_conja(Vr[n], G2[n], a);
+          X2[(size_t)(it * qb + P) * K + k] = a;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < MAXO; ++i) {
+          const int o = threadIdx.x + i * blockDim.x;
+          if (o < nout) {
+            const int it = o / (qb * qb);
+            const int rem = o - it * qb * qb;
+            const int Q = rem / qb, P = rem - Q * qb;
+            const double2 *x1 = X1 + (size_t)(it * qb + Q) * K;
+            const double2 *x2 = X2 + (size_t)(it * qb + P) * K;
+            double2 a = acc[i];
+            for (int k = 0; k < K; ++k) a = cfma(x1[k], x2[k], a);
+            acc[i] = a;
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < MAXO; ++i) {
+    const int o = threadIdx.x + i * blockDim.x;
+    if (o < nout) {
+      const int it = o / (qb * qb);
+      const int rem = o - it * qb * qb;
+      const int tau = tile.t0 + it;
+      const double2 v = cscale(acc[i], pref);
+      P0[tile.p + (size_t)tau * tile.pstride + rem] = v;
+      if (mirror) P0[tile.p + (size_t)(nts - 1 - tau) * tile.pstride + rem] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sigma contraction (restates gw_block.cpp:128-151 / cugw_qkpt_block.cu:343-412):
+//   Y1[Q][i][n] = sum_m V[Q][i][m] G^{k2}(tau)[m][n]
+//   Y2[i][n][P] = sum_Q Y1[Q][i][n] P(tau)[Q][P]
+//   Sigma(tau)[i][j] += sum_{n,P} Y2[i][n][P] conj(V[P][j][n])
+// The n range is processed in chunks so the intermediates fit in shared memory.
+// ---------------------------------------------------------------------------
+template <int MAXO>
+__global__ void __launch_bounds__(256) sigma_fp64_kernel(const SigTile *__restrict__ tiles,
+                                                         const SigContrib *__restrict__ contribs,
+                                                         const double2 *__restrict__ V,
+                                                         const double2 *__restrict__ G,
+                                                         const double2 *__restrict__ P,
+                                                         double2 *__restrict__ Sig, int ns,
+                                                         double scale, int smem_cap) {
+  extern __shared__ double2 sm[];
+  const SigTile tile = tiles[blockIdx.x];
+  const int b1 = tile.b1, nt = tile.nt, s = tile.s;
+  const int nout = nt * b1 * b1;
+  double2 acc[MAXO];
+#pragma unroll
+  for (int i = 0; i < MAXO; ++i) acc[i] = make_double2(0.0, 0.0);
+
+  for (int c = tile.c0; c < tile.c1; ++c) {
+    const SigContrib cb = contribs[c];
+    const int qb = cb.qb, b2 = cb.b2;
+    const double2 *Vb = V + cb.v;
+    int NT = smem_cap / (2 * qb * b1 * nt);
+    NT = NT < b2 ? NT : b2;
+    for (int n0 = 0; n0 < b2; n0 += NT) {
+      const int nn_n = (b2 - n0) < NT ? (b2 - n0) : NT;
+      double2 *Y1 = sm;                                  // [nt][qb][b1][nn]
+      double2 *Y2 = sm + (size_t)nt * qb * b1 * nn_n;    // [nt][b1][nn][qb]
+      __syncthreads();
+      for (int e = threadIdx.x; e < nt * qb * b1 * nn_n; e += blockDim.x) {
+        const int it = e / (qb * b1 * nn_n);
+        int rem = e - it * qb * b1 * nn_n;
+        const int Q = rem / (b1 * nn_n);
+        rem -= Q * b1 * nn_n;
+        const int i = rem / nn_n, nn = rem - i * nn_n;
+        const int tau = tile.t0 + it;
+        const double2 *G2 = G + cb.gb + ((size_t)tau * ns + s) * cb.sb + n0 + nn;
+        const double2 *Vr = Vb + ((size_t)Q * b1 + i) * b2;
+        double2 a = make_double2(0.0, 0.0);
+        for (int m = 0; m < b2; ++m) a = cfma(Vr[m], G2[(size_t)m * b2], a);
+        Y1[e] = a;
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < nt * b1 * nn_n * qb; e += blockDim.x) {
+        const int it = e / (b1 * nn_n * qb);
+        int rem = e - it * b1 * nn_n * qb;
+        const int i = rem / (nn_n * qb);
+        rem -= i * nn_n * qb;
+        const int nn = rem / qb, Pi = rem - nn * qb;
+        const int tau = tile.t0 + it;
+        const double2 *Pt = P + cb.pq + (size_t)tau * cb.pstride + Pi;
+        const double2 *y1 = Y1 + ((size_t)it * qb * b1 + i) * nn_n + nn;
+        double2 a = make_double2(0.0, 0.0);
+        for (int Q = 0; Q < qb; ++Q) a = cfma(y1[(size_t)Q * b1 * nn_n], Pt[(size_t)Q * qb], a);
+        Y2[e] = a;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int ii = 0; ii < MAXO; ++ii) {
+        const int o = threadIdx.x + ii * blockDim.x;
+        if (o < nout) {
+          const int it = o / (b1 * b1);
+          const int rem = o - it * b1 * b1;
+          const int i = rem / b1, j = rem - i * b1;
+          const double2 *y2 = Y2 + ((size_t)it * b1 + i) * nn_n * qb;
+          double2 a = acc[ii];
+          for (int nn = 0; nn < nn_n; ++nn) {
+            const double2 *vc = Vb + (size_t)j * b2 + n0 + nn;
+            for (int Pi = 0; Pi < qb; ++Pi)
+              a = cfma(y2[nn * qb + Pi], cconj(vc[(size_t)Pi * b1 * b2]), a);
+          }
+          acc[ii] = a;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int ii = 0; ii < MAXO; ++ii) {
+    const int o = threadIdx.x + ii * blockDim.x;
+    if (o < nout) {
+      const int it = o / (b1 * b1);
+      const int rem = o - it * b1 * b1;
+      Sig[tile.sig + (size_t)(tile.t0 + it) * tile.sstride + rem] = cscale(acc[ii], scale);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Block rotation dst = O src O^H (+conj), or slice copy (+conj); restates
+// cugw_routines_block.cu:134-186 (G) and cugw_qkpt_block.cu:288-340 (P).
+// grid = (tasks, batch)
+// ---------------------------------------------------------------------------
+__global__ void rotate_kernel(const RotTask *__restrict__ tasks, const double2 *__restrict__ src,
+                              const double2 *__restrict__ O, double2 *__restrict__ dst) {
+  extern __shared__ double2 sm[];
+  const RotTask t = tasks[blockIdx.x];
+  const double2 *s = src + t.src + (size_t)blockIdx.y * t.sstride;
+  double2 *d = dst + t.dst + (size_t)blockIdx.y * t.dstride;
+  if (!t.rotate) {
+    for (int i = threadIdx.x; i < t.m; i += blockDim.x) d[i] = t.conj ? cconj(s[i]) : s[i];
+    return;
+  }
+  const int m = t.m, n = t.n;
+  double2 *Os = sm;               // m x n
+  double2 *X = sm + m * n;        // n x n
+  double2 *T = X + n * n;         // m x n
+  const double2 *Og = O + t.o;
+  for (int i = threadIdx.x; i < m * n; i += blockDim.x) Os[i] = Og[i];
+  for (int i = threadIdx.x; i < n * n; i += blockDim.x) X[i] = s[i];
+  __syncthreads();
+  for (int e = threadIdx.x; e < m * n; e += blockDim.x) {
+    const int i = e / n, j = e - i * n;
+    double2 a = make_double2(0.0, 0.0);
+    for (int p = 0; p < n; ++p) a = cfma(Os[i * n + p], X[p * n + j], a);
+    T[e] = a;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+    const int i = e / m, j = e - i * m;
+    double2 a = make_double2(0.0, 0.0);
+    for (int p = 0; p < n; ++p) a = cfma(T[i * n + p], cconj(Os[j * n + p]), a);
+    d[e] = t.conj ? cconj(a) : a;
+  }
+}
+
+// P0(beta - t) = P0(t) (cugw_solver_block.cpp:441-456); grid over q, threads over elements.
+__global__ void mirror_kernel(double2 *__restrict__ P, const int64_t *__restrict__ qoff,
+                              const int32_t *__restrict__ qsz, int nts) {
+  const int q = blockIdx.x;
+  const int64_t base = (int64_t)nts * qoff[q];
+  const int sz = qsz[q];
+  const int half = nts / 2;
+  for (int64_t e = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; e < (int64_t)half * sz;
+       e += (int64_t)gridDim.y * blockDim.x) {
+    const int t = (int)(e / sz);
+    const int i = (int)(e - (int64_t)t * sz);
+    P[base + (int64_t)(nts - 1 - t) * sz + i] = P[base + (int64_t)t * sz + i];
+  }
+}
+
+// Zero rows t >= nts/2 of every P0 slice (state left by solve_P0).
+__global__ void zero_upper_kernel(double2 *__restrict__ P, const int64_t *__restrict__ qoff,
+                                  const int32_t *__restrict__ qsz, int nts) {
+  const int q = blockIdx.x;
+  const int64_t base = (int64_t)nts * qoff[q];
+  const int sz = qsz[q];
+  const int half = nts / 2;
+  for (int64_t e = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; e < (int64_t)(nts - half) * sz;
+       e += (int64_t)gridDim.y * blockDim.x)
+    P[base + (int64_t)half * sz + e] = make_double2(0.0, 0.0);
+}
+
+// ---------------------------------------------------------------------------
+// tau <-> omega transform (transformer_t.h:66-99, 226-308):
+//   Y[slab][r][c] = sum_i T[r][i] X[slab][row0 + i][c],  r < nout, i < nin.
+// 256 threads = 32 columns x 8 row groups; T staged through shared memory in
+// 32-column chunks; each thread keeps up to 20 output rows in registers.
+// ---------------------------------------------------------------------------
+constexpr int TR_MAXR = 20;  // nout <= 8 * TR_MAXR = 160
+__global__ void __launch_bounds__(256) transform_kernel(const TSlab *__restrict__ slabs,
+                                                        const double2 *__restrict__ T, int nout,
+                                                        int nin, int row0,
+                                                        const double2 *__restrict__ X,
+                                                        double2 *__restrict__ Y) {
+  extern __shared__ double2 Ts[];  // [nout][33]
+  const TSlab sl = slabs[blockIdx.x];
+  const int cl = threadIdx.x & 31, rg = threadIdx.x >> 5;
+  const int c = blockIdx.y * 32 + cl;
+  const bool active = c < sl.ncols;
+  double2 acc[TR_MAXR];
+#pragma unroll
+  for (int r = 0; r < TR_MAXR; ++r) acc[r] = make_double2(0.0, 0.0);
+  const double2 *x = X + sl.x + (int64_t)row0 * sl.ldx + c;
+  for (int i0 = 0; i0 < nin; i0 += 32) {
+    const int ni = (nin - i0) < 32 ? (nin - i0) : 32;
+    __syncthreads();
+    for (int e = threadIdx.x; e < nout * 32; e += 256) {
+      const int r = e >> 5, ii = e & 31;
+      Ts[r * 33 + ii] = (ii < ni) ? T[(int64_t)r * nin + i0 + ii] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    if (active) {
+      for (int ii = 0; ii < ni; ++ii) {
+        const double2 xv = x[(int64_t)(i0 + ii) * sl.ldx];
+#pragma unroll
+        for (int r = 0; r < TR_MAXR; ++r) {
+          const int rr = rg + 8 * r;
+          if (rr < nout) acc[r] = cfma(Ts[rr * 33 + ii], xv, acc[r]);
+        }
+      }
+    }
+  }
+  if (active) {
+#pragma unroll
+    for (int r = 0; r < TR_MAXR; ++r) {
+      const int rr = rg + 8 * r;
+      if (rr < nout) Y[sl.y + (int64_t)rr * sl.ldy + c] = acc[r];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched block inverses by Gauss-Jordan elimination with partial (row)
+// pivoting, one warp per matrix, rows owned by lanes.  Returns a non-zero
+// status through *bad for an exactly singular block.
+//   mode 0 (W~ solve, cugw_solver_block.cpp:412-424):
+//     A = I - (P + P^H)/2 ; A^-1 ; R = (A^-1 + A^-H)/2 ; P <- R P
+//   mode 1 (Dyson, sc_type_block.cpp:48-57):
+//     A = (i w_n + mu) S - F - Sigma(i w_n) ; G = A^-1   (in place)
+// ---------------------------------------------------------------------------
+template <int NMAX>
+__global__ void inverse_kernel(const InvTask *__restrict__ tasks, int ntasks, double2 *__restrict__ W,
+                               const double2 *__restrict__ S, const double2 *__restrict__ F,
+                               const int64_t *__restrict__ wsample, double beta, double mu, int mode,
+                               int *__restrict__ bad) {
+  constexpr int WPB = inv_warps_per_block(NMAX);
+  extern __shared__ double2 smem_inv[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double2 *A = smem_inv + (size_t)warp * 2 * NMAX * NMAX;
+  double2 *B = A + NMAX * NMAX;
+  int *pv = reinterpret_cast<int *>(smem_inv + (size_t)WPB * 2 * NMAX * NMAX) + warp * NMAX;
+  const int ti = blockIdx.x * WPB + warp;
+  if (ti >= ntasks) return;
+  const InvTask tk = tasks[ti];
+  const int n = tk.n;
+  double2 *g = W + tk.a;
+  if (mode == 0) {
+    for (int e = lane; e < n * n; e += 32) B[e] = g[e];
+    __syncwarp();
+    for (int e = lane; e < n * n; e += 32) {
+      const int i = e / n, j = e - i * n;
+      const double2 pij = B[e], pji = B[j * n + i];
+      A[e] = make_double2((i == j ? 1.0 : 0.0) - 0.5 * (pij.x + pji.x), -0.5 * (pij.y - pji.y));
+    }
+  } else {
+    const double wn = (2.0 * (double)wsample[tk.w] + 1.0) * 3.14159265358979323846 / beta;
+    for (int e = lane; e < n * n; e += 32) {
+      const double2 sv = S[tk.s + e], fv = F[tk.f + e], sg = g[e];
+      // (mu + i wn) * S - F - Sigma
+      A[e] = make_double2(mu * sv.x - wn * sv.y - fv.x - sg.x, mu * sv.y + wn * sv.x - fv.y - sg.y);
+    }
+  }
+  __syncwarp();
+  int singular = 0;
+  for (int k = 0; k < n; ++k) {
+    // pivot: largest |A[i][k]|, i >= k
+    double best = -1.0;
+    int bi = k;
+    for (int i = k + lane; i < n; i += 32) {
+      const double2 v = A[i * n + k];
+      const double av = v.x * v.x + v.y * v.y;
+      if (av > best) { best = av; bi = i; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, off);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    bi = __shfl_sync(0xffffffffu, bi, 0);
+    best = __shfl_sync(0xffffffffu, best, 0);
+    if (lane == 0) pv[k] = bi;
+    if (!(best > 0.0)) { singular = 1; break; }
+    if (bi != k)
+      for (int j = lane; j < n; j += 32) {
+        const double2 t = A[k * n + j];
+        A[k * n + j] = A[bi * n + j];
+        A[bi * n + j] = t;
+      }
+    __syncwarp();
+    const double2 pv = A[k * n + k];
+    const double den = pv.x * pv.x + pv.y * pv.y;
+    const double2 pinv = make_double2(pv.x / den, -pv.y / den);
+    __syncwarp();
+    for (int j = lane; j < n; j += 32) {
+      const double2 v = (j == k) ? make_double2(1.0, 0.0) : A[k * n + j];
+      A[k * n + j] = cmul(v, pinv);
+    }
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) {
+      if (i == k) continue;
+      const double2 f = A[i * n + k];
+      A[i * n + k] = make_double2(0.0, 0.0);
+      for (int j = 0; j < n; ++j) {
+        const double2 r = A[k * n + j];
+        A[i * n + j] = make_double2(A[i * n + j].x - (f.x * r.x - f.y * r.y),
+                                    A[i * n + j].y - (f.x * r.y + f.y * r.x));
+      }
+    }
+    __syncwarp();
+  }
+  if (singular) {
+    if (lane == 0) atomicExch(bad, 1);
+    return;
+  }
+  // undo the row interchanges as column interchanges, in reverse order
+  for (int k = n - 1; k >= 0; --k) {
+    const int p = pv[k];
+    if (p != k)
+      for (int i = lane; i < n; i += 32) {
+        const double2 t = A[i * n + k];
+        A[i * n + k] = A[i * n + p];
+        A[i * n + p] = t;
+      }
+    __syncwarp();
+  }
+  if (mode == 1) {
+    for (int e = lane; e < n * n; e += 32) g[e] = A[e];
+    return;
+  }
+  // R = (A^-1 + A^-H)/2, each unordered pair by one lane
+  for (int e = lane; e < n * n; e += 32) {
+    const int i = e / n, j = e - i * n;
+    if (j < i) continue;
+    const double2 aij = A[e], aji = A[j * n + i];
+    const double2 r = make_double2(0.5 * (aij.x + aji.x), 0.5 * (aij.y - aji.y));
+    A[e] = r;
+    A[j * n + i] = cconj(r);
+  }
+  __syncwarp();
+  for (int e = lane; e < n * n; e += 32) {
+    const int i = e / n, j = e - i * n;
+    double2 a = make_double2(0.0, 0.0);
+    for (int l = 0; l < n; ++l) a = cfma(A[i * n + l], B[l * n + j], a);
+    g[e] = a;
+  }
+}
+
+// Leakage check of G (sc_type_block.cpp:66-71): max over elements of
+// |sum_t tct[t] G(tau_{t+1})| for the first and last IR coefficient.
+__global__ void leakage_kernel(const TSlab *__restrict__ slabs, const double2 *__restrict__ G,
+                               const double *__restrict__ tct_first, const double *__restrict__ tct_last,
+                               int ncheb, unsigned long long *__restrict__ out) {
+  const TSlab sl = slabs[blockIdx.x];
+  double mf = 0.0, ml = 0.0;
+  for (int c = blockIdx.y * blockDim.x + threadIdx.x; c < sl.ncols; c += gridDim.y * blockDim.x) {
+    double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
+    for (int t = 0; t < ncheb; ++t) {
+      const double2 g = G[sl.y + (int64_t)(t + 1) * sl.ldy + c];
+      a.x += tct_first[t] * g.x; a.y += tct_first[t] * g.y;
+      b.x += tct_last[t] * g.x;  b.y += tct_last[t] * g.y;
+    }
+    mf = fmax(mf, sqrt(a.x * a.x + a.y * a.y));
+    ml = fmax(ml, sqrt(b.x * b.x + b.y * b.y));
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    mf = fmax(mf, __shfl_down_sync(0xffffffffu, mf, off));
+    ml = fmax(ml, __shfl_down_sync(0xffffffffu, ml, off));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(out, (unsigned long long)__double_as_longlong(mf));
+    atomicMax(out + 1, (unsigned long long)__double_as_longlong(ml));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+void launch_p0_fp64(const P0Tile *tiles, int ntiles, int maxo, const P0Contrib *contribs,
+                    const double2 *V, const double2 *G, double2 *P0, int ns, int nts, double pref,
+                    int mirror, int smem_bytes, cudaStream_t st) {
+  if (ntiles == 0) return;
+  const int cap = smem_bytes / (int)sizeof(double2);
+  if (maxo <= 8)
+    p0_fp64_kernel<8><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P0, ns, nts, pref, mirror, cap);
+  else
+    p0_fp64_kernel<16><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P0, ns, nts, pref, mirror, cap);
+}
+
+void launch_sigma_fp64(const SigTile *tiles, int ntiles, int maxo, const SigContrib *contribs,
+                       const double2 *V, const double2 *G, const double2 *P, double2 *Sig, int ns,
+                       double scale, int smem_bytes, cudaStream_t st) {
+  if (ntiles == 0) return;
+  const int cap = smem_bytes / (int)sizeof(double2);
+  if (maxo <= 8)
+    sigma_fp64_kernel<8><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P, Sig, ns, scale, cap);
+  else
+    sigma_fp64_kernel<16><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P, Sig, ns, scale, cap);
+}
+
+void launch_rotate(const RotTask *tasks, int ntasks, int nbatch, int smem_bytes, const double2 *src,
+                   const double2 *O, double2 *dst, cudaStream_t st) {
+  if (ntasks == 0 || nbatch == 0) return;
+  rotate_kernel<<<dim3(ntasks, nbatch), 128, smem_bytes, st>>>(tasks, src, O, dst);
+}
+
+void launch_mirror(double2 *P, const int64_t *qoff, const int32_t *qsz, int nq, int nts, cudaStream_t st) {
+  mirror_kernel<<<dim3(nq, 8), 256, 0, st>>>(P, qoff, qsz, nts);
+}
+
+void launch_zero_upper(double2 *P, const int64_t *qoff, const int32_t *qsz, int nq, int nts, cudaStream_t st) {
+  zero_upper_kernel<<<dim3(nq, 8), 256, 0, st>>>(P, qoff, qsz, nts);
+}
+
+void launch_transform(const TSlab *slabs, int nslabs, int max_cols, const double2 *T, int nout, int nin,
+                      int row0, const double2 *X, double2 *Y, cudaStream_t st) {
+  if (nslabs == 0) return;
+  transform_kernel<<<dim3(nslabs, (max_cols + 31) / 32), 256, (size_t)nout * 33 * sizeof(double2), st>>>(slabs, T, nout, nin, row0, X, Y);
+}
+
+void launch_inverse(const InvTask *tasks, int ntasks, int nmax, double2 *W, const double2 *S,
+                    const double2 *F, const int64_t *wsample, double beta, double mu, int mode, int *bad,
+                    cudaStream_t st) {
+  if (ntasks == 0) return;
+  if (nmax <= 16) {
+    constexpr int w = inv_warps_per_block(16);
+    inverse_kernel<16><<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(16), st>>>(tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad);
+  } else if (nmax <= 32) {
+    constexpr int w = inv_warps_per_block(32);
+    inverse_kernel<32><<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(32), st>>>(tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad);
+  } else {
+    constexpr int w = inv_warps_per_block(64);
+    inverse_kernel<64><<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(64), st>>>(tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad);
+  }
+}
+
+void launch_leakage(const TSlab *slabs, int nslabs, const double2 *G, const double *tf, const double *tl,
+                    int ncheb, unsigned long long *out, cudaStream_t st) {
+  if (nslabs == 0) return;
+  leakage_kernel<<<dim3(nslabs, 4), 256, 0, st>>>(slabs, G, tf, tl, ncheb, out);
+}
+
+void set_fp64_kernel_attributes(int smem_bytes) {
+  GWGB_CUDA(cudaFuncSetAttribute(p0_fp64_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(p0_fp64_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_fp64_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_fp64_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(rotate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rotate_smem_bytes(MAX_BLOCK)));
+  GWGB_CUDA(cudaFuncSetAttribute(transform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * TR_MAXR * 33 * (int)sizeof(double2)));
+  GWGB_CUDA(cudaFuncSetAttribute(inverse_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, inv_smem_bytes(16)));
+  GWGB_CUDA(cudaFuncSetAttribute(inverse_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, inv_smem_bytes(32)));
+  GWGB_CUDA(cudaFuncSetAttribute(inverse_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, inv_smem_bytes(64)));
+}
+
+}  // namespace gwgb

@@ -1,0 +1,145 @@
+"""Host-side mirror of the reference's GW solver interface over the C ABI.
+
+``GWSolver`` exposes the methods of SymmetryMBPT's ``solver_block_t`` /
+``cugw_solver_block_t`` (``SymmetryMBPT/include/solver/solver_block_t.h:37-65``,
+``SymmetryMBPT/include/solver/cugw_solver_block.h:117-180``) with the same
+names and meaning -- ``solve()``, ``solve_P0()``, ``solve_sigma()``,
+``compute_Pq_from_P0q()``, ``P0_q_t_QP()``, ``single_prec_run()`` -- plus the
+Dyson step of ``dyson_sc_block_t::compute_G``
+(``SymmetryMBPT/src/scmbpt/sc_type_block.cpp:6-87``).  G(tau) and Sigma(tau)
+live in caller-owned host arrays (the reference keeps them in MPI shared
+windows owned by ``sc_loop_block_t``); every call goes through
+``libgwgb.so``.  Errors raise :class:`~mbsymmetry_gb300._abi.GwgbError`, a
+``RuntimeError`` as the reference's ``std::runtime_error``.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from . import _abi
+from .layout import BlockLayout
+from .transformer import IRTransforms
+
+
+def _ptr(a: np.ndarray):
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+class GWSolver:
+    def __init__(self, layout: BlockLayout, ns: int, transforms: IRTransforms,
+                 precision: str = "fp64", device: int = 0):
+        self.lib = _abi.load()
+        self.layout = layout
+        self.ns = ns
+        self.tr = transforms
+        self.nts = transforms.nts
+        p = _abi.GwgbParams(ns=ns, nts=transforms.nts, nw=transforms.nw, nw_b=transforms.nw_b,
+                            beta=transforms.beta, precision=_abi.PREC_NAMES[precision], device=device,
+                            nt_batch=0, flags=0)
+        self._lay_c, self._keep = layout.to_c()
+        h = ctypes.c_void_p()
+        _abi.check(self.lib.gwgb_create(ctypes.byref(p), ctypes.byref(self._lay_c), ctypes.byref(h)))
+        self.h = h
+        L = layout
+        _abi.check(self.lib.gwgb_set_reps(self.h, _ptr(np.ascontiguousarray(L.orep)), L.orep.size,
+                                          _ptr(np.ascontiguousarray(L.auxrep)), L.auxrep.size))
+        tf = np.ascontiguousarray(transforms.Tct[0])
+        tl = np.ascontiguousarray(transforms.Tct[transforms.ncheb - 1])
+        _abi.check(self.lib.gwgb_set_transforms(
+            self.h, _ptr(transforms.Tnt), _ptr(transforms.Ttn), _ptr(transforms.Tnt_BF), _ptr(transforms.Ttn_FB),
+            _ptr(transforms.wsample_fermi), _ptr(tf), _ptr(tl)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gwgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    # -- sizes ----------------------------------------------------------------
+    @property
+    def g_size(self) -> int:
+        return self.nts * self.ns * self.layout.flat_ao_size
+
+    @property
+    def p_size(self) -> int:
+        return self.nts * self.layout.flat_aux_size
+
+    # -- inputs (set_shared_Coulomb, copy_*_host_to_device) --------------------
+    def set_shared_Coulomb(self, V: np.ndarray):
+        V = np.ascontiguousarray(V, dtype=np.complex128)
+        _abi.check(self.lib.gwgb_upload_V(self.h, _ptr(V), V.size))
+
+    def set_fock(self, F: np.ndarray, S: np.ndarray):
+        F = np.ascontiguousarray(F, dtype=np.complex128)
+        S = np.ascontiguousarray(S, dtype=np.complex128)
+        _abi.check(self.lib.gwgb_set_fock(self.h, _ptr(F), _ptr(S)))
+
+    def single_prec_run(self, run_sp: bool, kind: str = "tf32x3"):
+        _abi.check(self.lib.gwgb_set_precision(self.h, _abi.PREC_NAMES[kind if run_sp else "fp64"]))
+
+    # -- G / Sigma / P host <-> device ----------------------------------------
+    def set_G(self, G: np.ndarray):
+        G = np.ascontiguousarray(G, dtype=np.complex128)
+        assert G.size == self.g_size
+        _abi.check(self.lib.gwgb_set_G(self.h, _ptr(G)))
+
+    def G_tau(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        out = np.empty(self.g_size, np.complex128) if out is None else out
+        _abi.check(self.lib.gwgb_get_G(self.h, _ptr(out)))
+        return out
+
+    def set_Selfenergy(self, S: np.ndarray):
+        S = np.ascontiguousarray(S, dtype=np.complex128)
+        assert S.size == self.g_size
+        _abi.check(self.lib.gwgb_set_sigma(self.h, _ptr(S)))
+
+    def Selfenergy(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        out = np.empty(self.g_size, np.complex128) if out is None else out
+        _abi.check(self.lib.gwgb_get_sigma(self.h, _ptr(out)))
+        return out
+
+    def set_P0(self, P: np.ndarray):
+        P = np.ascontiguousarray(P, dtype=np.complex128)
+        assert P.size == self.p_size
+        _abi.check(self.lib.gwgb_set_P0(self.h, _ptr(P)))
+
+    def P0_q_t_QP(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        out = np.empty(self.p_size, np.complex128) if out is None else out
+        _abi.check(self.lib.gwgb_get_P0(self.h, _ptr(out)))
+        return out
+
+    # -- solver API (cugw_solver_block_t) --------------------------------------
+    def solve_P0(self):
+        _abi.check(self.lib.gwgb_solve_P0(self.h))
+
+    def compute_Pq_from_P0q(self):
+        _abi.check(self.lib.gwgb_solve_Pq(self.h))
+
+    def solve_sigma(self):
+        _abi.check(self.lib.gwgb_solve_sigma(self.h))
+
+    def solve(self):
+        _abi.check(self.lib.gwgb_solve(self.h))
+
+    def dyson(self, mu: float):
+        _abi.check(self.lib.gwgb_dyson(self.h, float(mu)))
+
+    def iteration(self, mu: float):
+        _abi.check(self.lib.gwgb_iteration(self.h, float(mu)))
+
+    def synchronize(self):
+        _abi.check(self.lib.gwgb_synchronize(self.h))
+
+    def stats(self) -> dict:
+        s = _abi.GwgbStats()
+        _abi.check(self.lib.gwgb_get_stats(self.h, ctypes.byref(s)))
+        return {name: getattr(s, name) for name, _ in _abi.GwgbStats._fields_}
+
+    def name(self) -> str:
+        return "GB300 GW solver"
