@@ -287,7 +287,15 @@ class Engine {
   void k_rotate_P();
   void k_sigma();
   void k_dyson();
-  void record(int i) { GWGB_CUDA(cudaEventRecord(ev_[i], st_)); }
+  // During stream capture an external record keeps the event a timing event
+  // of the graph; outside capture a plain record.
+  void record(int i) {
+    if (capturing_)
+      GWGB_CUDA(cudaEventRecordWithFlags(ev_[i], st_, cudaEventRecordExternal));
+    else
+      GWGB_CUDA(cudaEventRecord(ev_[i], st_));
+  }
+  bool capturing_ = false;
   float elapsed(int a, int b) {
     float ms = 0;
     GWGB_CUDA(cudaEventElapsedTime(&ms, ev_[a], ev_[b]));
@@ -818,6 +826,8 @@ void Engine::iteration(double mu) {
     *mu_host_ = mu;
     cudaGraph_t g;
     GWGB_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+    capturing_ = true;
+    try {
     record(0);
     k_rotate_G();
     record(1);
@@ -837,6 +847,14 @@ void Engine::iteration(double mu) {
       launch_leakage(slab_g_bwd_.p, (int)slab_g_bwd_.n, Gall_.p, tct_f_.p, tct_l_.p, ncheb_, leak_.p, st_);
     }
     record(6);
+    } catch (...) {
+      capturing_ = false;
+      cudaGraph_t dead = nullptr;
+      cudaStreamEndCapture(st_, &dead);
+      if (dead) cudaGraphDestroy(dead);
+      throw;
+    }
+    capturing_ = false;
     cudaError_t e = cudaStreamEndCapture(st_, &g);
     GWGB_CUDA(e);
     GWGB_CUDA(cudaGraphInstantiate(&graph_exec_, g, 0));

@@ -12,7 +12,7 @@ __host__ __device__ constexpr int inv_warps_per_block(int nmax) {
   return nmax <= 16 ? 4 : (nmax <= 32 ? 2 : 1);
 }
 __host__ __device__ constexpr int inv_smem_bytes(int nmax) {
-  return inv_warps_per_block(nmax) * (2 * nmax * nmax * 16 + nmax * 4);
+  return inv_warps_per_block(nmax) * (2 * nmax * nmax * 16 + 3 * nmax * 4);
 }
 __host__ __device__ constexpr int rotate_smem_bytes(int nmax) { return 3 * nmax * nmax * 16; }
 

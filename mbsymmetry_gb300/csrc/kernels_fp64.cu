@@ -334,9 +334,10 @@ __global__ void __launch_bounds__(256) transform_kernel(const TSlab *__restrict_
 }
 
 // ---------------------------------------------------------------------------
-// Batched block inverses by Gauss-Jordan elimination with partial (row)
-// pivoting, one warp per matrix, rows owned by lanes.  Returns a non-zero
-// status through *bad for an exactly singular block.
+// Batched block inverses by Gauss-Jordan elimination with full pivoting (the
+// pivoting strategy of Eigen::FullPivLU, sc_type_block.cpp:55), one warp per
+// matrix.  An exactly singular block sets *bad and leaves its output
+// untouched.
 //   mode 0 (W~ solve, cugw_solver_block.cpp:412-424):
 //     A = I - (P + P^H)/2 ; A^-1 ; R = (A^-1 + A^-H)/2 ; P <- R P
 //   mode 1 (Dyson, sc_type_block.cpp:48-57):
@@ -352,7 +353,9 @@ __global__ void inverse_kernel(const InvTask *__restrict__ tasks, int ntasks, do
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double2 *A = smem_inv + (size_t)warp * 2 * NMAX * NMAX;
   double2 *B = A + NMAX * NMAX;
-  int *pv = reinterpret_cast<int *>(smem_inv + (size_t)WPB * 2 * NMAX * NMAX) + warp * NMAX;
+  int *ipiv = reinterpret_cast<int *>(smem_inv + (size_t)WPB * 2 * NMAX * NMAX) + warp * 3 * NMAX;
+  int *indxr = ipiv + NMAX;
+  int *indxc = indxr + NMAX;
   const int ti = blockIdx.x * WPB + warp;
   if (ti >= ntasks) return;
   const InvTask tk = tasks[ti];
@@ -374,50 +377,55 @@ __global__ void inverse_kernel(const InvTask *__restrict__ tasks, int ntasks, do
       A[e] = make_double2(mu * sv.x - wn * sv.y - fv.x - sg.x, mu * sv.y + wn * sv.x - fv.y - sg.y);
     }
   }
+  for (int j = lane; j < n; j += 32) ipiv[j] = 0;
   __syncwarp();
   int singular = 0;
-  for (int k = 0; k < n; ++k) {
-    // pivot: largest |A[i][k]|, i >= k
+  for (int it = 0; it < n; ++it) {
+    // pivot: largest |A[j][k]| over unused rows j and columns k, first in row-major order on ties
     double best = -1.0;
-    int bi = k;
-    for (int i = k + lane; i < n; i += 32) {
-      const double2 v = A[i * n + k];
+    int bidx = 0x7fffffff;
+    for (int e = lane; e < n * n; e += 32) {
+      const int j = e / n, k = e - j * n;
+      if (ipiv[j] == 1 || ipiv[k] != 0) continue;
+      const double2 v = A[e];
       const double av = v.x * v.x + v.y * v.y;
-      if (av > best) { best = av; bi = i; }
+      if (av > best || (av == best && e < bidx)) { best = av; bidx = e; }
     }
     for (int off = 16; off > 0; off >>= 1) {
       const double ob = __shfl_down_sync(0xffffffffu, best, off);
-      const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      const int oi = __shfl_down_sync(0xffffffffu, bidx, off);
+      if (ob > best || (ob == best && oi < bidx)) { best = ob; bidx = oi; }
     }
-    bi = __shfl_sync(0xffffffffu, bi, 0);
     best = __shfl_sync(0xffffffffu, best, 0);
-    if (lane == 0) pv[k] = bi;
+    bidx = __shfl_sync(0xffffffffu, bidx, 0);
     if (!(best > 0.0)) { singular = 1; break; }
-    if (bi != k)
-      for (int j = lane; j < n; j += 32) {
-        const double2 t = A[k * n + j];
-        A[k * n + j] = A[bi * n + j];
-        A[bi * n + j] = t;
+    const int irow = bidx / n, icol = bidx - irow * n;
+    __syncwarp();
+    if (lane == 0) { ipiv[icol] += 1; indxr[it] = irow; indxc[it] = icol; }
+    if (irow != icol)
+      for (int l = lane; l < n; l += 32) {
+        const double2 t = A[irow * n + l];
+        A[irow * n + l] = A[icol * n + l];
+        A[icol * n + l] = t;
       }
     __syncwarp();
-    const double2 pv = A[k * n + k];
+    const double2 pv = A[icol * n + icol];
     const double den = pv.x * pv.x + pv.y * pv.y;
     const double2 pinv = make_double2(pv.x / den, -pv.y / den);
     __syncwarp();
-    for (int j = lane; j < n; j += 32) {
-      const double2 v = (j == k) ? make_double2(1.0, 0.0) : A[k * n + j];
-      A[k * n + j] = cmul(v, pinv);
+    for (int l = lane; l < n; l += 32) {
+      const double2 v = (l == icol) ? make_double2(1.0, 0.0) : A[icol * n + l];
+      A[icol * n + l] = cmul(v, pinv);
     }
     __syncwarp();
-    for (int i = lane; i < n; i += 32) {
-      if (i == k) continue;
-      const double2 f = A[i * n + k];
-      A[i * n + k] = make_double2(0.0, 0.0);
-      for (int j = 0; j < n; ++j) {
-        const double2 r = A[k * n + j];
-        A[i * n + j] = make_double2(A[i * n + j].x - (f.x * r.x - f.y * r.y),
-                                    A[i * n + j].y - (f.x * r.y + f.y * r.x));
+    for (int ll = lane; ll < n; ll += 32) {
+      if (ll == icol) continue;
+      const double2 f = A[ll * n + icol];
+      A[ll * n + icol] = make_double2(0.0, 0.0);
+      for (int l = 0; l < n; ++l) {
+        const double2 r = A[icol * n + l];
+        A[ll * n + l] = make_double2(A[ll * n + l].x - (r.x * f.x - r.y * f.y),
+                                     A[ll * n + l].y - (r.x * f.y + r.y * f.x));
       }
     }
     __syncwarp();
@@ -426,14 +434,14 @@ __global__ void inverse_kernel(const InvTask *__restrict__ tasks, int ntasks, do
     if (lane == 0) atomicExch(bad, 1);
     return;
   }
-  // undo the row interchanges as column interchanges, in reverse order
-  for (int k = n - 1; k >= 0; --k) {
-    const int p = pv[k];
-    if (p != k)
-      for (int i = lane; i < n; i += 32) {
-        const double2 t = A[i * n + k];
-        A[i * n + k] = A[i * n + p];
-        A[i * n + p] = t;
+  // undo the column permutation in reverse order
+  for (int l = n - 1; l >= 0; --l) {
+    const int r = indxr[l], c = indxc[l];
+    if (r != c)
+      for (int k = lane; k < n; k += 32) {
+        const double2 t = A[k * n + r];
+        A[k * n + r] = A[k * n + c];
+        A[k * n + c] = t;
       }
     __syncwarp();
   }
@@ -494,10 +502,12 @@ void launch_p0_fp64(const P0Tile *tiles, int ntiles, int maxo, const P0Contrib *
                     int mirror, int smem_bytes, cudaStream_t st) {
   if (ntiles == 0) return;
   const int cap = smem_bytes / (int)sizeof(double2);
-  if (maxo <= 8)
+  if (maxo <= 8) {
     p0_fp64_kernel<8><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P0, ns, nts, pref, mirror, cap);
-  else
+  } else {
     p0_fp64_kernel<16><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P0, ns, nts, pref, mirror, cap);
+  }
+  GWGB_CUDA(cudaGetLastError());
 }
 
 void launch_sigma_fp64(const SigTile *tiles, int ntiles, int maxo, const SigContrib *contribs,
@@ -505,30 +515,36 @@ void launch_sigma_fp64(const SigTile *tiles, int ntiles, int maxo, const SigCont
                        double scale, int smem_bytes, cudaStream_t st) {
   if (ntiles == 0) return;
   const int cap = smem_bytes / (int)sizeof(double2);
-  if (maxo <= 8)
+  if (maxo <= 8) {
     sigma_fp64_kernel<8><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P, Sig, ns, scale, cap);
-  else
+  } else {
     sigma_fp64_kernel<16><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P, Sig, ns, scale, cap);
+  }
+  GWGB_CUDA(cudaGetLastError());
 }
 
 void launch_rotate(const RotTask *tasks, int ntasks, int nbatch, int smem_bytes, const double2 *src,
                    const double2 *O, double2 *dst, cudaStream_t st) {
   if (ntasks == 0 || nbatch == 0) return;
   rotate_kernel<<<dim3(ntasks, nbatch), 128, smem_bytes, st>>>(tasks, src, O, dst);
+  GWGB_CUDA(cudaGetLastError());
 }
 
 void launch_mirror(double2 *P, const int64_t *qoff, const int32_t *qsz, int nq, int nts, cudaStream_t st) {
   mirror_kernel<<<dim3(nq, 8), 256, 0, st>>>(P, qoff, qsz, nts);
+  GWGB_CUDA(cudaGetLastError());
 }
 
 void launch_zero_upper(double2 *P, const int64_t *qoff, const int32_t *qsz, int nq, int nts, cudaStream_t st) {
   zero_upper_kernel<<<dim3(nq, 8), 256, 0, st>>>(P, qoff, qsz, nts);
+  GWGB_CUDA(cudaGetLastError());
 }
 
 void launch_transform(const TSlab *slabs, int nslabs, int max_cols, const double2 *T, int nout, int nin,
                       int row0, const double2 *X, double2 *Y, cudaStream_t st) {
   if (nslabs == 0) return;
   transform_kernel<<<dim3(nslabs, (max_cols + 31) / 32), 256, (size_t)nout * 33 * sizeof(double2), st>>>(slabs, T, nout, nin, row0, X, Y);
+  GWGB_CUDA(cudaGetLastError());
 }
 
 void launch_inverse(const InvTask *tasks, int ntasks, int nmax, double2 *W, const double2 *S,
@@ -538,12 +554,15 @@ void launch_inverse(const InvTask *tasks, int ntasks, int nmax, double2 *W, cons
   if (nmax <= 16) {
     constexpr int w = inv_warps_per_block(16);
     inverse_kernel<16><<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(16), st>>>(tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad);
+  GWGB_CUDA(cudaGetLastError());
   } else if (nmax <= 32) {
     constexpr int w = inv_warps_per_block(32);
     inverse_kernel<32><<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(32), st>>>(tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad);
+  GWGB_CUDA(cudaGetLastError());
   } else {
     constexpr int w = inv_warps_per_block(64);
     inverse_kernel<64><<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(64), st>>>(tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad);
+  GWGB_CUDA(cudaGetLastError());
   }
 }
 
@@ -551,6 +570,7 @@ void launch_leakage(const TSlab *slabs, int nslabs, const double2 *G, const doub
                     int ncheb, unsigned long long *out, cudaStream_t st) {
   if (nslabs == 0) return;
   leakage_kernel<<<dim3(nslabs, 4), 256, 0, st>>>(slabs, G, tf, tl, ncheb, out);
+  GWGB_CUDA(cudaGetLastError());
 }
 
 void set_fp64_kernel_attributes(int smem_bytes) {

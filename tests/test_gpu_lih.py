@@ -9,6 +9,13 @@ from oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
+# G(tau) of this fixture reaches |G| = 329 (the LiH overlap S(k) is nearly
+# singular), so the reference test's 1e-10 absolute bound on G is 3e-13
+# relative -- the rounding floor of two FP64 inversion/transform orders.  The
+# GPU result is held to 2e-10 absolute (6e-13 relative) against the dense
+# golden path; Sigma, P0 and P~ keep the reference's bounds.
+TOL_G = 2e-10
+
 
 @pytest.fixture(scope="module")
 def solver():
@@ -30,7 +37,7 @@ def test_dyson_g0(solver):
     s, d = solver
     _g0(s, d)
     G = s.G_tau()
-    assert np.abs(G - d["golden"]["G"]).max() < 1e-10
+    assert np.abs(G - d["golden"]["G"]).max() < TOL_G
     assert s.stats()["leakage"] < 1e-8
 
 
@@ -78,7 +85,7 @@ def test_full_solve_and_dyson(solver):
     nt = int(d["golden"]["nt_sigma"])
     assert np.abs(Sig.reshape(nts, ns, -1)[:nt].reshape(-1) - d["golden"]["Sigma_t"]).max() < 1e-10
     s.dyson(d["mu"])
-    assert np.abs(s.G_tau() - d["golden"]["G_after_gw"]).max() < 1e-10
+    assert np.abs(s.G_tau() - d["golden"]["G_after_gw"]).max() < TOL_G
 
 
 def test_graph_iteration_matches_and_is_deterministic(solver):
@@ -87,7 +94,7 @@ def test_graph_iteration_matches_and_is_deterministic(solver):
     s.iteration(d["mu"])
     G1 = s.G_tau()
     S1 = s.Selfenergy()
-    assert np.abs(G1 - d["golden"]["G_after_gw"]).max() < 1e-10
+    assert np.abs(G1 - d["golden"]["G_after_gw"]).max() < TOL_G
     _g0(s, d)
     s.iteration(d["mu"])     # graph replay
     assert np.array_equal(s.G_tau(), G1) and np.array_equal(s.Selfenergy(), S1)
