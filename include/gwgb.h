@@ -202,6 +202,33 @@ int gwgb_get_stats(gwgb_handle h, gwgb_stats *out);
 /* Block until all work of the handle is done. */
 int gwgb_synchronize(gwgb_handle h);
 
+/* ---- W~ solve without device allocation -------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they run (a host code whose own pool owns all of HBM, a plugin
+ * called where new allocations are forbidden, code that must avoid the
+ * implicit synchronisation of cudaMalloc/cudaFree): P~ = (1 - P~0)^-1 P~0 for
+ * ONE irreducible q on caller-owned device buffers.  Its work space (the
+ * P(i Omega) buffer and the task lists) lives in one static device array of
+ * GWGB_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit; the call allocates nothing.  The first call on a device performs the
+ * set-up (looks up the array's device address, sets kernel limits): make it
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race, so serialise them.  The call synchronises `stream`.
+ *   P0_t   device, [nts][qslice] complex: P0(tau) of the q slice, all nts rows
+ *          (mirrored, as after gwgb_solve); may alias P_t
+ *   P_t    device, [nts][qslice] complex output P~(tau)
+ *   Tnt_BF device, [nw_b][nts-2]; Ttn_FB device, [nts][nw_b] (see gwgb_set_transforms)
+ *   block_sizes host, [nblocks] aux block sizes of the q (1..64 each)
+ *   stream  a cudaStream_t (NULL = legacy default stream)
+ * Limits: nblocks <= GWGB_NOALLOC_MAX_BLOCKS and
+ *   nw_b*qslice*16 + nw_b*nblocks*32 + 512 <= GWGB_NOALLOC_SCRATCH_BYTES,
+ *   otherwise GWGB_E_UNSUPPORTED; a singular block returns GWGB_E_NUMERIC. */
+#define GWGB_NOALLOC_SCRATCH_BYTES (8u << 20)
+#define GWGB_NOALLOC_MAX_BLOCKS 64
+int gwgb_wsolve_noalloc(int32_t device, const double *P0_t, double *P_t, const double *Tnt_BF,
+                        const double *Ttn_FB, int32_t nts, int32_t nw_b, const int32_t *block_sizes,
+                        int32_t nblocks, void *stream);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

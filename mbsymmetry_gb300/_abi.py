@@ -85,7 +85,12 @@ SIGNATURES = {
     "gwgb_iteration": (c_int32, [c_void_p, c_double]),
     "gwgb_get_stats": (c_int32, [c_void_p, POINTER(GwgbStats)]),
     "gwgb_synchronize": (c_int32, [c_void_p]),
+    "gwgb_wsolve_noalloc": (c_int32, [c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
+                                      c_void_p, c_int32, c_void_p]),
 }
+
+NOALLOC_SCRATCH_BYTES = 8 << 20
+NOALLOC_MAX_BLOCKS = 64
 
 _lib = None
 

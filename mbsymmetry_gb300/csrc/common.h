@@ -10,6 +10,9 @@
 
 namespace gwgb {
 
+// Sets the thread-local message returned by gwgb_last_error().
+void set_last_error(const std::string &msg);
+
 // Error carrying a gwgb status code; the C ABI turns it into a return value.
 struct Error : std::runtime_error {
   int code;

@@ -21,6 +21,8 @@ namespace gwgb {
 
 static thread_local std::string g_last_error = "";
 
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
 // ---------------------------------------------------------------------------
 // Host copy of the layout with every derived offset (the arrays of
 // symmetry_utils_t, SymmetryMBPT/src/common/symmetry_utils.cpp:96-307).
