@@ -16,6 +16,7 @@
 
 #include "common.h"
 #include "kernels.h"
+#include "kernels_mixed.h"
 
 namespace gwgb {
 
@@ -213,8 +214,12 @@ class Engine {
   ~Engine();
 
   void set_precision(int prec) {
-    GWGB_REQUIRE(prec == GWGB_PREC_FP64, GWGB_E_UNSUPPORTED,
-                 "this build implements the FP64 contraction path only");
+    GWGB_REQUIRE(prec == GWGB_PREC_FP64 || prec == GWGB_PREC_TF32X3, GWGB_E_UNSUPPORTED,
+                 "precision not implemented (FP64 and TF32X3 are)");
+    if (prec != prec_ && graph_exec_) {  // the captured graph holds the old kernels
+      cudaGraphExecDestroy(graph_exec_);
+      graph_exec_ = nullptr;
+    }
     prec_ = prec;
   }
   void upload_V(const double *V, int64_t n);
@@ -258,14 +263,15 @@ class Engine {
   DBuf<int64_t> qoff_irr_;
   DBuf<int32_t> qsz_irr_;
   // work lists
-  DBuf<P0Tile> p0_tiles_;
+  DBuf<P0Tile> p0_tiles_, p0_tiles1_;   // tau-chunked (FP64) / one tau per tile (mixed)
   DBuf<P0Contrib> p0_contribs_;
-  DBuf<SigTile> sig_tiles_;
+  DBuf<SigTile> sig_tiles_, sig_tiles1_;
   DBuf<SigContrib> sig_contribs_;
   DBuf<RotTask> rotG_, rotP_;
   DBuf<TSlab> slab_p_fwd_, slab_p_bwd_, slab_s_fwd_, slab_g_bwd_;
   DBuf<InvTask> inv_w_, inv_d_;
   int p0_maxo_ = 8, sig_maxo_ = 8, rot_smem_ = 0;
+  int p0_mixed_smem_ = 0, sig_mixed_smem_ = 0;
   int max_cols_p_ = 0, max_cols_g_ = 0;
   int64_t g_rot_off_ = 0, p_rot_off_ = 0;  // start of the rotated parts
   double p0_flops_ = 0, sig_flops_ = 0;
@@ -323,6 +329,7 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
   GWGB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev_));
   smem_bytes_ = std::min(optin, 200 * 1024);
   set_fp64_kernel_attributes(smem_bytes_);
+  set_mixed_kernel_attributes(smem_bytes_);
   if (p.precision != GWGB_PREC_FP64) set_precision(p.precision);
   GWGB_CUDA(cudaMallocHost(&mu_host_, sizeof(double)));
   build_work_lists();
@@ -356,7 +363,7 @@ Engine::~Engine() {
   for (auto *b : bufs) b->free();
   tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
   qoff_irr_.free(); qsz_irr_.free();
-  p0_tiles_.free(); p0_contribs_.free(); sig_tiles_.free(); sig_contribs_.free();
+  p0_tiles_.free(); p0_tiles1_.free(); p0_contribs_.free(); sig_tiles_.free(); sig_tiles1_.free(); sig_contribs_.free();
   rotG_.free(); rotP_.free(); slab_p_fwd_.free(); slab_p_bwd_.free(); slab_s_fwd_.free(); slab_g_bwd_.free();
   inv_w_.free(); inv_d_.free();
   if (st_) cudaStreamDestroy(st_);
@@ -492,6 +499,25 @@ void Engine::build_work_lists() {
   std::stable_sort(pt.begin(), pt.end(), [](const P0Tile &a, const P0Tile &b) { return a.cost > b.cost; });
   p0_tiles_.upload(pt, st_);
   p0_contribs_.upload(pc, st_);
+  {  // mixed path: one tau per tile; shared memory = FP64 + FP32 accumulators + two intermediates
+    std::vector<P0Tile> pt1;
+    int need = 0;
+    for (const P0Tile &t : pt)
+      for (int i = 0; i < t.nt; ++i) {
+        P0Tile u = t;
+        u.t0 = t.t0 + i;
+        u.nt = 1;
+        u.cost = t.cost / std::max(1, t.nt);
+        pt1.push_back(u);
+        int b2max = 1;
+        for (int c = t.c0; c < t.c1; ++c) b2max = std::max(b2max, pc[c].b2);
+        need = std::max(need, 24 * t.qb * t.qb + 16 * b2max * t.qb);
+      }
+    std::stable_sort(pt1.begin(), pt1.end(), [](const P0Tile &a, const P0Tile &b) { return a.cost > b.cost; });
+    p0_tiles1_.upload(pt1, st_);
+    p0_mixed_smem_ = std::max(16 * 1024, ((need + 1023) / 1024) * 1024);
+    GWGB_REQUIRE(p0_mixed_smem_ <= smem_bytes_, GWGB_E_UNSUPPORTED, "P0 block too large for the mixed kernel");
+  }
 
   // --- Sigma tiles: owner = (k_irr, AO block i1, spin, tau range)
   std::vector<SigTile> stl;
@@ -539,6 +565,25 @@ void Engine::build_work_lists() {
   std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
   sig_tiles_.upload(stl, st_);
   sig_contribs_.upload(sc, st_);
+  {
+    std::vector<SigTile> st1;
+    int need = 0;
+    for (const SigTile &t : stl)
+      for (int i = 0; i < t.nt; ++i) {
+        SigTile u = t;
+        u.t0 = t.t0 + i;
+        u.nt = 1;
+        u.cost = t.cost / std::max(1, t.nt);
+        st1.push_back(u);
+        int qbmax = 1;
+        for (int c = t.c0; c < t.c1; ++c) qbmax = std::max(qbmax, sc[c].qb);
+        need = std::max(need, 24 * t.b1 * t.b1 + 16 * qbmax * t.b1);
+      }
+    std::stable_sort(st1.begin(), st1.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
+    sig_tiles1_.upload(st1, st_);
+    sig_mixed_smem_ = std::max(16 * 1024, ((need + 1023) / 1024) * 1024);
+    GWGB_REQUIRE(sig_mixed_smem_ <= smem_bytes_, GWGB_E_UNSUPPORTED, "Sigma block too large for the mixed kernel");
+  }
 
   // --- transforms and block inverses
   std::vector<TSlab> pf, pb, sf, gb;
@@ -677,8 +722,12 @@ void Engine::k_rotate_G() {
 
 void Engine::k_p0(int mirror) {
   const double pref = -1.0 / l_.nk * (ns_ == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
-  launch_p0_fp64(p0_tiles_.p, (int)p0_tiles_.n, p0_maxo_, p0_contribs_.p, V_.p, Gall_.p, Pall_.p, ns_, nts_, pref,
-                 mirror, smem_bytes_, st_);
+  if (prec_ == GWGB_PREC_TF32X3)
+    launch_p0_mixed(p0_tiles1_.p, (int)p0_tiles1_.n, p0_contribs_.p, V_.p, Gall_.p, Pall_.p, ns_, nts_, pref, mirror,
+                    p0_mixed_smem_, st_);
+  else
+    launch_p0_fp64(p0_tiles_.p, (int)p0_tiles_.n, p0_maxo_, p0_contribs_.p, V_.p, Gall_.p, Pall_.p, ns_, nts_, pref,
+                   mirror, smem_bytes_, st_);
 }
 
 void Engine::k_pq(bool mirror_first) {
@@ -693,8 +742,12 @@ void Engine::k_rotate_P() {
 }
 
 void Engine::k_sigma() {
-  launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Sig_.p, ns_,
-                    -1.0 / l_.nk, smem_bytes_, st_);
+  if (prec_ == GWGB_PREC_TF32X3)
+    launch_sigma_mixed(sig_tiles1_.p, (int)sig_tiles1_.n, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Sig_.p, ns_,
+                       -1.0 / l_.nk, sig_mixed_smem_, st_);
+  else
+    launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Sig_.p,
+                      ns_, -1.0 / l_.nk, smem_bytes_, st_);
 }
 
 void Engine::k_dyson() {
@@ -909,7 +962,7 @@ static int on_handle(gwgb_handle h, F &&f) {
 
 extern "C" {
 
-const char *gwgb_version(void) { return "gwgb 0.1 (sm_103a, FP64 contraction path)"; }
+const char *gwgb_version(void) { return "gwgb 0.2 (sm_103a, FP64 and TF32x3 contraction paths)"; }
 
 const char *gwgb_last_error(void) { return gwgb::g_last_error.c_str(); }
 

@@ -55,3 +55,28 @@ def test_c2_sigma_acceptance():
     orc = Oracle(L, cr.ns, tr.nts)
     Sr, _, _ = orc.gw_sigma(G0, cr.V, tr)
     assert np.abs(Sig - Sr).max() < 1e-10
+
+
+@pytest.mark.parametrize("name", ["C1", "C2"])
+def test_mixed_tf32x3_sigma_error(name):
+    """TF32 3-pass contractions against the FP64 path on the same input."""
+    from mbsymmetry_gb300.solver import GWSolver
+    cr, tr = crystal(name)
+    L = cr.layout
+    s = GWSolver(L, cr.ns, tr)
+    s.set_shared_Coulomb(cr.V)
+    s.set_fock(cr.F, cr.S)
+    s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+    s.dyson(cr.mu)
+    G0 = s.G_tau()
+    s.solve()
+    S64, P64 = s.Selfenergy(), s.P0_q_t_QP()
+    s.single_prec_run(True, "tf32x3")
+    s.set_G(G0)
+    s.solve()
+    S32, P32 = s.Selfenergy(), s.P0_q_t_QP()
+    s.close()
+    err = np.abs(S32 - S64).max()
+    print(f"{name}: max|Sigma_tf32x3 - Sigma_fp64| = {err:.3e} (max|Sigma| = {np.abs(S64).max():.3e}), "
+          f"max|P~ err| = {np.abs(P32 - P64).max():.3e}")
+    assert err < 1e-5 * max(1.0, np.abs(S64).max())
