@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -17,6 +18,7 @@
 #include "common.h"
 #include "kernels.h"
 #include "kernels_mixed.h"
+#include "kernels_tc.h"
 
 namespace gwgb {
 
@@ -221,6 +223,8 @@ class Engine {
       graph_exec_ = nullptr;
     }
     prec_ = prec;
+    if (prec_ == GWGB_PREC_TF32X3 && !Wbuf_.p && wbuf_elems_) Wbuf_.alloc((size_t)wbuf_elems_);
+    if (prec_ == GWGB_PREC_TF32X3 && !Zbuf_.p && zbuf_elems_) Zbuf_.alloc((size_t)zbuf_elems_);
   }
   void upload_V(const double *V, int64_t n);
   void set_reps(const double *orep, int64_t no, const double *auxrep, int64_t na);
@@ -272,6 +276,24 @@ class Engine {
   DBuf<InvTask> inv_w_, inv_d_;
   int p0_maxo_ = 8, sig_maxo_ = 8, rot_smem_ = 0;
   int p0_mixed_smem_ = 0, sig_mixed_smem_ = 0;
+  // tcgen05 Sigma path: W-GEMM tiles/columns, per-contribution W offsets, W buffer
+  DBuf<SwTile> sw_tiles_;
+  DBuf<SwCol> sw_cols_;
+  DBuf<int64_t> sig_woff_;
+  DBuf<float2> Wbuf_;
+  int sw_smem_ = 0, uv_smem_ = 0;
+  int64_t wbuf_elems_ = 0;
+  // tcgen05 P0 path: Z tasks, tiles, chunks, Z buffer
+  DBuf<PzTask> pz_tasks_;
+  DBuf<PtTile> pt_tiles_;
+  DBuf<PtChunk> pt_chunks_;
+  DBuf<float2> Zbuf_;
+  int64_t zbuf_elems_ = 0;
+  int pz_smem_ = 0, pt_smem_ = 0;
+  struct P0Group { int64_t pout; int32_t pstride, qb, c0, c1; };
+  std::vector<P0Group> p0_groups_;                            // host: P0 output blocks
+  std::vector<int> sig_b1_;                                  // host: b1 of every Sigma contribution
+  std::map<std::pair<int, int>, std::vector<int>> sig_groups_;  // host: (q, iq) -> contributions
   int max_cols_p_ = 0, max_cols_g_ = 0;
   int64_t g_rot_off_ = 0, p_rot_off_ = 0;  // start of the rotated parts
   double p0_flops_ = 0, sig_flops_ = 0;
@@ -330,9 +352,11 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
   smem_bytes_ = std::min(optin, 200 * 1024);
   set_fp64_kernel_attributes(smem_bytes_);
   set_mixed_kernel_attributes(smem_bytes_);
-  if (p.precision != GWGB_PREC_FP64) set_precision(p.precision);
+  set_tc_kernel_attributes(smem_bytes_);
+  set_tc_p0_kernel_attributes(smem_bytes_);
   GWGB_CUDA(cudaMallocHost(&mu_host_, sizeof(double)));
   build_work_lists();
+  if (p.precision != GWGB_PREC_FP64) set_precision(p.precision);
   // buffers
   const int64_t fa = l_.flat_ao, fq = l_.flat_aux;
   V_.alloc(l_.flat_V);
@@ -344,12 +368,12 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
   orep_.alloc(l_.flat_orep);
   auxrep_.alloc(l_.flat_auxrep);
   mu_dev_.alloc(1);
-  bad_.alloc(2);
+  bad_.alloc(4);
   leak_.alloc(2);
   GWGB_CUDA(cudaMemsetAsync(Gall_.p, 0, Gall_.n * sizeof(double2), st_));
   GWGB_CUDA(cudaMemsetAsync(Pall_.p, 0, Pall_.n * sizeof(double2), st_));
   GWGB_CUDA(cudaMemsetAsync(Sig_.p, 0, Sig_.n * sizeof(double2), st_));
-  GWGB_CUDA(cudaMemsetAsync(bad_.p, 0, 2 * sizeof(int), st_));
+  GWGB_CUDA(cudaMemsetAsync(bad_.p, 0, 4 * sizeof(int), st_));
   GWGB_CUDA(cudaStreamSynchronize(st_));
 }
 
@@ -360,6 +384,8 @@ Engine::~Engine() {
   if (mu_host_) cudaFreeHost(mu_host_);
   DBuf<double2> *bufs[] = {&V_, &Gall_, &Pall_, &Sig_, &Pw_, &Ww_, &F_, &S_, &orep_, &auxrep_,
                            &Tnt_, &Ttn_, &TntBF_, &TtnFB_};
+  sw_tiles_.free(); sw_cols_.free(); sig_woff_.free(); Wbuf_.free();
+  pz_tasks_.free(); pt_tiles_.free(); pt_chunks_.free(); Zbuf_.free();
   for (auto *b : bufs) b->free();
   tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
   qoff_irr_.free(); qsz_irr_.free();
@@ -480,6 +506,7 @@ void Engine::build_work_lists() {
         }
       }
       const int c1 = (int)pc.size();
+      p0_groups_.push_back({(int64_t)nts_ * l.qaux_off_irre[iqr] + l.auxoff(q, iq), (int32_t)l.qaux_sz[q], qb, c0, c1});
       p0_flops_ += flop * ns_ * half;
       int nt = std::max(1, std::min(half, (256 + qb * qb - 1) / (qb * qb)));
       while (nt > 1 && nt * qb * qb > 2048) --nt;
@@ -518,6 +545,41 @@ void Engine::build_work_lists() {
     p0_mixed_smem_ = std::max(16 * 1024, ((need + 1023) / 1024) * 1024);
     GWGB_REQUIRE(p0_mixed_smem_ <= smem_bytes_, GWGB_E_UNSUPPORTED, "P0 block too large for the mixed kernel");
   }
+  {  // tcgen05 P0: Z tasks per (contribution, spin), K chunks of 32 complex columns, 128-row tiles
+    std::vector<PzTask> zt;
+    std::vector<PtTile> ptt;
+    std::vector<PtChunk> chk;
+    int64_t zoff = 0;
+    int zneed = 0;
+    for (const auto &g : p0_groups_) {  // (pout, pstride, qb, c0, c1)
+      const int qb = g.qb;
+      const int k0 = (int)chk.size();
+      for (int c = g.c0; c < g.c1; ++c) {
+        const P0Contrib &cb = pc[c];
+        const int b1b2 = cb.b1 * cb.b2;
+        for (int s = 0; s < ns_; ++s) {
+          zt.push_back({cb.v, cb.ga, cb.gb, zoff, cb.sa, cb.sb, cb.b1, cb.b2, qb, s});
+          for (int kc0 = 0; kc0 < b1b2; kc0 += 32) chk.push_back({zoff, cb.v, b1b2, kc0, std::min(32, b1b2 - kc0), 0});
+          zoff += (int64_t)half * qb * b1b2;
+        }
+        zneed = std::max(zneed, 8 * (cb.b2 * cb.b2 + cb.b1 * cb.b1 + 2 * b1b2 * qb));
+        GWGB_REQUIRE(8 * (cb.b2 * cb.b2 + cb.b1 * cb.b1 + 2 * b1b2) <= smem_bytes_, GWGB_E_UNSUPPORTED,
+                     "P0 block too large for the tcgen05 path");
+      }
+      const int k1 = (int)chk.size();
+      const int nt = std::max(1, std::min(half, 128 / qb));
+      const int NP = ((2 * qb + 15) / 16) * 16;
+      for (int t0 = 0; t0 < half; t0 += nt)
+        ptt.push_back({g.pout, g.pstride, qb, t0, std::min(nt, half - t0), k0, k1, NP, 0});
+    }
+    std::stable_sort(ptt.begin(), ptt.end(), [](const PtTile &a, const PtTile &b) { return (a.k1 - a.k0) > (b.k1 - b.k0); });
+    pz_tasks_.upload(zt, st_);
+    pt_tiles_.upload(ptt, st_);
+    pt_chunks_.upload(chk, st_);
+    zbuf_elems_ = zoff;
+    pz_smem_ = std::min(smem_bytes_, std::max(16 * 1024, ((zneed + 1023) / 1024) * 1024));
+    pt_smem_ = 512 * (128 + 128);
+  }
 
   // --- Sigma tiles: owner = (k_irr, AO block i1, spin, tau range)
   std::vector<SigTile> stl;
@@ -540,6 +602,8 @@ void Engine::build_work_lists() {
           const int qb = l.auxsz(q, iq), b2 = l.aosz(k2, i2);
           sc.push_back({l.kp_off[p] + l.t_off[b], gref[k2].base + l.aooff(k2, i2), pref[q].base + l.auxoff(q, iq),
                         gref[k2].stride, pref[q].stride, b2, qb});
+          sig_b1_.push_back(b1);
+          sig_groups_[std::make_pair(q, iq)].push_back((int)sc.size() - 1);
           flop += 8.0 * ((double)qb * b1 * b2 * b2 + (double)b1 * b2 * qb * qb + (double)b1 * b1 * b2 * qb);
           qbmax = std::max(qbmax, qb);
         }
@@ -583,6 +647,68 @@ void Engine::build_work_lists() {
     sig_tiles1_.upload(st1, st_);
     sig_mixed_smem_ = std::max(16 * 1024, ((need + 1023) / 1024) * 1024);
     GWGB_REQUIRE(sig_mixed_smem_ <= smem_bytes_, GWGB_E_UNSUPPORTED, "Sigma block too large for the mixed kernel");
+  }
+  {  // tcgen05 Sigma: group the contributions by aux block (q, iq)
+    std::vector<int64_t> woff(sc.size());
+    int64_t wtot = 0;
+    for (size_t c = 0; c < sc.size(); ++c) {
+      woff[c] = wtot;
+      wtot += (int64_t)nts_ * sc[c].qb * sig_b1_[c] * sc[c].b2;
+    }
+    std::vector<SwTile> swt;
+    std::vector<SwCol> swc;
+    int wsmem = 0, uvneed = 0;
+    for (const auto &grp : sig_groups_) {
+      const std::vector<int> &cs = grp.second;
+      const int qb = sc[cs[0]].qb;
+      const int64_t pa = sc[cs[0]].pq;
+      const int pstride = sc[cs[0]].pstride;
+      const int KP = ((2 * qb + 7) / 8) * 8;
+      int ncap = std::min(256, ((200 * 1024 / (8 * KP) - 128) / 16) * 16);
+      GWGB_REQUIRE(ncap >= 16, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 Sigma kernel");
+      const int ccap = ncap / 2;  // complex columns per pack
+      const int nt = std::max(1, std::min(nts_, 128 / qb));
+      // column packs
+      struct Pack { int c0, c1, ncol; };
+      std::vector<Pack> packs;
+      Pack cur{(int)swc.size(), (int)swc.size(), 0};
+      for (int c : cs) {
+        const int b1 = sig_b1_[c], b2 = sc[c].b2, tot = b1 * b2;
+        int l = 0;
+        while (l < tot) {
+          if (cur.ncol == ccap) {
+            cur.c1 = (int)swc.size();
+            packs.push_back(cur);
+            cur = Pack{(int)swc.size(), (int)swc.size(), 0};
+          }
+          const int take = std::min(tot - l, ccap - cur.ncol);
+          swc.push_back({sc[c].v, woff[c], b1, b2, l, cur.ncol});
+          cur.ncol += take;
+          l += take;
+        }
+      }
+      cur.c1 = (int)swc.size();
+      if (cur.ncol > 0) packs.push_back(cur);
+      for (const Pack &pk : packs) {
+        const int NP = ((2 * pk.ncol + 15) / 16) * 16;
+        wsmem = std::max(wsmem, 8 * KP * (128 + NP));
+        for (int t0 = 0; t0 < nts_; t0 += nt)
+          swt.push_back({pa, pstride, qb, t0, std::min(nt, nts_ - t0), pk.c0, pk.c1, pk.ncol, KP, NP, 0});
+      }
+    }
+    for (const SigTile &t : stl) {
+      int b2max = 1, qbmax = 1;
+      for (int c = t.c0; c < t.c1; ++c) { b2max = std::max(b2max, sc[c].b2); qbmax = std::max(qbmax, sc[c].qb); }
+      uvneed = std::max(uvneed, 24 * t.b1 * t.b1 + 8 * b2max * b2max + 24 * t.b1 * b2max * qbmax);
+      GWGB_REQUIRE(24 * t.b1 * t.b1 + 8 * b2max * b2max + 24 * t.b1 * b2max <= smem_bytes_, GWGB_E_UNSUPPORTED,
+                   "Sigma block too large for the tcgen05 path");
+    }
+    sw_tiles_.upload(swt, st_);
+    sw_cols_.upload(swc, st_);
+    sig_woff_.upload(woff, st_);
+    sw_smem_ = std::max(16 * 1024, wsmem);
+    uv_smem_ = std::min(smem_bytes_, std::max(16 * 1024, ((uvneed + 1023) / 1024) * 1024));
+    wbuf_elems_ = wtot;
   }
 
   // --- transforms and block inverses
@@ -722,10 +848,11 @@ void Engine::k_rotate_G() {
 
 void Engine::k_p0(int mirror) {
   const double pref = -1.0 / l_.nk * (ns_ == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
-  if (prec_ == GWGB_PREC_TF32X3)
-    launch_p0_mixed(p0_tiles1_.p, (int)p0_tiles1_.n, p0_contribs_.p, V_.p, Gall_.p, Pall_.p, ns_, nts_, pref, mirror,
-                    p0_mixed_smem_, st_);
-  else
+  if (prec_ == GWGB_PREC_TF32X3) {
+    GWGB_REQUIRE(Zbuf_.p || !zbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
+    launch_p0_tc(pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pt_tiles_.p, (int)pt_tiles_.n, pt_smem_, pt_chunks_.p,
+                 V_.p, Gall_.p, Zbuf_.p, Pall_.p, ns_, nts_, pref, mirror, 4, bad_.p + 2, st_);
+  } else
     launch_p0_fp64(p0_tiles_.p, (int)p0_tiles_.n, p0_maxo_, p0_contribs_.p, V_.p, Gall_.p, Pall_.p, ns_, nts_, pref,
                    mirror, smem_bytes_, st_);
 }
@@ -742,10 +869,12 @@ void Engine::k_rotate_P() {
 }
 
 void Engine::k_sigma() {
-  if (prec_ == GWGB_PREC_TF32X3)
-    launch_sigma_mixed(sig_tiles1_.p, (int)sig_tiles1_.n, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Sig_.p, ns_,
-                       -1.0 / l_.nk, sig_mixed_smem_, st_);
-  else
+  if (prec_ == GWGB_PREC_TF32X3) {
+    GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
+    launch_sigma_tc(sw_tiles_.p, (int)sw_tiles_.n, sw_smem_, sw_cols_.p, sig_tiles1_.p, (int)sig_tiles1_.n,
+                    sig_contribs_.p, sig_woff_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p, Sig_.p, ns_, -1.0 / l_.nk, uv_smem_,
+                    bad_.p + 2, st_);
+  } else
     launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Sig_.p,
                       ns_, -1.0 / l_.nk, smem_bytes_, st_);
 }
@@ -761,10 +890,11 @@ void Engine::k_dyson() {
 }
 
 void Engine::check_device_flags() {
-  int bad[2] = {0, 0};
+  int bad[4] = {0, 0, 0, 0};
   GWGB_CUDA(cudaMemcpy(bad, bad_.p, sizeof(bad), cudaMemcpyDeviceToHost));
-  if (bad[0] || bad[1]) {
+  if (bad[0] || bad[1] || bad[2]) {
     GWGB_CUDA(cudaMemset(bad_.p, 0, sizeof(bad)));
+    if (bad[2]) throw Error(GWGB_E_TIMEOUT, "a tensor-core MMA completion wait ran out (tcgen05 commit not observed)");
     throw Error(GWGB_E_NUMERIC, bad[0] ? "singular block in the W~ solve (1 - P~0)" : "singular block in Dyson");
   }
 }
