@@ -223,8 +223,18 @@ class Engine {
       graph_exec_ = nullptr;
     }
     prec_ = prec;
-    if (prec_ == GWGB_PREC_TF32X3 && !Wbuf_.p && wbuf_elems_) Wbuf_.alloc((size_t)wbuf_elems_);
-    if (prec_ == GWGB_PREC_TF32X3 && !Zbuf_.p && zbuf_elems_) Zbuf_.alloc((size_t)zbuf_elems_);
+    if (prec_ == GWGB_PREC_TF32X3 && !Wbuf_.p && wbuf_elems_) {
+      Wbuf_.alloc((size_t)wbuf_elems_);
+      Bcat_.alloc((size_t)bcat_elems_);
+    }
+    if (prec_ == GWGB_PREC_TF32X3 && !Zbuf_.p && zbuf_elems_) {
+      Zbuf_.alloc((size_t)zbuf_elems_);
+      Vcat_.alloc((size_t)vcat_elems_);
+      Ppart_.alloc((size_t)ppart_elems_);
+      GWGB_CUDA(cudaMemsetAsync(Zbuf_.p, 0, Zbuf_.n * sizeof(float2), st_));   // K padding stays zero
+      GWGB_CUDA(cudaMemsetAsync(Vcat_.p, 0, Vcat_.n * sizeof(float2), st_));
+    }
+    if (prec_ == GWGB_PREC_TF32X3 && !vcat_ready_) build_vcat();
   }
   void upload_V(const double *V, int64_t n);
   void set_reps(const double *orep, int64_t no, const double *auxrep, int64_t na);
@@ -276,20 +286,31 @@ class Engine {
   DBuf<InvTask> inv_w_, inv_d_;
   int p0_maxo_ = 8, sig_maxo_ = 8, rot_smem_ = 0;
   int p0_mixed_smem_ = 0, sig_mixed_smem_ = 0;
-  // tcgen05 Sigma path: W-GEMM tiles/columns, per-contribution W offsets, W buffer
+  // tcgen05 Sigma path: W-GEMM tiles, conj(V) operand tasks, per-contribution W references
   DBuf<SwTile> sw_tiles_;
-  DBuf<SwCol> sw_cols_;
-  DBuf<int64_t> sig_woff_;
-  DBuf<float2> Wbuf_;
+  DBuf<BcTask> bc_tasks_;
+  DBuf<WRef> sig_wref_;
+  DBuf<float2> Wbuf_, Bcat_;
+  int64_t bcat_elems_ = 0;
   int sw_smem_ = 0, uv_smem_ = 0;
   int64_t wbuf_elems_ = 0;
-  // tcgen05 P0 path: Z tasks, tiles, chunks, Z buffer
+  // tcgen05 P0 path: Z tasks (into Zcat), Vcat tasks, split-K tiles, reduction tiles
   DBuf<PzTask> pz_tasks_;
-  DBuf<PtTile> pt_tiles_;
-  DBuf<PtChunk> pt_chunks_;
-  DBuf<float2> Zbuf_;
-  int64_t zbuf_elems_ = 0;
-  int pz_smem_ = 0, pt_smem_ = 0;
+  DBuf<VcTask> vc_tasks_;
+  DBuf<PkTile> pk_tiles_;
+  DBuf<PrTile> pr_tiles_;
+  DBuf<float2> Zbuf_, Vcat_;
+  DBuf<double2> Ppart_;
+  int64_t zbuf_elems_ = 0, vcat_elems_ = 0, ppart_elems_ = 0;
+  int pz_smem_ = 0;
+  bool vcat_ready_ = false;
+  void build_vcat() {  // tau-independent tensor-core operands derived from V
+    if (prec_ != GWGB_PREC_TF32X3 || !have_V_) return;
+    launch_vcat(vc_tasks_.p, (int)vc_tasks_.n, V_.p, Vcat_.p, st_);
+    launch_bcat(bc_tasks_.p, (int)bc_tasks_.n, V_.p, Bcat_.p, st_);
+    GWGB_CUDA(cudaStreamSynchronize(st_));
+    vcat_ready_ = true;
+  }
   struct P0Group { int64_t pout; int32_t pstride, qb, c0, c1; };
   std::vector<P0Group> p0_groups_;                            // host: P0 output blocks
   std::vector<int> sig_b1_;                                  // host: b1 of every Sigma contribution
@@ -384,8 +405,8 @@ Engine::~Engine() {
   if (mu_host_) cudaFreeHost(mu_host_);
   DBuf<double2> *bufs[] = {&V_, &Gall_, &Pall_, &Sig_, &Pw_, &Ww_, &F_, &S_, &orep_, &auxrep_,
                            &Tnt_, &Ttn_, &TntBF_, &TtnFB_};
-  sw_tiles_.free(); sw_cols_.free(); sig_woff_.free(); Wbuf_.free();
-  pz_tasks_.free(); pt_tiles_.free(); pt_chunks_.free(); Zbuf_.free();
+  sw_tiles_.free(); bc_tasks_.free(); sig_wref_.free(); Wbuf_.free(); Bcat_.free();
+  pz_tasks_.free(); vc_tasks_.free(); pk_tiles_.free(); pr_tiles_.free(); Zbuf_.free(); Vcat_.free(); Ppart_.free();
   for (auto *b : bufs) b->free();
   tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
   qoff_irr_.free(); qsz_irr_.free();
@@ -545,40 +566,63 @@ void Engine::build_work_lists() {
     p0_mixed_smem_ = std::max(16 * 1024, ((need + 1023) / 1024) * 1024);
     GWGB_REQUIRE(p0_mixed_smem_ <= smem_bytes_, GWGB_E_UNSUPPORTED, "P0 block too large for the mixed kernel");
   }
-  {  // tcgen05 P0: Z tasks per (contribution, spin), K chunks of 32 complex columns, 128-row tiles
+  {  // tcgen05 P0: per aux block, Zcat[(tau,P)][K] and Vcat[Q][K] with K over (contribution, spin)
     std::vector<PzTask> zt;
-    std::vector<PtTile> ptt;
-    std::vector<PtChunk> chk;
-    int64_t zoff = 0;
+    std::vector<VcTask> vt;
+    std::vector<PkTile> kt;
+    std::vector<PrTile> rt;
+    int64_t zoff = 0, voff = 0, poff = 0;
     int zneed = 0;
-    for (const auto &g : p0_groups_) {  // (pout, pstride, qb, c0, c1)
+    const int SL = 8;  // K slice: 8 chunks of 16 complex columns
+    for (const auto &g : p0_groups_) {
       const int qb = g.qb;
-      const int k0 = (int)chk.size();
+      int kofs = 0;
+      std::vector<std::pair<int, int>> ent;  // (contribution, spin) -> zcol
+      for (int c = g.c0; c < g.c1; ++c)
+        for (int s = 0; s < ns_; ++s) {
+          ent.push_back({c, kofs});
+          kofs += pc[c].b1 * pc[c].b2;
+        }
+      const int zld = ((kofs + 15) / 16) * 16;
+      int ei = 0;
       for (int c = g.c0; c < g.c1; ++c) {
         const P0Contrib &cb = pc[c];
         const int b1b2 = cb.b1 * cb.b2;
-        for (int s = 0; s < ns_; ++s) {
-          zt.push_back({cb.v, cb.ga, cb.gb, zoff, cb.sa, cb.sb, cb.b1, cb.b2, qb, s});
-          for (int kc0 = 0; kc0 < b1b2; kc0 += 32) chk.push_back({zoff, cb.v, b1b2, kc0, std::min(32, b1b2 - kc0), 0});
-          zoff += (int64_t)half * qb * b1b2;
+        for (int s = 0; s < ns_; ++s, ++ei) {
+          const int zcol = ent[ei].second;
+          zt.push_back({cb.v, cb.ga, cb.gb, zoff, cb.sa, cb.sb, cb.b1, cb.b2, qb, s, zld, zcol});
+          vt.push_back({cb.v, voff, qb, b1b2, zld, zcol});
         }
         zneed = std::max(zneed, 8 * (cb.b2 * cb.b2 + cb.b1 * cb.b1 + 2 * b1b2 * qb));
         GWGB_REQUIRE(8 * (cb.b2 * cb.b2 + cb.b1 * cb.b1 + 2 * b1b2) <= smem_bytes_, GWGB_E_UNSUPPORTED,
                      "P0 block too large for the tcgen05 path");
       }
-      const int k1 = (int)chk.size();
+      const int nchunks = zld / 16;
+      const int nslice = std::max(1, (nchunks + SL - 1) / SL);
       const int nt = std::max(1, std::min(half, 128 / qb));
       const int NP = ((2 * qb + 15) / 16) * 16;
-      for (int t0 = 0; t0 < half; t0 += nt)
-        ptt.push_back({g.pout, g.pstride, qb, t0, std::min(nt, half - t0), k0, k1, NP, 0});
+      GWGB_REQUIRE(NP <= 128, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 P0 kernel");
+      for (int t0 = 0; t0 < half; t0 += nt) {
+        const int n = std::min(nt, half - t0);
+        const int64_t slice = (int64_t)n * qb * qb;
+        for (int sl = 0; sl < nslice; ++sl)
+          kt.push_back({zoff, voff, poff + sl * slice, zld, qb, t0, n, sl * SL, std::max(0, std::min(SL, nchunks - sl * SL)),
+                        NP, 0});
+        rt.push_back({poff, g.pout, g.pstride, qb, t0, n, nslice, 0});
+        poff += nslice * slice;
+      }
+      zoff += (int64_t)half * qb * zld;
+      voff += (int64_t)qb * zld;
     }
-    std::stable_sort(ptt.begin(), ptt.end(), [](const PtTile &a, const PtTile &b) { return (a.k1 - a.k0) > (b.k1 - b.k0); });
+    std::stable_sort(kt.begin(), kt.end(), [](const PkTile &a, const PkTile &b) { return a.kcn > b.kcn; });
     pz_tasks_.upload(zt, st_);
-    pt_tiles_.upload(ptt, st_);
-    pt_chunks_.upload(chk, st_);
+    vc_tasks_.upload(vt, st_);
+    pk_tiles_.upload(kt, st_);
+    pr_tiles_.upload(rt, st_);
     zbuf_elems_ = zoff;
+    vcat_elems_ = voff;
+    ppart_elems_ = poff;
     pz_smem_ = std::min(smem_bytes_, std::max(16 * 1024, ((zneed + 1023) / 1024) * 1024));
-    pt_smem_ = 512 * (128 + 128);
   }
 
   // --- Sigma tiles: owner = (k_irr, AO block i1, spin, tau range)
@@ -648,53 +692,36 @@ void Engine::build_work_lists() {
     sig_mixed_smem_ = std::max(16 * 1024, ((need + 1023) / 1024) * 1024);
     GWGB_REQUIRE(sig_mixed_smem_ <= smem_bytes_, GWGB_E_UNSUPPORTED, "Sigma block too large for the mixed kernel");
   }
-  {  // tcgen05 Sigma: group the contributions by aux block (q, iq)
-    std::vector<int64_t> woff(sc.size());
-    int64_t wtot = 0;
-    for (size_t c = 0; c < sc.size(); ++c) {
-      woff[c] = wtot;
-      wtot += (int64_t)nts_ * sc[c].qb * sig_b1_[c] * sc[c].b2;
-    }
+  {  // tcgen05 Sigma: per aux block (q, iq), Bcat = conj(V) columns, Wcat = W rows (tau, Q)
+    std::vector<WRef> wr(sc.size());
+    std::vector<BcTask> bt;
     std::vector<SwTile> swt;
-    std::vector<SwCol> swc;
+    int64_t woff = 0, boff = 0;
     int wsmem = 0, uvneed = 0;
     for (const auto &grp : sig_groups_) {
       const std::vector<int> &cs = grp.second;
       const int qb = sc[cs[0]].qb;
       const int64_t pa = sc[cs[0]].pq;
       const int pstride = sc[cs[0]].pstride;
-      const int KP = ((2 * qb + 7) / 8) * 8;
-      int ncap = std::min(256, ((200 * 1024 / (8 * KP) - 128) / 16) * 16);
-      GWGB_REQUIRE(ncap >= 16, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 Sigma kernel");
-      const int ccap = ncap / 2;  // complex columns per pack
-      const int nt = std::max(1, std::min(nts_, 128 / qb));
-      // column packs
-      struct Pack { int c0, c1, ncol; };
-      std::vector<Pack> packs;
-      Pack cur{(int)swc.size(), (int)swc.size(), 0};
+      int ncol = 0;
       for (int c : cs) {
-        const int b1 = sig_b1_[c], b2 = sc[c].b2, tot = b1 * b2;
-        int l = 0;
-        while (l < tot) {
-          if (cur.ncol == ccap) {
-            cur.c1 = (int)swc.size();
-            packs.push_back(cur);
-            cur = Pack{(int)swc.size(), (int)swc.size(), 0};
-          }
-          const int take = std::min(tot - l, ccap - cur.ncol);
-          swc.push_back({sc[c].v, woff[c], b1, b2, l, cur.ncol});
-          cur.ncol += take;
-          l += take;
-        }
+        const int b1b2 = sig_b1_[c] * sc[c].b2;
+        bt.push_back({sc[c].v, boff, qb, b1b2, ncol, 0});
+        wr[c] = {woff + ncol, 0};
+        ncol += b1b2;
       }
-      cur.c1 = (int)swc.size();
-      if (cur.ncol > 0) packs.push_back(cur);
-      for (const Pack &pk : packs) {
-        const int NP = ((2 * pk.ncol + 15) / 16) * 16;
-        wsmem = std::max(wsmem, 8 * KP * (128 + NP));
-        for (int t0 = 0; t0 < nts_; t0 += nt)
-          swt.push_back({pa, pstride, qb, t0, std::min(nt, nts_ - t0), pk.c0, pk.c1, pk.ncol, KP, NP, 0});
-      }
+      for (int c : cs) wr[c].ld = ncol;
+      const int KP = ((2 * qb + 7) / 8) * 8;
+      int npk = 64;
+      while (npk > 16 && KP * (1024 + 32 * npk) > 200 * 1024) npk /= 2;
+      GWGB_REQUIRE(KP * (1024 + 32 * npk) <= 200 * 1024, GWGB_E_UNSUPPORTED,
+                   "aux block too large for the tcgen05 Sigma kernel");
+      wsmem = std::max(wsmem, KP * (1024 + 32 * npk));
+      const int nt = std::max(1, std::min(nts_, 128 / qb));
+      for (int t0 = 0; t0 < nts_; t0 += nt)
+        swt.push_back({pa, boff, woff, pstride, qb, t0, std::min(nt, nts_ - t0), ncol, KP, npk, 0});
+      boff += (int64_t)ncol * qb;
+      woff += (int64_t)nts_ * qb * ncol;
     }
     for (const SigTile &t : stl) {
       int b2max = 1, qbmax = 1;
@@ -703,12 +730,14 @@ void Engine::build_work_lists() {
       GWGB_REQUIRE(24 * t.b1 * t.b1 + 8 * b2max * b2max + 24 * t.b1 * b2max <= smem_bytes_, GWGB_E_UNSUPPORTED,
                    "Sigma block too large for the tcgen05 path");
     }
+    std::stable_sort(swt.begin(), swt.end(), [](const SwTile &a, const SwTile &b) { return a.ncol > b.ncol; });
     sw_tiles_.upload(swt, st_);
-    sw_cols_.upload(swc, st_);
-    sig_woff_.upload(woff, st_);
+    bc_tasks_.upload(bt, st_);
+    sig_wref_.upload(wr, st_);
     sw_smem_ = std::max(16 * 1024, wsmem);
     uv_smem_ = std::min(smem_bytes_, std::max(16 * 1024, ((uvneed + 1023) / 1024) * 1024));
-    wbuf_elems_ = wtot;
+    wbuf_elems_ = woff;
+    bcat_elems_ = boff;
   }
 
   // --- transforms and block inverses
@@ -773,6 +802,8 @@ void Engine::upload_V(const double *V, int64_t n) {
   h2d(V_.p, V, (size_t)n * sizeof(double2), st_);
   GWGB_CUDA(cudaStreamSynchronize(st_));
   have_V_ = true;
+  vcat_ready_ = false;
+  build_vcat();
 }
 
 void Engine::set_reps(const double *orep, int64_t no, const double *auxrep, int64_t na) {
@@ -849,9 +880,10 @@ void Engine::k_rotate_G() {
 void Engine::k_p0(int mirror) {
   const double pref = -1.0 / l_.nk * (ns_ == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
   if (prec_ == GWGB_PREC_TF32X3) {
-    GWGB_REQUIRE(Zbuf_.p || !zbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
-    launch_p0_tc(pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pt_tiles_.p, (int)pt_tiles_.n, pt_smem_, pt_chunks_.p,
-                 V_.p, Gall_.p, Zbuf_.p, Pall_.p, ns_, nts_, pref, mirror, 4, bad_.p + 2, st_);
+    GWGB_REQUIRE((Zbuf_.p || !zbuf_elems_) && vcat_ready_, GWGB_E_STATE, "mixed-precision work buffers missing");
+    launch_p0_tc(pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pk_tiles_.p, (int)pk_tiles_.n, pr_tiles_.p,
+                 (int)pr_tiles_.n, V_.p, Gall_.p, Zbuf_.p, Vcat_.p, Ppart_.p, Pall_.p, ns_, nts_, pref, mirror,
+                 bad_.p + 2, st_);
   } else
     launch_p0_fp64(p0_tiles_.p, (int)p0_tiles_.n, p0_maxo_, p0_contribs_.p, V_.p, Gall_.p, Pall_.p, ns_, nts_, pref,
                    mirror, smem_bytes_, st_);
@@ -871,8 +903,8 @@ void Engine::k_rotate_P() {
 void Engine::k_sigma() {
   if (prec_ == GWGB_PREC_TF32X3) {
     GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
-    launch_sigma_tc(sw_tiles_.p, (int)sw_tiles_.n, sw_smem_, sw_cols_.p, sig_tiles1_.p, (int)sig_tiles1_.n,
-                    sig_contribs_.p, sig_woff_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p, Sig_.p, ns_, -1.0 / l_.nk, uv_smem_,
+    launch_sigma_tc(sw_tiles_.p, (int)sw_tiles_.n, sw_smem_, Bcat_.p, sig_tiles1_.p, (int)sig_tiles1_.n,
+                    sig_contribs_.p, sig_wref_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p, Sig_.p, ns_, -1.0 / l_.nk, uv_smem_,
                     bad_.p + 2, st_);
   } else
     launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Sig_.p,

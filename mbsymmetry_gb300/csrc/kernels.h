@@ -8,11 +8,15 @@ namespace gwgb {
 // Largest irrep block (AO or aux) the FP64 kernels accept.
 constexpr int MAX_BLOCK = 64;
 
+// Block inverses: one warp per block; as many warps per CTA as fit in ~48 KB
+// of shared memory (2 n^2 complex + 3 n ints per warp), 1 to 8.
+__host__ __device__ constexpr int inv_bytes_per_warp(int nmax) { return 2 * nmax * nmax * 16 + 3 * nmax * 4; }
 __host__ __device__ constexpr int inv_warps_per_block(int nmax) {
-  return nmax <= 16 ? 4 : (nmax <= 32 ? 2 : 1);
+  return (48 * 1024) / inv_bytes_per_warp(nmax) < 1 ? 1
+         : ((48 * 1024) / inv_bytes_per_warp(nmax) > 8 ? 8 : (48 * 1024) / inv_bytes_per_warp(nmax));
 }
 __host__ __device__ constexpr int inv_smem_bytes(int nmax) {
-  return inv_warps_per_block(nmax) * (2 * nmax * nmax * 16 + 3 * nmax * 4);
+  return inv_warps_per_block(nmax) * inv_bytes_per_warp(nmax);
 }
 __host__ __device__ constexpr int rotate_smem_bytes(int nmax) { return 3 * nmax * nmax * 16; }
 

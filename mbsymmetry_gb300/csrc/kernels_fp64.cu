@@ -343,19 +343,20 @@ __global__ void __launch_bounds__(256) transform_kernel(const TSlab *__restrict_
 //   mode 1 (Dyson, sc_type_block.cpp:48-57):
 //     A = (i w_n + mu) S - F - Sigma(i w_n) ; G = A^-1   (in place)
 // ---------------------------------------------------------------------------
-template <int NMAX>
+// nm = largest block of the launch; every warp of the CTA owns 2*nm^2 complex
+// and 3*nm ints of shared memory.
 __global__ void inverse_kernel(const InvTask *__restrict__ tasks, int ntasks, double2 *__restrict__ W,
                                const double2 *__restrict__ S, const double2 *__restrict__ F,
                                const int64_t *__restrict__ wsample, double beta, double mu, int mode,
-                               int *__restrict__ bad) {
-  constexpr int WPB = inv_warps_per_block(NMAX);
+                               int *__restrict__ bad, int nm) {
+  const int WPB = blockDim.x >> 5;
   extern __shared__ double2 smem_inv[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double2 *A = smem_inv + (size_t)warp * 2 * NMAX * NMAX;
-  double2 *B = A + NMAX * NMAX;
-  int *ipiv = reinterpret_cast<int *>(smem_inv + (size_t)WPB * 2 * NMAX * NMAX) + warp * 3 * NMAX;
-  int *indxr = ipiv + NMAX;
-  int *indxc = indxr + NMAX;
+  double2 *A = smem_inv + (size_t)warp * 2 * nm * nm;
+  double2 *B = A + nm * nm;
+  int *ipiv = reinterpret_cast<int *>(smem_inv + (size_t)WPB * 2 * nm * nm) + warp * 3 * nm;
+  int *indxr = ipiv + nm;
+  int *indxc = indxr + nm;
   const int ti = blockIdx.x * WPB + warp;
   if (ti >= ntasks) return;
   const InvTask tk = tasks[ti];
@@ -551,19 +552,10 @@ void launch_inverse(const InvTask *tasks, int ntasks, int nmax, double2 *W, cons
                     const double2 *F, const int64_t *wsample, double beta, double mu, int mode, int *bad,
                     cudaStream_t st) {
   if (ntasks == 0) return;
-  if (nmax <= 16) {
-    constexpr int w = inv_warps_per_block(16);
-    inverse_kernel<16><<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(16), st>>>(tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad);
+  const int w = inv_warps_per_block(nmax);
+  inverse_kernel<<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(nmax), st>>>(tasks, ntasks, W, S, F, wsample,
+                                                                           beta, mu, mode, bad, nmax);
   GWGB_CUDA(cudaGetLastError());
-  } else if (nmax <= 32) {
-    constexpr int w = inv_warps_per_block(32);
-    inverse_kernel<32><<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(32), st>>>(tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad);
-  GWGB_CUDA(cudaGetLastError());
-  } else {
-    constexpr int w = inv_warps_per_block(64);
-    inverse_kernel<64><<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(64), st>>>(tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad);
-  GWGB_CUDA(cudaGetLastError());
-  }
 }
 
 void launch_leakage(const TSlab *slabs, int nslabs, const double2 *G, const double *tf, const double *tl,
@@ -580,9 +572,7 @@ void set_fp64_kernel_attributes(int smem_bytes) {
   GWGB_CUDA(cudaFuncSetAttribute(sigma_fp64_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(rotate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rotate_smem_bytes(MAX_BLOCK)));
   GWGB_CUDA(cudaFuncSetAttribute(transform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * TR_MAXR * 33 * (int)sizeof(double2)));
-  GWGB_CUDA(cudaFuncSetAttribute(inverse_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, inv_smem_bytes(16)));
-  GWGB_CUDA(cudaFuncSetAttribute(inverse_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, inv_smem_bytes(32)));
-  GWGB_CUDA(cudaFuncSetAttribute(inverse_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, inv_smem_bytes(64)));
+  GWGB_CUDA(cudaFuncSetAttribute(inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, inv_smem_bytes(MAX_BLOCK)));
 }
 
 }  // namespace gwgb

@@ -32,111 +32,140 @@ __device__ __forceinline__ void split_store(float *hi, float *lo, uint32_t off, 
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// (1): one CTA = one 128-row tile (tau, Q) x one column pack of contributions.
-// Shared memory: A_hi | A_lo (128 x KP) | B_hi | B_lo (NP x KP), KP = pad8(2 qb),
-// NP = pad16(2 * ncol).  Accumulator: TMEM, 128 lanes x NP columns.
+// (1): one CTA = 128 rows (tau, Q) of one aux block x all its columns.  A is
+// staged once; B packs of 64 complex columns are double-buffered against two
+// TMEM accumulators (MMA of pack i+1 overlaps the drain of pack i).
+// Shared: A_hi | A_lo (128 x KP) | B0_hi | B0_lo | B1_hi | B1_lo (128 x KP).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) sigma_w_tc_kernel(const SwTile *__restrict__ tiles,
-                                                         const SwCol *__restrict__ cols,
-                                                         const double2 *__restrict__ V,
+__global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restrict__ tiles,
+                                                         const float2 *__restrict__ Bcat,
                                                          const double2 *__restrict__ P, float2 *__restrict__ W,
                                                          int *__restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ uint32_t tmem_slot;
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar[2];
   const SwTile tl = tiles[blockIdx.x];
-  const int qb = tl.qb;
-  const int KP = tl.kp, NP = tl.np;
+  const int qb = tl.qb, KP = tl.kp;
+  const int SW_PACK = tl.npk, BR = 2 * tl.npk;  // complex columns per pack, B rows per pack
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   float *Ahi = reinterpret_cast<float *>(smem_raw);
   float *Alo = Ahi + 128 * KP;
-  float *Bhi = Alo + 128 * KP;
-  float *Blo = Bhi + NP * KP;
-  uint32_t ncols_alloc = 32;
-  while ((int)ncols_alloc < NP) ncols_alloc <<= 1;
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols_alloc);
-  if (tid == 0) tc::mbar_init(&mbar, 1);
-
-  // A: rows (tau, Q) of P(tau), K = (P, re/im)
+  float *Bb = Alo + 128 * KP;  // 2 buffers x (hi, lo) x BR x KP
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 256);
+  if (tid == 0) {
+    tc::mbar_init(&mbar[0], 1);
+    tc::mbar_init(&mbar[1], 1);
+  }
   const int rows = tl.nt * qb;
-  for (int e = tid; e < 128 * KP; e += blockDim.x) {
-    const int r = e / KP, k = e - r * KP;
-    const int kc = k >> 1;
-    float x = 0.f;
+  // A: rows (tau, Q) of P(tau), K = (P, re/im); every row is qb contiguous complex
+  for (int e = tid; e < 128 * (KP / 2); e += 256) {
+    const int r = e / (KP / 2), kc = e - r * (KP / 2);
+    double2 v = make_double2(0.0, 0.0);
     if (r < rows && kc < qb) {
       const int it = r / qb, Q = r - it * qb;
-      const double2 v = __ldg(P + tl.pa + (int64_t)(tl.t0 + it) * tl.pstride + (int64_t)Q * qb + kc);
-      x = (float)((k & 1) ? v.y : v.x);
+      v = __ldg(P + tl.pa + (int64_t)(tl.t0 + it) * tl.pstride + (int64_t)Q * qb + kc);
     }
-    split_store(Ahi, Alo, tc::kmajor_offset(r, k, KP), x);
+    split_store(Ahi, Alo, tc::kmajor_offset(r, 2 * kc, KP), (float)v.x);
+    split_store(Ahi, Alo, tc::kmajor_offset(r, 2 * kc + 1, KP), (float)v.y);
   }
-  // B: rows (col, d) of the real embedding of conj(V_c[P][j][n]), K = (P, c)
-  for (int e = tid; e < NP * KP; e += blockDim.x) {
-    const int n = e / KP, k = e - n * KP;
-    const int col = n >> 1, d = n & 1, kc = k >> 1, cpart = k & 1;
-    float x = 0.f;
-    if (col < tl.ncol && kc < qb) {
-      int ci = tl.c0;
-      while (ci + 1 < tl.c1 && cols[ci + 1].col0 <= col) ++ci;
-      const SwCol cc = cols[ci];
-      const int lc = col - cc.col0 + cc.l0;
-      const int jj = lc / cc.b2, nn = lc - jj * cc.b2;
-      const double2 v = __ldg(V + cc.v + ((int64_t)kc * cc.b1 + jj) * cc.b2 + nn);
-      // [[Br, Bi], [-Bi, Br]] with B = conj(v): Br = v.x, Bi = -v.y
-      x = (float)(d == 0 ? (cpart == 0 ? v.x : v.y) : (cpart == 0 ? -v.y : v.x));
+  const int npacks = (tl.ncol + SW_PACK - 1) / SW_PACK;
+  auto stage_b = [&](int pk) {
+    float *hi = Bb + (pk & 1) * 2 * BR * KP;
+    float *lo = hi + BR * KP;
+    const int c0 = pk * SW_PACK;
+    // rows (col, d) of the real embedding of B = conj(V): d=0 -> (Br, -Bi), d=1 -> (Bi, Br), Br = Vr, Bi = -Vi
+    for (int e = tid; e < SW_PACK * (KP / 2); e += 256) {
+      const int cl = e / (KP / 2), kc = e - cl * (KP / 2);
+      const int col = c0 + cl;
+      float2 b = make_float2(0.f, 0.f);  // b = conj(V) as stored
+      if (col < tl.ncol && kc < qb) b = Bcat[tl.bcat + (int64_t)col * qb + kc];
+      split_store(hi, lo, tc::kmajor_offset(2 * cl, 2 * kc, KP), b.x);
+      split_store(hi, lo, tc::kmajor_offset(2 * cl, 2 * kc + 1, KP), -b.y);
+      split_store(hi, lo, tc::kmajor_offset(2 * cl + 1, 2 * kc, KP), b.y);
+      split_store(hi, lo, tc::kmajor_offset(2 * cl + 1, 2 * kc + 1, KP), b.x);
     }
-    split_store(Bhi, Blo, tc::kmajor_offset(n, k, KP), x);
-  }
+  };
+  const uint32_t idesc = tc::idesc_tf32(128, 2 * SW_PACK);
+  const uint32_t sbo = (uint32_t)(KP / 4) * 128;
+  auto issue = [&](int pk, uint32_t tmem) {
+    const uint32_t a_hi = tc::smem_u32(Ahi), a_lo = tc::smem_u32(Alo);
+    const uint32_t b_hi = tc::smem_u32(Bb + (pk & 1) * 2 * BR * KP), b_lo = b_hi + BR * KP * 4;
+    const uint32_t d = tmem + (uint32_t)((pk & 1) * 2 * SW_PACK);
+    for (int s = 0; s < KP / 8; ++s) {
+      const uint32_t off = (uint32_t)s * 256;
+      tc::mma_tf32(d, tc::make_desc(a_lo + off, 128, sbo), tc::make_desc(b_hi + off, 128, sbo), idesc, s > 0);
+      tc::mma_tf32(d, tc::make_desc(a_hi + off, 128, sbo), tc::make_desc(b_lo + off, 128, sbo), idesc, 1);
+      tc::mma_tf32(d, tc::make_desc(a_hi + off, 128, sbo), tc::make_desc(b_hi + off, 128, sbo), idesc, 1);
+    }
+    tc::commit(&mbar[pk & 1]);
+  };
+  if (npacks > 0) stage_b(0);
   tc::fence_async_smem();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
-  if (tid == 0) {
-    const uint32_t idesc = tc::idesc_tf32(128, NP);
-    const uint32_t sboA = (uint32_t)(KP / 4) * 128, sboB = sboA;
-    const uint32_t a_hi = tc::smem_u32(Ahi), a_lo = tc::smem_u32(Alo);
-    const uint32_t b_hi = tc::smem_u32(Bhi), b_lo = tc::smem_u32(Blo);
-    for (int s = 0; s < KP / 8; ++s) {
-      const uint32_t off = (uint32_t)s * 256;
-      tc::mma_tf32(tmem, tc::make_desc(a_lo + off, 128, sboA), tc::make_desc(b_hi + off, 128, sboB), idesc, s > 0);
-      tc::mma_tf32(tmem, tc::make_desc(a_hi + off, 128, sboA), tc::make_desc(b_lo + off, 128, sboB), idesc, 1);
-      tc::mma_tf32(tmem, tc::make_desc(a_hi + off, 128, sboA), tc::make_desc(b_hi + off, 128, sboB), idesc, 1);
-    }
-    tc::commit(&mbar);
-  }
-  bool ok = tc::mbar_wait(&mbar, 0);
-  if (!ok && lane == 0) atomicExch(err, 1);
-  ok = __syncthreads_and(ok);
-  tc::fence_after_sync();
-  if (ok) {
-    // drain: lane r of warp w holds row 32w + lane
-    const int r = warp * 32 + lane;
-    const bool live = r < rows;
-    const int it = live ? r / qb : 0, Q = live ? r - (r / qb) * qb : 0;
-    const int tau = tl.t0 + it;
-    for (int c0 = 0; c0 < NP; c0 += 8) {
-      float v[8];
-      tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (live) {
+  if (tid == 0 && npacks > 0) issue(0, tmem);
+  uint32_t ph[2] = {0u, 0u};
+  bool ok = true;
+  const int r = (warp & 3) * 32 + lane;  // warps 0-3 drain (TMEM lanes), warps 4-7 only stage
+  const bool live = warp < 4 && r < rows;
+  const int it = live ? r / qb : 0, Q = live ? r - (r / qb) * qb : 0;
+  float2 *wrow = W + tl.wcat + ((int64_t)(tl.t0 + it) * qb + Q) * tl.ncol;
+  for (int pk = 0; pk < npacks && ok; ++pk) {
+    if (pk + 1 < npacks) stage_b(pk + 1);  // buffer (pk+1)&1 was read by MMA pk-1, already complete
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0 && pk + 1 < npacks) issue(pk + 1, tmem);
+    bool done = tc::mbar_wait(&mbar[pk & 1], ph[pk & 1]);
+    if (done) ph[pk & 1] ^= 1u;  // a phase that timed out is waited for again below
+    if (!done && lane == 0) atomicExch(err, 1);
+    ok = __syncthreads_and(done);
+    tc::fence_after_sync();
+    if (ok && warp < 4) {
+      const uint32_t acc = tmem + (uint32_t)((pk & 1) * 2 * SW_PACK) + ((uint32_t)(warp * 32) << 16);
+      const int c0 = pk * SW_PACK;
+      for (int j0 = 0; j0 < 2 * SW_PACK; j0 += 8) {
+        float v[8];
+        tc::tmem_ld8(acc + (uint32_t)j0, v);
+        if (live) {
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) {
-          const int col = (c0 + j) >> 1;
-          if (col < tl.ncol) {
-            int ci = tl.c0;
-            while (ci + 1 < tl.c1 && cols[ci + 1].col0 <= col) ++ci;
-            const SwCol cc = cols[ci];
-            const int lc = col - cc.col0 + cc.l0;
-            const int jj = lc / cc.b2, nn = lc - jj * cc.b2;
-            W[cc.w + (((int64_t)tau * qb + Q) * cc.b1 + jj) * cc.b2 + nn] = make_float2(v[j], v[j + 1]);
+          for (int j = 0; j < 8; j += 2) {
+            const int col = c0 + ((j0 + j) >> 1);
+            if (col < tl.ncol) wrow[col] = make_float2(v[j], v[j + 1]);
           }
         }
       }
     }
+    tc::fence_before_sync();
+    __syncthreads();  // accumulator pk&1 drained before MMA pk+2 reuses it
+    tc::fence_after_sync();
+  }
+  if (!ok) {  // let MMAs still in flight finish before the TMEM is released (bounded)
+    if (npacks > 0) tc::mbar_wait(&mbar[0], ph[0], 100000);
+    if (npacks > 1) tc::mbar_wait(&mbar[1], ph[1], 100000);
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, ncols_alloc);
+  if (warp == 0) tc::tmem_dealloc(tmem, 256);
+}
+
+// Bcat[col0 + (j*b2 + n)][P] = conj(V_c[P][j][n]) (FP32), once per V upload.
+__global__ void bcat_kernel(const BcTask *__restrict__ tasks, const double2 *__restrict__ V, float2 *__restrict__ Bcat) {
+  const BcTask tk = tasks[blockIdx.x];
+  for (int e = threadIdx.x; e < tk.qb * tk.b1b2; e += blockDim.x) {
+    const int P = e / tk.b1b2, jn = e - P * tk.b1b2;
+    const double2 v = __ldg(V + tk.v + e);
+    Bcat[tk.bcat + (int64_t)(tk.col0 + jn) * tk.qb + P] = make_float2((float)v.x, -(float)v.y);
+  }
+}
+
+void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat, cudaStream_t st) {
+  if (ntasks == 0) return;
+  bcat_kernel<<<ntasks, 256, 0, st>>>(tasks, V, Bcat);
+  GWGB_CUDA(cudaGetLastError());
 }
 
 // ---------------------------------------------------------------------------
@@ -146,7 +175,7 @@ __global__ void __launch_bounds__(128) sigma_w_tc_kernel(const SwTile *__restric
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) sigma_uv_kernel(const SigTile *__restrict__ tiles,
                                                        const SigContrib *__restrict__ contribs,
-                                                       const int64_t *__restrict__ woff,
+                                                       const WRef *__restrict__ wref,
                                                        const double2 *__restrict__ V,
                                                        const double2 *__restrict__ G, const float2 *__restrict__ W,
                                                        double2 *__restrict__ Sig, int ns, double scale,
@@ -171,7 +200,8 @@ __global__ void __launch_bounds__(128) sigma_uv_kernel(const SigTile *__restrict
     float2 *Us = Ws + QC * blk;
     const double2 *Vb = V + cb.v;
     const double2 *G2 = G + cb.gb + ((int64_t)tau * ns + s) * cb.sb;
-    const float2 *Wt = W + woff[c] + (int64_t)tau * qb * blk;
+    const WRef wr = wref[c];
+    const float2 *Wt = W + wr.base + (int64_t)tau * qb * wr.ld;
     __syncthreads();
     for (int e = threadIdx.x; e < b2 * b2; e += blockDim.x) {
       const double2 g = __ldg(G2 + e);
@@ -184,7 +214,8 @@ __global__ void __launch_bounds__(128) sigma_uv_kernel(const SigTile *__restrict
       for (int e = threadIdx.x; e < qn * blk; e += blockDim.x) {
         const double2 v = __ldg(Vb + (int64_t)q0 * blk + e);
         Vs[e] = make_float2((float)v.x, (float)v.y);
-        Ws[e] = Wt[(int64_t)q0 * blk + e];
+        const int Qr = e / blk, jn = e - Qr * blk;
+        Ws[e] = Wt[(int64_t)(q0 + Qr) * wr.ld + jn];
       }
       __syncthreads();
       // U[Q][j][m] = sum_n W[Q][j][n] G2[m][n]
@@ -231,16 +262,16 @@ __global__ void __launch_bounds__(128) sigma_uv_kernel(const SigTile *__restrict
     Sig[tile.sig + (int64_t)tau * tile.sstride + e] = make_double2(acc64[e].x * scale, acc64[e].y * scale);
 }
 
-void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const SwCol *wcols, const SigTile *tiles1,
-                     int ntiles1, const SigContrib *contribs, const int64_t *woff, const double2 *V,
+void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
+                     int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
                      const double2 *G, const double2 *P, float2 *W, double2 *Sig, int ns, double scale,
                      int uv_smem, int *err, cudaStream_t st) {
   if (nwtiles > 0) {
-    sigma_w_tc_kernel<<<nwtiles, 128, wsmem, st>>>(wtiles, wcols, V, P, W, err);
+    sigma_w_tc_kernel<<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, err);
     GWGB_CUDA(cudaGetLastError());
   }
   if (ntiles1 > 0) {
-    sigma_uv_kernel<<<ntiles1, 128, uv_smem, st>>>(tiles1, contribs, woff, V, G, W, Sig, ns, scale, uv_smem);
+    sigma_uv_kernel<<<ntiles1, 128, uv_smem, st>>>(tiles1, contribs, wref, V, G, W, Sig, ns, scale, uv_smem);
     GWGB_CUDA(cudaGetLastError());
   }
 }
@@ -315,8 +346,8 @@ __global__ void __launch_bounds__(128) p0_z_kernel(const PzTask *__restrict__ ta
         X2[e] = make_float2(xr, xi);
       }
       __syncthreads();
-      // Z[P][(p,m)] = sum_t Gm[t][p] X2[P][t][m]
-      float2 *Zt = Z + tk.z + ((int64_t)tau * qb + p0) * blk;
+      // Z[P][(p,m)] = sum_t Gm[t][p] X2[P][t][m]   -> Zcat row (tau, p0 + P), columns zcol + pm
+      float2 *Zt = Z + tk.z + ((int64_t)tau * qb + p0) * tk.zld + tk.zcol;
       for (int e = threadIdx.x; e < pn * blk; e += blockDim.x) {
         const int P = e / blk, pm = e - P * blk;
         const int p = pm / b2, m = pm - p * b2;
@@ -329,25 +360,25 @@ __global__ void __launch_bounds__(128) p0_z_kernel(const PzTask *__restrict__ ta
           zi = fmaf(g.x, xv.y, zi);
           zi = fmaf(g.y, xv.x, zi);
         }
-        Zt[e] = make_float2(zr, zi);
+        Zt[(int64_t)P * tk.zld + pm] = make_float2(zr, zi);
       }
     }
   }
 }
 
-// tcgen05 stage: D[(tau,P)][Q] = sum_chunks Z[(tau,P)][k] V[Q][k]; TMEM FP32,
-// drained every `drain_every` chunks into the FP64 output (owned by this CTA).
-// Shared: A_hi | A_lo (128 x 64) | B_hi | B_lo (NP x 64), 32-bit elements.
-__global__ void __launch_bounds__(128) p0_tc_kernel(const PtTile *__restrict__ tiles,
-                                                    const PtChunk *__restrict__ chunks,
-                                                    const double2 *__restrict__ V, const float2 *__restrict__ Z,
-                                                    double2 *__restrict__ P0, int nts, double pref, int mirror,
-                                                    int drain_every, int *__restrict__ err) {
-  constexpr int KP = 64;  // real K per chunk (32 complex)
+// tcgen05 stage, split-K: D[(tau,P)][Q] = sum_k Zcat[(tau,P)][k] Vcat[Q][k] over
+// this CTA's K slice (chunks of 16 complex = 32 real columns), FP32 in TMEM,
+// then FP64 partial sums to Ppart.  256 threads stage the operands (8 loads in
+// flight per thread); warps 0-3 drain TMEM lanes 0-127.
+// Shared: A_hi | A_lo (128 x 32) | B_hi | B_lo (NP x 32), 32-bit elements: 64 KB at NP = 128.
+__global__ void __launch_bounds__(256) p0_tc_kernel(const PkTile *__restrict__ tiles,
+                                                    const float2 *__restrict__ Z, const float2 *__restrict__ Vcat,
+                                                    double2 *__restrict__ Ppart, int *__restrict__ err) {
+  constexpr int KP = 32;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ uint32_t tmem_slot;
   __shared__ __align__(8) uint64_t mbar;
-  const PtTile tl = tiles[blockIdx.x];
+  const PkTile tl = tiles[blockIdx.x];
   const int qb = tl.qb, NP = tl.np;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   float *Ahi = reinterpret_cast<float *>(smem_raw);
@@ -363,37 +394,29 @@ __global__ void __launch_bounds__(128) p0_tc_kernel(const PtTile *__restrict__ t
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
   const int rows = tl.nt * qb;
-  const int r = warp * 32 + lane;
-  const bool live = r < rows;
-  const int it = live ? r / qb : 0, Prow = live ? r - (r / qb) * qb : 0;
-  const int tau = tl.t0 + it;
+  const float2 *Zb = Z + tl.z + (int64_t)tl.t0 * qb * tl.zld;
+  const float2 *Vb = Vcat + tl.vc;
   bool ok = true;
-  int since_drain = 0, ndrain = 0;
   uint32_t phase = 0;
-  for (int ch = tl.k0; ch < tl.k1 && ok; ++ch) {
-    const PtChunk cc = chunks[ch];
-    // stage A: Z rows (tau, P), K = (pm, re/im)
-    for (int e = tid; e < 128 * KP; e += blockDim.x) {
-      const int rr = e / KP, k = e - rr * KP;
-      const int kc = k >> 1;
-      float x = 0.f;
-      if (rr < rows && kc < cc.kn) {
-        const int i2 = rr / qb, P = rr - i2 * qb;
-        const float2 z = Z[cc.z + ((int64_t)(tl.t0 + i2) * qb + P) * cc.b1b2 + cc.kc0 + kc];
-        x = (k & 1) ? z.y : z.x;
-      }
-      split_store(Ahi, Alo, tc::kmajor_offset(rr, k, KP), x);
+  for (int ch = 0; ch < tl.kcn && ok; ++ch) {
+    const int kbase = (tl.kc0 + ch) * 16;
+    // A: 128 rows x 16 complex, row r = (tau, P); zero rows beyond `rows`
+#pragma unroll 4
+    for (int e = tid; e < 128 * 16; e += 256) {
+      const int r = e >> 4, kk = e & 15;
+      const float2 z = r < rows ? Zb[(int64_t)r * tl.zld + kbase + kk] : make_float2(0.f, 0.f);
+      split_store(Ahi, Alo, tc::kmajor_offset(r, 2 * kk, KP), z.x);
+      split_store(Ahi, Alo, tc::kmajor_offset(r, 2 * kk + 1, KP), z.y);
     }
-    // stage B: rows (Q, d) of the real embedding of V^T (B[k][Q] = V[Q][k]): d=0 -> (Vr, -Vi), d=1 -> (Vi, Vr)
-    for (int e = tid; e < NP * KP; e += blockDim.x) {
-      const int n = e / KP, k = e - n * KP;
-      const int Q = n >> 1, d = n & 1, kc = k >> 1, cp = k & 1;
-      float x = 0.f;
-      if (Q < qb && kc < cc.kn) {
-        const double2 v = __ldg(V + cc.v + (int64_t)Q * cc.b1b2 + cc.kc0 + kc);
-        x = (float)(d == 0 ? (cp == 0 ? v.x : -v.y) : (cp == 0 ? v.y : v.x));
-      }
-      split_store(Bhi, Blo, tc::kmajor_offset(n, k, KP), x);
+    // B: rows (Q, d) of the real embedding of V^T: d=0 -> (Vr, -Vi), d=1 -> (Vi, Vr)
+#pragma unroll 2
+    for (int e = tid; e < (NP / 2) * 16; e += 256) {
+      const int Q = e >> 4, kk = e & 15;
+      const float2 v = Q < qb ? Vb[(int64_t)Q * tl.zld + kbase + kk] : make_float2(0.f, 0.f);
+      split_store(Bhi, Blo, tc::kmajor_offset(2 * Q, 2 * kk, KP), v.x);
+      split_store(Bhi, Blo, tc::kmajor_offset(2 * Q, 2 * kk + 1, KP), -v.y);
+      split_store(Bhi, Blo, tc::kmajor_offset(2 * Q + 1, 2 * kk, KP), v.y);
+      split_store(Bhi, Blo, tc::kmajor_offset(2 * Q + 1, 2 * kk + 1, KP), v.x);
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
@@ -404,11 +427,11 @@ __global__ void __launch_bounds__(128) p0_tc_kernel(const PtTile *__restrict__ t
       const uint32_t sbo = (uint32_t)(KP / 4) * 128;
       const uint32_t a_hi = tc::smem_u32(Ahi), a_lo = tc::smem_u32(Alo);
       const uint32_t b_hi = tc::smem_u32(Bhi), b_lo = tc::smem_u32(Blo);
-      const int ksteps = (2 * cc.kn + 7) / 8;
-      for (int s = 0; s < ksteps; ++s) {
+#pragma unroll
+      for (int s = 0; s < KP / 8; ++s) {
         const uint32_t off = (uint32_t)s * 256;
         tc::mma_tf32(tmem, tc::make_desc(a_lo + off, 128, sbo), tc::make_desc(b_hi + off, 128, sbo), idesc,
-                     (since_drain > 0 || s > 0) ? 1u : 0u);
+                     (ch > 0 || s > 0) ? 1u : 0u);
         tc::mma_tf32(tmem, tc::make_desc(a_hi + off, 128, sbo), tc::make_desc(b_lo + off, 128, sbo), idesc, 1);
         tc::mma_tf32(tmem, tc::make_desc(a_hi + off, 128, sbo), tc::make_desc(b_hi + off, 128, sbo), idesc, 1);
       }
@@ -419,38 +442,21 @@ __global__ void __launch_bounds__(128) p0_tc_kernel(const PtTile *__restrict__ t
     if (!ok && lane == 0) atomicExch(err, 1);
     ok = __syncthreads_and(ok);
     tc::fence_after_sync();
-    ++since_drain;
-    const bool last = (ch + 1 == tl.k1);
-    if (ok && (since_drain >= drain_every || last)) {
-      for (int c0 = 0; c0 < NP; c0 += 8) {
-        float v[8];
-        tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-        if (live) {
+  }
+  if (warp < 4) {
+    const int r = warp * 32 + lane;
+    for (int c0 = 0; c0 < NP; c0 += 8) {
+      float v[8];
+      tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (r < rows) {
 #pragma unroll
-          for (int j = 0; j < 8; j += 2) {
-            const int Q = (c0 + j) >> 1;
-            if (Q < qb) {
-              double2 *o = P0 + tl.pout + (int64_t)tau * tl.pstride + (int64_t)Q * qb + Prow;
-              const double2 prev = ndrain ? *o : make_double2(0.0, 0.0);
-              *o = make_double2(prev.x + (double)v[j], prev.y + (double)v[j + 1]);
-            }
-          }
+        for (int j = 0; j < 8; j += 2) {
+          const int Q = (c0 + j) >> 1;
+          if (Q < qb)
+            Ppart[tl.part + (int64_t)r * qb + Q] =
+                (ok && tl.kcn > 0) ? make_double2((double)v[j], (double)v[j + 1]) : make_double2(0.0, 0.0);
         }
       }
-      since_drain = 0;
-      ++ndrain;
-    }
-    tc::fence_before_sync();
-    __syncthreads();  // operands and TMEM are free for the next chunk
-    tc::fence_after_sync();
-  }
-  // prefactor, tau mirror; blocks of a tile without contributions are zero
-  if (live) {
-    for (int Q = 0; Q < qb; ++Q) {
-      double2 *o = P0 + tl.pout + (int64_t)tau * tl.pstride + (int64_t)Q * qb + Prow;
-      const double2 v = (ndrain && ok) ? make_double2(o->x * pref, o->y * pref) : make_double2(0.0, 0.0);
-      *o = v;
-      if (mirror) P0[tl.pout + (int64_t)(nts - 1 - tau) * tl.pstride + (int64_t)Q * qb + Prow] = v;
     }
   }
   tc::fence_before_sync();
@@ -458,22 +464,64 @@ __global__ void __launch_bounds__(128) p0_tc_kernel(const PtTile *__restrict__ t
   if (warp == 0) tc::tmem_dealloc(tmem, ncols_alloc);
 }
 
-void launch_p0_tc(const PzTask *ztasks, int nz, int zsmem, const PtTile *ptiles, int npt, int psmem,
-                  const PtChunk *chunks, const double2 *V, const double2 *G, float2 *Z, double2 *P0, int ns,
-                  int nts, double pref, int mirror, int drain_every, int *err, cudaStream_t st) {
+// Sum the K slices in order, apply the prefactor and write P0 (and its mirror).
+__global__ void p0_reduce_kernel(const PrTile *__restrict__ tiles, const double2 *__restrict__ Ppart,
+                                 double2 *__restrict__ P0, int nts, double pref, int mirror) {
+  const PrTile tl = tiles[blockIdx.x];
+  const int qb = tl.qb, rows = tl.nt * qb;
+  const int64_t slice = (int64_t)rows * qb;
+  for (int e = threadIdx.x; e < rows * qb; e += blockDim.x) {
+    const int r = e / qb, Q = e - r * qb;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int sl = 0; sl < tl.nslice; ++sl) {
+      const double2 v = Ppart[tl.part + sl * slice + e];
+      acc.x += v.x;
+      acc.y += v.y;
+    }
+    const int it = r / qb, P = r - it * qb;
+    const int tau = tl.t0 + it;
+    const double2 o = make_double2(acc.x * pref, acc.y * pref);
+    P0[tl.pout + (int64_t)tau * tl.pstride + (int64_t)Q * qb + P] = o;
+    if (mirror) P0[tl.pout + (int64_t)(nts - 1 - tau) * tl.pstride + (int64_t)Q * qb + P] = o;
+  }
+}
+
+// Vcat[Q][zcol + pm] = V_c[Q][pm] (FP32), once per V upload.
+__global__ void vcat_kernel(const VcTask *__restrict__ tasks, const double2 *__restrict__ V, float2 *__restrict__ Vcat) {
+  const VcTask tk = tasks[blockIdx.x];
+  for (int e = threadIdx.x; e < tk.qb * tk.b1b2; e += blockDim.x) {
+    const int Q = e / tk.b1b2, pm = e - Q * tk.b1b2;
+    const double2 v = __ldg(V + tk.v + e);
+    Vcat[tk.vc + (int64_t)Q * tk.zld + tk.zcol + pm] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+void launch_vcat(const VcTask *tasks, int ntasks, const double2 *V, float2 *Vcat, cudaStream_t st) {
+  if (ntasks == 0) return;
+  vcat_kernel<<<ntasks, 256, 0, st>>>(tasks, V, Vcat);
+  GWGB_CUDA(cudaGetLastError());
+}
+
+void launch_p0_tc(const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
+                  int nr, const double2 *V, const double2 *G, float2 *Z, const float2 *Vcat, double2 *Ppart,
+                  double2 *P0, int ns, int nts, double pref, int mirror, int *err, cudaStream_t st) {
   if (nz > 0) {
     p0_z_kernel<<<nz, 128, zsmem, st>>>(ztasks, V, G, Z, ns, nts, zsmem);
     GWGB_CUDA(cudaGetLastError());
   }
-  if (npt > 0) {
-    p0_tc_kernel<<<npt, 128, psmem, st>>>(ptiles, chunks, V, Z, P0, nts, pref, mirror, drain_every, err);
+  if (nk > 0) {
+    p0_tc_kernel<<<nk, 256, 64 * 1024, st>>>(ktiles, Z, Vcat, Ppart, err);
+    GWGB_CUDA(cudaGetLastError());
+  }
+  if (nr > 0) {
+    p0_reduce_kernel<<<nr, 256, 0, st>>>(rtiles, Ppart, P0, nts, pref, mirror);
     GWGB_CUDA(cudaGetLastError());
   }
 }
 
 void set_tc_p0_kernel_attributes(int smem_bytes) {
   GWGB_CUDA(cudaFuncSetAttribute(p0_z_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
-  GWGB_CUDA(cudaFuncSetAttribute(p0_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(p0_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
 }
 
 }  // namespace gwgb

@@ -5,71 +5,98 @@
 
 namespace gwgb {
 
-// One CTA of the Sigma W-GEMM: 128 rows (tau, Q) of one aux block (q, iq)
-// times a pack of contribution columns (c, j, n).
+// One CTA of the Sigma W-GEMM: rows (tau, Q) of one aux block (q, iq), all
+// columns (c, j, n) of the block in packs of 64 complex columns.
+//   A = P(tau)[Q][P] (FP64, staged once), B = Bcat[col][P] = conj(V_c[P][j][n])
+//   (FP32, built once per V upload), W = Wcat[(tau*qb + Q)*ncol + col] (FP32).
 struct SwTile {
   int64_t pa;       // P(q) block base at tau = 0
+  int64_t bcat;     // Bcat base of the block: Bcat[col*qb + P]
+  int64_t wcat;     // Wcat base of the block
   int32_t pstride;  // per-tau stride of P(q)
   int32_t qb;
   int32_t t0, nt;   // tau range; nt * qb <= 128
-  int32_t c0, c1;   // SwCol range
-  int32_t ncol;     // complex columns of the pack
-  int32_t kp, np;   // padded real K (pad8(2 qb)) and real N (pad16(2 ncol))
+  int32_t ncol;     // complex columns of the block
+  int32_t kp;       // pad8(2 qb)
+  int32_t npk;      // complex columns per pack (16, 32 or 64)
   int32_t pad;
 };
 
-// A contiguous range of the flattened (j, n) columns of one contribution.
-struct SwCol {
+// Bcat entries: one per Sigma contribution.
+struct BcTask {
   int64_t v;        // V block [qb][b1][b2]
-  int64_t w;        // W_c base: W[((tau*qb + Q)*b1 + j)*b2 + n]
-  int32_t b1, b2;
-  int32_t l0;       // first flattened column (j*b2 + n) of the range
-  int32_t col0;     // first pack column of the range
+  int64_t bcat;     // Bcat base of the block
+  int32_t qb, b1b2, col0, pad;
 };
 
 void set_tc_kernel_attributes(int smem_bytes);
 void set_tc_p0_kernel_attributes(int smem_bytes);
 
-void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const SwCol *wcols, const SigTile *tiles1,
-                     int ntiles1, const SigContrib *contribs, const int64_t *woff, const double2 *V,
+// W reference of one Sigma contribution: W_c(tau)[Q][(j,n)] = W[base + (tau*qb + Q)*ld + j*b2 + n]
+struct WRef {
+  int64_t base;
+  int64_t ld;
+};
+
+void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
+                     int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
                      const double2 *G, const double2 *P, float2 *W, double2 *Sig, int ns, double scale,
                      int uv_smem, int *err, cudaStream_t st);
+
+void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat, cudaStream_t st);
 
 }  // namespace gwgb
 
 namespace gwgb {
 
-// P0, stage Z: one CTA per (contribution, spin) over all tau < nts/2.
+// P0, stage Z: one CTA per (contribution, spin) over all tau < nts/2.  Z of
+// the aux block is one matrix Zcat[(tau, P)][K] with K concatenating the
+// (p, m) columns of every (contribution, spin); this task writes columns
+// [zcol, zcol + b1*b2).
 struct PzTask {
   int64_t v;       // V block [qb][b1][b2]
   int64_t ga, gb;  // G^{k1}, G^{k2} block bases
-  int64_t z;       // Z base: Z[((tau*qb + P)*b1 + p)*b2 + m]
+  int64_t z;       // Zcat base of the aux block: Zcat[(tau*qb + P)*zld + zcol + p*b2 + m]
   int32_t sa, sb;  // (t, s) strides of the G slices
   int32_t b1, b2, qb, s;
+  int32_t zld, zcol;
 };
 
-// P0, tcgen05 stage: one CTA per (q_irr, aux block, tau range of nt*qb <= 128 rows).
-struct PtTile {
-  int64_t pout;     // P0 block base at tau = 0
-  int32_t pstride;
+// Vcat[Q][K] = V_c[Q][(p, m)] at the same K columns as Zcat (one entry per (contribution, spin)).
+struct VcTask {
+  int64_t v;        // V block
+  int64_t vc;       // Vcat base of the aux block: Vcat[Q*zld + zcol + pm]
+  int32_t qb, b1b2, zld, zcol;
+};
+
+// Split-K tcgen05 GEMM tile: rows (tau, P) of one aux block, a K slice; FP64
+// partial sums go to Ppart[part + r*qb + Q] and are summed in slice order.
+struct PkTile {
+  int64_t z;        // Zcat base of the block
+  int64_t vc;       // Vcat base of the block
+  int64_t part;     // partial-sum base of this (tile, slice)
+  int32_t zld;      // K row length (complex, multiple of 16)
   int32_t qb;
-  int32_t t0, nt;
-  int32_t k0, k1;   // PtChunk range (all contributions of the block, split in K chunks)
+  int32_t t0, nt;   // tau range, nt * qb <= 128
+  int32_t kc0, kcn; // K slice in 16-complex chunks
   int32_t np;       // pad16(2 qb)
   int32_t pad;
 };
 
-// A K chunk: columns [kc0, kc0 + kn) of the flattened (p, m) index of one (contribution, spin).
-struct PtChunk {
-  int64_t z;        // Z base of the (contribution, spin)
-  int64_t v;        // V block base
-  int32_t b1b2;     // row length of Z and of V[Q]
-  int32_t kc0, kn;
+// Reduction of the slices of one (aux block, tau range) into P0.
+struct PrTile {
+  int64_t part;     // first slice of the tile
+  int64_t pout;     // P0 block base at tau = 0
+  int32_t pstride, qb;
+  int32_t t0, nt;
+  int32_t nslice;
   int32_t pad;
 };
 
-void launch_p0_tc(const PzTask *ztasks, int nz, int zsmem, const PtTile *ptiles, int npt, int psmem,
-                  const PtChunk *chunks, const double2 *V, const double2 *G, float2 *Z, double2 *P0, int ns,
-                  int nts, double pref, int mirror, int drain_every, int *err, cudaStream_t st);
+void launch_p0_tc(const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
+                  int nr, const double2 *V, const double2 *G, float2 *Z, const float2 *Vcat, double2 *Ppart,
+                  double2 *P0, int ns, int nts, double pref, int mirror, int *err, cudaStream_t st);
+
+void launch_vcat(const VcTask *tasks, int ntasks, const double2 *V, float2 *Vcat, cudaStream_t st);
 
 }  // namespace gwgb
