@@ -49,6 +49,7 @@ struct P0Contrib {
 // One P0 output block P0[q_irr][t][block iq] for a tau range.
 struct P0Tile {
   int64_t p;        // offset of the block at t = 0 in the P0 buffer
+  int64_t part;     // FP64 path: this tile's partial-sum slice [nt][qb][qb]
   int32_t pstride;  // per-t stride (qslice size)
   int32_t qb;       // aux block size
   int32_t c0, c1;   // contribution range
@@ -70,6 +71,7 @@ struct SigContrib {
 // One Sigma output block Sigma[t][s][k_irr block ik1] for a tau range.
 struct SigTile {
   int64_t sig;        // offset of the block at t = 0, spin s
+  int64_t part;       // FP64 path: this tile's partial-sum slice [nt][b1][b1]
   int32_t sstride;    // per-t stride (ns * flat_ao)
   int32_t b1;
   int32_t c0, c1;
@@ -100,6 +102,19 @@ struct TSlab {
 };
 
 // One small dense block for a batched inverse.
+// Ordered sum of the contribution slices of one output block over a tau range:
+//   out[(t0 + it) * ostride + e] = scale * sum_sl part[(sl * nt + it) * elems + e]
+// and, when mirroring (P0), the same value at tau' = nts - 1 - tau.
+struct RedTask {
+  int64_t part;     // first slice
+  int64_t out;      // output block at tau = 0
+  int32_t ostride;  // per-tau stride of the output
+  int32_t elems;    // elements of the block
+  int32_t t0, nt;
+  int32_t nslice;
+  int32_t pad;
+};
+
 struct InvTask {
   int64_t a;       // matrix offset (row-major n x n) in the work buffer
   int64_t s, f;    // Dyson: S and F block offsets (in the [ns][flat_ao] buffers)

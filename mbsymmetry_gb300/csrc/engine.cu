@@ -17,7 +17,6 @@
 
 #include "common.h"
 #include "kernels.h"
-#include "kernels_mixed.h"
 #include "kernels_tc.h"
 
 namespace gwgb {
@@ -205,6 +204,41 @@ struct DBuf {
   }
 };
 
+// An output block of a contraction and the contributions it sums.
+struct Owner {
+  int64_t out;      // block base at tau = 0
+  int32_t ostride;  // per-tau stride
+  int32_t n;        // block size (qb for P0, b1 for Sigma)
+  int32_t c0, c1;   // contribution range
+  int32_t smem1;    // shared memory of one tau (complex elements)
+  int32_t s;        // spin (Sigma)
+};
+
+// Cut [c0, c1) into consecutive slices of at most `target` cost (a slice
+// holds at least one contribution; an empty range gives one empty slice).
+static std::vector<std::pair<int, int>> split_slices(const std::vector<double> &cost, int c0, int c1,
+                                                     double target) {
+  std::vector<std::pair<int, int>> out;
+  int a = c0;
+  double acc = 0;
+  for (int c = c0; c < c1; ++c) {
+    if (c > a && acc + cost[c] > target) {
+      out.push_back({a, c});
+      a = c;
+      acc = 0;
+    }
+    acc += cost[c];
+  }
+  out.push_back({a, c1});
+  return out;
+}
+
+static double slice_cost(const std::vector<double> &cost, const std::pair<int, int> &r) {
+  double f = 0;
+  for (int c = r.first; c < r.second; ++c) f += cost[c];
+  return f;
+}
+
 struct GRef {
   int64_t base;
   int32_t stride;
@@ -277,15 +311,17 @@ class Engine {
   DBuf<int64_t> qoff_irr_;
   DBuf<int32_t> qsz_irr_;
   // work lists
-  DBuf<P0Tile> p0_tiles_, p0_tiles1_;   // tau-chunked (FP64) / one tau per tile (mixed)
+  DBuf<P0Tile> p0_tiles_;              // FP64: (block, tau range, contribution slice)
   DBuf<P0Contrib> p0_contribs_;
-  DBuf<SigTile> sig_tiles_, sig_tiles1_;
+  DBuf<SigTile> sig_tiles_, sig_tiles1_;  // FP64 slices / one tau per tile (tcgen05 path)
+  DBuf<RedTask> p0_red_, sig_red_;       // FP64: ordered sums of the slices
+  DBuf<double2> Part_;                   // FP64: partial sums of the slices
   DBuf<SigContrib> sig_contribs_;
   DBuf<RotTask> rotG_, rotP_;
   DBuf<TSlab> slab_p_fwd_, slab_p_bwd_, slab_s_fwd_, slab_g_bwd_;
   DBuf<InvTask> inv_w_, inv_d_;
   int p0_maxo_ = 8, sig_maxo_ = 8, rot_smem_ = 0;
-  int p0_mixed_smem_ = 0, sig_mixed_smem_ = 0;
+  int fp64_smem_ = 0, nsm_ = 0;  // FP64 contraction CTA shared memory; SM count
   // tcgen05 Sigma path: W-GEMM tiles, conj(V) operand tasks, per-contribution W references
   DBuf<SwTile> sw_tiles_;
   DBuf<BcTask> bc_tasks_;
@@ -371,8 +407,11 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
   int optin = 0;
   GWGB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev_));
   smem_bytes_ = std::min(optin, 200 * 1024);
+  int per_sm = 0;
+  GWGB_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev_));
+  GWGB_CUDA(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
   set_fp64_kernel_attributes(smem_bytes_);
-  set_mixed_kernel_attributes(smem_bytes_);
+  fp64_smem_ = std::min(smem_bytes_, ((per_sm / 2 - 2048) / 1024) * 1024);  // two CTAs per SM
   set_tc_kernel_attributes(smem_bytes_);
   set_tc_p0_kernel_attributes(smem_bytes_);
   GWGB_CUDA(cudaMallocHost(&mu_host_, sizeof(double)));
@@ -410,7 +449,8 @@ Engine::~Engine() {
   for (auto *b : bufs) b->free();
   tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
   qoff_irr_.free(); qsz_irr_.free();
-  p0_tiles_.free(); p0_tiles1_.free(); p0_contribs_.free(); sig_tiles_.free(); sig_tiles1_.free(); sig_contribs_.free();
+  p0_tiles_.free(); p0_contribs_.free(); sig_tiles_.free(); sig_tiles1_.free(); sig_contribs_.free();
+  p0_red_.free(); sig_red_.free(); Part_.free();
   rotG_.free(); rotP_.free(); slab_p_fwd_.free(); slab_p_bwd_.free(); slab_s_fwd_.free(); slab_g_bwd_.free();
   inv_w_.free(); inv_d_.free();
   if (st_) cudaStreamDestroy(st_);
@@ -423,7 +463,6 @@ void Engine::build_work_lists() {
   const Lay &l = l_;
   const int nk = l.nk, ink = l.ink;
   const int64_t fa = l.flat_ao, fq = l.flat_aux;
-  const int cap = smem_bytes_ / (int)sizeof(double2);
 
   // --- G references: irreducible k read in place from the host-layout
   //     buffer, every other k from its rotated copy [k'][t][s][kslice].
@@ -500,18 +539,18 @@ void Engine::build_work_lists() {
   rotG_.upload(rg, st_);
   rotP_.upload(rp, st_);
 
-  // --- P0 tiles: owner = (q_irr, aux block iq, tau range)
-  std::vector<P0Tile> pt;
+  // --- P0: owner = (q_irr, aux block iq); the FP64 tiles are (owner, tau
+  //     range, slice of the owner's contributions), see make_fp64_tiles.
   std::vector<P0Contrib> pc;
+  std::vector<double> pcost;  // flops per contribution and tau (all spins)
+  std::vector<Owner> p0_own;
   p0_flops_ = 0;
-  int maxo = 1;
   const int half = nts_ / 2;
   for (int iqr = 0; iqr < ink; ++iqr) {
     const int q = l.irre_list[iqr];
     for (int iq = 0; iq < l.naux_blocks(q); ++iq) {
       const int qb = l.auxsz(q, iq);
       const int c0 = (int)pc.size();
-      double flop = 0;
       int b2max = 1;
       for (int k1 = 0; k1 < nk; ++k1) {
         const int k2 = l.mom_cons(k1, 0, q);  // k2 = k1 + q (cugw_routines_block.cu:283)
@@ -522,50 +561,21 @@ void Engine::build_work_lists() {
           const int b1 = l.aosz(k1, i1), b2 = l.aosz(k2, i2);
           pc.push_back({l.kp_off[p] + l.t_off[b], gref[k1].base + l.aooff(k1, i1), gref[k2].base + l.aooff(k2, i2),
                         gref[k1].stride, gref[k2].stride, b1, b2});
-          flop += 8.0 * ((double)b2 * qb * b1 * b1 + (double)qb * b1 * b2 * b2 + (double)qb * qb * b1 * b2);
+          const double f = 8.0 * ns_ *
+                           ((double)b2 * qb * b1 * b1 + (double)qb * b1 * b2 * b2 + (double)qb * qb * b1 * b2);
+          pcost.push_back(f);
+          p0_flops_ += f * half;
           b2max = std::max(b2max, b2);
         }
       }
       const int c1 = (int)pc.size();
-      p0_groups_.push_back({(int64_t)nts_ * l.qaux_off_irre[iqr] + l.auxoff(q, iq), (int32_t)l.qaux_sz[q], qb, c0, c1});
-      p0_flops_ += flop * ns_ * half;
-      int nt = std::max(1, std::min(half, (256 + qb * qb - 1) / (qb * qb)));
-      while (nt > 1 && nt * qb * qb > 2048) --nt;
-      while (nt > 1 && 2 * qb * b2max * nt > cap) --nt;
-      GWGB_REQUIRE(2 * qb * b2max * nt <= cap, GWGB_E_UNSUPPORTED, "P0 block too large for shared memory");
-      maxo = std::max(maxo, (nt * qb * qb + 255) / 256);
-      for (int t0 = 0; t0 < half; t0 += nt) {
-        const int n = std::min(nt, half - t0);
-        const double cost = flop * n * ns_;
-        pt.push_back({(int64_t)nts_ * l.qaux_off_irre[iqr] + l.auxoff(q, iq), (int32_t)l.qaux_sz[q], qb, c0, c1,
-                      t0, n, (int32_t)std::min(cost / 1e3, 2e9), 0});
-      }
+      const int64_t pout = (int64_t)nts_ * l.qaux_off_irre[iqr] + l.auxoff(q, iq);
+      p0_groups_.push_back({pout, (int32_t)l.qaux_sz[q], qb, c0, c1});
+      p0_own.push_back({pout, (int32_t)l.qaux_sz[q], qb, c0, c1, 2 * qb * b2max, 0});
     }
   }
-  GWGB_REQUIRE(maxo <= 16, GWGB_E_UNSUPPORTED, "P0 output tile too large");
-  p0_maxo_ = maxo;
-  std::stable_sort(pt.begin(), pt.end(), [](const P0Tile &a, const P0Tile &b) { return a.cost > b.cost; });
-  p0_tiles_.upload(pt, st_);
   p0_contribs_.upload(pc, st_);
-  {  // mixed path: one tau per tile; shared memory = FP64 + FP32 accumulators + two intermediates
-    std::vector<P0Tile> pt1;
-    int need = 0;
-    for (const P0Tile &t : pt)
-      for (int i = 0; i < t.nt; ++i) {
-        P0Tile u = t;
-        u.t0 = t.t0 + i;
-        u.nt = 1;
-        u.cost = t.cost / std::max(1, t.nt);
-        pt1.push_back(u);
-        int b2max = 1;
-        for (int c = t.c0; c < t.c1; ++c) b2max = std::max(b2max, pc[c].b2);
-        need = std::max(need, 24 * t.qb * t.qb + 16 * b2max * t.qb);
-      }
-    std::stable_sort(pt1.begin(), pt1.end(), [](const P0Tile &a, const P0Tile &b) { return a.cost > b.cost; });
-    p0_tiles1_.upload(pt1, st_);
-    p0_mixed_smem_ = std::max(16 * 1024, ((need + 1023) / 1024) * 1024);
-    GWGB_REQUIRE(p0_mixed_smem_ <= smem_bytes_, GWGB_E_UNSUPPORTED, "P0 block too large for the mixed kernel");
-  }
+
   {  // tcgen05 P0: per aux block, Zcat[(tau,P)][K] and Vcat[Q][K] with K over (contribution, spin)
     std::vector<PzTask> zt;
     std::vector<VcTask> vt;
@@ -625,17 +635,17 @@ void Engine::build_work_lists() {
     pz_smem_ = std::min(smem_bytes_, std::max(16 * 1024, ((zneed + 1023) / 1024) * 1024));
   }
 
-  // --- Sigma tiles: owner = (k_irr, AO block i1, spin, tau range)
-  std::vector<SigTile> stl;
+  // --- Sigma: owner = (k_irr, AO block i1, spin)
   std::vector<SigContrib> sc;
+  std::vector<double> scost;  // flops per contribution and tau
+  std::vector<Owner> sig_own;
+  std::vector<SigTile> stl;   // one tile per (owner, tau): the tcgen05 path
   sig_flops_ = 0;
-  maxo = 1;
   for (int ik = 0; ik < ink; ++ik) {
     const int k1 = l.irre_list[ik];
     for (int i1 = 0; i1 < l.nao_blocks(k1); ++i1) {
       const int b1 = l.aosz(k1, i1);
       const int c0 = (int)sc.size();
-      double flop = 0;
       int qbmax = 1;
       for (int q = 0; q < nk; ++q) {
         const int k2 = l.mom_cons(k1, q, 0);  // k2 = k1 - q (cugw_routines_block.cu:307)
@@ -648,49 +658,84 @@ void Engine::build_work_lists() {
                         gref[k2].stride, pref[q].stride, b2, qb});
           sig_b1_.push_back(b1);
           sig_groups_[std::make_pair(q, iq)].push_back((int)sc.size() - 1);
-          flop += 8.0 * ((double)qb * b1 * b2 * b2 + (double)b1 * b2 * qb * qb + (double)b1 * b1 * b2 * qb);
+          const double f = 8.0 * ((double)qb * b1 * b2 * b2 + (double)b1 * b2 * qb * qb + (double)b1 * b1 * b2 * qb);
+          scost.push_back(f);
+          sig_flops_ += f * ns_ * nts_;
           qbmax = std::max(qbmax, qb);
         }
       }
       const int c1 = (int)sc.size();
-      sig_flops_ += flop * ns_ * nts_;
-      int nt = std::max(1, std::min(nts_, (256 + b1 * b1 - 1) / (b1 * b1)));
-      while (nt > 1 && nt * b1 * b1 > 2048) --nt;
-      while (nt > 1 && 2 * qbmax * b1 * nt > cap) --nt;
-      GWGB_REQUIRE(2 * qbmax * b1 * nt <= cap, GWGB_E_UNSUPPORTED, "Sigma block too large for shared memory");
-      maxo = std::max(maxo, (nt * b1 * b1 + 255) / 256);
-      for (int s = 0; s < ns_; ++s)
-        for (int t0 = 0; t0 < nts_; t0 += nt) {
-          const int n = std::min(nt, nts_ - t0);
-          const double cost = flop * n;
-          stl.push_back({(int64_t)s * fa + l.kao_off_irre[ik] + l.aooff(k1, i1), (int32_t)(ns_ * fa), b1, c0, c1, t0,
-                         n, s, (int32_t)std::min(cost / 1e3, 2e9)});
-        }
+      for (int s = 0; s < ns_; ++s) {
+        const int64_t out = (int64_t)s * fa + l.kao_off_irre[ik] + l.aooff(k1, i1);
+        sig_own.push_back({out, (int32_t)(ns_ * fa), b1, c0, c1, 2 * qbmax * b1, s});
+        double f = 0;
+        for (int c = c0; c < c1; ++c) f += scost[c];
+        for (int t = 0; t < nts_; ++t)
+          stl.push_back({out, 0, (int32_t)(ns_ * fa), b1, c0, c1, t, 1, s, (int32_t)std::min(f / 1e3, 2e9)});
+      }
     }
   }
-  GWGB_REQUIRE(maxo <= 16, GWGB_E_UNSUPPORTED, "Sigma output tile too large");
-  sig_maxo_ = maxo;
-  std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
-  sig_tiles_.upload(stl, st_);
   sig_contribs_.upload(sc, st_);
+  std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
+  sig_tiles1_.upload(stl, st_);
+
+  // --- FP64 tiles of both contractions and their partial-sum buffer
   {
-    std::vector<SigTile> st1;
-    int need = 0;
-    for (const SigTile &t : stl)
-      for (int i = 0; i < t.nt; ++i) {
-        SigTile u = t;
-        u.t0 = t.t0 + i;
-        u.nt = 1;
-        u.cost = t.cost / std::max(1, t.nt);
-        st1.push_back(u);
-        int qbmax = 1;
-        for (int c = t.c0; c < t.c1; ++c) qbmax = std::max(qbmax, sc[c].qb);
-        need = std::max(need, 24 * t.b1 * t.b1 + 16 * qbmax * t.b1);
+    int need = 0;  // shared memory of the largest owner at one tau
+    for (const Owner &o : p0_own) need = std::max(need, 16 * o.smem1);
+    for (const Owner &o : sig_own) need = std::max(need, 16 * o.smem1);
+    GWGB_REQUIRE(need <= smem_bytes_, GWGB_E_UNSUPPORTED, "irrep block too large for the FP64 contraction kernels");
+    if (need > fp64_smem_) fp64_smem_ = smem_bytes_;  // one CTA per SM for very large blocks
+    const int cap = fp64_smem_ / (int)sizeof(double2);
+    const double waves = 2.0 * 6.0 * nsm_;  // two CTAs per SM, about six waves
+    int64_t part0 = 0, part1 = 0;
+    std::vector<P0Tile> pt;
+    std::vector<SigTile> st;
+    std::vector<RedTask> pr, sr;
+    p0_maxo_ = 1;
+    for (const Owner &o : p0_own) {
+      const int qq = o.n * o.n;
+      int nt = std::max(1, std::min(half, (256 + qq - 1) / qq));
+      while (nt > 1 && nt * qq > 2048) --nt;
+      while (nt > 1 && o.smem1 * nt > cap) --nt;
+      p0_maxo_ = std::max(p0_maxo_, (nt * qq + 255) / 256);
+      for (int t0 = 0; t0 < half; t0 += nt) {
+        const int n = std::min(nt, half - t0);
+        const auto sl = split_slices(pcost, o.c0, o.c1, p0_flops_ / waves / n);
+        pr.push_back({part0, o.out, o.ostride, qq, t0, n, (int32_t)sl.size(), 0});
+        for (const auto &r : sl) {
+          pt.push_back({o.out, part0, o.ostride, o.n, r.first, r.second, t0, n,
+                        (int32_t)std::min(slice_cost(pcost, r) * n / 1e3, 2e9), 0});
+          part0 += (int64_t)n * qq;
+        }
       }
-    std::stable_sort(st1.begin(), st1.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
-    sig_tiles1_.upload(st1, st_);
-    sig_mixed_smem_ = std::max(16 * 1024, ((need + 1023) / 1024) * 1024);
-    GWGB_REQUIRE(sig_mixed_smem_ <= smem_bytes_, GWGB_E_UNSUPPORTED, "Sigma block too large for the mixed kernel");
+    }
+    sig_maxo_ = 1;
+    for (const Owner &o : sig_own) {
+      const int bb = o.n * o.n;
+      int nt = std::max(1, std::min(nts_, (256 + bb - 1) / bb));
+      while (nt > 1 && nt * bb > 2048) --nt;
+      while (nt > 1 && o.smem1 * nt > cap) --nt;
+      sig_maxo_ = std::max(sig_maxo_, (nt * bb + 255) / 256);
+      for (int t0 = 0; t0 < nts_; t0 += nt) {
+        const int n = std::min(nt, nts_ - t0);
+        const auto sl = split_slices(scost, o.c0, o.c1, sig_flops_ / waves / n);
+        sr.push_back({part1, o.out, o.ostride, bb, t0, n, (int32_t)sl.size(), 0});
+        for (const auto &r : sl) {
+          st.push_back({o.out, part1, o.ostride, o.n, r.first, r.second, t0, n, o.s,
+                        (int32_t)std::min(slice_cost(scost, r) * n / 1e3, 2e9)});
+          part1 += (int64_t)n * bb;
+        }
+      }
+    }
+    GWGB_REQUIRE(p0_maxo_ <= 16 && sig_maxo_ <= 16, GWGB_E_UNSUPPORTED, "contraction output tile too large");
+    std::stable_sort(pt.begin(), pt.end(), [](const P0Tile &a, const P0Tile &b) { return a.cost > b.cost; });
+    std::stable_sort(st.begin(), st.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
+    p0_tiles_.upload(pt, st_);
+    sig_tiles_.upload(st, st_);
+    p0_red_.upload(pr, st_);
+    sig_red_.upload(sr, st_);
+    Part_.alloc((size_t)std::max<int64_t>(1, std::max(part0, part1)));
   }
   {  // tcgen05 Sigma: per aux block (q, iq), Bcat = conj(V) columns, Wcat = W rows (tau, Q)
     std::vector<WRef> wr(sc.size());
@@ -884,9 +929,11 @@ void Engine::k_p0(int mirror) {
     launch_p0_tc(pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pk_tiles_.p, (int)pk_tiles_.n, pr_tiles_.p,
                  (int)pr_tiles_.n, V_.p, Gall_.p, Zbuf_.p, Vcat_.p, Ppart_.p, Pall_.p, ns_, nts_, pref, mirror,
                  bad_.p + 2, st_);
-  } else
-    launch_p0_fp64(p0_tiles_.p, (int)p0_tiles_.n, p0_maxo_, p0_contribs_.p, V_.p, Gall_.p, Pall_.p, ns_, nts_, pref,
-                   mirror, smem_bytes_, st_);
+  } else {
+    launch_p0_fp64(p0_tiles_.p, (int)p0_tiles_.n, p0_maxo_, p0_contribs_.p, V_.p, Gall_.p, Part_.p, ns_, nts_,
+                   fp64_smem_, st_);
+    launch_reduce_slices(p0_red_.p, (int)p0_red_.n, Part_.p, Pall_.p, nts_, pref, mirror, st_);
+  }
 }
 
 void Engine::k_pq(bool mirror_first) {
@@ -906,9 +953,11 @@ void Engine::k_sigma() {
     launch_sigma_tc(sw_tiles_.p, (int)sw_tiles_.n, sw_smem_, Bcat_.p, sig_tiles1_.p, (int)sig_tiles1_.n,
                     sig_contribs_.p, sig_wref_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p, Sig_.p, ns_, -1.0 / l_.nk, uv_smem_,
                     bad_.p + 2, st_);
-  } else
-    launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Sig_.p,
-                      ns_, -1.0 / l_.nk, smem_bytes_, st_);
+  } else {
+    launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Part_.p,
+                      ns_, fp64_smem_, st_);
+    launch_reduce_slices(sig_red_.p, (int)sig_red_.n, Part_.p, Sig_.p, nts_, -1.0 / l_.nk, 0, st_);
+  }
 }
 
 void Engine::k_dyson() {
@@ -957,7 +1006,14 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
   }
   s.total_ms = elapsed(with_gw ? 0 : 5, with_dyson ? 6 : 5);
   int64_t launches = 0;
-  if (with_gw) launches += (rotG_.n ? 1 : 0) + (p0_tiles_.n ? 1 : 0) + 3 + (rotP_.n ? 1 : 0) + (sig_tiles_.n ? 1 : 0);
+  if (with_gw) {
+    const bool tc = prec_ == GWGB_PREC_TF32X3;
+    const int64_t p0 = tc ? (pz_tasks_.n ? 1 : 0) + (pk_tiles_.n ? 1 : 0) + (pr_tiles_.n ? 1 : 0)
+                          : (p0_tiles_.n ? 1 : 0) + (p0_red_.n ? 1 : 0);
+    const int64_t sg = tc ? (sw_tiles_.n ? 1 : 0) + (sig_tiles1_.n ? 1 : 0)
+                          : (sig_tiles_.n ? 1 : 0) + (sig_red_.n ? 1 : 0);
+    launches += (rotG_.n ? 1 : 0) + p0 + 3 + (rotP_.n ? 1 : 0) + sg;
+  }
   if (with_dyson) launches += 3 + (has_tct_ ? 1 : 0);
   s.kernel_launches = launches;
   stats_ = s;

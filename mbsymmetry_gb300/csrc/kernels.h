@@ -22,13 +22,18 @@ __host__ __device__ constexpr int rotate_smem_bytes(int nmax) { return 3 * nmax 
 
 void set_fp64_kernel_attributes(int smem_bytes);
 
+// FP64 contractions: each tile writes its partial block to Part[tile.part];
+// launch_reduce_slices then sums the slices in order into P0 / Sigma.
 void launch_p0_fp64(const P0Tile *tiles, int ntiles, int maxo, const P0Contrib *contribs,
-                    const double2 *V, const double2 *G, double2 *P0, int ns, int nts, double pref,
-                    int mirror, int smem_bytes, cudaStream_t st);
+                    const double2 *V, const double2 *G, double2 *Part, int ns, int nts, int smem_bytes,
+                    cudaStream_t st);
 
 void launch_sigma_fp64(const SigTile *tiles, int ntiles, int maxo, const SigContrib *contribs,
-                       const double2 *V, const double2 *G, const double2 *P, double2 *Sig, int ns,
-                       double scale, int smem_bytes, cudaStream_t st);
+                       const double2 *V, const double2 *G, const double2 *P, double2 *Part, int ns,
+                       int smem_bytes, cudaStream_t st);
+
+void launch_reduce_slices(const RedTask *tasks, int ntasks, const double2 *part, double2 *out, int nts,
+                          double scale, int mirror, cudaStream_t st);
 
 void launch_rotate(const RotTask *tasks, int ntasks, int nbatch, int smem_bytes, const double2 *src,
                    const double2 *O, double2 *dst, cudaStream_t st);

@@ -41,15 +41,17 @@ __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_dou
 //   X2[P][t,m] = sum_n conj(V[P][t][n]) G^{k2}(tau)[m][n]
 //   P0(tau)[Q][P] += sum_{t,m} X1[t,m][Q] X2[P][t,m]
 // The t (row of the k1 block) range is processed in chunks so the
-// intermediates of any block size fit in shared memory.
+// intermediates of any block size fit in shared memory.  A tile sums one
+// slice of the block's contributions into its own partial block; the slices
+// are added in a fixed order by reduce_slices_kernel.
 // ---------------------------------------------------------------------------
 template <int MAXO>
-__global__ void __launch_bounds__(256) p0_fp64_kernel(const P0Tile *__restrict__ tiles,
-                                                      const P0Contrib *__restrict__ contribs,
-                                                      const double2 *__restrict__ V,
-                                                      const double2 *__restrict__ G,
-                                                      double2 *__restrict__ P0, int ns, int nts,
-                                                      double pref, int mirror, int smem_cap) {
+__global__ void __launch_bounds__(256, 2) p0_fp64_kernel(const P0Tile *__restrict__ tiles,
+                                                         const P0Contrib *__restrict__ contribs,
+                                                         const double2 *__restrict__ V,
+                                                         const double2 *__restrict__ G,
+                                                         double2 *__restrict__ Part, int ns, int nts,
+                                                         int smem_cap) {
   extern __shared__ double2 sm[];
   const P0Tile tile = tiles[blockIdx.x];
   const int qb = tile.qb, nt = tile.nt;
@@ -116,14 +118,7 @@ __global__ void __launch_bounds__(256) p0_fp64_kernel(const P0Tile *__restrict__
 #pragma unroll
   for (int i = 0; i < MAXO; ++i) {
     const int o = threadIdx.x + i * blockDim.x;
-    if (o < nout) {
-      const int it = o / (qb * qb);
-      const int rem = o - it * qb * qb;
-      const int tau = tile.t0 + it;
-      const double2 v = cscale(acc[i], pref);
-      P0[tile.p + (size_t)tau * tile.pstride + rem] = v;
-      if (mirror) P0[tile.p + (size_t)(nts - 1 - tau) * tile.pstride + rem] = v;
-    }
+    if (o < nout) Part[tile.part + o] = acc[i];
   }
 }
 
@@ -133,15 +128,15 @@ __global__ void __launch_bounds__(256) p0_fp64_kernel(const P0Tile *__restrict__
 //   Y2[i][n][P] = sum_Q Y1[Q][i][n] P(tau)[Q][P]
 //   Sigma(tau)[i][j] += sum_{n,P} Y2[i][n][P] conj(V[P][j][n])
 // The n range is processed in chunks so the intermediates fit in shared memory.
+// Like P0, a tile writes the partial sum of one slice of the contributions.
 // ---------------------------------------------------------------------------
 template <int MAXO>
-__global__ void __launch_bounds__(256) sigma_fp64_kernel(const SigTile *__restrict__ tiles,
-                                                         const SigContrib *__restrict__ contribs,
-                                                         const double2 *__restrict__ V,
-                                                         const double2 *__restrict__ G,
-                                                         const double2 *__restrict__ P,
-                                                         double2 *__restrict__ Sig, int ns,
-                                                         double scale, int smem_cap) {
+__global__ void __launch_bounds__(256, 2) sigma_fp64_kernel(const SigTile *__restrict__ tiles,
+                                                            const SigContrib *__restrict__ contribs,
+                                                            const double2 *__restrict__ V,
+                                                            const double2 *__restrict__ G,
+                                                            const double2 *__restrict__ P,
+                                                            double2 *__restrict__ Part, int ns, int smem_cap) {
   extern __shared__ double2 sm[];
   const SigTile tile = tiles[blockIdx.x];
   const int b1 = tile.b1, nt = tile.nt, s = tile.s;
@@ -211,11 +206,23 @@ __global__ void __launch_bounds__(256) sigma_fp64_kernel(const SigTile *__restri
 #pragma unroll
   for (int ii = 0; ii < MAXO; ++ii) {
     const int o = threadIdx.x + ii * blockDim.x;
-    if (o < nout) {
-      const int it = o / (b1 * b1);
-      const int rem = o - it * b1 * b1;
-      Sig[tile.sig + (size_t)(tile.t0 + it) * tile.sstride + rem] = cscale(acc[ii], scale);
-    }
+    if (o < nout) Part[tile.part + o] = acc[ii];
+  }
+}
+
+// Fixed-order sum of the slices (deterministic), scaled, into P0 or Sigma.
+__global__ void reduce_slices_kernel(const RedTask *__restrict__ tasks, const double2 *__restrict__ part,
+                                     double2 *__restrict__ out, int nts, double scale, int mirror) {
+  const RedTask tk = tasks[blockIdx.x];
+  const int n = tk.nt * tk.elems;
+  for (int o = threadIdx.x; o < n; o += blockDim.x) {
+    double2 a = part[tk.part + o];
+    for (int sl = 1; sl < tk.nslice; ++sl) a = cadd(a, part[tk.part + (int64_t)sl * n + o]);
+    const int it = o / tk.elems, e = o - it * tk.elems;
+    const int tau = tk.t0 + it;
+    const double2 v = cscale(a, scale);
+    out[tk.out + (int64_t)tau * tk.ostride + e] = v;
+    if (mirror) out[tk.out + (int64_t)(nts - 1 - tau) * tk.ostride + e] = v;
   }
 }
 
@@ -499,27 +506,34 @@ __global__ void leakage_kernel(const TSlab *__restrict__ slabs, const double2 *_
 // host launchers
 // ---------------------------------------------------------------------------
 void launch_p0_fp64(const P0Tile *tiles, int ntiles, int maxo, const P0Contrib *contribs,
-                    const double2 *V, const double2 *G, double2 *P0, int ns, int nts, double pref,
-                    int mirror, int smem_bytes, cudaStream_t st) {
+                    const double2 *V, const double2 *G, double2 *Part, int ns, int nts, int smem_bytes,
+                    cudaStream_t st) {
   if (ntiles == 0) return;
   const int cap = smem_bytes / (int)sizeof(double2);
   if (maxo <= 8) {
-    p0_fp64_kernel<8><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P0, ns, nts, pref, mirror, cap);
+    p0_fp64_kernel<8><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, Part, ns, nts, cap);
   } else {
-    p0_fp64_kernel<16><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P0, ns, nts, pref, mirror, cap);
+    p0_fp64_kernel<16><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, Part, ns, nts, cap);
   }
   GWGB_CUDA(cudaGetLastError());
 }
 
+void launch_reduce_slices(const RedTask *tasks, int ntasks, const double2 *part, double2 *out, int nts,
+                          double scale, int mirror, cudaStream_t st) {
+  if (ntasks == 0) return;
+  reduce_slices_kernel<<<ntasks, 256, 0, st>>>(tasks, part, out, nts, scale, mirror);
+  GWGB_CUDA(cudaGetLastError());
+}
+
 void launch_sigma_fp64(const SigTile *tiles, int ntiles, int maxo, const SigContrib *contribs,
-                       const double2 *V, const double2 *G, const double2 *P, double2 *Sig, int ns,
-                       double scale, int smem_bytes, cudaStream_t st) {
+                       const double2 *V, const double2 *G, const double2 *P, double2 *Part, int ns,
+                       int smem_bytes, cudaStream_t st) {
   if (ntiles == 0) return;
   const int cap = smem_bytes / (int)sizeof(double2);
   if (maxo <= 8) {
-    sigma_fp64_kernel<8><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P, Sig, ns, scale, cap);
+    sigma_fp64_kernel<8><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P, Part, ns, cap);
   } else {
-    sigma_fp64_kernel<16><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P, Sig, ns, scale, cap);
+    sigma_fp64_kernel<16><<<ntiles, 256, smem_bytes, st>>>(tiles, contribs, V, G, P, Part, ns, cap);
   }
   GWGB_CUDA(cudaGetLastError());
 }
