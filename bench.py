@@ -257,8 +257,13 @@ def run_gpu(args):
     flops = st[f"{dom}_flops"]
     dom_ms = stages[f"{dom}_ms"]
     achieved = flops / (dom_ms * 1e-3) / 1e12
+    # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the same
+    # kernel on this workload, from the ncu capture summarised in
+    # profiles/c2_contraction_kernels.md; the kernels are FP64-pipe bound.
+    traffic = {"sigma": 1.390e9, "p0": 0.0565e9}[dom]
     roofline = {"bound": "tensor", "kernel": f"{dom}_fp64_kernel", "achieved": achieved, "peak": fp64_peak,
-                "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": traffic,
+                "traffic_unit": "bytes per launch (ncu)",
                 "peak_source": "FP64 FMA microbenchmark measured in this run (MEASURED_PEAKS.json has no FP64 "
                                "figure); contraction FLOPs = 8MNK per complex GEMM of the block layout",
                 "flop_alg_per_launch": flops, "kernel_ms": dom_ms}
@@ -293,8 +298,10 @@ def run_gpu(args):
              "contraction_tflops_alg": {"p0": stm["p0_flops"] / (mstage["p0_ms"] * 1e-3) / 1e12,
                                         "sigma": stm["sigma_flops"] / (mstage["sigma_ms"] * 1e-3) / 1e12}}
 
+    # replicas: every rank runs the whole iteration, so the job completes `world`
+    # iterations per max-over-ranks time
     line = {
-        "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": ms / 1e3 / world, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "precision": "fp64", "l2": "flushed (256 MiB write) before each step",
@@ -320,6 +327,28 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_profile(args):
+    """One FP64 and one TF32x3 iteration of the workload and nothing else: the
+    command that ncu captures (a plain run of it must exit 0 first)."""
+    import torch
+    from mbsymmetry_gb300.solver import GWSolver
+    torch.cuda.set_device(0)
+    cr, tr = _setup()
+    s = GWSolver(cr.layout, cr.ns, tr, device=0)
+    s.set_shared_Coulomb(cr.V)
+    s.set_fock(cr.F, cr.S)
+    s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+    s.dyson(cr.mu)
+    G0 = s.G_tau()
+    s.iteration(cr.mu)
+    s.single_prec_run(True, "tf32x3")
+    s.set_G(G0)
+    s.iteration(cr.mu)
+    st = s.stats()
+    s.close()
+    print(f"profile run: {CONFIG}, one FP64 and one TF32x3 iteration (last {st['total_ms']:.2f} ms)")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -327,8 +356,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="run one FP64 and one TF32x3 iteration only (the command for ncu captures)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
