@@ -202,6 +202,61 @@ int gwgb_get_stats(gwgb_handle h, gwgb_stats *out);
 /* Block until all work of the handle is done. */
 int gwgb_synchronize(gwgb_handle h);
 
+/* ---- self-consistent loop ----------------------------------------------
+ * No counterpart in the reference: sc_loop_block_t keeps mu fixed
+ * (sc_loop_block_t.h:25), never assigns its energy (:123), does not mix and
+ * does not iterate (params_t.cpp:74).  These entry points add, on the device:
+ *   N(mu)  = -(2/ns)/nk sum_{s,k} Re Tr[G_k,s(beta) S_k,s]       (electrons)
+ *   E_corr = -(1/ns)/nk sum_{s,k} Re sum_{ij} M_ij Tr[Sigma_k,s(tau_i) G_k,s(tau_j)]
+ *            (Galitskii-Migdal; M is the caller's interior-tau quadrature of
+ *             int_0^beta Sigma(tau) G(beta - tau) dtau)
+ *   E_one  = -(1/ns)/nk sum_{s,k} Re Tr[G_k,s(beta) (H_k,s + F_k,s)]  (when H is set)
+ * with k summed over the full mesh through the irreducible weights
+ * (#k mapped to each stored k), and linear mixing
+ *   Sigma <- alpha Sigma_new + (1 - alpha) Sigma_old.                     */
+
+/* Core Hamiltonian H [ns][flat_ao] (complex); enables E_one. */
+int gwgb_set_hcore(gwgb_handle h, const double *H);
+
+/* Galitskii-Migdal weights M [(nts-2) x (nts-2)] (real, row-major). */
+int gwgb_set_energy_matrix(gwgb_handle h, const double *M, int32_t n);
+
+typedef struct gwgb_mu_search {
+  double n_electrons;  /* target N */
+  double mu0;          /* first trial */
+  double step;         /* first bracket step (> 0); doubled while the root is not bracketed */
+  double tol;          /* |N - target| accepted; later evaluations are skipped */
+  int32_t max_evals;   /* Dyson evaluations per search (fixed in the graph), 2..64 */
+  int32_t pad;
+} gwgb_mu_search;
+
+typedef struct gwgb_sc_record {
+  double mu;           /* chemical potential used by the iteration's Dyson */
+  double n_electrons;  /* N(mu) of the new G */
+  double e_corr;       /* Galitskii-Migdal energy of (Sigma, new G) */
+  double e_one;        /* one-body energy of the new G (0 without H) */
+  double leakage;      /* max |c_last| / max |c_0| of the new G (0 without tct) */
+  int32_t mu_evals;    /* Dyson evaluations the search used */
+  int32_t precision;   /* GWGB_PREC_* of the iteration's contractions */
+} gwgb_sc_record;
+
+/* Dyson with a device-side search for mu (bracketed Illinois regula falsi,
+ * at most max_evals Dyson evaluations): the G at the best mu found.  Writes
+ * the mu used and N to mu_out / n_out (either may be NULL). */
+int gwgb_find_mu(gwgb_handle h, const gwgb_mu_search *ms, double *mu_out, double *n_out);
+
+/* E_corr and E_one of the resident Sigma and G (either pointer may be NULL). */
+int gwgb_energy(gwgb_handle h, double *e_corr, double *e_one);
+
+/* niter self-consistent iterations, each one CUDA graph launch with no host
+ * synchronisation in between: GW Sigma from G, Sigma mixed with the previous
+ * Sigma (alpha), mu search (ms, starting from the previous iteration's mu),
+ * Dyson, energies.  The Sigma resident at the call is the first Sigma_old.
+ * final_fp64 != 0 runs the last iteration with the FP64 contractions whatever
+ * the handle's precision.  One record per iteration goes to out[niter]. */
+int gwgb_sc_loop(gwgb_handle h, int32_t niter, double alpha, const gwgb_mu_search *ms, int32_t final_fp64,
+                 gwgb_sc_record *out);
+
 /* ---- W~ solve without device allocation -------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory while they run (a host code whose own pool owns all of HBM, a plugin

@@ -59,6 +59,20 @@ class GwgbStats(ctypes.Structure):
     ]
 
 
+class GwgbMuSearch(ctypes.Structure):
+    _fields_ = [
+        ("n_electrons", c_double), ("mu0", c_double), ("step", c_double), ("tol", c_double),
+        ("max_evals", c_int32), ("pad", c_int32),
+    ]
+
+
+class GwgbScRecord(ctypes.Structure):
+    _fields_ = [
+        ("mu", c_double), ("n_electrons", c_double), ("e_corr", c_double), ("e_one", c_double),
+        ("leakage", c_double), ("mu_evals", c_int32), ("precision", c_int32),
+    ]
+
+
 #: every symbol include/gwgb.h declares, with (restype, argtypes)
 SIGNATURES = {
     "gwgb_version": (c_char_p, []),
@@ -85,6 +99,12 @@ SIGNATURES = {
     "gwgb_iteration": (c_int32, [c_void_p, c_double]),
     "gwgb_get_stats": (c_int32, [c_void_p, POINTER(GwgbStats)]),
     "gwgb_synchronize": (c_int32, [c_void_p]),
+    "gwgb_set_hcore": (c_int32, [c_void_p, c_void_p]),
+    "gwgb_set_energy_matrix": (c_int32, [c_void_p, c_void_p, c_int32]),
+    "gwgb_find_mu": (c_int32, [c_void_p, POINTER(GwgbMuSearch), POINTER(c_double), POINTER(c_double)]),
+    "gwgb_energy": (c_int32, [c_void_p, POINTER(c_double), POINTER(c_double)]),
+    "gwgb_sc_loop": (c_int32, [c_void_p, c_int32, c_double, POINTER(GwgbMuSearch), c_int32,
+                               POINTER(GwgbScRecord)]),
     "gwgb_wsolve_noalloc": (c_int32, [c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
                                       c_void_p, c_int32, c_void_p]),
 }

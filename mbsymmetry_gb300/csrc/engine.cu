@@ -8,6 +8,7 @@
 // work lists, so it is captured once as a CUDA graph and replayed.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -18,6 +19,7 @@
 #include "common.h"
 #include "kernels.h"
 #include "kernels_tc.h"
+#include "kernels_sc.h"
 
 namespace gwgb {
 
@@ -252,10 +254,7 @@ class Engine {
   void set_precision(int prec) {
     GWGB_REQUIRE(prec == GWGB_PREC_FP64 || prec == GWGB_PREC_TF32X3, GWGB_E_UNSUPPORTED,
                  "precision not implemented (FP64 and TF32X3 are)");
-    if (prec != prec_ && graph_exec_) {  // the captured graph holds the old kernels
-      cudaGraphExecDestroy(graph_exec_);
-      graph_exec_ = nullptr;
-    }
+    if (prec != prec_) drop_graphs();  // the captured graphs hold the old kernels
     prec_ = prec;
     if (prec_ == GWGB_PREC_TF32X3 && !Wbuf_.p && wbuf_elems_) {
       Wbuf_.alloc((size_t)wbuf_elems_);
@@ -287,6 +286,11 @@ class Engine {
   void solve();
   void dyson(double mu);
   void iteration(double mu);
+  void set_hcore(const double *H);
+  void set_energy_matrix(const double *M, int n);
+  void find_mu(const gwgb_mu_search &ms, double *mu_out, double *n_out);
+  void energy(double *e_corr, double *e_one);
+  void sc_loop(int niter, double alpha, const gwgb_mu_search &ms, int final_fp64, gwgb_sc_record *out);
   void stats(gwgb_stats *out) const { *out = stats_; }
   void synchronize() { GWGB_CUDA(cudaStreamSynchronize(st_)); check_device_flags(); }
   int device() const { return dev_; }
@@ -355,6 +359,32 @@ class Engine {
   int64_t g_rot_off_ = 0, p_rot_off_ = 0;  // start of the rotated parts
   double p0_flops_ = 0, sig_flops_ = 0;
   bool has_tct_ = false;
+  // self-consistent loop: mu search state, G(i w) scratch of the search, G(beta),
+  // previous Sigma, core H, Galitskii-Migdal weights and M G, records
+  DBuf<double2> Wg_, Gb_, Sold_, Hc_, Me_, Hm_;
+  DBuf<MuState> mus_;
+  DBuf<gwgb_sc_record> recs_;
+  DBuf<int> counter_;
+  DBuf<TrTask> tr_tasks_;
+  DBuf<TSlab> slab_e_;
+  bool have_H_ = false, have_M_ = false;
+  cudaGraphExec_t sc_exec_ = nullptr;
+  double sc_alpha_ = 0.0;
+  gwgb_mu_search sc_ms_{};
+  cudaEvent_t sc_ev_[2] = {nullptr, nullptr};
+  void drop_graphs() {
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (sc_exec_) cudaGraphExecDestroy(sc_exec_);
+    graph_exec_ = sc_exec_ = nullptr;
+  }
+  void check_mu_search(const gwgb_mu_search &ms) const;
+  void init_mu_state(const gwgb_mu_search &ms);
+  void k_mu_search(const gwgb_mu_search &ms);
+  void k_dyson_dev();
+  void k_energy_record(bool with_energy);
+  void k_sc_iteration(double alpha, const gwgb_mu_search &ms);
+  template <typename F> void capture(cudaGraphExec_t *exec, F &&body);
+  gwgb_sc_record read_record(int i);
   // graph
   cudaGraphExec_t graph_exec_ = nullptr;
   cudaEvent_t ev_[8];
@@ -430,6 +460,14 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
   mu_dev_.alloc(1);
   bad_.alloc(4);
   leak_.alloc(2);
+  Wg_.alloc((size_t)nw_ * ns_ * fa);
+  Gb_.alloc((size_t)ns_ * fa);
+  Sold_.alloc((size_t)nts_ * ns_ * fa);
+  Hm_.alloc((size_t)ncheb_ * ns_ * fa);
+  mus_.alloc(1);
+  counter_.alloc(1);
+  recs_.alloc(16);
+  for (auto &e : sc_ev_) GWGB_CUDA(cudaEventCreate(&e));
   GWGB_CUDA(cudaMemsetAsync(Gall_.p, 0, Gall_.n * sizeof(double2), st_));
   GWGB_CUDA(cudaMemsetAsync(Pall_.p, 0, Pall_.n * sizeof(double2), st_));
   GWGB_CUDA(cudaMemsetAsync(Sig_.p, 0, Sig_.n * sizeof(double2), st_));
@@ -439,8 +477,11 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
 
 Engine::~Engine() {
   if (st_) cudaStreamSynchronize(st_);
-  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  drop_graphs();
   for (auto &e : ev_) if (e) cudaEventDestroy(e);
+  for (auto &e : sc_ev_) if (e) cudaEventDestroy(e);
+  Wg_.free(); Gb_.free(); Sold_.free(); Hc_.free(); Me_.free(); Hm_.free();
+  mus_.free(); recs_.free(); counter_.free(); tr_tasks_.free(); slab_e_.free();
   if (mu_host_) cudaFreeHost(mu_host_);
   DBuf<double2> *bufs[] = {&V_, &Gall_, &Pall_, &Sig_, &Pw_, &Ww_, &F_, &S_, &orep_, &auxrep_,
                            &Tnt_, &Ttn_, &TntBF_, &TtnFB_};
@@ -822,6 +863,21 @@ void Engine::build_work_lists() {
   slab_p_bwd_.upload(pb, st_);
   slab_s_fwd_.upload(sf, st_);
   slab_g_bwd_.upload(gb, st_);
+  {  // traces over the stored k (weight = mesh k mapped to each) and the M G slabs
+    std::vector<double> wk(ink, 0.0);
+    for (int k = 0; k < nk; ++k) wk[l.irre_index[k]] += 1.0;
+    std::vector<TrTask> tt;
+    std::vector<TSlab> se;
+    for (int s = 0; s < ns_; ++s)
+      for (int ik = 0; ik < ink; ++ik) {
+        const int k = l.irre_list[ik];
+        const int64_t koff = s * fa + l.kao_off_irre[ik];
+        se.push_back({koff, koff, (int32_t)(ns_ * fa), (int32_t)(ns_ * fa), (int32_t)l.kao_sz[k], 0});
+        for (int b = 0; b < l.nao_blocks(k); ++b) tt.push_back({koff + l.aooff(k, b), l.aosz(k, b), 0, wk[ik]});
+      }
+    tr_tasks_.upload(tt, st_);
+    slab_e_.upload(se, st_);
+  }
   inv_w_.upload(iw, st_);
   inv_d_.upload(id, st_);
   qoff_irr_.upload(qo, st_);
@@ -862,6 +918,7 @@ void Engine::set_reps(const double *orep, int64_t no, const double *auxrep, int6
 void Engine::set_transforms(const double *Tnt, const double *Ttn, const double *TntBF, const double *TtnFB,
                             const int64_t *ws, const double *tf, const double *tl) {
   GWGB_REQUIRE(Tnt && Ttn && TntBF && TtnFB && ws, GWGB_E_INVALID, "transform matrices must not be NULL");
+  drop_graphs();  // the buffers below are reallocated
   Tnt_.alloc((size_t)nw_ * ncheb_);
   Ttn_.alloc((size_t)nts_ * nw_);
   TntBF_.alloc((size_t)nw_b_ * ncheb_);
@@ -1137,6 +1194,225 @@ void Engine::iteration(double mu) {
   finish_stats(true, true);
 }
 
+
+// ---------------------------------------------------------------------------
+// self-consistent loop (no counterpart in the reference; formulas in gwgb.h)
+// ---------------------------------------------------------------------------
+void Engine::set_hcore(const double *H) {
+  GWGB_REQUIRE(H, GWGB_E_INVALID, "NULL H");
+  if (!Hc_.p) Hc_.alloc((size_t)ns_ * l_.flat_ao);
+  h2d(Hc_.p, H, Hc_.n * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  if (!have_H_) drop_graphs();
+  have_H_ = true;
+}
+
+void Engine::set_energy_matrix(const double *M, int n) {
+  GWGB_REQUIRE(M, GWGB_E_INVALID, "NULL energy matrix");
+  GWGB_REQUIRE(n == ncheb_, GWGB_E_INVALID, "energy matrix must be (nts-2) x (nts-2)");
+  std::vector<double2> m((size_t)n * n);
+  for (size_t i = 0; i < m.size(); ++i) m[i] = make_double2(M[i], 0.0);
+  if (!Me_.p) Me_.alloc(m.size());
+  h2d(Me_.p, m.data(), m.size() * sizeof(double2), st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  if (!have_M_) drop_graphs();
+  have_M_ = true;
+}
+
+void Engine::check_mu_search(const gwgb_mu_search &ms) const {
+  GWGB_REQUIRE(ms.max_evals >= 2 && ms.max_evals <= 64, GWGB_E_INVALID, "max_evals must be in [2, 64]");
+  GWGB_REQUIRE(ms.step > 0.0 && std::isfinite(ms.step), GWGB_E_INVALID, "mu search step must be positive");
+  GWGB_REQUIRE(ms.tol > 0.0 && std::isfinite(ms.tol), GWGB_E_INVALID, "mu search tolerance must be positive");
+  GWGB_REQUIRE(std::isfinite(ms.mu0) && std::isfinite(ms.n_electrons), GWGB_E_INVALID, "mu0 and N must be finite");
+}
+
+void Engine::init_mu_state(const gwgb_mu_search &ms) {
+  MuState h{};
+  h.target = ms.n_electrons;
+  h.tol = ms.tol;
+  h.mu = h.best_mu = ms.mu0;
+  h.best_f = 1e300;
+  h2d(mus_.p, &h, sizeof(MuState), st_);
+  GWGB_CUDA(cudaMemsetAsync(counter_.p, 0, sizeof(int), st_));
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+
+// Ww_ holds Sigma(i w).  Ends with *mu_dev_ = the best mu found.
+void Engine::k_mu_search(const gwgb_mu_search &ms) {
+  const double nscale = -(2.0 / ns_) / l_.nk;
+  const int *done = reinterpret_cast<const int *>(reinterpret_cast<const char *>(mus_.p) + offsetof(MuState, done));
+  launch_mu_begin(mus_.p, mu_dev_.p, ms.step, st_);
+  for (int e = 0; e < ms.max_evals; ++e) {
+    launch_inverse(inv_d_.p, (int)inv_d_.n, l_.max_ao, Ww_.p, S_.p, F_.p, ws_.p, beta_, 0.0, 1, bad_.p + 1, st_,
+                   mu_dev_.p, Wg_.p, done);
+    // G(beta) only: the last row of Ttn
+    launch_transform(slab_g_bwd_.p, (int)slab_g_bwd_.n, max_cols_g_, Ttn_.p + (int64_t)(nts_ - 1) * nw_, 1, nw_, 0,
+                     Wg_.p, Gb_.p, st_);
+    launch_mu_update(tr_tasks_.p, (int)tr_tasks_.n, Gb_.p, S_.p, nscale, mus_.p, mu_dev_.p,
+                     e == ms.max_evals - 1, st_);
+  }
+}
+
+void Engine::k_dyson_dev() {
+  launch_inverse(inv_d_.p, (int)inv_d_.n, l_.max_ao, Ww_.p, S_.p, F_.p, ws_.p, beta_, 0.0, 1, bad_.p + 1, st_,
+                 mu_dev_.p);
+  launch_transform(slab_g_bwd_.p, (int)slab_g_bwd_.n, max_cols_g_, Ttn_.p, nts_, nw_, 0, Ww_.p, Gall_.p, st_);
+  if (has_tct_) {
+    GWGB_CUDA(cudaMemsetAsync(leak_.p, 0, 2 * sizeof(unsigned long long), st_));
+    launch_leakage(slab_g_bwd_.p, (int)slab_g_bwd_.n, Gall_.p, tct_f_.p, tct_l_.p, ncheb_, leak_.p, st_);
+  }
+}
+
+void Engine::k_energy_record(bool with_energy) {
+  if (with_energy)
+    launch_transform(slab_e_.p, (int)slab_e_.n, max_cols_g_, Me_.p, ncheb_, ncheb_, 1, Gall_.p, Hm_.p, st_);
+  EnergyArgs a{};
+  a.tasks = tr_tasks_.p;
+  a.ntasks = (int)tr_tasks_.n;
+  a.ncheb = ncheb_;
+  a.nts = nts_;
+  a.ldt = (int64_t)ns_ * l_.flat_ao;
+  a.sig = Sig_.p;
+  a.hm = Hm_.p;
+  a.g = Gall_.p;
+  a.f = F_.p;
+  a.hc = have_H_ ? Hc_.p : nullptr;
+  a.s = S_.p;
+  a.st = mus_.p;
+  a.leak = has_tct_ ? leak_.p : nullptr;
+  a.nscale = -(2.0 / ns_) / l_.nk;
+  a.ecorr_scale = -(1.0 / ns_) / l_.nk;
+  a.eone_scale = -(1.0 / ns_) / l_.nk;
+  a.precision = prec_;
+  a.with_energy = with_energy ? 1 : 0;
+  a.rec = recs_.p;
+  a.counter = counter_.p;
+  launch_energy_record(a, st_);
+}
+
+void Engine::k_sc_iteration(double alpha, const gwgb_mu_search &ms) {
+  k_rotate_G();
+  k_p0(1);
+  k_pq(false);
+  k_rotate_P();
+  k_sigma();
+  launch_mix(Sig_.p, Sold_.p, (int64_t)Sig_.n, alpha, st_);
+  launch_transform(slab_s_fwd_.p, (int)slab_s_fwd_.n, max_cols_g_, Tnt_.p, nw_, ncheb_, 1, Sig_.p, Ww_.p, st_);
+  k_mu_search(ms);
+  k_dyson_dev();
+  k_energy_record(have_M_);
+}
+
+template <typename F>
+void Engine::capture(cudaGraphExec_t *exec, F &&body) {
+  cudaGraph_t g = nullptr;
+  GWGB_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+  capturing_ = true;
+  try {
+    body();
+  } catch (...) {
+    capturing_ = false;
+    cudaGraph_t dead = nullptr;
+    cudaStreamEndCapture(st_, &dead);
+    if (dead) cudaGraphDestroy(dead);
+    throw;
+  }
+  capturing_ = false;
+  GWGB_CUDA(cudaStreamEndCapture(st_, &g));
+  const cudaError_t e = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  GWGB_CUDA(e);
+}
+
+gwgb_sc_record Engine::read_record(int i) {
+  gwgb_sc_record r{};
+  GWGB_CUDA(cudaMemcpy(&r, recs_.p + i, sizeof(r), cudaMemcpyDeviceToHost));
+  return r;
+}
+
+void Engine::find_mu(const gwgb_mu_search &ms, double *mu_out, double *n_out) {
+  GWGB_REQUIRE(have_T_, GWGB_E_STATE, "transform matrices have not been set");
+  GWGB_REQUIRE(have_F_, GWGB_E_STATE, "F and S have not been set");
+  check_mu_search(ms);
+  init_mu_state(ms);
+  record(5);
+  launch_transform(slab_s_fwd_.p, (int)slab_s_fwd_.n, max_cols_g_, Tnt_.p, nw_, ncheb_, 1, Sig_.p, Ww_.p, st_);
+  k_mu_search(ms);
+  k_dyson_dev();
+  k_energy_record(false);
+  record(6);
+  finish_stats(true, false);
+  const gwgb_sc_record r = read_record(0);
+  if (mu_out) *mu_out = r.mu;
+  if (n_out) *n_out = r.n_electrons;
+}
+
+void Engine::energy(double *e_corr, double *e_one) {
+  GWGB_REQUIRE(!e_corr || have_M_, GWGB_E_STATE, "the energy matrix has not been set");
+  GWGB_REQUIRE(!e_one || have_H_, GWGB_E_STATE, "the core Hamiltonian has not been set");
+  GWGB_REQUIRE(have_F_, GWGB_E_STATE, "F and S have not been set");
+  GWGB_CUDA(cudaMemsetAsync(counter_.p, 0, sizeof(int), st_));
+  k_energy_record(have_M_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  check_device_flags();
+  const gwgb_sc_record r = read_record(0);
+  if (e_corr) *e_corr = r.e_corr;
+  if (e_one) *e_one = r.e_one;
+}
+
+void Engine::sc_loop(int niter, double alpha, const gwgb_mu_search &ms, int final_fp64, gwgb_sc_record *out) {
+  require_ready(true);
+  GWGB_REQUIRE(have_F_, GWGB_E_STATE, "F and S have not been set");
+  GWGB_REQUIRE(out, GWGB_E_INVALID, "NULL record array");
+  GWGB_REQUIRE(niter >= 1 && niter <= 100000, GWGB_E_INVALID, "niter must be in [1, 100000]");
+  GWGB_REQUIRE(alpha > 0.0 && alpha <= 1.0, GWGB_E_INVALID, "mixing alpha must be in (0, 1]");
+  check_mu_search(ms);
+  if ((int)recs_.n < niter) {  // the graph records through recs_.p
+    drop_graphs();
+    recs_.alloc((size_t)niter);
+  }
+  init_mu_state(ms);
+  GWGB_CUDA(cudaMemcpyAsync(Sold_.p, Sig_.p, Sig_.n * sizeof(double2), cudaMemcpyDeviceToDevice, st_));
+  const bool same = sc_exec_ && alpha == sc_alpha_ && std::memcmp(&ms, &sc_ms_, sizeof(ms)) == 0;
+  if (!same && sc_exec_) {
+    cudaGraphExecDestroy(sc_exec_);
+    sc_exec_ = nullptr;
+  }
+  const int prec0 = prec_;
+  const int nmain = (final_fp64 && prec0 != GWGB_PREC_FP64) ? niter - 1 : niter;
+  GWGB_CUDA(cudaEventRecord(sc_ev_[0], st_));
+  if (nmain > 0) {
+    if (!sc_exec_) {
+      capture(&sc_exec_, [&] { k_sc_iteration(alpha, ms); });
+      sc_alpha_ = alpha;
+      sc_ms_ = ms;
+    }
+    for (int i = 0; i < nmain; ++i) GWGB_CUDA(cudaGraphLaunch(sc_exec_, st_));
+  }
+  if (nmain < niter) {  // the last iteration with the FP64 contractions
+    GWGB_CUDA(cudaStreamSynchronize(st_));
+    set_precision(GWGB_PREC_FP64);
+    capture(&sc_exec_, [&] { k_sc_iteration(alpha, ms); });
+    sc_alpha_ = alpha;
+    sc_ms_ = ms;
+    GWGB_CUDA(cudaGraphLaunch(sc_exec_, st_));
+    GWGB_CUDA(cudaStreamSynchronize(st_));
+    set_precision(prec0);
+  }
+  GWGB_CUDA(cudaEventRecord(sc_ev_[1], st_));
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  check_device_flags();
+  GWGB_CUDA(cudaMemcpy(out, recs_.p, (size_t)niter * sizeof(gwgb_sc_record), cudaMemcpyDeviceToHost));
+  float ms_total = 0;
+  GWGB_CUDA(cudaEventElapsedTime(&ms_total, sc_ev_[0], sc_ev_[1]));
+  gwgb_stats st{};
+  st.total_ms = ms_total / niter;
+  st.p0_flops = p0_flops_;
+  st.sigma_flops = sig_flops_;
+  st.leakage = out[niter - 1].leakage;
+  stats_ = st;
+}
+
 }  // namespace gwgb
 
 // ===========================================================================
@@ -1232,5 +1508,14 @@ GWGB_FORWARD(gwgb_dyson, (gwgb_handle h, double mu), e.dyson(mu))
 GWGB_FORWARD(gwgb_iteration, (gwgb_handle h, double mu), e.iteration(mu))
 GWGB_FORWARD(gwgb_get_stats, (gwgb_handle h, gwgb_stats *out), GWGB_REQUIRE(out, GWGB_E_INVALID, "NULL stats"); e.stats(out))
 GWGB_FORWARD(gwgb_synchronize, (gwgb_handle h), e.synchronize())
+GWGB_FORWARD(gwgb_set_hcore, (gwgb_handle h, const double *H), e.set_hcore(H))
+GWGB_FORWARD(gwgb_set_energy_matrix, (gwgb_handle h, const double *M, int32_t n), e.set_energy_matrix(M, n))
+GWGB_FORWARD(gwgb_find_mu, (gwgb_handle h, const gwgb_mu_search *ms, double *mu_out, double *n_out),
+             GWGB_REQUIRE(ms, GWGB_E_INVALID, "NULL mu search"); e.find_mu(*ms, mu_out, n_out))
+GWGB_FORWARD(gwgb_energy, (gwgb_handle h, double *e_corr, double *e_one), e.energy(e_corr, e_one))
+GWGB_FORWARD(gwgb_sc_loop,
+             (gwgb_handle h, int32_t niter, double alpha, const gwgb_mu_search *ms, int32_t final_fp64,
+              gwgb_sc_record *out),
+             GWGB_REQUIRE(ms, GWGB_E_INVALID, "NULL mu search"); e.sc_loop(niter, alpha, *ms, final_fp64, out))
 
 }  // extern "C"

@@ -44,9 +44,13 @@ void launch_zero_upper(double2 *P, const int64_t *qoff, const int32_t *qsz, int 
 void launch_transform(const TSlab *slabs, int nslabs, int max_cols, const double2 *T, int nout, int nin,
                       int row0, const double2 *X, double2 *Y, cudaStream_t st);
 
+// Batched block inverses.  mode 0: W~ (R = sym((1 - sym(P))^-1), R P); mode 1:
+// Dyson ((mu + i w_n) S - F - Sigma)^-1.  Optional: mu read from *mu_ptr,
+// output to Wout instead of in place, nothing done while *skip != 0.
 void launch_inverse(const InvTask *tasks, int ntasks, int nmax, double2 *W, const double2 *S,
                     const double2 *F, const int64_t *wsample, double beta, double mu, int mode, int *bad,
-                    cudaStream_t st);
+                    cudaStream_t st, const double *mu_ptr = nullptr, double2 *Wout = nullptr,
+                    const int *skip = nullptr);
 
 void launch_leakage(const TSlab *slabs, int nslabs, const double2 *G, const double *tf, const double *tl,
                     int ncheb, unsigned long long *out, cudaStream_t st);

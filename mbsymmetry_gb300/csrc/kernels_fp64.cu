@@ -355,7 +355,9 @@ __global__ void __launch_bounds__(256) transform_kernel(const TSlab *__restrict_
 __global__ void inverse_kernel(const InvTask *__restrict__ tasks, int ntasks, double2 *__restrict__ W,
                                const double2 *__restrict__ S, const double2 *__restrict__ F,
                                const int64_t *__restrict__ wsample, double beta, double mu, int mode,
-                               int *__restrict__ bad, int nm) {
+                               int *__restrict__ bad, int nm, const double *__restrict__ mu_ptr,
+                               double2 *__restrict__ Wout, const int *__restrict__ skip) {
+  if (skip && *skip) return;  // the mu search has converged (uniform over the grid)
   const int WPB = blockDim.x >> 5;
   extern __shared__ double2 smem_inv[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -378,6 +380,7 @@ __global__ void inverse_kernel(const InvTask *__restrict__ tasks, int ntasks, do
       A[e] = make_double2((i == j ? 1.0 : 0.0) - 0.5 * (pij.x + pji.x), -0.5 * (pij.y - pji.y));
     }
   } else {
+    if (mu_ptr) mu = *mu_ptr;
     const double wn = (2.0 * (double)wsample[tk.w] + 1.0) * 3.14159265358979323846 / beta;
     for (int e = lane; e < n * n; e += 32) {
       const double2 sv = S[tk.s + e], fv = F[tk.f + e], sg = g[e];
@@ -454,7 +457,8 @@ __global__ void inverse_kernel(const InvTask *__restrict__ tasks, int ntasks, do
     __syncwarp();
   }
   if (mode == 1) {
-    for (int e = lane; e < n * n; e += 32) g[e] = A[e];
+    double2 *o = Wout ? Wout + tk.a : g;
+    for (int e = lane; e < n * n; e += 32) o[e] = A[e];
     return;
   }
   // R = (A^-1 + A^-H)/2, each unordered pair by one lane
@@ -564,11 +568,11 @@ void launch_transform(const TSlab *slabs, int nslabs, int max_cols, const double
 
 void launch_inverse(const InvTask *tasks, int ntasks, int nmax, double2 *W, const double2 *S,
                     const double2 *F, const int64_t *wsample, double beta, double mu, int mode, int *bad,
-                    cudaStream_t st) {
+                    cudaStream_t st, const double *mu_ptr, double2 *Wout, const int *skip) {
   if (ntasks == 0) return;
   const int w = inv_warps_per_block(nmax);
-  inverse_kernel<<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(nmax), st>>>(tasks, ntasks, W, S, F, wsample,
-                                                                           beta, mu, mode, bad, nmax);
+  inverse_kernel<<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(nmax), st>>>(
+      tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad, nmax, mu_ptr, Wout, skip);
   GWGB_CUDA(cudaGetLastError());
 }
 

@@ -21,7 +21,7 @@ import numpy as np
 
 from . import _abi
 from .layout import BlockLayout
-from .transformer import IRTransforms
+from .transformer import IRTransforms, gm_matrix
 
 
 def _ptr(a: np.ndarray):
@@ -52,6 +52,8 @@ class GWSolver:
         _abi.check(self.lib.gwgb_set_transforms(
             self.h, _ptr(transforms.Tnt), _ptr(transforms.Ttn), _ptr(transforms.Tnt_BF), _ptr(transforms.Ttn_FB),
             _ptr(transforms.wsample_fermi), _ptr(tf), _ptr(tl)))
+        M = gm_matrix(transforms)
+        _abi.check(self.lib.gwgb_set_energy_matrix(self.h, _ptr(M), M.shape[0]))
 
     def close(self):
         if getattr(self, "h", None):
@@ -132,6 +134,40 @@ class GWSolver:
 
     def iteration(self, mu: float):
         _abi.check(self.lib.gwgb_iteration(self.h, float(mu)))
+
+    # -- self-consistent loop (not in the reference; see include/gwgb.h) -------
+    def set_hcore(self, H: np.ndarray):
+        H = np.ascontiguousarray(H, dtype=np.complex128)
+        _abi.check(self.lib.gwgb_set_hcore(self.h, _ptr(H)))
+
+    @staticmethod
+    def _mu_search(n_electrons, mu0, step, tol, max_evals):
+        return _abi.GwgbMuSearch(n_electrons=float(n_electrons), mu0=float(mu0), step=float(step),
+                                 tol=float(tol), max_evals=int(max_evals), pad=0)
+
+    def find_mu(self, n_electrons: float, mu0: float, step: float = 0.05, tol: float = 1e-10,
+                max_evals: int = 32):
+        """Dyson with a device-side mu search; returns (mu, N(mu))."""
+        ms = self._mu_search(n_electrons, mu0, step, tol, max_evals)
+        mu, n = ctypes.c_double(), ctypes.c_double()
+        _abi.check(self.lib.gwgb_find_mu(self.h, ctypes.byref(ms), ctypes.byref(mu), ctypes.byref(n)))
+        return mu.value, n.value
+
+    def energy(self, with_one_body: bool = False):
+        """(E_corr, E_one) of the resident Sigma and G (E_one needs set_hcore)."""
+        ec, eo = ctypes.c_double(), ctypes.c_double()
+        _abi.check(self.lib.gwgb_energy(self.h, ctypes.byref(ec), ctypes.byref(eo) if with_one_body else None))
+        return ec.value, (eo.value if with_one_body else None)
+
+    def sc_loop(self, niter: int, alpha: float, n_electrons: float, mu0: float, step: float = 0.05,
+                tol: float = 1e-10, max_evals: int = 32, final_fp64: bool = False) -> list:
+        """niter self-consistent GW iterations (one CUDA graph launch each);
+        one dict per iteration: mu, n_electrons, e_corr, e_one, leakage, mu_evals, precision."""
+        ms = self._mu_search(n_electrons, mu0, step, tol, max_evals)
+        recs = (_abi.GwgbScRecord * niter)()
+        _abi.check(self.lib.gwgb_sc_loop(self.h, int(niter), float(alpha), ctypes.byref(ms),
+                                         1 if final_fp64 else 0, recs))
+        return [{name: getattr(r, name) for name, _ in _abi.GwgbScRecord._fields_} for r in recs]
 
     def synchronize(self):
         _abi.check(self.lib.gwgb_synchronize(self.h))

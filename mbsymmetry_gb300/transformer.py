@@ -101,6 +101,21 @@ def build_transforms(ir: Dict[str, np.ndarray], beta: float) -> IRTransforms:
     )
 
 
+def gm_matrix(tr: IRTransforms) -> np.ndarray:
+    """Interior-tau quadrature M of the Galitskii-Migdal integral:
+
+        int_0^beta A(tau) B(beta - tau) dtau = sum_ij M_ij A(tau_i) B(tau_j)
+
+    for fermionic A, B represented in the IR basis.  With a_l = sum_i C_li
+    A(tau_i) (C = ``Tct``, the scaled fit onto u_l(tau), orthonormal on
+    [0, beta]) and the parity u_l(beta - tau) = (-1)^l u_l(tau),
+    the integral is sum_l (-1)^l a_l b_l, so M = C^T diag((-1)^l) C.
+    Returns an (nts-2) x (nts-2) float64 array."""
+    C = np.asarray(tr.Tct, dtype=np.float64)
+    sign = np.where(np.arange(C.shape[0]) % 2 == 0, 1.0, -1.0)
+    return np.ascontiguousarray(C.T @ (sign[:, None] * C))
+
+
 def read_ir_file(path: str) -> Dict[str, np.ndarray]:
     """Read the IR sampling fields of a reference IR grid file (e.g. ``1e3_72.h5``)."""
     from .h5lite import H5File

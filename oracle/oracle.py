@@ -162,3 +162,98 @@ class Oracle:
         Sigma, P0, P = self.gw_sigma(G_irr, V, tr)
         G, leak = self.dyson(Sigma, F, S, tr, mu)
         return G, Sigma, P0, P, leak
+
+    # -- self-consistent loop: electron count, energies, mu search, mixing -- #
+    # Not in the reference (sc_loop_block_t keeps mu fixed, never assigns its
+    # energy and does not iterate); these restate the formulas of the engine's
+    # loop with dense numpy traces, independently of its block-wise kernels.
+    def k_weights(self):
+        """Mesh k points mapped to each stored k."""
+        L = self.layout
+        return np.bincount(L.irre_index, minlength=L.ink).astype(np.float64)
+
+    def _trace(self, A, B):
+        """sum_{s,k} w_k Re Tr[A_k,s B_k,s] for two [ns][flat_ao] arrays."""
+        L = self.layout
+        fa = L.flat_ao_size
+        Ab = L.G_flat_to_block(np.asarray(A).reshape(self.ns, fa))
+        Bb = L.G_flat_to_block(np.asarray(B).reshape(self.ns, fa))
+        t = np.einsum("skab,skba->sk", Ab, Bb).real
+        return float((t * self.k_weights()[None, :]).sum())
+
+    def n_electrons(self, G, S):
+        """N = -(2/ns)/nk sum_{s,k} Re Tr[G(beta) S]."""
+        L = self.layout
+        Gb = np.asarray(G).reshape(self.nts, self.ns * L.flat_ao_size)[-1]
+        return -(2.0 / self.ns) / L.nk * self._trace(Gb, S)
+
+    def energy(self, Sigma, G, F, S, M, H=None):
+        """(E_corr, E_one, N): Galitskii-Migdal energy with the interior-tau
+        weights M, the one-body energy (with H) and the electron count."""
+        L = self.layout
+        nf = self.ns * L.flat_ao_size
+        Sg = np.asarray(Sigma).reshape(self.nts, nf)
+        Gt = np.asarray(G).reshape(self.nts, nf)
+        MG = np.asarray(M) @ Gt[1:-1]
+        ec = sum(self._trace(Sg[1 + i], MG[i]) for i in range(self.nts - 2))
+        ec *= -(1.0 / self.ns) / L.nk
+        eo = 0.0
+        if H is not None:
+            eo = -(1.0 / self.ns) / L.nk * (self._trace(Gt[-1], H) + self._trace(Gt[-1], F))
+        return ec, eo, self.n_electrons(G, S)
+
+    def find_mu(self, Sigma, F, S, tr, n_target, mu0, step=0.05, tol=1e-12, maxit=400):
+        """Bracket, then bisect N(mu) = n_target.  Returns (mu, G, leakage)."""
+        def f(mu):
+            G, leak = self.dyson(Sigma, F, S, tr, mu)
+            return self.n_electrons(G, S) - n_target, G, leak
+
+        f0, G0, l0 = f(mu0)
+        if abs(f0) <= tol:
+            return mu0, G0, l0
+        lo = hi = mu0
+        flo = fhi = f0
+        d = step
+        while flo > 0:
+            hi, fhi = lo, flo
+            lo -= d
+            d *= 2
+            flo = f(lo)[0]
+        while fhi < 0:
+            lo, flo = hi, fhi
+            hi += d
+            d *= 2
+            fhi = f(hi)[0]
+        best = (abs(f0), mu0, G0, l0)
+        for _ in range(maxit):
+            mid = 0.5 * (lo + hi)
+            fm, Gm, lm = f(mid)
+            if abs(fm) < best[0]:
+                best = (abs(fm), mid, Gm, lm)
+            if abs(fm) <= tol or hi - lo < 1e-15 * max(1.0, abs(mid)):
+                break
+            if fm < 0:
+                lo = mid
+            else:
+                hi = mid
+        return best[1], best[2], best[3]
+
+    def sc_loop(self, G, Sigma, V, F, S, tr, M, niter, alpha, n_target, mu0, H=None, mus=None):
+        """niter iterations: Sigma_new = GW(G); Sigma = alpha Sigma_new +
+        (1 - alpha) Sigma_old; mu from N(mu) = n_target (or mus[it] when
+        given); G = Dyson(Sigma, mu); energies.  Returns (G, Sigma, records)."""
+        Sold = np.asarray(Sigma, dtype=np.complex128).copy()
+        mu = mu0
+        recs = []
+        for it in range(niter):
+            Snew, _, _ = self.gw_sigma(G, V, tr)
+            Sig = alpha * Snew + (1.0 - alpha) * Sold
+            Sold = Sig
+            if mus is not None:
+                mu = mus[it]
+                G, leak = self.dyson(Sig, F, S, tr, mu)
+            else:
+                mu, G, leak = self.find_mu(Sig, F, S, tr, n_target, mu)
+            ec, eo, n = self.energy(Sig, G, F, S, M, H)
+            recs.append({"mu": mu, "n_electrons": n, "e_corr": ec, "e_one": eo, "leakage": leak})
+        return G, Sold, recs
