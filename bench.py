@@ -300,6 +300,29 @@ def run_gpu(args):
 
     # replicas: every rank runs the whole iteration, so the job completes `world`
     # iterations per max-over-ranks time
+    # ---- self-consistent loop: 10 graph-launched iterations, alpha = 0.5 ----
+    # Each iteration: GW Sigma, linear mixing, device-side mu search (half
+    # filling, N = nao), Dyson, energies.  FP64 throughout, and TF32x3 with the
+    # last iteration in FP64; the final Sigma / energy of the two are compared.
+    zeros = np.zeros(s.g_size, np.complex128)
+    sc = {"iterations": 10, "alpha": 0.5, "n_electrons": float(L.nao),
+          "note": "graph launches back to back (no L2 flush between iterations)"}
+    finals = {}
+    for label, prec, final in (("fp64", "fp64", False), ("tf32x3_final_fp64", "tf32x3", True)):
+        s.single_prec_run(prec != "fp64", "tf32x3")
+        s.set_G(G0)
+        s.set_Selfenergy(zeros)
+        recs = s.sc_loop(10, 0.5, float(L.nao), cr.mu, step=0.05, tol=1e-10, max_evals=24, final_fp64=final)
+        stl = s.stats()
+        finals[label] = (s.Selfenergy(), recs[-1])
+        sc[label] = {"s_per_iteration": stl["total_ms"] / 1e3, "mu": [r["mu"] for r in recs],
+                     "e_corr": [r["e_corr"] for r in recs], "mu_evals": [r["mu_evals"] for r in recs],
+                     "n_final": recs[-1]["n_electrons"], "leakage_final": recs[-1]["leakage"]}
+    s.single_prec_run(False)
+    sc["final_sigma_max_abs_diff"] = float(np.abs(finals["fp64"][0] - finals["tf32x3_final_fp64"][0]).max())
+    sc["final_e_corr_diff"] = abs(finals["fp64"][1]["e_corr"] - finals["tf32x3_final_fp64"][1]["e_corr"])
+    sc["speedup"] = sc["fp64"]["s_per_iteration"] / sc["tf32x3_final_fp64"]["s_per_iteration"]
+
     line = {
         "metric": METRIC, "value": ms / 1e3 / world, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
@@ -314,6 +337,7 @@ def run_gpu(args):
         "roofline": roofline,
         "clocks": clocks.summary(),
         "mixed": mixed,
+        "sc_loop": sc,
         "peaks": {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops"),
                   "fp64_tflops_measured": fp64_peak},
     }
@@ -328,8 +352,9 @@ def run_gpu(args):
 
 
 def run_profile(args):
-    """One FP64 and one TF32x3 iteration of the workload and nothing else: the
-    command that ncu captures (a plain run of it must exit 0 first)."""
+    """One FP64 and one TF32x3 iteration of the workload, then two FP64
+    self-consistent iterations: the command that ncu captures (a plain run of
+    it must exit 0 first)."""
     import torch
     from mbsymmetry_gb300.solver import GWSolver
     torch.cuda.set_device(0)
@@ -345,8 +370,13 @@ def run_profile(args):
     s.set_G(G0)
     s.iteration(cr.mu)
     st = s.stats()
+    s.single_prec_run(False)
+    s.set_G(G0)
+    s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+    s.sc_loop(2, 0.5, float(cr.layout.nao), cr.mu, step=0.05, tol=1e-10, max_evals=24)
     s.close()
-    print(f"profile run: {CONFIG}, one FP64 and one TF32x3 iteration (last {st['total_ms']:.2f} ms)")
+    print(f"profile run: {CONFIG}, one FP64 and one TF32x3 iteration (last {st['total_ms']:.2f} ms), "
+          "then two FP64 self-consistent iterations")
 
 
 def main():
@@ -357,7 +387,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
-                    help="run one FP64 and one TF32x3 iteration only (the command for ncu captures)")
+                    help="one FP64 and one TF32x3 iteration and two self-consistent iterations only "
+                         "(the command for ncu captures)")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

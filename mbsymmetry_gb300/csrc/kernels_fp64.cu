@@ -294,48 +294,50 @@ __global__ void zero_upper_kernel(double2 *__restrict__ P, const int64_t *__rest
 // ---------------------------------------------------------------------------
 // tau <-> omega transform (transformer_t.h:66-99, 226-308):
 //   Y[slab][r][c] = sum_i T[r][i] X[slab][row0 + i][c],  r < nout, i < nin.
-// 256 threads = 32 columns x 8 row groups; T staged through shared memory in
-// 32-column chunks; each thread keeps up to 20 output rows in registers.
+// One CTA = 32 columns x 8R output rows (R per warp, rows r0 + warp*R + j),
+// grid = (slab, column tile, row tile).  The T rows of the tile are staged
+// through shared memory in 32-wide chunks of i.  Warps whose rows all lie
+// beyond nout skip the arithmetic (the FP64 pipe is the bound).
 // ---------------------------------------------------------------------------
-constexpr int TR_MAXR = 20;  // nout <= 8 * TR_MAXR = 160
+constexpr int TR_MAXOUT = 160;  // nout limit of the engine's grids
+template <int R>
 __global__ void __launch_bounds__(256) transform_kernel(const TSlab *__restrict__ slabs,
                                                         const double2 *__restrict__ T, int nout,
                                                         int nin, int row0,
                                                         const double2 *__restrict__ X,
                                                         double2 *__restrict__ Y) {
-  extern __shared__ double2 Ts[];  // [nout][33]
+  __shared__ double2 Ts[8 * R][33];
   const TSlab sl = slabs[blockIdx.x];
-  const int cl = threadIdx.x & 31, rg = threadIdx.x >> 5;
+  const int cl = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int c = blockIdx.y * 32 + cl;
-  const bool active = c < sl.ncols;
-  double2 acc[TR_MAXR];
+  const int r0 = blockIdx.z * 8 * R;
+  const int nr = min(8 * R, nout - r0);
+  const bool active = c < sl.ncols && w * R < nr;
+  double2 acc[R];
 #pragma unroll
-  for (int r = 0; r < TR_MAXR; ++r) acc[r] = make_double2(0.0, 0.0);
+  for (int j = 0; j < R; ++j) acc[j] = make_double2(0.0, 0.0);
   const double2 *x = X + sl.x + (int64_t)row0 * sl.ldx + c;
   for (int i0 = 0; i0 < nin; i0 += 32) {
     const int ni = (nin - i0) < 32 ? (nin - i0) : 32;
     __syncthreads();
-    for (int e = threadIdx.x; e < nout * 32; e += 256) {
+    for (int e = threadIdx.x; e < nr * 32; e += 256) {
       const int r = e >> 5, ii = e & 31;
-      Ts[r * 33 + ii] = (ii < ni) ? T[(int64_t)r * nin + i0 + ii] : make_double2(0.0, 0.0);
+      Ts[r][ii] = (ii < ni) ? T[(int64_t)(r0 + r) * nin + i0 + ii] : make_double2(0.0, 0.0);
     }
     __syncthreads();
     if (active) {
       for (int ii = 0; ii < ni; ++ii) {
         const double2 xv = x[(int64_t)(i0 + ii) * sl.ldx];
 #pragma unroll
-        for (int r = 0; r < TR_MAXR; ++r) {
-          const int rr = rg + 8 * r;
-          if (rr < nout) acc[r] = cfma(Ts[rr * 33 + ii], xv, acc[r]);
-        }
+        for (int j = 0; j < R; ++j) acc[j] = cfma(Ts[w * R + j][ii], xv, acc[j]);
       }
     }
   }
   if (active) {
 #pragma unroll
-    for (int r = 0; r < TR_MAXR; ++r) {
-      const int rr = rg + 8 * r;
-      if (rr < nout) Y[sl.y + (int64_t)rr * sl.ldy + c] = acc[r];
+    for (int j = 0; j < R; ++j) {
+      const int rl = w * R + j;
+      if (rl < nr) Y[sl.y + (int64_t)(r0 + rl) * sl.ldy + c] = acc[j];
     }
   }
 }
@@ -479,6 +481,150 @@ __global__ void inverse_kernel(const InvTask *__restrict__ tasks, int ntasks, do
   }
 }
 
+// Same Gauss-Jordan inverse with one CTA per block (blocks larger than 16):
+// the pivot search, the row scaling and the elimination run over all n^2
+// elements with the same per-element arithmetic and the same pivot order as
+// inverse_kernel.  Shared: A [n^2] | B [n^2] | fcol [n] (complex) | 3n ints.
+constexpr int INV_CTA_THREADS = 128;
+__host__ __device__ constexpr int inv_cta_smem_bytes(int n) { return (2 * n * n + n) * 16 + 3 * n * 4 + 64; }
+
+__global__ void __launch_bounds__(INV_CTA_THREADS) inverse_cta_kernel(
+    const InvTask *__restrict__ tasks, double2 *__restrict__ W, const double2 *__restrict__ S,
+    const double2 *__restrict__ F, const int64_t *__restrict__ wsample, double beta, double mu, int mode,
+    int *__restrict__ bad, int nm, const double *__restrict__ mu_ptr, double2 *__restrict__ Wout,
+    const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  constexpr int NT = INV_CTA_THREADS, NW = NT / 32;
+  extern __shared__ double2 smem_inv[];
+  __shared__ double red_best[NW];
+  __shared__ int red_idx[NW];
+  __shared__ int piv[3];  // irow, icol, singular
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const InvTask tk = tasks[blockIdx.x];
+  const int n = tk.n;
+  double2 *A = smem_inv;
+  double2 *B = A + nm * nm;
+  double2 *fcol = B + nm * nm;
+  int *ipiv = reinterpret_cast<int *>(fcol + nm);
+  int *indxr = ipiv + nm;
+  int *indxc = indxr + nm;
+  double2 *g = W + tk.a;
+  if (mode == 0) {
+    for (int e = tid; e < n * n; e += NT) B[e] = g[e];
+    __syncthreads();
+    for (int e = tid; e < n * n; e += NT) {
+      const int i = e / n, j = e - i * n;
+      const double2 pij = B[e], pji = B[j * n + i];
+      A[e] = make_double2((i == j ? 1.0 : 0.0) - 0.5 * (pij.x + pji.x), -0.5 * (pij.y - pji.y));
+    }
+  } else {
+    if (mu_ptr) mu = *mu_ptr;
+    const double wn = (2.0 * (double)wsample[tk.w] + 1.0) * 3.14159265358979323846 / beta;
+    for (int e = tid; e < n * n; e += NT) {
+      const double2 sv = S[tk.s + e], fv = F[tk.f + e], sg = g[e];
+      A[e] = make_double2(mu * sv.x - wn * sv.y - fv.x - sg.x, mu * sv.y + wn * sv.x - fv.y - sg.y);
+    }
+  }
+  for (int j = tid; j < n; j += NT) ipiv[j] = 0;
+  __syncthreads();
+  for (int it = 0; it < n; ++it) {
+    double best = -1.0;
+    int bidx = 0x7fffffff;
+    for (int e = tid; e < n * n; e += NT) {
+      const int j = e / n, k = e - j * n;
+      if (ipiv[j] == 1 || ipiv[k] != 0) continue;
+      const double2 v = A[e];
+      const double av = v.x * v.x + v.y * v.y;
+      if (av > best || (av == best && e < bidx)) { best = av; bidx = e; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, off);
+      const int oi = __shfl_down_sync(0xffffffffu, bidx, off);
+      if (ob > best || (ob == best && oi < bidx)) { best = ob; bidx = oi; }
+    }
+    if (lane == 0) { red_best[warp] = best; red_idx[warp] = bidx; }
+    __syncthreads();
+    if (tid == 0) {
+      double b = red_best[0];
+      int bi = red_idx[0];
+      for (int w = 1; w < NW; ++w)
+        if (red_best[w] > b || (red_best[w] == b && red_idx[w] < bi)) { b = red_best[w]; bi = red_idx[w]; }
+      if (!(b > 0.0)) {
+        piv[2] = 1;
+      } else {
+        const int irow = bi / n, icol = bi - irow * n;
+        piv[0] = irow; piv[1] = icol; piv[2] = 0;
+        ipiv[icol] += 1; indxr[it] = irow; indxc[it] = icol;
+      }
+    }
+    __syncthreads();
+    if (piv[2]) break;
+    const int irow = piv[0], icol = piv[1];
+    if (irow != icol) {
+      for (int l = tid; l < n; l += NT) {
+        const double2 t = A[irow * n + l];
+        A[irow * n + l] = A[icol * n + l];
+        A[icol * n + l] = t;
+      }
+      __syncthreads();
+    }
+    const double2 pv = A[icol * n + icol];
+    const double den = pv.x * pv.x + pv.y * pv.y;
+    const double2 pinv = make_double2(pv.x / den, -pv.y / den);
+    __syncthreads();
+    for (int l = tid; l < n; l += NT) {
+      const double2 v = (l == icol) ? make_double2(1.0, 0.0) : A[icol * n + l];
+      A[icol * n + l] = cmul(v, pinv);
+    }
+    for (int ll = tid; ll < n; ll += NT) fcol[ll] = A[ll * n + icol];
+    __syncthreads();
+    for (int e = tid; e < n * n; e += NT) {
+      const int ll = e / n, l = e - ll * n;
+      if (ll == icol) continue;
+      const double2 f = fcol[ll];
+      const double2 r = A[icol * n + l];
+      const double2 a = (l == icol) ? make_double2(0.0, 0.0) : A[e];
+      A[e] = make_double2(a.x - (r.x * f.x - r.y * f.y), a.y - (r.x * f.y + r.y * f.x));
+    }
+    __syncthreads();
+  }
+  if (piv[2]) {
+    if (tid == 0) atomicExch(bad, 1);
+    return;
+  }
+  for (int l = n - 1; l >= 0; --l) {
+    const int r = indxr[l], c = indxc[l];
+    if (r != c) {
+      for (int k = tid; k < n; k += NT) {
+        const double2 t = A[k * n + r];
+        A[k * n + r] = A[k * n + c];
+        A[k * n + c] = t;
+      }
+      __syncthreads();
+    }
+  }
+  if (mode == 1) {
+    double2 *o = Wout ? Wout + tk.a : g;
+    for (int e = tid; e < n * n; e += NT) o[e] = A[e];
+    return;
+  }
+  for (int e = tid; e < n * n; e += NT) {
+    const int i = e / n, j = e - i * n;
+    if (j < i) continue;
+    const double2 aij = A[e], aji = A[j * n + i];
+    const double2 r = make_double2(0.5 * (aij.x + aji.x), 0.5 * (aij.y - aji.y));
+    A[e] = r;
+    A[j * n + i] = cconj(r);
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += NT) {
+    const int i = e / n, j = e - i * n;
+    double2 a = make_double2(0.0, 0.0);
+    for (int l = 0; l < n; ++l) a = cfma(A[i * n + l], B[l * n + j], a);
+    g[e] = a;
+  }
+}
+
 // Leakage check of G (sc_type_block.cpp:66-71): max over elements of
 // |sum_t tct[t] G(tau_{t+1})| for the first and last IR coefficient.
 __global__ void leakage_kernel(const TSlab *__restrict__ slabs, const double2 *__restrict__ G,
@@ -561,8 +707,18 @@ void launch_zero_upper(double2 *P, const int64_t *qoff, const int32_t *qsz, int 
 
 void launch_transform(const TSlab *slabs, int nslabs, int max_cols, const double2 *T, int nout, int nin,
                       int row0, const double2 *X, double2 *Y, cudaStream_t st) {
-  if (nslabs == 0) return;
-  transform_kernel<<<dim3(nslabs, (max_cols + 31) / 32), 256, (size_t)nout * 33 * sizeof(double2), st>>>(slabs, T, nout, nin, row0, X, Y);
+  if (nslabs == 0 || nout == 0) return;
+  GWGB_REQUIRE(nout <= TR_MAXOUT, GWGB_E_UNSUPPORTED, "transform output longer than 160 rows");
+  const int ct = (max_cols + 31) / 32;
+  // the largest rows-per-warp that still gives about two CTAs per SM
+  auto ctas = [&](int R) { return (int64_t)nslabs * ct * ((nout + 8 * R - 1) / (8 * R)); };
+  if (nout > 8 && ctas(4) >= 304) {
+    transform_kernel<4><<<dim3(nslabs, ct, (nout + 31) / 32), 256, 0, st>>>(slabs, T, nout, nin, row0, X, Y);
+  } else if (nout > 8 && ctas(2) >= 304) {
+    transform_kernel<2><<<dim3(nslabs, ct, (nout + 15) / 16), 256, 0, st>>>(slabs, T, nout, nin, row0, X, Y);
+  } else {
+    transform_kernel<1><<<dim3(nslabs, ct, (nout + 7) / 8), 256, 0, st>>>(slabs, T, nout, nin, row0, X, Y);
+  }
   GWGB_CUDA(cudaGetLastError());
 }
 
@@ -570,9 +726,14 @@ void launch_inverse(const InvTask *tasks, int ntasks, int nmax, double2 *W, cons
                     const double2 *F, const int64_t *wsample, double beta, double mu, int mode, int *bad,
                     cudaStream_t st, const double *mu_ptr, double2 *Wout, const int *skip) {
   if (ntasks == 0) return;
-  const int w = inv_warps_per_block(nmax);
-  inverse_kernel<<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(nmax), st>>>(
-      tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad, nmax, mu_ptr, Wout, skip);
+  if (nmax > 16) {  // one CTA per block
+    inverse_cta_kernel<<<ntasks, INV_CTA_THREADS, inv_cta_smem_bytes(nmax), st>>>(
+        tasks, W, S, F, wsample, beta, mu, mode, bad, nmax, mu_ptr, Wout, skip);
+  } else {          // one warp per block
+    const int w = inv_warps_per_block(nmax);
+    inverse_kernel<<<(ntasks + w - 1) / w, 32 * w, inv_smem_bytes(nmax), st>>>(
+        tasks, ntasks, W, S, F, wsample, beta, mu, mode, bad, nmax, mu_ptr, Wout, skip);
+  }
   GWGB_CUDA(cudaGetLastError());
 }
 
@@ -589,8 +750,9 @@ void set_fp64_kernel_attributes(int smem_bytes) {
   GWGB_CUDA(cudaFuncSetAttribute(sigma_fp64_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(sigma_fp64_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(rotate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rotate_smem_bytes(MAX_BLOCK)));
-  GWGB_CUDA(cudaFuncSetAttribute(transform_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * TR_MAXR * 33 * (int)sizeof(double2)));
   GWGB_CUDA(cudaFuncSetAttribute(inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, inv_smem_bytes(MAX_BLOCK)));
+  GWGB_CUDA(cudaFuncSetAttribute(inverse_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 inv_cta_smem_bytes(MAX_BLOCK)));
 }
 
 }  // namespace gwgb
