@@ -317,7 +317,7 @@ class Engine {
   // work lists
   DBuf<P0Tile> p0_tiles_;              // FP64: (block, tau range, contribution slice)
   DBuf<P0Contrib> p0_contribs_;
-  DBuf<SigTile> sig_tiles_, sig_tiles1_;  // FP64 slices / one tau per tile (tcgen05 path)
+  DBuf<SigTile> sig_tiles_, sig_tiles1_;  // FP64 slices / (owner, tau range) tiles of the tcgen05 path
   DBuf<RedTask> p0_red_, sig_red_;       // FP64: ordered sums of the slices
   DBuf<double2> Part_;                   // FP64: partial sums of the slices
   DBuf<SigContrib> sig_contribs_;
@@ -680,7 +680,7 @@ void Engine::build_work_lists() {
   std::vector<SigContrib> sc;
   std::vector<double> scost;  // flops per contribution and tau
   std::vector<Owner> sig_own;
-  std::vector<SigTile> stl;   // one tile per (owner, tau): the tcgen05 path
+  std::vector<SigTile> stl;   // (owner, tau range) tiles of the tcgen05 path
   sig_flops_ = 0;
   for (int ik = 0; ik < ink; ++ik) {
     const int k1 = l.irre_list[ik];
@@ -709,16 +709,24 @@ void Engine::build_work_lists() {
       for (int s = 0; s < ns_; ++s) {
         const int64_t out = (int64_t)s * fa + l.kao_off_irre[ik] + l.aooff(k1, i1);
         sig_own.push_back({out, (int32_t)(ns_ * fa), b1, c0, c1, 2 * qbmax * b1, s});
-        double f = 0;
-        for (int c = c0; c < c1; ++c) f += scost[c];
-        for (int t = 0; t < nts_; ++t)
-          stl.push_back({out, 0, (int32_t)(ns_ * fa), b1, c0, c1, t, 1, s, (int32_t)std::min(f / 1e3, 2e9)});
       }
     }
   }
   sig_contribs_.upload(sc, st_);
-  std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
-  sig_tiles1_.upload(stl, st_);
+  {  // tcgen05 path, U/Sigma stage: (owner, range of nt tau) tiles, about six waves of two CTAs per SM
+    const int nt_uv = std::max(1, std::min(8, (int)((int64_t)sig_own.size() * nts_ / (12 * std::max(1, nsm_)))));
+    for (const Owner &o : sig_own) {
+      int nt = std::max(1, std::min(nt_uv, (smem_bytes_ / 2) / (24 * o.n * o.n)));
+      double f = 0;
+      for (int c = o.c0; c < o.c1; ++c) f += scost[c];
+      for (int t0 = 0; t0 < nts_; t0 += nt) {
+        const int n = std::min(nt, nts_ - t0);
+        stl.push_back({o.out, 0, o.ostride, o.n, o.c0, o.c1, t0, n, o.s, (int32_t)std::min(f * n / 1e3, 2e9)});
+      }
+    }
+    std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
+    sig_tiles1_.upload(stl, st_);
+  }
 
   // --- FP64 tiles of both contractions and their partial-sum buffer
   {
@@ -812,8 +820,9 @@ void Engine::build_work_lists() {
     for (const SigTile &t : stl) {
       int b2max = 1, qbmax = 1;
       for (int c = t.c0; c < t.c1; ++c) { b2max = std::max(b2max, sc[c].b2); qbmax = std::max(qbmax, sc[c].qb); }
-      uvneed = std::max(uvneed, 24 * t.b1 * t.b1 + 8 * b2max * b2max + 24 * t.b1 * b2max * qbmax);
-      GWGB_REQUIRE(24 * t.b1 * t.b1 + 8 * b2max * b2max + 24 * t.b1 * b2max <= smem_bytes_, GWGB_E_UNSUPPORTED,
+      const int fixed = 24 * t.nt * t.b1 * t.b1 + 8 * b2max * b2max;
+      uvneed = std::max(uvneed, fixed + 24 * t.b1 * b2max * qbmax);
+      GWGB_REQUIRE(fixed + 24 * t.b1 * b2max <= smem_bytes_, GWGB_E_UNSUPPORTED,
                    "Sigma block too large for the tcgen05 path");
     }
     std::stable_sort(swt.begin(), swt.end(), [](const SwTile &a, const SwTile &b) { return a.ncol > b.ncol; });

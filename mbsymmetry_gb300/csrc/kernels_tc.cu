@@ -169,11 +169,15 @@ void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat
 }
 
 // ---------------------------------------------------------------------------
-// (2) + (3): one CTA per (k_irr, AO block, spin, tau); FP32 per contribution,
-// FP64 across.  Shared: acc64 [b1^2] double2 | acc32 [b1^2] float2 |
-// G2 [b2^2] | V [QC][b1][b2] | W [QC][b1][b2] | U [QC][b1][b2] (float2).
+// (2) + (3): one CTA per (k_irr, AO block, spin, range of nt tau); FP32 per
+// contribution, FP64 across.  Per contribution and chunk of QC aux rows the
+// V rows are staged once and reused for every tau of the range:
+//   U[Q][j][m]   = sum_n W(tau)[Q][j][n] G2(tau)[m][n]       (all threads)
+//   S[i][j]     += sum_{Q,m} V[Q][i][m] U[Q][j][m]            (KS lanes per (i, j))
+// Shared: acc64 [nt][b1^2] double2 | acc32 [nt][b1^2] | G2 [b2^2] |
+//         V [QC][b1][b2] | W [QC][b1][b2] | U [QC][b1][b2] (float2).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) sigma_uv_kernel(const SigTile *__restrict__ tiles,
+__global__ void __launch_bounds__(256) sigma_uv_kernel(const SigTile *__restrict__ tiles,
                                                        const SigContrib *__restrict__ contribs,
                                                        const WRef *__restrict__ wref,
                                                        const double2 *__restrict__ V,
@@ -182,84 +186,117 @@ __global__ void __launch_bounds__(128) sigma_uv_kernel(const SigTile *__restrict
                                                        int smem_bytes) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const SigTile tile = tiles[blockIdx.x];
-  const int b1 = tile.b1, s = tile.s, tau = tile.t0;
+  const int b1 = tile.b1, s = tile.s, nt = tile.nt, bb = b1 * b1;
+  const int tid = threadIdx.x;
   double2 *acc64 = reinterpret_cast<double2 *>(smem_raw);
-  float2 *acc32 = reinterpret_cast<float2 *>(acc64 + b1 * b1);
-  float2 *G2s = acc32 + b1 * b1;
-  for (int e = threadIdx.x; e < b1 * b1; e += blockDim.x) acc64[e] = make_double2(0.0, 0.0);
+  float2 *acc32 = reinterpret_cast<float2 *>(acc64 + nt * bb);
+  float2 *G2s = acc32 + nt * bb;
+  // lanes per (i, j) output in the S stage: a power of two with bb * KS <= 256
+  int KS = 1;
+  while (KS < 32 && bb * KS * 2 <= 256) KS *= 2;
+  for (int e = tid; e < nt * bb; e += 256) acc64[e] = make_double2(0.0, 0.0);
   for (int c = tile.c0; c < tile.c1; ++c) {
     const SigContrib cb = contribs[c];
     const int qb = cb.qb, b2 = cb.b2;
     const int blk = b1 * b2;
     float2 *Vs = G2s + b2 * b2;
-    const int per_q = 3 * blk;
     const int avail = (smem_bytes - (int)((char *)Vs - (char *)smem_raw)) / 8;
-    int QC = avail / per_q;
+    int QC = avail / (3 * blk);
     QC = QC < qb ? QC : qb;
     float2 *Ws = Vs + QC * blk;
     float2 *Us = Ws + QC * blk;
     const double2 *Vb = V + cb.v;
-    const double2 *G2 = G + cb.gb + ((int64_t)tau * ns + s) * cb.sb;
     const WRef wr = wref[c];
-    const float2 *Wt = W + wr.base + (int64_t)tau * qb * wr.ld;
     __syncthreads();
-    for (int e = threadIdx.x; e < b2 * b2; e += blockDim.x) {
-      const double2 g = __ldg(G2 + e);
-      G2s[e] = make_float2((float)g.x, (float)g.y);
-    }
-    for (int e = threadIdx.x; e < b1 * b1; e += blockDim.x) acc32[e] = make_float2(0.f, 0.f);
+    for (int e = tid; e < nt * bb; e += 256) acc32[e] = make_float2(0.f, 0.f);
     for (int q0 = 0; q0 < qb; q0 += QC) {
       const int qn = (qb - q0) < QC ? (qb - q0) : QC;
       __syncthreads();
-      for (int e = threadIdx.x; e < qn * blk; e += blockDim.x) {
+      for (int e = tid; e < qn * blk; e += 256) {
         const double2 v = __ldg(Vb + (int64_t)q0 * blk + e);
         Vs[e] = make_float2((float)v.x, (float)v.y);
-        const int Qr = e / blk, jn = e - Qr * blk;
-        Ws[e] = Wt[(int64_t)(q0 + Qr) * wr.ld + jn];
       }
-      __syncthreads();
-      // U[Q][j][m] = sum_n W[Q][j][n] G2[m][n]
-      for (int e = threadIdx.x; e < qn * blk; e += blockDim.x) {
-        const int Qj = e / b2, m = e - Qj * b2;
-        const float2 *w = Ws + Qj * b2;
-        const float2 *g = G2s + m * b2;
-        float ur = 0.f, ui = 0.f;
-        for (int n = 0; n < b2; ++n) {
-          ur = fmaf(w[n].x, g[n].x, ur);
-          ur = fmaf(-w[n].y, g[n].y, ur);
-          ui = fmaf(w[n].x, g[n].y, ui);
-          ui = fmaf(w[n].y, g[n].x, ui);
+      for (int it = 0; it < nt; ++it) {
+        const int tau = tile.t0 + it;
+        const double2 *G2 = G + cb.gb + ((int64_t)tau * ns + s) * cb.sb;
+        const float2 *Wt = W + wr.base + ((int64_t)tau * qb + q0) * wr.ld;
+        __syncthreads();
+        for (int e = tid; e < b2 * b2; e += 256) {
+          const double2 g = __ldg(G2 + e);
+          G2s[e] = make_float2((float)g.x, (float)g.y);
         }
-        Us[e] = make_float2(ur, ui);
-      }
-      __syncthreads();
-      // acc32[i][j] += sum_{Q,m} V[Q][i][m] U[Q][j][m]
-      for (int o = threadIdx.x; o < b1 * b1; o += blockDim.x) {
-        const int i = o / b1, j = o - i * b1;
-        float ar = 0.f, ai = 0.f;
-        for (int Q = 0; Q < qn; ++Q) {
-          const float2 *vv = Vs + Q * blk + i * b2;
-          const float2 *uu = Us + Q * blk + j * b2;
-          for (int m = 0; m < b2; ++m) {
-            ar = fmaf(vv[m].x, uu[m].x, ar);
-            ar = fmaf(-vv[m].y, uu[m].y, ar);
-            ai = fmaf(vv[m].x, uu[m].y, ai);
-            ai = fmaf(vv[m].y, uu[m].x, ai);
+        for (int e = tid; e < qn * blk; e += 256) {
+          const int Qr = e / blk, jn = e - Qr * blk;
+          Ws[e] = Wt[(int64_t)Qr * wr.ld + jn];
+        }
+        __syncthreads();
+        for (int e = tid; e < qn * blk; e += 256) {
+          const int Qj = e / b2, m = e - Qj * b2;
+          const float2 *w = Ws + Qj * b2;
+          const float2 *g = G2s + m * b2;
+          float ur = 0.f, ui = 0.f;
+          for (int n = 0; n < b2; ++n) {
+            ur = fmaf(w[n].x, g[n].x, ur);
+            ur = fmaf(-w[n].y, g[n].y, ur);
+            ui = fmaf(w[n].x, g[n].y, ui);
+            ui = fmaf(w[n].y, g[n].x, ui);
+          }
+          Us[e] = make_float2(ur, ui);
+        }
+        __syncthreads();
+        const int K = qn * b2;
+        float2 *acc = acc32 + it * bb;
+        if (KS == 1) {
+          for (int o = tid; o < bb; o += 256) {
+            const int i = o / b1, j = o - i * b1;
+            float ar = 0.f, ai = 0.f;
+            for (int k = 0; k < K; ++k) {
+              const int Q = k / b2, m = k - Q * b2;
+              const float2 vv = Vs[Q * blk + i * b2 + m], uu = Us[Q * blk + j * b2 + m];
+              ar = fmaf(vv.x, uu.x, ar);
+              ar = fmaf(-vv.y, uu.y, ar);
+              ai = fmaf(vv.x, uu.y, ai);
+              ai = fmaf(vv.y, uu.x, ai);
+            }
+            acc[o].x += ar;
+            acc[o].y += ai;
+          }
+        } else {
+          const int o = tid / KS, ks = tid - (tid / KS) * KS;
+          float ar = 0.f, ai = 0.f;
+          if (o < bb) {
+            const int i = o / b1, j = o - i * b1;
+            for (int k = ks; k < K; k += KS) {
+              const int Q = k / b2, m = k - Q * b2;
+              const float2 vv = Vs[Q * blk + i * b2 + m], uu = Us[Q * blk + j * b2 + m];
+              ar = fmaf(vv.x, uu.x, ar);
+              ar = fmaf(-vv.y, uu.y, ar);
+              ai = fmaf(vv.x, uu.y, ai);
+              ai = fmaf(vv.y, uu.x, ai);
+            }
+          }
+          for (int off = KS / 2; off > 0; off >>= 1) {
+            ar += __shfl_xor_sync(0xffffffffu, ar, off);
+            ai += __shfl_xor_sync(0xffffffffu, ai, off);
+          }
+          if (ks == 0 && o < bb) {
+            acc[o].x += ar;
+            acc[o].y += ai;
           }
         }
-        acc32[o].x += ar;
-        acc32[o].y += ai;
       }
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < b1 * b1; e += blockDim.x) {
+    for (int e = tid; e < nt * bb; e += 256) {
       acc64[e].x += (double)acc32[e].x;
       acc64[e].y += (double)acc32[e].y;
     }
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < b1 * b1; e += blockDim.x)
-    Sig[tile.sig + (int64_t)tau * tile.sstride + e] = make_double2(acc64[e].x * scale, acc64[e].y * scale);
+  for (int e = tid; e < nt * bb; e += 256) {
+    const int it = e / bb, r = e - it * bb;
+    Sig[tile.sig + (int64_t)(tile.t0 + it) * tile.sstride + r] = make_double2(acc64[e].x * scale, acc64[e].y * scale);
+  }
 }
 
 void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
@@ -271,7 +308,7 @@ void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const float2 
     GWGB_CUDA(cudaGetLastError());
   }
   if (ntiles1 > 0) {
-    sigma_uv_kernel<<<ntiles1, 128, uv_smem, st>>>(tiles1, contribs, wref, V, G, W, Sig, ns, scale, uv_smem);
+    sigma_uv_kernel<<<ntiles1, 256, uv_smem, st>>>(tiles1, contribs, wref, V, G, W, Sig, ns, scale, uv_smem);
     GWGB_CUDA(cudaGetLastError());
   }
 }
