@@ -31,8 +31,13 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 CONFIG = "C2"
-WORKLOAD = ("C2: Fm-3m 3x3x3 k mesh (27 k, 4 irreducible), nao=26, naux=120, nts=100, beta=100, "
-            "ns=1, V stored for all 729 k pairs, irrep blocks 1-8 (AO) / 2-40 (aux)")
+WORKLOADS = {
+    "C2": ("C2: Fm-3m 3x3x3 k mesh (27 k, 4 irreducible), nao=26, naux=120, nts=100, beta=100, "
+           "ns=1, V stored for all 729 k pairs, irrep blocks 1-8 (AO) / 2-40 (aux)"),
+    "C3": ("C3: Fm-3m 4x4x4 k mesh (64 k, 8 irreducible), nao=52, naux=250, nts=120, beta=100, "
+           "ns=1, V stored for all 4096 k pairs (12.2 GB), irrep blocks 2-16 (AO) / 4-64 (aux)"),
+}
+WORKLOAD = WORKLOADS[CONFIG]
 METRIC = "s/GW iteration (FP64 drop-in, P0 -> W~ -> Sigma -> Dyson)"
 L2_BYTES = 129 * 1024 * 1024
 
@@ -352,7 +357,7 @@ def run_gpu(args):
 
 
 def run_profile(args):
-    """One FP64 and one TF32x3 iteration of the workload, then two FP64
+    """One FP64 and one TF32x3 iteration of the workload, then (C2) two FP64
     self-consistent iterations: the command that ncu captures (a plain run of
     it must exit 0 first)."""
     import torch
@@ -370,10 +375,11 @@ def run_profile(args):
     s.set_G(G0)
     s.iteration(cr.mu)
     st = s.stats()
-    s.single_prec_run(False)
-    s.set_G(G0)
-    s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
-    s.sc_loop(2, 0.5, float(cr.layout.nao), cr.mu, step=0.05, tol=1e-10, max_evals=24)
+    if CONFIG == "C2":
+        s.single_prec_run(False)
+        s.set_G(G0)
+        s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+        s.sc_loop(2, 0.5, float(cr.layout.nao), cr.mu, step=0.05, tol=1e-10, max_evals=24)
     s.close()
     print(f"profile run: {CONFIG}, one FP64 and one TF32x3 iteration (last {st['total_ms']:.2f} ms), "
           "then two FP64 self-consistent iterations")
@@ -386,10 +392,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", default="C2", choices=sorted(WORKLOADS),
+                    help="workload (C2 is the benchmark; C3 is for profiling and manual runs)")
     ap.add_argument("--profile", action="store_true",
                     help="one FP64 and one TF32x3 iteration and two self-consistent iterations only "
                          "(the command for ncu captures)")
     args = ap.parse_args()
+    global CONFIG, WORKLOAD
+    CONFIG, WORKLOAD = args.config, WORKLOADS[args.config]
     if args.profile:
         run_profile(args)
     elif args.impl == "reference":

@@ -317,7 +317,7 @@ class Engine {
   // work lists
   DBuf<P0Tile> p0_tiles_;              // FP64: (block, tau range, contribution slice)
   DBuf<P0Contrib> p0_contribs_;
-  DBuf<SigTile> sig_tiles_, sig_tiles1_;  // FP64 slices / (owner, tau range) tiles of the tcgen05 path
+  DBuf<SigTile> sig_tiles_, sig_tiles1_;  // FP64 slices / tcgen05-path (owner, tau range) tiles
   DBuf<RedTask> p0_red_, sig_red_;       // FP64: ordered sums of the slices
   DBuf<double2> Part_;                   // FP64: partial sums of the slices
   DBuf<SigContrib> sig_contribs_;
@@ -332,7 +332,8 @@ class Engine {
   DBuf<WRef> sig_wref_;
   DBuf<float2> Wbuf_, Bcat_;
   int64_t bcat_elems_ = 0;
-  int sw_smem_ = 0, uv_smem_ = 0;
+  int sw_smem_ = 0, uv_smem_ = 0, uv_smem_small_ = 0, uv_nblocked_ = 0;
+  std::vector<SigTile> sig_tiles1_host_;
   int64_t wbuf_elems_ = 0;
   // tcgen05 P0 path: Z tasks (into Zcat), Vcat tasks, split-K tiles, reduction tiles
   DBuf<PzTask> pz_tasks_;
@@ -716,7 +717,7 @@ void Engine::build_work_lists() {
   {  // tcgen05 path, U/Sigma stage: (owner, range of nt tau) tiles, about six waves of two CTAs per SM
     const int nt_uv = std::max(1, std::min(8, (int)((int64_t)sig_own.size() * nts_ / (12 * std::max(1, nsm_)))));
     for (const Owner &o : sig_own) {
-      int nt = std::max(1, std::min(nt_uv, (smem_bytes_ / 2) / (24 * o.n * o.n)));
+      int nt = std::max(1, std::min(nt_uv, (smem_bytes_ / 4) / (24 * o.n * o.n)));
       double f = 0;
       for (int c = o.c0; c < o.c1; ++c) f += scost[c];
       for (int t0 = 0; t0 < nts_; t0 += nt) {
@@ -725,7 +726,19 @@ void Engine::build_work_lists() {
       }
     }
     std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
-    sig_tiles1_.upload(stl, st_);
+    // owners whose contributions average fewer than 200 (Q, m) terms take the
+    // unblocked variant (barriers dominate there); tiles = [blocked | small]
+    std::vector<SigTile> big, small;
+    for (const SigTile &t : stl) {
+      double k = 0;
+      for (int c = t.c0; c < t.c1; ++c) k += (double)sc[c].qb * sc[c].b2;
+      const bool sm = t.c1 > t.c0 && k < 200.0 * (t.c1 - t.c0);
+      (sm ? small : big).push_back(t);
+    }
+    uv_nblocked_ = (int)big.size();
+    big.insert(big.end(), small.begin(), small.end());
+    sig_tiles1_.upload(big, st_);
+    sig_tiles1_host_ = big;
   }
 
   // --- FP64 tiles of both contractions and their partial-sum buffer
@@ -817,14 +830,20 @@ void Engine::build_work_lists() {
       boff += (int64_t)ncol * qb;
       woff += (int64_t)nts_ * qb * ncol;
     }
-    for (const SigTile &t : stl) {
+    int uvneed_small = 0;
+    for (size_t n = 0; n < sig_tiles1_host_.size(); ++n) {  // [blocked | small]
+      const SigTile &t = sig_tiles1_host_[n];
+      const bool blocked = (int)n < uv_nblocked_;
       int b2max = 1, qbmax = 1;
       for (int c = t.c0; c < t.c1; ++c) { b2max = std::max(b2max, sc[c].b2); qbmax = std::max(qbmax, sc[c].qb); }
-      const int fixed = 24 * t.nt * t.b1 * t.b1 + 8 * b2max * b2max;
-      uvneed = std::max(uvneed, fixed + 24 * t.b1 * b2max * qbmax);
+      // acc64, acc32, red (blocked variant only), G2
+      const int fixed = 24 * t.nt * t.b1 * t.b1 + (blocked ? 256 * 16 * 8 : 0) + 8 * b2max * b2max;
+      int &need = blocked ? uvneed : uvneed_small;
+      need = std::max(need, fixed + 24 * t.b1 * b2max * qbmax);
       GWGB_REQUIRE(fixed + 24 * t.b1 * b2max <= smem_bytes_, GWGB_E_UNSUPPORTED,
                    "Sigma block too large for the tcgen05 path");
     }
+    uv_smem_small_ = std::min(smem_bytes_, std::max(16 * 1024, ((uvneed_small + 1023) / 1024) * 1024));
     std::stable_sort(swt.begin(), swt.end(), [](const SwTile &a, const SwTile &b) { return a.ncol > b.ncol; });
     sw_tiles_.upload(swt, st_);
     bc_tasks_.upload(bt, st_);
@@ -1018,7 +1037,7 @@ void Engine::k_sigma() {
     GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
     launch_sigma_tc(sw_tiles_.p, (int)sw_tiles_.n, sw_smem_, Bcat_.p, sig_tiles1_.p, (int)sig_tiles1_.n,
                     sig_contribs_.p, sig_wref_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p, Sig_.p, ns_, -1.0 / l_.nk, uv_smem_,
-                    bad_.p + 2, st_);
+                    uv_nblocked_, uv_smem_small_, bad_.p + 2, st_);
   } else {
     launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Part_.p,
                       ns_, fp64_smem_, st_);
@@ -1076,7 +1095,7 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
     const bool tc = prec_ == GWGB_PREC_TF32X3;
     const int64_t p0 = tc ? (pz_tasks_.n ? 1 : 0) + (pk_tiles_.n ? 1 : 0) + (pr_tiles_.n ? 1 : 0)
                           : (p0_tiles_.n ? 1 : 0) + (p0_red_.n ? 1 : 0);
-    const int64_t sg = tc ? (sw_tiles_.n ? 1 : 0) + (sig_tiles1_.n ? 1 : 0)
+    const int64_t sg = tc ? (sw_tiles_.n ? 1 : 0) + (uv_nblocked_ > 0 ? 1 : 0) + ((int)sig_tiles1_.n > uv_nblocked_ ? 1 : 0)
                           : (sig_tiles_.n ? 1 : 0) + (sig_red_.n ? 1 : 0);
     launches += (rotG_.n ? 1 : 0) + p0 + 3 + (rotP_.n ? 1 : 0) + sg;
   }

@@ -169,23 +169,19 @@ void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat
 }
 
 // ---------------------------------------------------------------------------
-// (2) + (3): one CTA per (k_irr, AO block, spin, range of nt tau); FP32 per
-// contribution, FP64 across.  Per contribution and chunk of QC aux rows the
-// V rows are staged once and reused for every tau of the range:
-//   U[Q][j][m]   = sum_n W(tau)[Q][j][n] G2(tau)[m][n]       (all threads)
-//   S[i][j]     += sum_{Q,m} V[Q][i][m] U[Q][j][m]            (KS lanes per (i, j))
+// (2) + (3) for owners with small contributions (fewer than 200 (Q, m) terms
+// on average): the same stages with one output per thread in U and KS lanes
+// (shuffle-reduced) per (i, j) in the Sigma stage; at these sizes the
+// per-contribution barriers dominate and the tile reduction of
+// sigma_uv_blocked costs more than its register blocking saves.
 // Shared: acc64 [nt][b1^2] double2 | acc32 [nt][b1^2] | G2 [b2^2] |
 //         V [QC][b1][b2] | W [QC][b1][b2] | U [QC][b1][b2] (float2).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) sigma_uv_kernel(const SigTile *__restrict__ tiles,
-                                                       const SigContrib *__restrict__ contribs,
-                                                       const WRef *__restrict__ wref,
-                                                       const double2 *__restrict__ V,
-                                                       const double2 *__restrict__ G, const float2 *__restrict__ W,
-                                                       double2 *__restrict__ Sig, int ns, double scale,
-                                                       int smem_bytes) {
+__device__ __forceinline__ void sigma_uv_small(const SigTile &tile, const SigContrib *__restrict__ contribs,
+                                               const WRef *__restrict__ wref, const double2 *__restrict__ V,
+                                               const double2 *__restrict__ G, const float2 *__restrict__ W,
+                                               double2 *__restrict__ Sig, int ns, double scale, int smem_bytes) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  const SigTile tile = tiles[blockIdx.x];
   const int b1 = tile.b1, s = tile.s, nt = tile.nt, bb = b1 * b1;
   const int tid = threadIdx.x;
   double2 *acc64 = reinterpret_cast<double2 *>(smem_raw);
@@ -299,23 +295,210 @@ __global__ void __launch_bounds__(256) sigma_uv_kernel(const SigTile *__restrict
   }
 }
 
+// ---------------------------------------------------------------------------
+// (2) + (3): one CTA per (k_irr, AO block, spin, range of nt tau); FP32 per
+// contribution, FP64 across.  Per contribution and chunk of QC aux rows the
+// V rows are staged once and reused for every tau of the range:
+//   U[Q][j][m]   = sum_n W(tau)[Q][j][n] G2(tau)[m][n]   (a thread: one (Q, j), up to 8 m)
+//   S[i][j]     += sum_{Q,m} V[Q][i][m] U[Q][j][m]        (a thread: a 4x4 (i, j) tile over
+//                                                          every NG-th (Q, m); the NG
+//                                                          partial tiles are summed in order)
+// Shared: acc64 [nt][b1^2] double2 | acc32 [nt][b1^2] | red [256][16] | G2 [b2^2] |
+//         V [QC][b1][b2] | W [QC][b1][b2] | U [QC][b1][b2] (float2).
+// ---------------------------------------------------------------------------
+constexpr int UV_TB = 4;   // Sigma-stage tile edge
+constexpr int UV_MB = 8;   // U-stage outputs per thread
+__device__ __forceinline__ void sigma_uv_blocked(const SigTile &tile, const SigContrib *__restrict__ contribs,
+                                                 const WRef *__restrict__ wref, const double2 *__restrict__ V,
+                                                 const double2 *__restrict__ G, const float2 *__restrict__ W,
+                                                 double2 *__restrict__ Sig, int ns, double scale, int smem_bytes) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const int b1 = tile.b1, s = tile.s, nt = tile.nt, bb = b1 * b1;
+  const int tid = threadIdx.x;
+  double2 *acc64 = reinterpret_cast<double2 *>(smem_raw);
+  float2 *acc32 = reinterpret_cast<float2 *>(acc64 + nt * bb);
+  float2 *red = acc32 + nt * bb;
+  float2 *G2s = red + 256 * UV_TB * UV_TB;
+  const int nT = (b1 + UV_TB - 1) / UV_TB, ntile = nT * nT;
+  const int NGmax = ntile >= 256 ? 1 : 256 / ntile;  // groups splitting the (Q, m) sum
+  const int mytile = tid % ntile, g = tid / ntile;
+  const int i0 = (mytile / nT) * UV_TB, j0 = (mytile % nT) * UV_TB;
+  for (int e = tid; e < nt * bb; e += 256) acc64[e] = make_double2(0.0, 0.0);
+  for (int c = tile.c0; c < tile.c1; ++c) {
+    const SigContrib cb = contribs[c];
+    const int qb = cb.qb, b2 = cb.b2;
+    const int blk = b1 * b2;
+    const int mch = (b2 + UV_MB - 1) / UV_MB;
+    float2 *Vs = G2s + b2 * b2;
+    const int avail = (smem_bytes - (int)((char *)Vs - (char *)smem_raw)) / 8;
+    int QC = avail / (3 * blk);
+    QC = QC < qb ? QC : qb;
+    float2 *Ws = Vs + QC * blk;
+    float2 *Us = Ws + QC * blk;
+    const double2 *Vb = V + cb.v;
+    const WRef wr = wref[c];
+    __syncthreads();
+    for (int e = tid; e < nt * bb; e += 256) acc32[e] = make_float2(0.f, 0.f);
+    for (int q0 = 0; q0 < qb; q0 += QC) {
+      const int qn = (qb - q0) < QC ? (qb - q0) : QC;
+      __syncthreads();
+      for (int e = tid; e < qn * blk; e += 256) {
+        const double2 v = __ldg(Vb + (int64_t)q0 * blk + e);
+        Vs[e] = make_float2((float)v.x, (float)v.y);
+      }
+      for (int it = 0; it < nt; ++it) {
+        const int tau = tile.t0 + it;
+        const double2 *G2 = G + cb.gb + ((int64_t)tau * ns + s) * cb.sb;
+        const float2 *Wt = W + wr.base + ((int64_t)tau * qb + q0) * wr.ld;
+        __syncthreads();
+        for (int e = tid; e < b2 * b2; e += 256) {
+          const double2 gg = __ldg(G2 + e);
+          G2s[e] = make_float2((float)gg.x, (float)gg.y);
+        }
+        for (int e = tid; e < qn * blk; e += 256) {
+          const int Qr = e / blk, jn = e - Qr * blk;
+          Ws[e] = Wt[(int64_t)Qr * wr.ld + jn];
+        }
+        __syncthreads();
+        for (int item = tid; item < qn * b1 * mch; item += 256) {
+          const int r = item / mch, m0 = (item - r * mch) * UV_MB;
+          const float2 *w = Ws + r * b2;
+          float ur[UV_MB], ui[UV_MB];
+#pragma unroll
+          for (int j = 0; j < UV_MB; ++j) ur[j] = ui[j] = 0.f;
+          for (int n = 0; n < b2; ++n) {
+            const float2 wv = w[n];
+#pragma unroll
+            for (int j = 0; j < UV_MB; ++j) {
+              if (m0 + j < b2) {
+                const float2 gv = G2s[(m0 + j) * b2 + n];
+                ur[j] = fmaf(wv.x, gv.x, ur[j]);
+                ur[j] = fmaf(-wv.y, gv.y, ur[j]);
+                ui[j] = fmaf(wv.x, gv.y, ui[j]);
+                ui[j] = fmaf(wv.y, gv.x, ui[j]);
+              }
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < UV_MB; ++j)
+            if (m0 + j < b2) Us[r * b2 + m0 + j] = make_float2(ur[j], ui[j]);
+        }
+        __syncthreads();
+        const int K = qn * b2;
+        // at least 16 (Q, m) terms per group: the group sums below are serial
+        const int NG = max(1, min(NGmax, K / 16));
+        if (g < NG) {
+          float ar[UV_TB][UV_TB], ai[UV_TB][UV_TB];
+#pragma unroll
+          for (int x = 0; x < UV_TB; ++x)
+#pragma unroll
+            for (int y = 0; y < UV_TB; ++y) ar[x][y] = ai[x][y] = 0.f;
+          for (int k = g; k < K; k += NG) {
+            const int Q = k / b2, m = k - Q * b2;
+            float2 va[UV_TB], ua[UV_TB];
+#pragma unroll
+            for (int x = 0; x < UV_TB; ++x) {
+              va[x] = (i0 + x < b1) ? Vs[Q * blk + (i0 + x) * b2 + m] : make_float2(0.f, 0.f);
+              ua[x] = (j0 + x < b1) ? Us[Q * blk + (j0 + x) * b2 + m] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int x = 0; x < UV_TB; ++x)
+#pragma unroll
+              for (int y = 0; y < UV_TB; ++y) {
+                ar[x][y] = fmaf(va[x].x, ua[y].x, ar[x][y]);
+                ar[x][y] = fmaf(-va[x].y, ua[y].y, ar[x][y]);
+                ai[x][y] = fmaf(va[x].x, ua[y].y, ai[x][y]);
+                ai[x][y] = fmaf(va[x].y, ua[y].x, ai[x][y]);
+              }
+          }
+          float2 *rp = red + (g * ntile + mytile) * (UV_TB * UV_TB);
+#pragma unroll
+          for (int x = 0; x < UV_TB; ++x)
+#pragma unroll
+            for (int y = 0; y < UV_TB; ++y) rp[x * UV_TB + y] = make_float2(ar[x][y], ai[x][y]);
+        }
+        __syncthreads();
+        float2 *acc = acc32 + it * bb;
+        for (int o = tid; o < bb; o += 256) {
+          const int i = o / b1, j = o - i * b1;
+          const int tl = (i / UV_TB) * nT + j / UV_TB, e = (i % UV_TB) * UV_TB + (j % UV_TB);
+          float sr = 0.f, si = 0.f;
+          for (int gg = 0; gg < NG; ++gg) {
+            const float2 v = red[(gg * ntile + tl) * (UV_TB * UV_TB) + e];
+            sr += v.x;
+            si += v.y;
+          }
+          acc[o].x += sr;
+          acc[o].y += si;
+        }
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < nt * bb; e += 256) {
+      acc64[e].x += (double)acc32[e].x;
+      acc64[e].y += (double)acc32[e].y;
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < nt * bb; e += 256) {
+    const int it = e / bb, r = e - it * bb;
+    Sig[tile.sig + (int64_t)(tile.t0 + it) * tile.sstride + r] = make_double2(acc64[e].x * scale, acc64[e].y * scale);
+  }
+}
+
+// The two variants as separate kernels (each launch gets its own shared
+// memory size and register count): tiles [0, nblocked) take sigma_uv_blocked,
+// the rest (owners whose contributions average fewer than 200 (Q, m) terms)
+// sigma_uv_small.
+__global__ void __launch_bounds__(256) sigma_uv_blocked_kernel(const SigTile *__restrict__ tiles,
+                                                               const SigContrib *__restrict__ contribs,
+                                                               const WRef *__restrict__ wref,
+                                                               const double2 *__restrict__ V,
+                                                               const double2 *__restrict__ G,
+                                                               const float2 *__restrict__ W,
+                                                               double2 *__restrict__ Sig, int ns, double scale,
+                                                               int smem_bytes) {
+  const SigTile tile = tiles[blockIdx.x];
+  sigma_uv_blocked(tile, contribs, wref, V, G, W, Sig, ns, scale, smem_bytes);
+}
+
+__global__ void __launch_bounds__(256) sigma_uv_small_kernel(const SigTile *__restrict__ tiles,
+                                                             const SigContrib *__restrict__ contribs,
+                                                             const WRef *__restrict__ wref,
+                                                             const double2 *__restrict__ V,
+                                                             const double2 *__restrict__ G,
+                                                             const float2 *__restrict__ W,
+                                                             double2 *__restrict__ Sig, int ns, double scale,
+                                                             int smem_bytes) {
+  const SigTile tile = tiles[blockIdx.x];
+  sigma_uv_small(tile, contribs, wref, V, G, W, Sig, ns, scale, smem_bytes);
+}
+
 void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
                      int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
                      const double2 *G, const double2 *P, float2 *W, double2 *Sig, int ns, double scale,
-                     int uv_smem, int *err, cudaStream_t st) {
+                     int uv_smem, int nblocked, int uv_smem_small, int *err, cudaStream_t st) {
   if (nwtiles > 0) {
     sigma_w_tc_kernel<<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, err);
     GWGB_CUDA(cudaGetLastError());
   }
-  if (ntiles1 > 0) {
-    sigma_uv_kernel<<<ntiles1, 256, uv_smem, st>>>(tiles1, contribs, wref, V, G, W, Sig, ns, scale, uv_smem);
+  // tiles1 = [blocked tiles (nblocked) | small tiles]
+  if (nblocked > 0) {
+    sigma_uv_blocked_kernel<<<nblocked, 256, uv_smem, st>>>(tiles1, contribs, wref, V, G, W, Sig, ns, scale,
+                                                             uv_smem);
+    GWGB_CUDA(cudaGetLastError());
+  }
+  if (ntiles1 > nblocked) {
+    sigma_uv_small_kernel<<<ntiles1 - nblocked, 256, uv_smem_small, st>>>(tiles1 + nblocked, contribs, wref, V, G, W,
+                                                                          Sig, ns, scale, uv_smem_small);
     GWGB_CUDA(cudaGetLastError());
   }
 }
 
 void set_tc_kernel_attributes(int smem_bytes) {
   GWGB_CUDA(cudaFuncSetAttribute(sigma_w_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
-  GWGB_CUDA(cudaFuncSetAttribute(sigma_uv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_uv_blocked_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_uv_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
 }
 
 }  // namespace gwgb
@@ -332,14 +515,19 @@ void set_tc_kernel_attributes(int smem_bytes) {
 // ===========================================================================
 namespace gwgb {
 
-// Z stage, FP32: one CTA per (contribution, spin), all tau < nts/2.
+// Z stage, FP32: one CTA per (contribution, spin), all tau < nts/2.  Both
+// small products are register-blocked: a thread owns up to 8 outputs of one
+// row and reads each staged operand once per inner step (the other operand
+// is a shared-memory broadcast).
 // Shared: G2 [b2^2] | Gm [b1^2] | V [PC][b1][b2] | X2 [PC][b1][b2]  (float2)
-__global__ void __launch_bounds__(128) p0_z_kernel(const PzTask *__restrict__ tasks, const double2 *__restrict__ V,
+constexpr int ZB = 8;  // outputs per thread in the Z stage products
+__global__ void __launch_bounds__(256) p0_z_kernel(const PzTask *__restrict__ tasks, const double2 *__restrict__ V,
                                                    const double2 *__restrict__ G, float2 *__restrict__ Z, int ns,
                                                    int nts, int smem_bytes) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const PzTask tk = tasks[blockIdx.x];
   const int b1 = tk.b1, b2 = tk.b2, qb = tk.qb, blk = b1 * b2;
+  const int tid = threadIdx.x;
   float2 *G2s = reinterpret_cast<float2 *>(smem_raw);
   float2 *Gms = G2s + b2 * b2;
   float2 *Vs = Gms + b1 * b1;
@@ -348,10 +536,11 @@ __global__ void __launch_bounds__(128) p0_z_kernel(const PzTask *__restrict__ ta
   PC = PC < qb ? PC : qb;
   float2 *X2 = Vs + PC * blk;
   const double2 *Vb = V + tk.v;
+  const int mch = (b2 + ZB - 1) / ZB, pch = (b1 + ZB - 1) / ZB;
   for (int p0 = 0; p0 < qb; p0 += PC) {
     const int pn = (qb - p0) < PC ? (qb - p0) : PC;
     __syncthreads();
-    for (int e = threadIdx.x; e < pn * blk; e += blockDim.x) {
+    for (int e = tid; e < pn * blk; e += 256) {
       const double2 v = __ldg(Vb + (int64_t)p0 * blk + e);
       Vs[e] = make_float2((float)v.x, (float)v.y);
     }
@@ -359,45 +548,67 @@ __global__ void __launch_bounds__(128) p0_z_kernel(const PzTask *__restrict__ ta
       const double2 *G2 = G + tk.gb + ((int64_t)tau * ns + tk.s) * tk.sb;
       const double2 *Gm = G + tk.ga + ((int64_t)(nts - 1 - tau) * ns + tk.s) * tk.sa;
       __syncthreads();
-      for (int e = threadIdx.x; e < b2 * b2; e += blockDim.x) {
+      for (int e = tid; e < b2 * b2; e += 256) {
         const double2 g = __ldg(G2 + e);
         G2s[e] = make_float2((float)g.x, (float)g.y);
       }
-      for (int e = threadIdx.x; e < b1 * b1; e += blockDim.x) {
+      for (int e = tid; e < b1 * b1; e += 256) {
         const double2 g = __ldg(Gm + e);
         Gms[e] = make_float2((float)g.x, (float)g.y);
       }
       __syncthreads();
-      // X2[P][t][m] = sum_n conj(V[P][t][n]) G2[m][n]
-      for (int e = threadIdx.x; e < pn * blk; e += blockDim.x) {
-        const int Pt = e / b2, m = e - Pt * b2;
-        const float2 *vr = Vs + Pt * b2;
-        const float2 *g = G2s + m * b2;
-        float xr = 0.f, xi = 0.f;
+      // X2[P][t][m] = sum_n conj(V[P][t][n]) G2[m][n]: row (P, t), up to ZB values of m
+      for (int item = tid; item < pn * b1 * mch; item += 256) {
+        const int r = item / mch, m0 = (item - r * mch) * ZB;
+        const float2 *vr = Vs + r * b2;
+        float xr[ZB], xi[ZB];
+#pragma unroll
+        for (int j = 0; j < ZB; ++j) xr[j] = xi[j] = 0.f;
         for (int n = 0; n < b2; ++n) {
-          xr = fmaf(vr[n].x, g[n].x, xr);
-          xr = fmaf(vr[n].y, g[n].y, xr);
-          xi = fmaf(vr[n].x, g[n].y, xi);
-          xi = fmaf(-vr[n].y, g[n].x, xi);
+          const float2 v = vr[n];
+#pragma unroll
+          for (int j = 0; j < ZB; ++j) {
+            if (m0 + j < b2) {
+              const float2 g = G2s[(m0 + j) * b2 + n];
+              xr[j] = fmaf(v.x, g.x, xr[j]);
+              xr[j] = fmaf(v.y, g.y, xr[j]);
+              xi[j] = fmaf(v.x, g.y, xi[j]);
+              xi[j] = fmaf(-v.y, g.x, xi[j]);
+            }
+          }
         }
-        X2[e] = make_float2(xr, xi);
+#pragma unroll
+        for (int j = 0; j < ZB; ++j)
+          if (m0 + j < b2) X2[r * b2 + m0 + j] = make_float2(xr[j], xi[j]);
       }
       __syncthreads();
-      // Z[P][(p,m)] = sum_t Gm[t][p] X2[P][t][m]   -> Zcat row (tau, p0 + P), columns zcol + pm
+      // Z[P][(p,m)] = sum_t Gm[t][p] X2[P][t][m]: (P, m), up to ZB values of p
+      //   -> Zcat row (tau, p0 + P), columns zcol + p*b2 + m
       float2 *Zt = Z + tk.z + ((int64_t)tau * qb + p0) * tk.zld + tk.zcol;
-      for (int e = threadIdx.x; e < pn * blk; e += blockDim.x) {
-        const int P = e / blk, pm = e - P * blk;
-        const int p = pm / b2, m = pm - p * b2;
+      for (int item = tid; item < pn * b2 * pch; item += 256) {
+        const int P = item / (b2 * pch);
+        const int rem = item - P * b2 * pch;
+        const int m = rem / pch, pb = (rem - (rem / pch) * pch) * ZB;
         const float2 *x = X2 + P * blk + m;
-        float zr = 0.f, zi = 0.f;
+        float zr[ZB], zi[ZB];
+#pragma unroll
+        for (int j = 0; j < ZB; ++j) zr[j] = zi[j] = 0.f;
         for (int t = 0; t < b1; ++t) {
-          const float2 g = Gms[t * b1 + p], xv = x[t * b2];
-          zr = fmaf(g.x, xv.x, zr);
-          zr = fmaf(-g.y, xv.y, zr);
-          zi = fmaf(g.x, xv.y, zi);
-          zi = fmaf(g.y, xv.x, zi);
+          const float2 xv = x[t * b2];
+#pragma unroll
+          for (int j = 0; j < ZB; ++j) {
+            if (pb + j < b1) {
+              const float2 g = Gms[t * b1 + pb + j];
+              zr[j] = fmaf(g.x, xv.x, zr[j]);
+              zr[j] = fmaf(-g.y, xv.y, zr[j]);
+              zi[j] = fmaf(g.x, xv.y, zi[j]);
+              zi[j] = fmaf(g.y, xv.x, zi[j]);
+            }
+          }
         }
-        Zt[(int64_t)P * tk.zld + pm] = make_float2(zr, zi);
+#pragma unroll
+        for (int j = 0; j < ZB; ++j)
+          if (pb + j < b1) Zt[(int64_t)P * tk.zld + (pb + j) * b2 + m] = make_float2(zr[j], zi[j]);
       }
     }
   }
@@ -543,7 +754,7 @@ void launch_p0_tc(const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles,
                   int nr, const double2 *V, const double2 *G, float2 *Z, const float2 *Vcat, double2 *Ppart,
                   double2 *P0, int ns, int nts, double pref, int mirror, int *err, cudaStream_t st) {
   if (nz > 0) {
-    p0_z_kernel<<<nz, 128, zsmem, st>>>(ztasks, V, G, Z, ns, nts, zsmem);
+    p0_z_kernel<<<nz, 256, zsmem, st>>>(ztasks, V, G, Z, ns, nts, zsmem);
     GWGB_CUDA(cudaGetLastError());
   }
   if (nk > 0) {
