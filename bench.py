@@ -273,35 +273,42 @@ def run_gpu(args):
                                "figure); contraction FLOPs = 8MNK per complex GEMM of the block layout",
                 "flop_alg_per_launch": flops, "kernel_ms": dom_ms}
 
-    # ---- mixed precision (TF32 3-pass contractions) on the same input --------
+    # ---- split tensor-core precisions on the same input ---------------------
     sig64 = s.Selfenergy()
     g64 = s.G_tau()
-    s.single_prec_run(True, "tf32x3")
-    for _ in range(args.warmup):
-        s.set_G(G0)
-        s.iteration(cr.mu)
-    mtimes, mstage = [], {}
-    for _ in range(args.steps):
-        s.set_G(G0)
-        flush.zero_()
-        torch.cuda.synchronize()
-        s.iteration(cr.mu)
-        stm = s.stats()
-        mtimes.append(stm["total_ms"])
-        for k in ("p0_ms", "sigma_ms", "pq_ms", "dyson_ms"):
-            mstage[k] = mstage.get(k, 0.0) + stm[k] / args.steps
-    sig32 = s.Selfenergy()
-    g32 = s.G_tau()
-    s.single_prec_run(False)
-    mixed = {"precision": "tf32x3 (3-pass TF32 mma, FP32 accumulate per contribution, FP64 across)",
-             "s_per_iteration": float(np.mean(mtimes)) / 1e3,
-             "speedup_vs_fp64": ms / float(np.mean(mtimes)),
-             "sigma_max_abs_err_vs_fp64": float(np.abs(sig32 - sig64).max()),
-             "sigma_max_abs": float(np.abs(sig64).max()),
-             "G_max_abs_err_vs_fp64": float(np.abs(g32 - g64).max()),
-             "stages_ms": mstage,
-             "contraction_tflops_alg": {"p0": stm["p0_flops"] / (mstage["p0_ms"] * 1e-3) / 1e12,
-                                        "sigma": stm["sigma_flops"] / (mstage["sigma_ms"] * 1e-3) / 1e12}}
+
+    def run_mixed(kind, label):
+        s.single_prec_run(True, kind)
+        for _ in range(args.warmup):
+            s.set_G(G0)
+            s.iteration(cr.mu)
+        mtimes, mstage = [], {}
+        for _ in range(args.steps):
+            s.set_G(G0)
+            flush.zero_()
+            torch.cuda.synchronize()
+            s.iteration(cr.mu)
+            stm = s.stats()
+            mtimes.append(stm["total_ms"])
+            for k in ("p0_ms", "sigma_ms", "pq_ms", "rotate_P_ms", "dyson_ms"):
+                mstage[k] = mstage.get(k, 0.0) + stm[k] / args.steps
+        sig32 = s.Selfenergy()
+        g32 = s.G_tau()
+        s.single_prec_run(False)
+        return {"precision": label,
+                "s_per_iteration": float(np.mean(mtimes)) / 1e3,
+                "speedup_vs_fp64": ms / float(np.mean(mtimes)),
+                "sigma_max_abs_err_vs_fp64": float(np.abs(sig32 - sig64).max()),
+                "sigma_max_abs": float(np.abs(sig64).max()),
+                "G_max_abs_err_vs_fp64": float(np.abs(g32 - g64).max()),
+                "stages_ms": mstage,
+                "contraction_tflops_alg": {"p0": stm["p0_flops"] / (mstage["p0_ms"] * 1e-3) / 1e12,
+                                           "sigma": stm["sigma_flops"] / (mstage["sigma_ms"] * 1e-3) / 1e12}}
+
+    mixed = run_mixed("tf32x3", "tf32x3 (tcgen05 kind::tf32, 2 planes, 3 products, FP32 accumulate per "
+                                "contribution, FP64 across)")
+    mixed_bf16 = run_mixed("bf16x3", "bf16x3 (tcgen05 kind::f16, 3 BF16 planes, 6 products, FP32 accumulate per "
+                                     "contribution, FP64 across)")
 
     # replicas: every rank runs the whole iteration, so the job completes `world`
     # iterations per max-over-ranks time
@@ -342,6 +349,7 @@ def run_gpu(args):
         "roofline": roofline,
         "clocks": clocks.summary(),
         "mixed": mixed,
+        "mixed_bf16x3": mixed_bf16,
         "sc_loop": sc,
         "peaks": {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops"),
                   "fp64_tflops_measured": fp64_peak},

@@ -44,7 +44,7 @@ extern "C" {
 /* ---- contraction precision -------------------------------------------- */
 #define GWGB_PREC_FP64       0  /* complex128 everywhere: the drop-in path */
 #define GWGB_PREC_TF32X3     1  /* P0/Sigma on tcgen05 kind::tf32, 3-pass split, FP32 accumulate */
-#define GWGB_PREC_BF16X3     2  /* P0/Sigma on tcgen05 kind::f16 (bf16), 3-way split */
+#define GWGB_PREC_BF16X3     2  /* P0/Sigma on tcgen05 kind::f16 (BF16), 3-way split, 6 products, FP32 accumulate */
 
 typedef struct gwgb_handle_s *gwgb_handle;
 

@@ -252,22 +252,22 @@ class Engine {
   ~Engine();
 
   void set_precision(int prec) {
-    GWGB_REQUIRE(prec == GWGB_PREC_FP64 || prec == GWGB_PREC_TF32X3, GWGB_E_UNSUPPORTED,
-                 "precision not implemented (FP64 and TF32X3 are)");
+    GWGB_REQUIRE(prec == GWGB_PREC_FP64 || prec == GWGB_PREC_TF32X3 || prec == GWGB_PREC_BF16X3, GWGB_E_INVALID,
+                 "unknown precision");
     if (prec != prec_) drop_graphs();  // the captured graphs hold the old kernels
     prec_ = prec;
-    if (prec_ == GWGB_PREC_TF32X3 && !Wbuf_.p && wbuf_elems_) {
+    if (prec_ != GWGB_PREC_FP64 && !Wbuf_.p && wbuf_elems_) {
       Wbuf_.alloc((size_t)wbuf_elems_);
       Bcat_.alloc((size_t)bcat_elems_);
     }
-    if (prec_ == GWGB_PREC_TF32X3 && !Zbuf_.p && zbuf_elems_) {
+    if (prec_ != GWGB_PREC_FP64 && !Zbuf_.p && zbuf_elems_) {
       Zbuf_.alloc((size_t)zbuf_elems_);
       Vcat_.alloc((size_t)vcat_elems_);
       Ppart_.alloc((size_t)ppart_elems_);
       GWGB_CUDA(cudaMemsetAsync(Zbuf_.p, 0, Zbuf_.n * sizeof(float2), st_));   // K padding stays zero
       GWGB_CUDA(cudaMemsetAsync(Vcat_.p, 0, Vcat_.n * sizeof(float2), st_));
     }
-    if (prec_ == GWGB_PREC_TF32X3 && !vcat_ready_) build_vcat();
+    if (prec_ != GWGB_PREC_FP64 && !vcat_ready_) build_vcat();
   }
   void upload_V(const double *V, int64_t n);
   void set_reps(const double *orep, int64_t no, const double *auxrep, int64_t na);
@@ -346,7 +346,7 @@ class Engine {
   int pz_smem_ = 0;
   bool vcat_ready_ = false;
   void build_vcat() {  // tau-independent tensor-core operands derived from V
-    if (prec_ != GWGB_PREC_TF32X3 || !have_V_) return;
+    if (prec_ == GWGB_PREC_FP64 || !have_V_) return;
     launch_vcat(vc_tasks_.p, (int)vc_tasks_.n, V_.p, Vcat_.p, st_);
     launch_bcat(bc_tasks_.p, (int)bc_tasks_.n, V_.p, Bcat_.p, st_);
     GWGB_CUDA(cudaStreamSynchronize(st_));
@@ -818,12 +818,13 @@ void Engine::build_work_lists() {
         ncol += b1b2;
       }
       for (int c : cs) wr[c].ld = ncol;
-      const int KP = ((2 * qb + 7) / 8) * 8;
+      const int KP = ((2 * qb + 7) / 8) * 8, KP16 = ((2 * qb + 15) / 16) * 16;
+      // shared memory: TF32x3 2 planes x 4 B, BF16x3 3 planes x 2 B (K padded to 16)
+      auto need = [&](int npk) { return std::max(KP * (1024 + 32 * npk), KP16 * (768 + 24 * npk)); };
       int npk = 64;
-      while (npk > 16 && KP * (1024 + 32 * npk) > 200 * 1024) npk /= 2;
-      GWGB_REQUIRE(KP * (1024 + 32 * npk) <= 200 * 1024, GWGB_E_UNSUPPORTED,
-                   "aux block too large for the tcgen05 Sigma kernel");
-      wsmem = std::max(wsmem, KP * (1024 + 32 * npk));
+      while (npk > 16 && need(npk) > 200 * 1024) npk /= 2;
+      GWGB_REQUIRE(need(npk) <= 200 * 1024, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 Sigma kernel");
+      wsmem = std::max(wsmem, need(npk));
       const int nt = std::max(1, std::min(nts_, 128 / qb));
       for (int t0 = 0; t0 < nts_; t0 += nt)
         swt.push_back({pa, boff, woff, pstride, qb, t0, std::min(nt, nts_ - t0), ncol, KP, npk, 0});
@@ -1009,9 +1010,9 @@ void Engine::k_rotate_G() {
 
 void Engine::k_p0(int mirror) {
   const double pref = -1.0 / l_.nk * (ns_ == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
-  if (prec_ == GWGB_PREC_TF32X3) {
+  if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE((Zbuf_.p || !zbuf_elems_) && vcat_ready_, GWGB_E_STATE, "mixed-precision work buffers missing");
-    launch_p0_tc(pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pk_tiles_.p, (int)pk_tiles_.n, pr_tiles_.p,
+    launch_p0_tc(prec_ == GWGB_PREC_BF16X3, pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pk_tiles_.p, (int)pk_tiles_.n, pr_tiles_.p,
                  (int)pr_tiles_.n, V_.p, Gall_.p, Zbuf_.p, Vcat_.p, Ppart_.p, Pall_.p, ns_, nts_, pref, mirror,
                  bad_.p + 2, st_);
   } else {
@@ -1033,9 +1034,9 @@ void Engine::k_rotate_P() {
 }
 
 void Engine::k_sigma() {
-  if (prec_ == GWGB_PREC_TF32X3) {
+  if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
-    launch_sigma_tc(sw_tiles_.p, (int)sw_tiles_.n, sw_smem_, Bcat_.p, sig_tiles1_.p, (int)sig_tiles1_.n,
+    launch_sigma_tc(prec_ == GWGB_PREC_BF16X3, sw_tiles_.p, (int)sw_tiles_.n, sw_smem_, Bcat_.p, sig_tiles1_.p, (int)sig_tiles1_.n,
                     sig_contribs_.p, sig_wref_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p, Sig_.p, ns_, -1.0 / l_.nk, uv_smem_,
                     uv_nblocked_, uv_smem_small_, bad_.p + 2, st_);
   } else {
@@ -1092,7 +1093,7 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
   s.total_ms = elapsed(with_gw ? 0 : 5, with_dyson ? 6 : 5);
   int64_t launches = 0;
   if (with_gw) {
-    const bool tc = prec_ == GWGB_PREC_TF32X3;
+    const bool tc = prec_ != GWGB_PREC_FP64;
     const int64_t p0 = tc ? (pz_tasks_.n ? 1 : 0) + (pk_tiles_.n ? 1 : 0) + (pr_tiles_.n ? 1 : 0)
                           : (p0_tiles_.n ? 1 : 0) + (p0_red_.n ? 1 : 0);
     const int64_t sg = tc ? (sw_tiles_.n ? 1 : 0) + (uv_nblocked_ > 0 ? 1 : 0) + ((int)sig_tiles1_.n > uv_nblocked_ ? 1 : 0)
@@ -1484,7 +1485,7 @@ static int on_handle(gwgb_handle h, F &&f) {
 
 extern "C" {
 
-const char *gwgb_version(void) { return "gwgb 0.2 (sm_103a, FP64 and TF32x3 contraction paths)"; }
+const char *gwgb_version(void) { return "gwgb 0.3 (sm_103a, FP64, TF32x3 and BF16x3 contraction paths)"; }
 
 const char *gwgb_last_error(void) { return gwgb::g_last_error.c_str(); }
 

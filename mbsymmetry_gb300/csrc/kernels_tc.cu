@@ -16,41 +16,91 @@
 #include "common.h"
 #include "kernels.h"
 #include "kernels_tc.h"
+#include <cuda_bf16.h>
+
 #include "tc_common.cuh"
 
 namespace gwgb {
 
 namespace {
 
-__device__ __forceinline__ void split_store(float *hi, float *lo, uint32_t off, float x) {
-  const uint32_t h = tc::to_tf32(x);
-  const uint32_t l = tc::to_tf32(x - __uint_as_float(h));
-  *reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(hi) + off) = h;
-  *reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(lo) + off) = l;
-}
+// Operand planes of the split products.  TF32x3: x = hi + lo (two TF32
+// planes), products lo*hi + hi*lo + hi*hi.  BF16x3: x = b0 + b1 + b2 (three
+// BF16 planes), products b2*b0 + b1*b1 + b0*b2 + b1*b0 + b0*b1 + b0*b0 (the
+// terms below 2^-24 relative are dropped; smallest first).  Each plane is a
+// K-major no-swizzle tile; plane i of an operand starts i * plane_bytes in.
+template <bool BF>
+struct Planes {
+  static constexpr int N = BF ? 3 : 2;      // planes per operand
+  static constexpr int EB = BF ? 2 : 4;     // bytes per element
+  static constexpr int KSTEP = BF ? 16 : 8; // K of one MMA
+  __device__ static uint32_t off(int r, int k, int K) {
+    return BF ? tc::kmajor_offset16(r, k, K) : tc::kmajor_offset(r, k, K);
+  }
+  __device__ static uint32_t sbo(int K) { return (uint32_t)(K * EB / 16) * 128; }
+  __device__ static void store(unsigned char *base, uint32_t plane_bytes, uint32_t off, float x) {
+    if constexpr (BF) {
+      const __nv_bfloat16 b0 = __float2bfloat16_rn(x);
+      const float r1 = x - __bfloat162float(b0);
+      const __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
+      const __nv_bfloat16 b2 = __float2bfloat16_rn(r1 - __bfloat162float(b1));
+      *reinterpret_cast<unsigned short *>(base + off) = __bfloat16_as_ushort(b0);
+      *reinterpret_cast<unsigned short *>(base + plane_bytes + off) = __bfloat16_as_ushort(b1);
+      *reinterpret_cast<unsigned short *>(base + 2 * plane_bytes + off) = __bfloat16_as_ushort(b2);
+    } else {
+      const uint32_t h = tc::to_tf32(x);
+      const uint32_t l = tc::to_tf32(x - __uint_as_float(h));
+      *reinterpret_cast<uint32_t *>(base + off) = h;
+      *reinterpret_cast<uint32_t *>(base + plane_bytes + off) = l;
+    }
+  }
+  __device__ static uint32_t idesc(int M, int Nn) { return BF ? tc::idesc_bf16(M, Nn) : tc::idesc_tf32(M, Nn); }
+  // all split products of one K step (byte offset koff inside every plane)
+  __device__ static void mma_step(uint32_t d, uint32_t a, uint32_t apl, uint32_t b, uint32_t bpl, uint32_t koff,
+                                  uint32_t sbo_a, uint32_t sbo_b, uint32_t idesc, uint32_t acc_first) {
+    auto da = [&](int i) { return tc::make_desc(a + i * apl + koff, 128, sbo_a); };
+    auto db = [&](int i) { return tc::make_desc(b + i * bpl + koff, 128, sbo_b); };
+    if constexpr (BF) {
+      tc::mma_bf16(d, da(2), db(0), idesc, acc_first);
+      tc::mma_bf16(d, da(1), db(1), idesc, 1);
+      tc::mma_bf16(d, da(0), db(2), idesc, 1);
+      tc::mma_bf16(d, da(1), db(0), idesc, 1);
+      tc::mma_bf16(d, da(0), db(1), idesc, 1);
+      tc::mma_bf16(d, da(0), db(0), idesc, 1);
+    } else {
+      tc::mma_tf32(d, da(1), db(0), idesc, acc_first);
+      tc::mma_tf32(d, da(0), db(1), idesc, 1);
+      tc::mma_tf32(d, da(0), db(0), idesc, 1);
+    }
+  }
+};
 
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // (1): one CTA = 128 rows (tau, Q) of one aux block x all its columns.  A is
-// staged once; B packs of 64 complex columns are double-buffered against two
+// staged once; B packs of npk complex columns are double-buffered against two
 // TMEM accumulators (MMA of pack i+1 overlaps the drain of pack i).
-// Shared: A_hi | A_lo (128 x KP) | B0_hi | B0_lo | B1_hi | B1_lo (128 x KP).
+// Shared: A planes (128 x K) | B buffer 0 planes (2 npk x K) | buffer 1 planes;
+// K = 2 q_b padded to the MMA K step.
 // ---------------------------------------------------------------------------
+template <bool BF>
 __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restrict__ tiles,
                                                          const float2 *__restrict__ Bcat,
                                                          const double2 *__restrict__ P, float2 *__restrict__ W,
                                                          int *__restrict__ err) {
+  using PL = Planes<BF>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ uint32_t tmem_slot;
   __shared__ __align__(8) uint64_t mbar[2];
   const SwTile tl = tiles[blockIdx.x];
-  const int qb = tl.qb, KP = tl.kp;
+  const int qb = tl.qb;
+  const int KP = BF ? ((tl.kp + 15) & ~15) : tl.kp;
   const int SW_PACK = tl.npk, BR = 2 * tl.npk;  // complex columns per pack, B rows per pack
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  float *Ahi = reinterpret_cast<float *>(smem_raw);
-  float *Alo = Ahi + 128 * KP;
-  float *Bb = Alo + 128 * KP;  // 2 buffers x (hi, lo) x BR x KP
+  const uint32_t apl = 128u * KP * PL::EB, bpl = (uint32_t)BR * KP * PL::EB;  // plane bytes
+  unsigned char *A = smem_raw;
+  unsigned char *Bb = A + PL::N * apl;  // 2 buffers x N planes
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 256);
   if (tid == 0) {
     tc::mbar_init(&mbar[0], 1);
@@ -65,38 +115,32 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
       const int it = r / qb, Q = r - it * qb;
       v = __ldg(P + tl.pa + (int64_t)(tl.t0 + it) * tl.pstride + (int64_t)Q * qb + kc);
     }
-    split_store(Ahi, Alo, tc::kmajor_offset(r, 2 * kc, KP), (float)v.x);
-    split_store(Ahi, Alo, tc::kmajor_offset(r, 2 * kc + 1, KP), (float)v.y);
+    PL::store(A, apl, PL::off(r, 2 * kc, KP), (float)v.x);
+    PL::store(A, apl, PL::off(r, 2 * kc + 1, KP), (float)v.y);
   }
   const int npacks = (tl.ncol + SW_PACK - 1) / SW_PACK;
   auto stage_b = [&](int pk) {
-    float *hi = Bb + (pk & 1) * 2 * BR * KP;
-    float *lo = hi + BR * KP;
+    unsigned char *B = Bb + (pk & 1) * PL::N * bpl;
     const int c0 = pk * SW_PACK;
     // rows (col, d) of the real embedding of B = conj(V): d=0 -> (Br, -Bi), d=1 -> (Bi, Br), Br = Vr, Bi = -Vi
     for (int e = tid; e < SW_PACK * (KP / 2); e += 256) {
       const int cl = e / (KP / 2), kc = e - cl * (KP / 2);
       const int col = c0 + cl;
-      float2 b = make_float2(0.f, 0.f);  // b = conj(V) as stored
-      if (col < tl.ncol && kc < qb) b = Bcat[tl.bcat + (int64_t)col * qb + kc];
-      split_store(hi, lo, tc::kmajor_offset(2 * cl, 2 * kc, KP), b.x);
-      split_store(hi, lo, tc::kmajor_offset(2 * cl, 2 * kc + 1, KP), -b.y);
-      split_store(hi, lo, tc::kmajor_offset(2 * cl + 1, 2 * kc, KP), b.y);
-      split_store(hi, lo, tc::kmajor_offset(2 * cl + 1, 2 * kc + 1, KP), b.x);
+      float2 bv = make_float2(0.f, 0.f);  // conj(V) as stored
+      if (col < tl.ncol && kc < qb) bv = Bcat[tl.bcat + (int64_t)col * qb + kc];
+      PL::store(B, bpl, PL::off(2 * cl, 2 * kc, KP), bv.x);
+      PL::store(B, bpl, PL::off(2 * cl, 2 * kc + 1, KP), -bv.y);
+      PL::store(B, bpl, PL::off(2 * cl + 1, 2 * kc, KP), bv.y);
+      PL::store(B, bpl, PL::off(2 * cl + 1, 2 * kc + 1, KP), bv.x);
     }
   };
-  const uint32_t idesc = tc::idesc_tf32(128, 2 * SW_PACK);
-  const uint32_t sbo = (uint32_t)(KP / 4) * 128;
+  const uint32_t idesc = PL::idesc(128, 2 * SW_PACK);
+  const uint32_t sbo = PL::sbo(KP);
   auto issue = [&](int pk, uint32_t tmem) {
-    const uint32_t a_hi = tc::smem_u32(Ahi), a_lo = tc::smem_u32(Alo);
-    const uint32_t b_hi = tc::smem_u32(Bb + (pk & 1) * 2 * BR * KP), b_lo = b_hi + BR * KP * 4;
+    const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(Bb + (pk & 1) * PL::N * bpl);
     const uint32_t d = tmem + (uint32_t)((pk & 1) * 2 * SW_PACK);
-    for (int s = 0; s < KP / 8; ++s) {
-      const uint32_t off = (uint32_t)s * 256;
-      tc::mma_tf32(d, tc::make_desc(a_lo + off, 128, sbo), tc::make_desc(b_hi + off, 128, sbo), idesc, s > 0);
-      tc::mma_tf32(d, tc::make_desc(a_hi + off, 128, sbo), tc::make_desc(b_lo + off, 128, sbo), idesc, 1);
-      tc::mma_tf32(d, tc::make_desc(a_hi + off, 128, sbo), tc::make_desc(b_hi + off, 128, sbo), idesc, 1);
-    }
+    for (int st = 0; st < KP / PL::KSTEP; ++st)
+      PL::mma_step(d, a, apl, b, bpl, (uint32_t)st * 256, sbo, sbo, idesc, st > 0);
     tc::commit(&mbar[pk & 1]);
   };
   if (npacks > 0) stage_b(0);
@@ -474,12 +518,15 @@ __global__ void __launch_bounds__(256) sigma_uv_small_kernel(const SigTile *__re
   sigma_uv_small(tile, contribs, wref, V, G, W, Sig, ns, scale, smem_bytes);
 }
 
-void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
+void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
                      int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
                      const double2 *G, const double2 *P, float2 *W, double2 *Sig, int ns, double scale,
                      int uv_smem, int nblocked, int uv_smem_small, int *err, cudaStream_t st) {
   if (nwtiles > 0) {
-    sigma_w_tc_kernel<<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, err);
+    if (bf16)
+      sigma_w_tc_kernel<true><<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, err);
+    else
+      sigma_w_tc_kernel<false><<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, err);
     GWGB_CUDA(cudaGetLastError());
   }
   // tiles1 = [blocked tiles (nblocked) | small tiles]
@@ -496,7 +543,8 @@ void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const float2 
 }
 
 void set_tc_kernel_attributes(int smem_bytes) {
-  GWGB_CUDA(cudaFuncSetAttribute(sigma_w_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_w_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_w_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(sigma_uv_blocked_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(sigma_uv_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
 }
@@ -618,10 +666,12 @@ __global__ void __launch_bounds__(256) p0_z_kernel(const PzTask *__restrict__ ta
 // this CTA's K slice (chunks of 16 complex = 32 real columns), FP32 in TMEM,
 // then FP64 partial sums to Ppart.  256 threads stage the operands (8 loads in
 // flight per thread); warps 0-3 drain TMEM lanes 0-127.
-// Shared: A_hi | A_lo (128 x 32) | B_hi | B_lo (NP x 32), 32-bit elements: 64 KB at NP = 128.
+// Shared: A planes (128 x 32) | B planes (NP x 32): 64 KB (TF32) / 48 KB (BF16) at NP = 128.
+template <bool BF>
 __global__ void __launch_bounds__(256) p0_tc_kernel(const PkTile *__restrict__ tiles,
                                                     const float2 *__restrict__ Z, const float2 *__restrict__ Vcat,
                                                     double2 *__restrict__ Ppart, int *__restrict__ err) {
+  using PL = Planes<BF>;
   constexpr int KP = 32;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ uint32_t tmem_slot;
@@ -629,10 +679,9 @@ __global__ void __launch_bounds__(256) p0_tc_kernel(const PkTile *__restrict__ t
   const PkTile tl = tiles[blockIdx.x];
   const int qb = tl.qb, NP = tl.np;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  float *Ahi = reinterpret_cast<float *>(smem_raw);
-  float *Alo = Ahi + 128 * KP;
-  float *Bhi = Alo + 128 * KP;
-  float *Blo = Bhi + NP * KP;
+  const uint32_t apl = 128u * KP * PL::EB, bpl = (uint32_t)NP * KP * PL::EB;
+  unsigned char *A = smem_raw;
+  unsigned char *B = A + PL::N * apl;
   uint32_t ncols_alloc = 32;
   while ((int)ncols_alloc < NP) ncols_alloc <<= 1;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols_alloc);
@@ -653,36 +702,30 @@ __global__ void __launch_bounds__(256) p0_tc_kernel(const PkTile *__restrict__ t
     for (int e = tid; e < 128 * 16; e += 256) {
       const int r = e >> 4, kk = e & 15;
       const float2 z = r < rows ? Zb[(int64_t)r * tl.zld + kbase + kk] : make_float2(0.f, 0.f);
-      split_store(Ahi, Alo, tc::kmajor_offset(r, 2 * kk, KP), z.x);
-      split_store(Ahi, Alo, tc::kmajor_offset(r, 2 * kk + 1, KP), z.y);
+      PL::store(A, apl, PL::off(r, 2 * kk, KP), z.x);
+      PL::store(A, apl, PL::off(r, 2 * kk + 1, KP), z.y);
     }
     // B: rows (Q, d) of the real embedding of V^T: d=0 -> (Vr, -Vi), d=1 -> (Vi, Vr)
 #pragma unroll 2
     for (int e = tid; e < (NP / 2) * 16; e += 256) {
       const int Q = e >> 4, kk = e & 15;
       const float2 v = Q < qb ? Vb[(int64_t)Q * tl.zld + kbase + kk] : make_float2(0.f, 0.f);
-      split_store(Bhi, Blo, tc::kmajor_offset(2 * Q, 2 * kk, KP), v.x);
-      split_store(Bhi, Blo, tc::kmajor_offset(2 * Q, 2 * kk + 1, KP), -v.y);
-      split_store(Bhi, Blo, tc::kmajor_offset(2 * Q + 1, 2 * kk, KP), v.y);
-      split_store(Bhi, Blo, tc::kmajor_offset(2 * Q + 1, 2 * kk + 1, KP), v.x);
+      PL::store(B, bpl, PL::off(2 * Q, 2 * kk, KP), v.x);
+      PL::store(B, bpl, PL::off(2 * Q, 2 * kk + 1, KP), -v.y);
+      PL::store(B, bpl, PL::off(2 * Q + 1, 2 * kk, KP), v.y);
+      PL::store(B, bpl, PL::off(2 * Q + 1, 2 * kk + 1, KP), v.x);
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     if (tid == 0) {
-      const uint32_t idesc = tc::idesc_tf32(128, NP);
-      const uint32_t sbo = (uint32_t)(KP / 4) * 128;
-      const uint32_t a_hi = tc::smem_u32(Ahi), a_lo = tc::smem_u32(Alo);
-      const uint32_t b_hi = tc::smem_u32(Bhi), b_lo = tc::smem_u32(Blo);
+      const uint32_t idesc = PL::idesc(128, NP);
+      const uint32_t sbo = PL::sbo(KP);
+      const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(B);
 #pragma unroll
-      for (int s = 0; s < KP / 8; ++s) {
-        const uint32_t off = (uint32_t)s * 256;
-        tc::mma_tf32(tmem, tc::make_desc(a_lo + off, 128, sbo), tc::make_desc(b_hi + off, 128, sbo), idesc,
-                     (ch > 0 || s > 0) ? 1u : 0u);
-        tc::mma_tf32(tmem, tc::make_desc(a_hi + off, 128, sbo), tc::make_desc(b_lo + off, 128, sbo), idesc, 1);
-        tc::mma_tf32(tmem, tc::make_desc(a_hi + off, 128, sbo), tc::make_desc(b_hi + off, 128, sbo), idesc, 1);
-      }
+      for (int st = 0; st < KP / PL::KSTEP; ++st)
+        PL::mma_step(tmem, a, apl, b, bpl, (uint32_t)st * 256, sbo, sbo, idesc, (ch > 0 || st > 0) ? 1u : 0u);
       tc::commit(&mbar);
     }
     ok = tc::mbar_wait(&mbar, phase);
@@ -750,7 +793,7 @@ void launch_vcat(const VcTask *tasks, int ntasks, const double2 *V, float2 *Vcat
   GWGB_CUDA(cudaGetLastError());
 }
 
-void launch_p0_tc(const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
+void launch_p0_tc(bool bf16, const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
                   int nr, const double2 *V, const double2 *G, float2 *Z, const float2 *Vcat, double2 *Ppart,
                   double2 *P0, int ns, int nts, double pref, int mirror, int *err, cudaStream_t st) {
   if (nz > 0) {
@@ -758,7 +801,10 @@ void launch_p0_tc(const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles,
     GWGB_CUDA(cudaGetLastError());
   }
   if (nk > 0) {
-    p0_tc_kernel<<<nk, 256, 64 * 1024, st>>>(ktiles, Z, Vcat, Ppart, err);
+    if (bf16)
+      p0_tc_kernel<true><<<nk, 256, 64 * 1024, st>>>(ktiles, Z, Vcat, Ppart, err);
+    else
+      p0_tc_kernel<false><<<nk, 256, 64 * 1024, st>>>(ktiles, Z, Vcat, Ppart, err);
     GWGB_CUDA(cudaGetLastError());
   }
   if (nr > 0) {
@@ -769,7 +815,8 @@ void launch_p0_tc(const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles,
 
 void set_tc_p0_kernel_attributes(int smem_bytes) {
   GWGB_CUDA(cudaFuncSetAttribute(p0_z_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
-  GWGB_CUDA(cudaFuncSetAttribute(p0_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+  GWGB_CUDA(cudaFuncSetAttribute(p0_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+  GWGB_CUDA(cudaFuncSetAttribute(p0_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
 }
 
 }  // namespace gwgb

@@ -38,7 +38,7 @@ struct WRef {
   int64_t ld;
 };
 
-void launch_sigma_tc(const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
+void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
                      int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
                      const double2 *G, const double2 *P, float2 *W, double2 *Sig, int ns, double scale,
                      int uv_smem, int nblocked, int uv_smem_small, int *err, cudaStream_t st);
@@ -93,7 +93,7 @@ struct PrTile {
   int32_t pad;
 };
 
-void launch_p0_tc(const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
+void launch_p0_tc(bool bf16, const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
                   int nr, const double2 *V, const double2 *G, float2 *Z, const float2 *Vcat, double2 *Ppart,
                   double2 *P0, int ns, int nts, double pref, int mirror, int *err, cudaStream_t st);
 

@@ -1,6 +1,6 @@
 // tcgen05 building blocks (sm_100a/sm_103a): TMEM allocation, shared-memory
-// matrix descriptors, the kind::tf32 MMA, commit to an mbarrier with a
-// bounded wait, and TMEM loads.
+// matrix descriptors, the kind::tf32 and kind::f16 (BF16) MMAs, commit to an
+// mbarrier with a bounded wait, and TMEM loads.
 //
 // Operand layout ("K-major, no swizzle"): a tile of R rows x K 32-bit elements
 // is stored as 8-row x 16-byte core matrices; element (r, k) lives at byte
@@ -92,6 +92,27 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
   for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// kind::f16 with BF16 A and B (same K-major no-swizzle layout with 8 16-bit
+// elements per core-matrix row: one MMA consumes K = 16).
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+// Instruction descriptor: D = F32, A = B = BF16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Byte offset of element (r, k) of a K-major no-swizzle tile of 16-bit
+// elements with K columns (core matrix: 8 rows x 8 elements).
+__device__ __forceinline__ uint32_t kmajor_offset16(int r, int k, int K) {
+  return (uint32_t)((r >> 3) * (K >> 3) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 
 __device__ __forceinline__ uint32_t to_tf32(float x) {

@@ -57,9 +57,10 @@ def test_c2_sigma_acceptance():
     assert np.abs(Sig - Sr).max() < 1e-10
 
 
-@pytest.mark.parametrize("name", ["C1", "C2"])
-def test_mixed_tf32x3_sigma_error(name):
-    """TF32 3-pass contractions against the FP64 path on the same input."""
+@pytest.mark.parametrize("name,kind", [("C1", "tf32x3"), ("C2", "tf32x3"), ("C1", "bf16x3"), ("C2", "bf16x3")])
+def test_mixed_sigma_error(name, kind):
+    """Split tensor-core contractions (TF32x3: 3 products of 2 TF32 planes;
+    BF16x3: 6 products of 3 BF16 planes) against the FP64 path on the same input."""
     from mbsymmetry_gb300.solver import GWSolver
     cr, tr = crystal(name)
     L = cr.layout
@@ -71,12 +72,12 @@ def test_mixed_tf32x3_sigma_error(name):
     G0 = s.G_tau()
     s.solve()
     S64, P64 = s.Selfenergy(), s.P0_q_t_QP()
-    s.single_prec_run(True, "tf32x3")
+    s.single_prec_run(True, kind)
     s.set_G(G0)
     s.solve()
     S32, P32 = s.Selfenergy(), s.P0_q_t_QP()
     s.close()
     err = np.abs(S32 - S64).max()
-    print(f"{name}: max|Sigma_tf32x3 - Sigma_fp64| = {err:.3e} (max|Sigma| = {np.abs(S64).max():.3e}), "
+    print(f"{name}: max|Sigma_{kind} - Sigma_fp64| = {err:.3e} (max|Sigma| = {np.abs(S64).max():.3e}), "
           f"max|P~ err| = {np.abs(P32 - P64).max():.3e}")
     assert err < 1e-5 * max(1.0, np.abs(S64).max())
