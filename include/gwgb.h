@@ -257,6 +257,21 @@ int gwgb_energy(gwgb_handle h, double *e_corr, double *e_one);
 int gwgb_sc_loop(gwgb_handle h, int32_t niter, double alpha, const gwgb_mu_search *ms, int32_t final_fp64,
                  gwgb_sc_record *out);
 
+/* ---- test hooks (no counterpart in the reference) ----------------------
+ * Failure paths exercised without faulting, trapping or hanging a GPU. */
+
+/* Raise one of the handle's device status words as a kernel would
+ * (0: singular W~ block, 1: singular Dyson block, 2: tensor-core completion
+ * wait ran out).  The next call that reads them (gwgb_synchronize, any solve)
+ * returns the mapped error (GWGB_E_NUMERIC / GWGB_E_TIMEOUT) and clears them. */
+int gwgb_test_raise_status(gwgb_handle h, int32_t which);
+
+/* Launch a kernel whose bounded wait on an mbarrier that nothing arrives on
+ * gives up after `polls` polls (1..10^7) and records that in a device status
+ * word; returns GWGB_E_TIMEOUT when the host read the status back, GWGB_OK if
+ * the wait did not run out. */
+int gwgb_test_wait_timeout(int32_t device, int32_t polls);
+
 /* ---- W~ solve without device allocation -------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory while they run (a host code whose own pool owns all of HBM, a plugin

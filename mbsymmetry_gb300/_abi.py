@@ -105,6 +105,8 @@ SIGNATURES = {
     "gwgb_energy": (c_int32, [c_void_p, POINTER(c_double), POINTER(c_double)]),
     "gwgb_sc_loop": (c_int32, [c_void_p, c_int32, c_double, POINTER(GwgbMuSearch), c_int32,
                                POINTER(GwgbScRecord)]),
+    "gwgb_test_raise_status": (c_int32, [c_void_p, c_int32]),
+    "gwgb_test_wait_timeout": (c_int32, [c_int32, c_int32]),
     "gwgb_wsolve_noalloc": (c_int32, [c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
                                       c_void_p, c_int32, c_void_p]),
 }

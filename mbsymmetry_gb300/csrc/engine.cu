@@ -246,6 +246,14 @@ struct GRef {
   int32_t stride;
 };
 
+// Host-side bounds check of one work item: [begin, begin + len) must lie in a
+// buffer of `size` elements.  Every task list is checked when it is built, so
+// no kernel launch can read or write outside its buffers whatever the layout.
+static void check_range(int64_t begin, int64_t len, int64_t size, const char *what) {
+  if (begin < 0 || len < 0 || begin + len > size)
+    throw Error(GWGB_E_INVALID, std::string("internal work list out of bounds: ") + what);
+}
+
 class Engine {
  public:
   Engine(const gwgb_params &p, const gwgb_layout &L);
@@ -292,6 +300,11 @@ class Engine {
   void energy(double *e_corr, double *e_one);
   void sc_loop(int niter, double alpha, const gwgb_mu_search &ms, int final_fp64, gwgb_sc_record *out);
   void stats(gwgb_stats *out) const { *out = stats_; }
+  void test_raise_status(int which) {
+    GWGB_REQUIRE(which >= 0 && which <= 2, GWGB_E_INVALID, "status word must be 0, 1 or 2");
+    const int one = 1;
+    GWGB_CUDA(cudaMemcpy(bad_.p + which, &one, sizeof(int), cudaMemcpyHostToDevice));
+  }
   void synchronize() { GWGB_CUDA(cudaStreamSynchronize(st_)); check_device_flags(); }
   int device() const { return dev_; }
   std::mutex mu_lock;
@@ -578,6 +591,17 @@ void Engine::build_work_lists() {
     po += (int64_t)nts_ * l.qaux_sz[q];
   }
   Pall_.alloc((size_t)po);
+  for (const RotTask &t : rg) {  // G rotations: batch = nts * ns
+    const int64_t nb = (int64_t)nts_ * ns_;
+    check_range(t.dst, (nb - 1) * t.dstride + (t.rotate ? (int64_t)t.m * t.m : t.m), go, "G rotation target");
+    check_range(t.src, (nb - 1) * t.sstride + (t.rotate ? (int64_t)t.n * t.n : t.m), go, "G rotation source");
+    if (t.rotate) check_range(t.o, (int64_t)t.m * t.n, l.flat_orep, "orep block");
+  }
+  for (const RotTask &t : rp) {  // P rotations: batch = nts
+    check_range(t.dst, (int64_t)(nts_ - 1) * t.dstride + (t.rotate ? (int64_t)t.m * t.m : t.m), po, "P rotation target");
+    check_range(t.src, (int64_t)(nts_ - 1) * t.sstride + (t.rotate ? (int64_t)t.n * t.n : t.m), po, "P rotation source");
+    if (t.rotate) check_range(t.o, (int64_t)t.m * t.n, l.flat_auxrep, "auxrep block");
+  }
   rotG_.upload(rg, st_);
   rotP_.upload(rp, st_);
 
@@ -616,6 +640,14 @@ void Engine::build_work_lists() {
       p0_own.push_back({pout, (int32_t)l.qaux_sz[q], qb, c0, c1, 2 * qb * b2max, 0});
     }
   }
+  for (const Owner &o : p0_own)
+    for (int c = o.c0; c < o.c1; ++c) {
+      const P0Contrib &cb = pc[c];
+      check_range(cb.v, (int64_t)o.n * cb.b1 * cb.b2, l.flat_V, "P0 V block");
+      const int64_t last = (int64_t)(nts_ - 1) * ns_ + (ns_ - 1);
+      check_range(cb.ga, last * cb.sa + (int64_t)cb.b1 * cb.b1, go, "P0 G(k1) block");
+      check_range(cb.gb, last * cb.sb + (int64_t)cb.b2 * cb.b2, go, "P0 G(k2) block");
+    }
   p0_contribs_.upload(pc, st_);
 
   {  // tcgen05 P0: per aux block, Zcat[(tau,P)][K] and Vcat[Q][K] with K over (contribution, spin)
@@ -667,6 +699,18 @@ void Engine::build_work_lists() {
       voff += (int64_t)qb * zld;
     }
     std::stable_sort(kt.begin(), kt.end(), [](const PkTile &a, const PkTile &b) { return a.kcn > b.kcn; });
+    for (const PzTask &t : zt)
+      check_range(t.z + t.zcol, ((int64_t)(half - 1) * t.qb + (t.qb - 1)) * t.zld + (int64_t)t.b1 * t.b2, zoff,
+                  "Z operand rows");
+    for (const VcTask &t : vt) check_range(t.vc + t.zcol, (int64_t)(t.qb - 1) * t.zld + t.b1b2, voff, "V operand rows");
+    for (const PkTile &t : kt) {
+      check_range(t.z, (int64_t)(t.t0 + t.nt) * t.qb * t.zld, zoff, "P0 tensor-core A tile");
+      check_range(t.vc, (int64_t)t.qb * t.zld, voff, "P0 tensor-core B tile");
+      check_range(t.part, (int64_t)t.nt * t.qb * t.qb, poff, "P0 tensor-core partials");
+      GWGB_REQUIRE(t.nt * t.qb <= 128 && t.np <= 128 && (t.kc0 + t.kcn) * 16 <= t.zld, GWGB_E_INVALID,
+                   "internal work list out of bounds: P0 tensor-core tile shape");
+    }
+    for (const PrTile &t : rt) check_range(t.part, (int64_t)t.nslice * t.nt * t.qb * t.qb, poff, "P0 partial sums");
     pz_tasks_.upload(zt, st_);
     vc_tasks_.upload(vt, st_);
     pk_tiles_.upload(kt, st_);
@@ -712,6 +756,13 @@ void Engine::build_work_lists() {
         sig_own.push_back({out, (int32_t)(ns_ * fa), b1, c0, c1, 2 * qbmax * b1, s});
       }
     }
+  }
+  for (size_t c = 0; c < sc.size(); ++c) {
+    const SigContrib &cb = sc[c];
+    check_range(cb.v, (int64_t)cb.qb * sig_b1_[c] * cb.b2, l.flat_V, "Sigma V block");
+    check_range(cb.gb, ((int64_t)(nts_ - 1) * ns_ + (ns_ - 1)) * cb.sb + (int64_t)cb.b2 * cb.b2, go,
+                "Sigma G(k2) block");
+    check_range(cb.pq, (int64_t)(nts_ - 1) * cb.pstride + (int64_t)cb.qb * cb.qb, po, "Sigma P(q) block");
   }
   sig_contribs_.upload(sc, st_);
   {  // tcgen05 path, U/Sigma stage: (owner, range of nt tau) tiles, about six waves of two CTAs per SM
@@ -797,7 +848,19 @@ void Engine::build_work_lists() {
     sig_tiles_.upload(st, st_);
     p0_red_.upload(pr, st_);
     sig_red_.upload(sr, st_);
-    Part_.alloc((size_t)std::max<int64_t>(1, std::max(part0, part1)));
+    const int64_t npart = std::max<int64_t>(1, std::max(part0, part1));
+    for (const P0Tile &t : pt) check_range(t.part, (int64_t)t.nt * t.qb * t.qb, npart, "P0 partial slice");
+    for (const SigTile &t : st) check_range(t.part, (int64_t)t.nt * t.b1 * t.b1, npart, "Sigma partial slice");
+    for (const RedTask &r : pr) {
+      check_range(r.part, (int64_t)r.nslice * r.nt * r.elems, npart, "P0 slice sum");
+      check_range(r.out, (int64_t)(nts_ - 1) * r.ostride + r.elems, po, "P0 output block");
+    }
+    for (const RedTask &r : sr) {
+      check_range(r.part, (int64_t)r.nslice * r.nt * r.elems, npart, "Sigma slice sum");
+      check_range(r.out, (int64_t)(r.t0 + r.nt - 1) * r.ostride + r.elems, (int64_t)nts_ * ns_ * fa,
+                  "Sigma output block");
+    }
+    Part_.alloc((size_t)npart);
   }
   {  // tcgen05 Sigma: per aux block (q, iq), Bcat = conj(V) columns, Wcat = W rows (tau, Q)
     std::vector<WRef> wr(sc.size());
@@ -846,6 +909,16 @@ void Engine::build_work_lists() {
     }
     uv_smem_small_ = std::min(smem_bytes_, std::max(16 * 1024, ((uvneed_small + 1023) / 1024) * 1024));
     std::stable_sort(swt.begin(), swt.end(), [](const SwTile &a, const SwTile &b) { return a.ncol > b.ncol; });
+    for (const SwTile &t : swt) {
+      check_range(t.wcat, (int64_t)(t.t0 + t.nt) * t.qb * t.ncol, woff, "W rows");
+      check_range(t.bcat, (int64_t)t.ncol * t.qb, boff, "conj(V) operand");
+      GWGB_REQUIRE(t.nt * t.qb <= 128 && 2 * t.npk <= 128, GWGB_E_INVALID,
+                   "internal work list out of bounds: Sigma tensor-core tile shape");
+    }
+    for (const BcTask &t : bt) {
+      check_range(t.v, (int64_t)t.qb * t.b1b2, l.flat_V, "conj(V) source");
+      check_range(t.bcat + (int64_t)t.col0 * t.qb, (int64_t)t.b1b2 * t.qb, boff, "conj(V) target");
+    }
     sw_tiles_.upload(swt, st_);
     bc_tasks_.upload(bt, st_);
     sig_wref_.upload(wr, st_);
@@ -906,6 +979,24 @@ void Engine::build_work_lists() {
       }
     tr_tasks_.upload(tt, st_);
     slab_e_.upload(se, st_);
+  }
+  {
+    const int64_t gsz = (int64_t)nts_ * ns_ * fa, wsz = (int64_t)nw_ * ns_ * fa, pwsz = (int64_t)nw_b_ * fq;
+    auto slabs = [&](const std::vector<TSlab> &v, int nin, int row0, int64_t xs, int nout, int64_t ys, const char *w) {
+      for (const TSlab &t : v) {
+        check_range(t.x + (int64_t)row0 * t.ldx, (int64_t)(nin - 1) * t.ldx + t.ncols, xs, w);
+        check_range(t.y, (int64_t)(nout - 1) * t.ldy + t.ncols, ys, w);
+      }
+    };
+    slabs(pf, ncheb_, 1, po, nw_b_, pwsz, "P tau->Omega slab");
+    slabs(pb, nw_b_, 0, pwsz, nts_, po, "P Omega->tau slab");
+    slabs(sf, ncheb_, 1, gsz, nw_, wsz, "Sigma tau->omega slab");
+    slabs(gb, nw_, 0, wsz, nts_, gsz, "G omega->tau slab");
+    for (const InvTask &t : iw) check_range(t.a, (int64_t)t.n * t.n, pwsz, "W~ block");
+    for (const InvTask &t : id) {
+      check_range(t.a, (int64_t)t.n * t.n, wsz, "Dyson block");
+      check_range(t.s, (int64_t)t.n * t.n, (int64_t)ns_ * fa, "S/F block");
+    }
   }
   inv_w_.upload(iw, st_);
   inv_d_.upload(id, st_);
@@ -1537,6 +1628,23 @@ GWGB_FORWARD(gwgb_dyson, (gwgb_handle h, double mu), e.dyson(mu))
 GWGB_FORWARD(gwgb_iteration, (gwgb_handle h, double mu), e.iteration(mu))
 GWGB_FORWARD(gwgb_get_stats, (gwgb_handle h, gwgb_stats *out), GWGB_REQUIRE(out, GWGB_E_INVALID, "NULL stats"); e.stats(out))
 GWGB_FORWARD(gwgb_synchronize, (gwgb_handle h), e.synchronize())
+GWGB_FORWARD(gwgb_test_raise_status, (gwgb_handle h, int32_t which), e.test_raise_status(which))
+
+int gwgb_test_wait_timeout(int32_t device, int32_t polls) {
+  int status = 0;
+  const int rc = guarded([&] {
+    GWGB_REQUIRE(polls >= 1 && polls <= 10000000, GWGB_E_INVALID, "polls must be in [1, 1e7]");
+    GWGB_CUDA(cudaSetDevice(device));
+    status = gwgb::run_wait_timeout_test(polls);
+  });
+  if (rc != GWGB_OK) return rc;
+  if (status) {
+    gwgb::g_last_error = "a bounded device-side wait ran out (test hook)";
+    return GWGB_E_TIMEOUT;
+  }
+  return GWGB_OK;
+}
+
 GWGB_FORWARD(gwgb_set_hcore, (gwgb_handle h, const double *H), e.set_hcore(H))
 GWGB_FORWARD(gwgb_set_energy_matrix, (gwgb_handle h, const double *M, int32_t n), e.set_energy_matrix(M, n))
 GWGB_FORWARD(gwgb_find_mu, (gwgb_handle h, const gwgb_mu_search *ms, double *mu_out, double *n_out),

@@ -820,3 +820,32 @@ void set_tc_p0_kernel_attributes(int smem_bytes) {
 }
 
 }  // namespace gwgb
+
+// ===========================================================================
+// Test hook: a bounded mbarrier wait that runs out (nothing arrives on the
+// barrier); the kernel records it in a status word and returns.
+// ===========================================================================
+namespace gwgb {
+
+__device__ int g_wait_test_status;
+
+__global__ void wait_timeout_kernel(int polls) {
+  __shared__ __align__(8) uint64_t mbar;
+  if (threadIdx.x != 0) return;
+  tc::mbar_init(&mbar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;");
+  const bool done = tc::mbar_wait(&mbar, 0u, polls);
+  g_wait_test_status = done ? 0 : 1;
+}
+
+int run_wait_timeout_test(int polls) {
+  int zero = 0, status = 0;
+  GWGB_CUDA(cudaMemcpyToSymbol(g_wait_test_status, &zero, sizeof(int)));
+  wait_timeout_kernel<<<1, 32>>>(polls);
+  GWGB_CUDA(cudaGetLastError());
+  GWGB_CUDA(cudaDeviceSynchronize());
+  GWGB_CUDA(cudaMemcpyFromSymbol(&status, g_wait_test_status, sizeof(int)));
+  return status;
+}
+
+}  // namespace gwgb

@@ -99,4 +99,7 @@ void launch_p0_tc(bool bf16, const PzTask *ztasks, int nz, int zsmem, const PkTi
 
 void launch_vcat(const VcTask *tasks, int ntasks, const double2 *V, float2 *Vcat, cudaStream_t st);
 
+// Runs the bounded-wait test kernel; returns 1 when the wait ran out.
+int run_wait_timeout_test(int polls);
+
 }  // namespace gwgb

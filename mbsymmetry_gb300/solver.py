@@ -160,14 +160,54 @@ class GWSolver:
         return ec.value, (eo.value if with_one_body else None)
 
     def sc_loop(self, niter: int, alpha: float, n_electrons: float, mu0: float, step: float = 0.05,
-                tol: float = 1e-10, max_evals: int = 32, final_fp64: bool = False) -> list:
+                tol: float = 1e-10, max_evals: int = 32, final_fp64: bool = False, log=None) -> list:
         """niter self-consistent GW iterations (one CUDA graph launch each);
-        one dict per iteration: mu, n_electrons, e_corr, e_one, leakage, mu_evals, precision."""
+        one dict per iteration: mu, n_electrons, e_corr, e_one, leakage, mu_evals, precision.
+        With ``log`` (a writable text file) one JSON line per iteration is
+        written, with the mean device time per iteration."""
         ms = self._mu_search(n_electrons, mu0, step, tol, max_evals)
         recs = (_abi.GwgbScRecord * niter)()
         _abi.check(self.lib.gwgb_sc_loop(self.h, int(niter), float(alpha), ctypes.byref(ms),
                                          1 if final_fp64 else 0, recs))
-        return [{name: getattr(r, name) for name, _ in _abi.GwgbScRecord._fields_} for r in recs]
+        out = [{name: getattr(r, name) for name, _ in _abi.GwgbScRecord._fields_} for r in recs]
+        if log is not None:
+            import json
+            ms_it = self.stats()["total_ms"]
+            for i, r in enumerate(out):
+                log.write(json.dumps({"iteration": i, "ms_per_iteration_mean": ms_it, **r}) + "\n")
+        return out
+
+    # -- checkpoint / resume (the reference writes none) ----------------------
+    def save_state(self, path: str, mu: float, iteration: int = 0, **extra) -> None:
+        """Write G(tau), Sigma(tau) and mu: ``<path>.npz`` (the arrays, host
+        layout [nts][ns][flat_ao]) and ``<path>.json`` (a header), so that a
+        self-consistent run can resume with :meth:`load_state` + :meth:`sc_loop`."""
+        import json
+        np.savez(path + ".npz", G=self.G_tau(), Sigma=self.Selfenergy())
+        hdr = {"format": "gwgb-state-1", "nts": self.nts, "ns": self.ns,
+               "flat_ao": int(self.layout.flat_ao_size), "nk": int(self.layout.nk),
+               "ink": int(self.layout.ink), "beta": float(self.tr.beta), "mu": float(mu),
+               "iteration": int(iteration), "engine": self.lib.gwgb_version().decode()}
+        hdr.update(extra)
+        with open(path + ".json", "w") as f:
+            json.dump(hdr, f, indent=1)
+
+    def load_state(self, path: str) -> dict:
+        """Read a state written by :meth:`save_state` into the engine; returns
+        its header (``mu``, ``iteration``, ...).  Shapes are checked."""
+        import json
+        with open(path + ".json") as f:
+            hdr = json.load(f)
+        if hdr.get("format") != "gwgb-state-1":
+            raise ValueError(f"{path}.json: not a gwgb state file")
+        for key, val in (("nts", self.nts), ("ns", self.ns), ("flat_ao", self.layout.flat_ao_size),
+                         ("nk", self.layout.nk), ("ink", self.layout.ink)):
+            if int(hdr[key]) != int(val):
+                raise ValueError(f"{path}: {key} = {hdr[key]} does not match this solver ({val})")
+        z = np.load(path + ".npz")
+        self.set_G(z["G"])
+        self.set_Selfenergy(z["Sigma"])
+        return hdr
 
     def synchronize(self):
         _abi.check(self.lib.gwgb_synchronize(self.h))

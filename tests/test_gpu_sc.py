@@ -104,3 +104,33 @@ def test_sc_loop_reproducible_and_mixed_final_fp64():
     assert [r["precision"] for r in r3] == [1, 1, 0]
     assert abs(r3[-1]["e_corr"] - r1[-1]["e_corr"]) < 1e-5
     assert np.abs(g3 - g1).max() < 1e-5
+
+
+def test_sc_loop_checkpoint_resume_is_exact(tmp_path):
+    """2 iterations, checkpoint (G, Sigma, mu), a new handle resumes for 1:
+    bitwise the same G and records as 3 iterations in one run."""
+    import io
+    import json
+    cr, tr = crystal("C1")
+    target = float(cr.layout.nao)
+    s = _solver(cr, tr, 1)
+    s.dyson(cr.mu)
+    G0 = s.G_tau()
+    r3 = s.sc_loop(3, 0.5, target, cr.mu, tol=TOL_MU_SEARCH, max_evals=40)
+    g3 = s.G_tau()
+    s.set_G(G0)
+    s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+    log = io.StringIO()
+    r2 = s.sc_loop(2, 0.5, target, cr.mu, tol=TOL_MU_SEARCH, max_evals=40, log=log)
+    s.save_state(str(tmp_path / "state"), mu=r2[-1]["mu"], iteration=2)
+    s.close()
+    lines = [json.loads(x) for x in log.getvalue().splitlines()]
+    assert [x["iteration"] for x in lines] == [0, 1] and lines[1]["mu"] == r2[1]["mu"]
+    s2 = _solver(cr, tr, 1)
+    hdr = s2.load_state(str(tmp_path / "state"))
+    assert hdr["iteration"] == 2
+    r1 = s2.sc_loop(1, 0.5, target, hdr["mu"], tol=TOL_MU_SEARCH, max_evals=40)
+    g = s2.G_tau()
+    s2.close()
+    assert r2 == r3[:2] and r1[0] == r3[2]
+    assert np.array_equal(g, g3)
