@@ -243,6 +243,7 @@ __device__ __forceinline__ void sigma_uv_small(const SigTile &tile, const SigCon
     const int avail = (smem_bytes - (int)((char *)Vs - (char *)smem_raw)) / 8;
     int QC = avail / (3 * blk);
     QC = QC < qb ? QC : qb;
+    if (QC < 1) return;  // the host sizes shared memory for QC >= 1; never loop without progress
     float2 *Ws = Vs + QC * blk;
     float2 *Us = Ws + QC * blk;
     const double2 *Vb = V + cb.v;
@@ -377,6 +378,7 @@ __device__ __forceinline__ void sigma_uv_blocked(const SigTile &tile, const SigC
     const int avail = (smem_bytes - (int)((char *)Vs - (char *)smem_raw)) / 8;
     int QC = avail / (3 * blk);
     QC = QC < qb ? QC : qb;
+    if (QC < 1) return;  // the host sizes shared memory for QC >= 1; never loop without progress
     float2 *Ws = Vs + QC * blk;
     float2 *Us = Ws + QC * blk;
     const double2 *Vb = V + cb.v;
@@ -582,6 +584,7 @@ __global__ void __launch_bounds__(256) p0_z_kernel(const PzTask *__restrict__ ta
   const int avail = smem_bytes / 8 - b2 * b2 - b1 * b1;
   int PC = avail / (2 * blk);
   PC = PC < qb ? PC : qb;
+  if (PC < 1) return;  // the host sizes shared memory for PC >= 1; never loop without progress
   float2 *X2 = Vs + PC * blk;
   const double2 *Vb = V + tk.v;
   const int mch = (b2 + ZB - 1) / ZB, pch = (b1 + ZB - 1) / ZB;
