@@ -94,6 +94,10 @@ CONFIGS: Dict[str, CrystalSpec] = {
     "C3": CrystalSpec("C3", "fcc", (4, 4, 4), 52, 250, 120, 100.0, ao_block=(2, 16), aux_block=(4, 64), seed=20260103),
     "C4": CrystalSpec("C4", "hex", (4, 4, 3), 72, 350, 120, 200.0, ao_block=(2, 30), aux_block=(2, 30), seed=20260104),
     "C5": CrystalSpec("C5", "fcc", (5, 5, 5), 100, 500, 150, 200.0, ao_block=(4, 40), aux_block=(8, 64), seed=20260105),
+    # profiling case: C3's orbitals, grid and block sizes on the 3x3x3 mesh (V ~2 GB
+    # instead of 12 GB), small enough for multi-pass kernel captures
+    "C3m": CrystalSpec("C3m", "fcc", (3, 3, 3), 52, 250, 120, 100.0, ao_block=(2, 16), aux_block=(4, 64),
+                       seed=20260106),
 }
 
 

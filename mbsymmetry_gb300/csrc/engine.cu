@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -345,8 +346,21 @@ class Engine {
   DBuf<WRef> sig_wref_;
   DBuf<float2> Wbuf_, Bcat_;
   int64_t bcat_elems_ = 0;
-  int sw_smem_ = 0, uv_smem_ = 0, uv_smem_small_ = 0, uv_nblocked_ = 0;
+  int sw_smem_ = 0, uv_smem_ = 0, uv_smem_small_ = 0;
   std::vector<SigTile> sig_tiles1_host_;
+  std::vector<char> uv_blocked_host_;
+  // tau chunks of the tensor-core operands (W for Sigma, Zcat for P0), each
+  // buffer sized to tc_chunk_bytes_: [t0, t1) and the work items of the chunk
+  struct SigChunk { int t0, t1, uv0, nuv_blocked, nuv, w0, nw; };
+  struct P0Chunk { int t0, t1, k0, nk; };
+  std::vector<SigChunk> sig_chunks_;
+  std::vector<P0Chunk> p0_chunks_;
+  int tch_w_ = 1, tch_z_ = 1;
+  int64_t tc_chunk_bytes_ = 1ll << 30;
+  int chunk_len(int64_t elems_per_tau, int ntau) const {  // float2 elements per tau -> tau per chunk
+    const int64_t t = tc_chunk_bytes_ / std::max<int64_t>(1, elems_per_tau * 8);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(ntau, t));
+  }
   int64_t wbuf_elems_ = 0;
   // tcgen05 P0 path: Z tasks (into Zcat), Vcat tasks, split-K tiles, reduction tiles
   DBuf<PzTask> pz_tasks_;
@@ -459,6 +473,18 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
   set_tc_kernel_attributes(smem_bytes_);
   set_tc_p0_kernel_attributes(smem_bytes_);
   GWGB_CUDA(cudaMallocHost(&mu_host_, sizeof(double)));
+  // device memory for one tau chunk of each tensor-core operand buffer (W, Zcat):
+  // an eighth of the free memory, 1 to 16 GiB, unless GWGB_TC_CHUNK_MB says otherwise
+  {
+    size_t free_b = 0, total_b = 0;
+    GWGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    tc_chunk_bytes_ = std::max<int64_t>(1ll << 30, std::min<int64_t>(16ll << 30, (int64_t)(free_b / 8)));
+  }
+  if (const char *e = std::getenv("GWGB_TC_CHUNK_MB")) {
+    const long long mb = std::atoll(e);
+    GWGB_REQUIRE(mb >= 1, GWGB_E_INVALID, "GWGB_TC_CHUNK_MB must be a positive integer");
+    tc_chunk_bytes_ = (int64_t)mb << 20;
+  }
   build_work_lists();
   if (p.precision != GWGB_PREC_FP64) set_precision(p.precision);
   // buffers
@@ -650,76 +676,98 @@ void Engine::build_work_lists() {
     }
   p0_contribs_.upload(pc, st_);
 
-  {  // tcgen05 P0: per aux block, Zcat[(tau,P)][K] and Vcat[Q][K] with K over (contribution, spin)
+  {  // tcgen05 P0: per aux block, Zcat[(tau,P)][K] and Vcat[Q][K] with K over (contribution, spin);
+     // Zcat holds one chunk of tau at a time (tch_z_ values), sized to the chunk budget
     std::vector<PzTask> zt;
     std::vector<VcTask> vt;
     std::vector<PkTile> kt;
     std::vector<PrTile> rt;
-    int64_t zoff = 0, voff = 0, poff = 0;
     int zneed = 0;
     const int SL = 8;  // K slice: 8 chunks of 16 complex columns
+    int zcap = 110 * 1024;  // two CTAs per SM when the one-row minimum of every task fits
+    struct ZGroup { int qb, zld; int64_t zoff, voff; };
+    std::vector<ZGroup> zg;
+    int64_t zrow = 0, voff = 0;
     for (const auto &g : p0_groups_) {
-      const int qb = g.qb;
       int kofs = 0;
-      std::vector<std::pair<int, int>> ent;  // (contribution, spin) -> zcol
-      for (int c = g.c0; c < g.c1; ++c)
-        for (int s = 0; s < ns_; ++s) {
-          ent.push_back({c, kofs});
-          kofs += pc[c].b1 * pc[c].b2;
-        }
+      for (int c = g.c0; c < g.c1; ++c) kofs += ns_ * pc[c].b1 * pc[c].b2;
       const int zld = ((kofs + 15) / 16) * 16;
-      int ei = 0;
+      zg.push_back({g.qb, zld, zrow, voff});
+      zrow += (int64_t)g.qb * zld;
+      voff += (int64_t)g.qb * zld;
+    }
+    tch_z_ = chunk_len(zrow, half);
+    for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {
+      const auto &g = p0_groups_[gi];
+      const int qb = g.qb, zld = zg[gi].zld;
+      const int64_t zoff = zg[gi].zoff * tch_z_;  // group block: tch_z_ rows of qb x zld
+      int zcol = 0;
       for (int c = g.c0; c < g.c1; ++c) {
         const P0Contrib &cb = pc[c];
         const int b1b2 = cb.b1 * cb.b2;
-        for (int s = 0; s < ns_; ++s, ++ei) {
-          const int zcol = ent[ei].second;
+        for (int s = 0; s < ns_; ++s, zcol += b1b2) {
           zt.push_back({cb.v, cb.ga, cb.gb, zoff, cb.sa, cb.sb, cb.b1, cb.b2, qb, s, zld, zcol});
-          vt.push_back({cb.v, voff, qb, b1b2, zld, zcol});
+          vt.push_back({cb.v, zg[gi].voff, qb, b1b2, zld, zcol});
         }
         zneed = std::max(zneed, 8 * (cb.b2 * cb.b2 + cb.b1 * cb.b1 + 2 * b1b2 * qb));
         GWGB_REQUIRE(8 * (cb.b2 * cb.b2 + cb.b1 * cb.b1 + 2 * b1b2) <= smem_bytes_, GWGB_E_UNSUPPORTED,
                      "P0 block too large for the tcgen05 path");
+        if (8 * (cb.b2 * cb.b2 + cb.b1 * cb.b1 + 2 * b1b2) > zcap) zcap = smem_bytes_;
       }
-      const int nchunks = zld / 16;
-      const int nslice = std::max(1, (nchunks + SL - 1) / SL);
-      const int nt = std::max(1, std::min(half, 128 / qb));
       const int NP = ((2 * qb + 15) / 16) * 16;
       GWGB_REQUIRE(NP <= 128, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 P0 kernel");
-      for (int t0 = 0; t0 < half; t0 += nt) {
-        const int n = std::min(nt, half - t0);
-        const int64_t slice = (int64_t)n * qb * qb;
-        for (int sl = 0; sl < nslice; ++sl)
-          kt.push_back({zoff, voff, poff + sl * slice, zld, qb, t0, n, sl * SL, std::max(0, std::min(SL, nchunks - sl * SL)),
-                        NP, 0});
-        rt.push_back({poff, g.pout, g.pstride, qb, t0, n, nslice, 0});
-        poff += nslice * slice;
-      }
-      zoff += (int64_t)half * qb * zld;
-      voff += (int64_t)qb * zld;
     }
-    std::stable_sort(kt.begin(), kt.end(), [](const PkTile &a, const PkTile &b) { return a.kcn > b.kcn; });
+    const int64_t zbuf = zrow * tch_z_;
+    int64_t poff = 0;
+    p0_chunks_.clear();
+    for (int c0 = 0; c0 < half; c0 += tch_z_) {
+      const int c1 = std::min(half, c0 + tch_z_);
+      const size_t k0 = kt.size();
+      for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {
+        const auto &g = p0_groups_[gi];
+        const int qb = g.qb, zld = zg[gi].zld;
+        const int64_t zoff = zg[gi].zoff * tch_z_;
+        const int nchunks = zld / 16;
+        const int nslice = std::max(1, (nchunks + SL - 1) / SL);
+        const int nt = std::max(1, std::min(c1 - c0, 128 / qb));
+        const int NP = ((2 * qb + 15) / 16) * 16;
+        for (int t0 = c0; t0 < c1; t0 += nt) {
+          const int n = std::min(nt, c1 - t0);
+          const int64_t slice = (int64_t)n * qb * qb;
+          for (int sl = 0; sl < nslice; ++sl) {
+            const PkTile t{zoff, zg[gi].voff, poff + sl * slice, zld, qb, t0, n, sl * SL,
+                           std::max(0, std::min(SL, nchunks - sl * SL)), NP, 0};
+            check_range(t.z, (int64_t)(t.t0 - c0 + t.nt) * t.qb * t.zld, zbuf, "P0 tensor-core A tile");
+            GWGB_REQUIRE(t.nt * t.qb <= 128 && t.np <= 128 && (t.kc0 + t.kcn) * 16 <= t.zld, GWGB_E_INVALID,
+                         "internal work list out of bounds: P0 tensor-core tile shape");
+            kt.push_back(t);
+          }
+          rt.push_back({poff, g.pout, g.pstride, qb, t0, n, nslice, 0});
+          poff += nslice * slice;
+        }
+      }
+      std::stable_sort(kt.begin() + k0, kt.end(), [](const PkTile &a, const PkTile &b) { return a.kcn > b.kcn; });
+      p0_chunks_.push_back({c0, c1, (int)k0, (int)(kt.size() - k0)});
+    }
     for (const PzTask &t : zt)
-      check_range(t.z + t.zcol, ((int64_t)(half - 1) * t.qb + (t.qb - 1)) * t.zld + (int64_t)t.b1 * t.b2, zoff,
+      check_range(t.z + t.zcol, ((int64_t)(tch_z_ - 1) * t.qb + (t.qb - 1)) * t.zld + (int64_t)t.b1 * t.b2, zbuf,
                   "Z operand rows");
     for (const VcTask &t : vt) check_range(t.vc + t.zcol, (int64_t)(t.qb - 1) * t.zld + t.b1b2, voff, "V operand rows");
     for (const PkTile &t : kt) {
-      check_range(t.z, (int64_t)(t.t0 + t.nt) * t.qb * t.zld, zoff, "P0 tensor-core A tile");
       check_range(t.vc, (int64_t)t.qb * t.zld, voff, "P0 tensor-core B tile");
       check_range(t.part, (int64_t)t.nt * t.qb * t.qb, poff, "P0 tensor-core partials");
-      GWGB_REQUIRE(t.nt * t.qb <= 128 && t.np <= 128 && (t.kc0 + t.kcn) * 16 <= t.zld, GWGB_E_INVALID,
-                   "internal work list out of bounds: P0 tensor-core tile shape");
     }
     for (const PrTile &t : rt) check_range(t.part, (int64_t)t.nslice * t.nt * t.qb * t.qb, poff, "P0 partial sums");
     pz_tasks_.upload(zt, st_);
     vc_tasks_.upload(vt, st_);
     pk_tiles_.upload(kt, st_);
     pr_tiles_.upload(rt, st_);
-    zbuf_elems_ = zoff;
+    zbuf_elems_ = zbuf;
     vcat_elems_ = voff;
     ppart_elems_ = poff;
-    pz_smem_ = std::min(smem_bytes_, std::max(16 * 1024, ((zneed + 1023) / 1024) * 1024));
+    pz_smem_ = std::min(zcap, std::max(16 * 1024, ((zneed + 1023) / 1024) * 1024));
   }
+
 
   // --- Sigma: owner = (k_irr, AO block i1, spin)
   std::vector<SigContrib> sc;
@@ -765,32 +813,46 @@ void Engine::build_work_lists() {
     check_range(cb.pq, (int64_t)(nts_ - 1) * cb.pstride + (int64_t)cb.qb * cb.qb, po, "Sigma P(q) block");
   }
   sig_contribs_.upload(sc, st_);
-  {  // tcgen05 path, U/Sigma stage: (owner, range of nt tau) tiles, about six waves of two CTAs per SM
+  {  // tcgen05 path, U/Sigma stage: (owner, range of nt tau) tiles, about six waves of two CTAs per SM,
+     // grouped by the tau chunks of the W buffer (tch_w_ values each)
+    int64_t wrow = 0;  // W elements per tau: sum over contributions of q_b k1_b k2_b
+    for (size_t c = 0; c < sc.size(); ++c) wrow += (int64_t)sc[c].qb * sig_b1_[c] * sc[c].b2;
+    tch_w_ = chunk_len(wrow, nts_);
     const int nt_uv = std::max(1, std::min(8, (int)((int64_t)sig_own.size() * nts_ / (12 * std::max(1, nsm_)))));
-    for (const Owner &o : sig_own) {
-      int nt = std::max(1, std::min(nt_uv, (smem_bytes_ / 4) / (24 * o.n * o.n)));
-      double f = 0;
-      for (int c = o.c0; c < o.c1; ++c) f += scost[c];
-      for (int t0 = 0; t0 < nts_; t0 += nt) {
-        const int n = std::min(nt, nts_ - t0);
-        stl.push_back({o.out, 0, o.ostride, o.n, o.c0, o.c1, t0, n, o.s, (int32_t)std::min(f * n / 1e3, 2e9)});
+    std::vector<SigTile> all;
+    uv_blocked_host_.clear();
+    sig_chunks_.clear();
+    for (int c0 = 0; c0 < nts_; c0 += tch_w_) {
+      const int c1 = std::min(nts_, c0 + tch_w_);
+      std::vector<SigTile> stl;
+      for (const Owner &o : sig_own) {
+        int nt = std::max(1, std::min(nt_uv, (smem_bytes_ / 4) / (24 * o.n * o.n)));
+        double f = 0;
+        for (int c = o.c0; c < o.c1; ++c) f += scost[c];
+        for (int t0 = c0; t0 < c1; t0 += nt) {
+          const int n = std::min(nt, c1 - t0);
+          stl.push_back({o.out, 0, o.ostride, o.n, o.c0, o.c1, t0, n, o.s, (int32_t)std::min(f * n / 1e3, 2e9)});
+        }
       }
+      std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
+      // owners whose contributions average fewer than 200 (Q, m) terms take the
+      // unblocked variant (barriers dominate there); each chunk = [blocked | small]
+      std::vector<SigTile> big, small;
+      for (const SigTile &t : stl) {
+        double k = 0;
+        for (int c = t.c0; c < t.c1; ++c) k += (double)sc[c].qb * sc[c].b2;
+        const bool sm = t.c1 > t.c0 && k < 200.0 * (t.c1 - t.c0);
+        (sm ? small : big).push_back(t);
+      }
+      SigChunk ch{c0, c1, (int)all.size(), (int)big.size(), (int)(big.size() + small.size()), 0, 0};
+      for (const SigTile &t : big) { all.push_back(t); uv_blocked_host_.push_back(1); }
+      for (const SigTile &t : small) { all.push_back(t); uv_blocked_host_.push_back(0); }
+      sig_chunks_.push_back(ch);
     }
-    std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
-    // owners whose contributions average fewer than 200 (Q, m) terms take the
-    // unblocked variant (barriers dominate there); tiles = [blocked | small]
-    std::vector<SigTile> big, small;
-    for (const SigTile &t : stl) {
-      double k = 0;
-      for (int c = t.c0; c < t.c1; ++c) k += (double)sc[c].qb * sc[c].b2;
-      const bool sm = t.c1 > t.c0 && k < 200.0 * (t.c1 - t.c0);
-      (sm ? small : big).push_back(t);
-    }
-    uv_nblocked_ = (int)big.size();
-    big.insert(big.end(), small.begin(), small.end());
-    sig_tiles1_.upload(big, st_);
-    sig_tiles1_host_ = big;
+    sig_tiles1_.upload(all, st_);
+    sig_tiles1_host_ = all;
   }
+
 
   // --- FP64 tiles of both contractions and their partial-sum buffer
   {
@@ -877,7 +939,7 @@ void Engine::build_work_lists() {
       for (int c : cs) {
         const int b1b2 = sig_b1_[c] * sc[c].b2;
         bt.push_back({sc[c].v, boff, qb, b1b2, ncol, 0});
-        wr[c] = {woff + ncol, 0};
+        wr[c] = {woff + ncol, 0};  // W rows are (tau - chunk start, Q)
         ncol += b1b2;
       }
       for (int c : cs) wr[c].ld = ncol;
@@ -888,16 +950,20 @@ void Engine::build_work_lists() {
       while (npk > 16 && need(npk) > 200 * 1024) npk /= 2;
       GWGB_REQUIRE(need(npk) <= 200 * 1024, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 Sigma kernel");
       wsmem = std::max(wsmem, need(npk));
-      const int nt = std::max(1, std::min(nts_, 128 / qb));
-      for (int t0 = 0; t0 < nts_; t0 += nt)
-        swt.push_back({pa, boff, woff, pstride, qb, t0, std::min(nt, nts_ - t0), ncol, KP, npk, 0});
+      const int nt = std::max(1, std::min(tch_w_, 128 / qb));
+      for (const SigChunk &ch : sig_chunks_)
+        for (int t0 = ch.t0; t0 < ch.t1; t0 += nt)
+          swt.push_back({pa, boff, woff, pstride, qb, t0, std::min(nt, ch.t1 - t0), ncol, KP, npk, 0});
       boff += (int64_t)ncol * qb;
-      woff += (int64_t)nts_ * qb * ncol;
+      woff += (int64_t)tch_w_ * qb * ncol;
     }
     int uvneed_small = 0;
-    for (size_t n = 0; n < sig_tiles1_host_.size(); ++n) {  // [blocked | small]
+    // the U/Sigma stage keeps large Q chunks (one CTA per SM measured faster than two
+    // CTAs with half the chunk); the Z stage of P0 takes two CTAs per SM
+    int uv_cap = smem_bytes_;
+    for (size_t n = 0; n < sig_tiles1_host_.size(); ++n) {
       const SigTile &t = sig_tiles1_host_[n];
-      const bool blocked = (int)n < uv_nblocked_;
+      const bool blocked = uv_blocked_host_[n] != 0;
       int b2max = 1, qbmax = 1;
       for (int c = t.c0; c < t.c1; ++c) { b2max = std::max(b2max, sc[c].b2); qbmax = std::max(qbmax, sc[c].qb); }
       // acc64, acc32, red (blocked variant only), G2
@@ -906,11 +972,25 @@ void Engine::build_work_lists() {
       need = std::max(need, fixed + 24 * t.b1 * b2max * qbmax);
       GWGB_REQUIRE(fixed + 24 * t.b1 * b2max <= smem_bytes_, GWGB_E_UNSUPPORTED,
                    "Sigma block too large for the tcgen05 path");
+      if (fixed + 24 * t.b1 * b2max > uv_cap) uv_cap = smem_bytes_;
     }
-    uv_smem_small_ = std::min(smem_bytes_, std::max(16 * 1024, ((uvneed_small + 1023) / 1024) * 1024));
-    std::stable_sort(swt.begin(), swt.end(), [](const SwTile &a, const SwTile &b) { return a.ncol > b.ncol; });
+    uv_smem_small_ = std::min(uv_cap, std::max(16 * 1024, ((uvneed_small + 1023) / 1024) * 1024));
+    // tiles grouped by W chunk, widest first within a chunk
+    std::stable_sort(swt.begin(), swt.end(), [&](const SwTile &a, const SwTile &b) {
+      const int ca = a.t0 / tch_w_, cb = b.t0 / tch_w_;
+      return ca != cb ? ca < cb : a.ncol > b.ncol;
+    });
+    for (SigChunk &ch : sig_chunks_) {
+      ch.w0 = (int)(std::lower_bound(swt.begin(), swt.end(), ch.t0,
+                                     [&](const SwTile &t, int v) { return t.t0 / tch_w_ < v / tch_w_; }) -
+                    swt.begin());
+      ch.nw = (int)(std::upper_bound(swt.begin(), swt.end(), ch.t0,
+                                     [&](int v, const SwTile &t) { return v / tch_w_ < t.t0 / tch_w_; }) -
+                    swt.begin()) - ch.w0;
+    }
     for (const SwTile &t : swt) {
-      check_range(t.wcat, (int64_t)(t.t0 + t.nt) * t.qb * t.ncol, woff, "W rows");
+      const int t0c = (t.t0 / tch_w_) * tch_w_;  // chunk start
+      check_range(t.wcat, (int64_t)(t.t0 - t0c + t.nt) * t.qb * t.ncol, woff, "W rows");
       check_range(t.bcat, (int64_t)t.ncol * t.qb, boff, "conj(V) operand");
       GWGB_REQUIRE(t.nt * t.qb <= 128 && 2 * t.npk <= 128, GWGB_E_INVALID,
                    "internal work list out of bounds: Sigma tensor-core tile shape");
@@ -923,7 +1003,7 @@ void Engine::build_work_lists() {
     bc_tasks_.upload(bt, st_);
     sig_wref_.upload(wr, st_);
     sw_smem_ = std::max(16 * 1024, wsmem);
-    uv_smem_ = std::min(smem_bytes_, std::max(16 * 1024, ((uvneed + 1023) / 1024) * 1024));
+    uv_smem_ = std::min(uv_cap, std::max(16 * 1024, ((uvneed + 1023) / 1024) * 1024));
     wbuf_elems_ = woff;
     bcat_elems_ = boff;
   }
@@ -1103,9 +1183,13 @@ void Engine::k_p0(int mirror) {
   const double pref = -1.0 / l_.nk * (ns_ == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
   if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE((Zbuf_.p || !zbuf_elems_) && vcat_ready_, GWGB_E_STATE, "mixed-precision work buffers missing");
-    launch_p0_tc(prec_ == GWGB_PREC_BF16X3, pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pk_tiles_.p, (int)pk_tiles_.n, pr_tiles_.p,
-                 (int)pr_tiles_.n, V_.p, Gall_.p, Zbuf_.p, Vcat_.p, Ppart_.p, Pall_.p, ns_, nts_, pref, mirror,
-                 bad_.p + 2, st_);
+    for (size_t i = 0; i < p0_chunks_.size(); ++i) {
+      const P0Chunk &ch = p0_chunks_[i];
+      const bool last = i + 1 == p0_chunks_.size();  // the slice sums run once, after the last chunk
+      launch_p0_tc(prec_ == GWGB_PREC_BF16X3, pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pk_tiles_.p + ch.k0, ch.nk,
+                   pr_tiles_.p, last ? (int)pr_tiles_.n : 0, V_.p, Gall_.p, Zbuf_.p, Vcat_.p, Ppart_.p, Pall_.p, ns_,
+                   nts_, ch.t0, ch.t1, pref, mirror, bad_.p + 2, st_);
+    }
   } else {
     launch_p0_fp64(p0_tiles_.p, (int)p0_tiles_.n, p0_maxo_, p0_contribs_.p, V_.p, Gall_.p, Part_.p, ns_, nts_,
                    fp64_smem_, st_);
@@ -1127,9 +1211,10 @@ void Engine::k_rotate_P() {
 void Engine::k_sigma() {
   if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
-    launch_sigma_tc(prec_ == GWGB_PREC_BF16X3, sw_tiles_.p, (int)sw_tiles_.n, sw_smem_, Bcat_.p, sig_tiles1_.p, (int)sig_tiles1_.n,
-                    sig_contribs_.p, sig_wref_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p, Sig_.p, ns_, -1.0 / l_.nk, uv_smem_,
-                    uv_nblocked_, uv_smem_small_, bad_.p + 2, st_);
+    for (const SigChunk &ch : sig_chunks_)
+      launch_sigma_tc(prec_ == GWGB_PREC_BF16X3, sw_tiles_.p + ch.w0, ch.nw, sw_smem_, Bcat_.p,
+                      sig_tiles1_.p + ch.uv0, ch.nuv, sig_contribs_.p, sig_wref_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p,
+                      Sig_.p, ns_, -1.0 / l_.nk, uv_smem_, ch.nuv_blocked, uv_smem_small_, ch.t0, bad_.p + 2, st_);
   } else {
     launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Part_.p,
                       ns_, fp64_smem_, st_);
@@ -1185,9 +1270,13 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
   int64_t launches = 0;
   if (with_gw) {
     const bool tc = prec_ != GWGB_PREC_FP64;
-    const int64_t p0 = tc ? (pz_tasks_.n ? 1 : 0) + (pk_tiles_.n ? 1 : 0) + (pr_tiles_.n ? 1 : 0)
+    int64_t sgt = 0, p0t = 0;
+    for (const SigChunk &ch : sig_chunks_)
+      sgt += (ch.nw ? 1 : 0) + (ch.nuv_blocked ? 1 : 0) + (ch.nuv > ch.nuv_blocked ? 1 : 0);
+    for (const P0Chunk &ch : p0_chunks_) p0t += (pz_tasks_.n ? 1 : 0) + (ch.nk ? 1 : 0);
+    const int64_t p0 = tc ? p0t + (pr_tiles_.n ? 1 : 0)
                           : (p0_tiles_.n ? 1 : 0) + (p0_red_.n ? 1 : 0);
-    const int64_t sg = tc ? (sw_tiles_.n ? 1 : 0) + (uv_nblocked_ > 0 ? 1 : 0) + ((int)sig_tiles1_.n > uv_nblocked_ ? 1 : 0)
+    const int64_t sg = tc ? sgt
                           : (sig_tiles_.n ? 1 : 0) + (sig_red_.n ? 1 : 0);
     launches += (rotG_.n ? 1 : 0) + p0 + 3 + (rotP_.n ? 1 : 0) + sg;
   }

@@ -88,7 +88,7 @@ template <bool BF>
 __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restrict__ tiles,
                                                          const float2 *__restrict__ Bcat,
                                                          const double2 *__restrict__ P, float2 *__restrict__ W,
-                                                         int *__restrict__ err) {
+                                                         int tau0, int *__restrict__ err) {
   using PL = Planes<BF>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ uint32_t tmem_slot;
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
   const int r = (warp & 3) * 32 + lane;  // warps 0-3 drain (TMEM lanes), warps 4-7 only stage
   const bool live = warp < 4 && r < rows;
   const int it = live ? r / qb : 0, Q = live ? r - (r / qb) * qb : 0;
-  float2 *wrow = W + tl.wcat + ((int64_t)(tl.t0 + it) * qb + Q) * tl.ncol;
+  float2 *wrow = W + tl.wcat + ((int64_t)(tl.t0 - tau0 + it) * qb + Q) * tl.ncol;  // W holds one tau chunk
   for (int pk = 0; pk < npacks && ok; ++pk) {
     if (pk + 1 < npacks) stage_b(pk + 1);  // buffer (pk+1)&1 was read by MMA pk-1, already complete
     tc::fence_async_smem();
@@ -224,7 +224,8 @@ void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat
 __device__ __forceinline__ void sigma_uv_small(const SigTile &tile, const SigContrib *__restrict__ contribs,
                                                const WRef *__restrict__ wref, const double2 *__restrict__ V,
                                                const double2 *__restrict__ G, const float2 *__restrict__ W,
-                                               double2 *__restrict__ Sig, int ns, double scale, int smem_bytes) {
+                                               double2 *__restrict__ Sig, int ns, double scale, int smem_bytes,
+    int tau0) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const int b1 = tile.b1, s = tile.s, nt = tile.nt, bb = b1 * b1;
   const int tid = threadIdx.x;
@@ -260,7 +261,7 @@ __device__ __forceinline__ void sigma_uv_small(const SigTile &tile, const SigCon
       for (int it = 0; it < nt; ++it) {
         const int tau = tile.t0 + it;
         const double2 *G2 = G + cb.gb + ((int64_t)tau * ns + s) * cb.sb;
-        const float2 *Wt = W + wr.base + ((int64_t)tau * qb + q0) * wr.ld;
+        const float2 *Wt = W + wr.base + ((int64_t)(tau - tau0) * qb + q0) * wr.ld;  // W holds one tau chunk
         __syncthreads();
         for (int e = tid; e < b2 * b2; e += 256) {
           const double2 g = __ldg(G2 + e);
@@ -356,7 +357,8 @@ constexpr int UV_MB = 8;   // U-stage outputs per thread
 __device__ __forceinline__ void sigma_uv_blocked(const SigTile &tile, const SigContrib *__restrict__ contribs,
                                                  const WRef *__restrict__ wref, const double2 *__restrict__ V,
                                                  const double2 *__restrict__ G, const float2 *__restrict__ W,
-                                                 double2 *__restrict__ Sig, int ns, double scale, int smem_bytes) {
+                                                 double2 *__restrict__ Sig, int ns, double scale, int smem_bytes,
+    int tau0) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const int b1 = tile.b1, s = tile.s, nt = tile.nt, bb = b1 * b1;
   const int tid = threadIdx.x;
@@ -395,7 +397,7 @@ __device__ __forceinline__ void sigma_uv_blocked(const SigTile &tile, const SigC
       for (int it = 0; it < nt; ++it) {
         const int tau = tile.t0 + it;
         const double2 *G2 = G + cb.gb + ((int64_t)tau * ns + s) * cb.sb;
-        const float2 *Wt = W + wr.base + ((int64_t)tau * qb + q0) * wr.ld;
+        const float2 *Wt = W + wr.base + ((int64_t)(tau - tau0) * qb + q0) * wr.ld;  // W holds one tau chunk
         __syncthreads();
         for (int e = tid; e < b2 * b2; e += 256) {
           const double2 gg = __ldg(G2 + e);
@@ -503,9 +505,9 @@ __global__ void __launch_bounds__(256) sigma_uv_blocked_kernel(const SigTile *__
                                                                const double2 *__restrict__ G,
                                                                const float2 *__restrict__ W,
                                                                double2 *__restrict__ Sig, int ns, double scale,
-                                                               int smem_bytes) {
+                                                               int smem_bytes, int tau0) {
   const SigTile tile = tiles[blockIdx.x];
-  sigma_uv_blocked(tile, contribs, wref, V, G, W, Sig, ns, scale, smem_bytes);
+  sigma_uv_blocked(tile, contribs, wref, V, G, W, Sig, ns, scale, smem_bytes, tau0);
 }
 
 __global__ void __launch_bounds__(256) sigma_uv_small_kernel(const SigTile *__restrict__ tiles,
@@ -515,31 +517,31 @@ __global__ void __launch_bounds__(256) sigma_uv_small_kernel(const SigTile *__re
                                                              const double2 *__restrict__ G,
                                                              const float2 *__restrict__ W,
                                                              double2 *__restrict__ Sig, int ns, double scale,
-                                                             int smem_bytes) {
+                                                             int smem_bytes, int tau0) {
   const SigTile tile = tiles[blockIdx.x];
-  sigma_uv_small(tile, contribs, wref, V, G, W, Sig, ns, scale, smem_bytes);
+  sigma_uv_small(tile, contribs, wref, V, G, W, Sig, ns, scale, smem_bytes, tau0);
 }
 
 void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
                      int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
                      const double2 *G, const double2 *P, float2 *W, double2 *Sig, int ns, double scale,
-                     int uv_smem, int nblocked, int uv_smem_small, int *err, cudaStream_t st) {
+                     int uv_smem, int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st) {
   if (nwtiles > 0) {
     if (bf16)
-      sigma_w_tc_kernel<true><<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, err);
+      sigma_w_tc_kernel<true><<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, tau0, err);
     else
-      sigma_w_tc_kernel<false><<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, err);
+      sigma_w_tc_kernel<false><<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, tau0, err);
     GWGB_CUDA(cudaGetLastError());
   }
   // tiles1 = [blocked tiles (nblocked) | small tiles]
   if (nblocked > 0) {
     sigma_uv_blocked_kernel<<<nblocked, 256, uv_smem, st>>>(tiles1, contribs, wref, V, G, W, Sig, ns, scale,
-                                                             uv_smem);
+                                                             uv_smem, tau0);
     GWGB_CUDA(cudaGetLastError());
   }
   if (ntiles1 > nblocked) {
     sigma_uv_small_kernel<<<ntiles1 - nblocked, 256, uv_smem_small, st>>>(tiles1 + nblocked, contribs, wref, V, G, W,
-                                                                          Sig, ns, scale, uv_smem_small);
+                                                                          Sig, ns, scale, uv_smem_small, tau0);
     GWGB_CUDA(cudaGetLastError());
   }
 }
@@ -573,7 +575,7 @@ namespace gwgb {
 constexpr int ZB = 8;  // outputs per thread in the Z stage products
 __global__ void __launch_bounds__(256) p0_z_kernel(const PzTask *__restrict__ tasks, const double2 *__restrict__ V,
                                                    const double2 *__restrict__ G, float2 *__restrict__ Z, int ns,
-                                                   int nts, int smem_bytes) {
+                                                   int nts, int smem_bytes, int tau0, int tau1) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const PzTask tk = tasks[blockIdx.x];
   const int b1 = tk.b1, b2 = tk.b2, qb = tk.qb, blk = b1 * b2;
@@ -595,7 +597,7 @@ __global__ void __launch_bounds__(256) p0_z_kernel(const PzTask *__restrict__ ta
       const double2 v = __ldg(Vb + (int64_t)p0 * blk + e);
       Vs[e] = make_float2((float)v.x, (float)v.y);
     }
-    for (int tau = 0; tau < nts / 2; ++tau) {
+    for (int tau = tau0; tau < tau1; ++tau) {  // one tau chunk of Zcat
       const double2 *G2 = G + tk.gb + ((int64_t)tau * ns + tk.s) * tk.sb;
       const double2 *Gm = G + tk.ga + ((int64_t)(nts - 1 - tau) * ns + tk.s) * tk.sa;
       __syncthreads();
@@ -635,7 +637,7 @@ __global__ void __launch_bounds__(256) p0_z_kernel(const PzTask *__restrict__ ta
       __syncthreads();
       // Z[P][(p,m)] = sum_t Gm[t][p] X2[P][t][m]: (P, m), up to ZB values of p
       //   -> Zcat row (tau, p0 + P), columns zcol + p*b2 + m
-      float2 *Zt = Z + tk.z + ((int64_t)tau * qb + p0) * tk.zld + tk.zcol;
+      float2 *Zt = Z + tk.z + ((int64_t)(tau - tau0) * qb + p0) * tk.zld + tk.zcol;
       for (int item = tid; item < pn * b2 * pch; item += 256) {
         const int P = item / (b2 * pch);
         const int rem = item - P * b2 * pch;
@@ -673,7 +675,7 @@ __global__ void __launch_bounds__(256) p0_z_kernel(const PzTask *__restrict__ ta
 template <bool BF>
 __global__ void __launch_bounds__(256) p0_tc_kernel(const PkTile *__restrict__ tiles,
                                                     const float2 *__restrict__ Z, const float2 *__restrict__ Vcat,
-                                                    double2 *__restrict__ Ppart, int *__restrict__ err) {
+                                                    double2 *__restrict__ Ppart, int tau0, int *__restrict__ err) {
   using PL = Planes<BF>;
   constexpr int KP = 32;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -694,7 +696,7 @@ __global__ void __launch_bounds__(256) p0_tc_kernel(const PkTile *__restrict__ t
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
   const int rows = tl.nt * qb;
-  const float2 *Zb = Z + tl.z + (int64_t)tl.t0 * qb * tl.zld;
+  const float2 *Zb = Z + tl.z + (int64_t)(tl.t0 - tau0) * qb * tl.zld;  // Zcat holds one tau chunk
   const float2 *Vb = Vcat + tl.vc;
   bool ok = true;
   uint32_t phase = 0;
@@ -798,16 +800,17 @@ void launch_vcat(const VcTask *tasks, int ntasks, const double2 *V, float2 *Vcat
 
 void launch_p0_tc(bool bf16, const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
                   int nr, const double2 *V, const double2 *G, float2 *Z, const float2 *Vcat, double2 *Ppart,
-                  double2 *P0, int ns, int nts, double pref, int mirror, int *err, cudaStream_t st) {
+                  double2 *P0, int ns, int nts, int tau0, int tau1, double pref, int mirror, int *err,
+                  cudaStream_t st) {
   if (nz > 0) {
-    p0_z_kernel<<<nz, 256, zsmem, st>>>(ztasks, V, G, Z, ns, nts, zsmem);
+    p0_z_kernel<<<nz, 256, zsmem, st>>>(ztasks, V, G, Z, ns, nts, zsmem, tau0, tau1);
     GWGB_CUDA(cudaGetLastError());
   }
   if (nk > 0) {
     if (bf16)
-      p0_tc_kernel<true><<<nk, 256, 64 * 1024, st>>>(ktiles, Z, Vcat, Ppart, err);
+      p0_tc_kernel<true><<<nk, 256, 64 * 1024, st>>>(ktiles, Z, Vcat, Ppart, tau0, err);
     else
-      p0_tc_kernel<false><<<nk, 256, 64 * 1024, st>>>(ktiles, Z, Vcat, Ppart, err);
+      p0_tc_kernel<false><<<nk, 256, 64 * 1024, st>>>(ktiles, Z, Vcat, Ppart, tau0, err);
     GWGB_CUDA(cudaGetLastError());
   }
   if (nr > 0) {

@@ -41,7 +41,7 @@ struct WRef {
 void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
                      int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
                      const double2 *G, const double2 *P, float2 *W, double2 *Sig, int ns, double scale,
-                     int uv_smem, int nblocked, int uv_smem_small, int *err, cudaStream_t st);
+                     int uv_smem, int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st);
 
 void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat, cudaStream_t st);
 
@@ -95,7 +95,8 @@ struct PrTile {
 
 void launch_p0_tc(bool bf16, const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
                   int nr, const double2 *V, const double2 *G, float2 *Z, const float2 *Vcat, double2 *Ppart,
-                  double2 *P0, int ns, int nts, double pref, int mirror, int *err, cudaStream_t st);
+                  double2 *P0, int ns, int nts, int tau0, int tau1, double pref, int mirror, int *err,
+                  cudaStream_t st);
 
 void launch_vcat(const VcTask *tasks, int ntasks, const double2 *V, float2 *Vcat, cudaStream_t st);
 

@@ -81,3 +81,29 @@ def test_mixed_sigma_error(name, kind):
     print(f"{name}: max|Sigma_{kind} - Sigma_fp64| = {err:.3e} (max|Sigma| = {np.abs(S64).max():.3e}), "
           f"max|P~ err| = {np.abs(P32 - P64).max():.3e}")
     assert err < 1e-5 * max(1.0, np.abs(S64).max())
+
+
+@pytest.mark.parametrize("kind", ["tf32x3", "bf16x3"])
+def test_mixed_tau_chunks_are_exact(kind, monkeypatch):
+    """The tensor-core operand buffers (W, Zcat) hold one tau chunk at a time,
+    sized to a memory budget.  Forcing one tau per chunk (GWGB_TC_CHUNK_MB=1)
+    must give bitwise the same Sigma and P~ as the default single chunk."""
+    from mbsymmetry_gb300.solver import GWSolver
+    cr, tr = crystal("C2")
+    out = []
+    for env in (None, "1"):
+        if env is None:
+            monkeypatch.delenv("GWGB_TC_CHUNK_MB", raising=False)
+        else:
+            monkeypatch.setenv("GWGB_TC_CHUNK_MB", env)
+        s = GWSolver(cr.layout, cr.ns, tr, precision=kind)
+        s.set_shared_Coulomb(cr.V)
+        s.set_fock(cr.F, cr.S)
+        s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+        s.dyson(cr.mu)
+        s.solve()
+        out.append((s.Selfenergy(), s.P0_q_t_QP(), s.stats()["kernel_launches"]))
+        s.close()
+    (s1, p1, n1), (s2, p2, n2) = out
+    assert n2 > n1                      # the chunked run really launched per chunk
+    assert np.array_equal(p1, p2) and np.array_equal(s1, s2)
