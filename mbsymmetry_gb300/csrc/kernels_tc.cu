@@ -54,6 +54,41 @@ struct Planes {
       *reinterpret_cast<uint32_t *>(base + plane_bytes + off) = l;
     }
   }
+  // four consecutive K elements of one row (a 16-byte TF32 / 8-byte BF16 segment
+  // of a core-matrix row): one vector store per plane
+  __device__ static void store4(unsigned char *base, uint32_t plane_bytes, uint32_t off, float4 x) {
+    if constexpr (BF) {
+      const float v[4] = {x.x, x.y, x.z, x.w};
+      uint32_t w[3][2];
+#pragma unroll
+      for (int j = 0; j < 4; j += 2) {
+        unsigned short b[3][2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const __nv_bfloat16 b0 = __float2bfloat16_rn(v[j + h]);
+          const float r1 = v[j + h] - __bfloat162float(b0);
+          const __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
+          const __nv_bfloat16 b2 = __float2bfloat16_rn(r1 - __bfloat162float(b1));
+          b[0][h] = __bfloat16_as_ushort(b0);
+          b[1][h] = __bfloat16_as_ushort(b1);
+          b[2][h] = __bfloat16_as_ushort(b2);
+        }
+#pragma unroll
+        for (int pl = 0; pl < 3; ++pl) w[pl][j / 2] = (uint32_t)b[pl][0] | ((uint32_t)b[pl][1] << 16);
+      }
+#pragma unroll
+      for (int pl = 0; pl < 3; ++pl)
+        *reinterpret_cast<uint2 *>(base + pl * plane_bytes + off) = make_uint2(w[pl][0], w[pl][1]);
+    } else {
+      uint4 h, l;
+      h.x = tc::to_tf32(x.x); l.x = tc::to_tf32(x.x - __uint_as_float(h.x));
+      h.y = tc::to_tf32(x.y); l.y = tc::to_tf32(x.y - __uint_as_float(h.y));
+      h.z = tc::to_tf32(x.z); l.z = tc::to_tf32(x.z - __uint_as_float(h.z));
+      h.w = tc::to_tf32(x.w); l.w = tc::to_tf32(x.w - __uint_as_float(h.w));
+      *reinterpret_cast<uint4 *>(base + off) = h;
+      *reinterpret_cast<uint4 *>(base + plane_bytes + off) = l;
+    }
+  }
   __device__ static uint32_t idesc(int M, int Nn) { return BF ? tc::idesc_bf16(M, Nn) : tc::idesc_tf32(M, Nn); }
   // all split products of one K step (byte offset koff inside every plane)
   __device__ static void mma_step(uint32_t d, uint32_t a, uint32_t apl, uint32_t b, uint32_t bpl, uint32_t koff,
@@ -107,31 +142,40 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
     tc::mbar_init(&mbar[1], 1);
   }
   const int rows = tl.nt * qb;
-  // A: rows (tau, Q) of P(tau), K = (P, re/im); every row is qb contiguous complex
-  for (int e = tid; e < 128 * (KP / 2); e += 256) {
-    const int r = e / (KP / 2), kc = e - r * (KP / 2);
-    double2 v = make_double2(0.0, 0.0);
-    if (r < rows && kc < qb) {
+  // A: rows (tau, Q) of P(tau), K = (P, re/im); every row is qb contiguous complex.
+  // A lane writes one K quad (two complex) of one row; a warp covers 8 rows x 4 quads
+  // (contiguous core-matrix bytes: conflict-free vector stores).
+  const int nq = KP / 4;
+  for (int e = tid; e < 128 * nq; e += 256) {
+    const int rl = e & 7, rest = e >> 3;
+    const int q = rest % nq, r = (rest / nq) * 8 + rl;
+    double2 v0 = make_double2(0.0, 0.0), v1 = v0;
+    if (r < rows) {
       const int it = r / qb, Q = r - it * qb;
-      v = __ldg(P + tl.pa + (int64_t)(tl.t0 + it) * tl.pstride + (int64_t)Q * qb + kc);
+      const double2 *row = P + tl.pa + (int64_t)(tl.t0 + it) * tl.pstride + (int64_t)Q * qb;
+      if (2 * q < qb) v0 = __ldg(row + 2 * q);
+      if (2 * q + 1 < qb) v1 = __ldg(row + 2 * q + 1);
     }
-    PL::store(A, apl, PL::off(r, 2 * kc, KP), (float)v.x);
-    PL::store(A, apl, PL::off(r, 2 * kc + 1, KP), (float)v.y);
+    PL::store4(A, apl, PL::off(r, 4 * q, KP), make_float4((float)v0.x, (float)v0.y, (float)v1.x, (float)v1.y));
   }
   const int npacks = (tl.ncol + SW_PACK - 1) / SW_PACK;
   auto stage_b = [&](int pk) {
     unsigned char *B = Bb + (pk & 1) * PL::N * bpl;
     const int c0 = pk * SW_PACK;
-    // rows (col, d) of the real embedding of B = conj(V): d=0 -> (Br, -Bi), d=1 -> (Bi, Br), Br = Vr, Bi = -Vi
-    for (int e = tid; e < SW_PACK * (KP / 2); e += 256) {
-      const int cl = e / (KP / 2), kc = e - cl * (KP / 2);
+    // rows (col, d) of the real embedding of B = conj(V): d=0 -> (Br, -Bi), d=1 -> (Bi, Br), Br = Vr, Bi = -Vi;
+    // a lane writes one K quad (two complex) of both rows of one column
+    for (int e = tid; e < SW_PACK * nq; e += 256) {
+      const int cll = e & 3, rest = e >> 2;
+      const int q = rest % nq, cl = (rest / nq) * 4 + cll;
       const int col = c0 + cl;
-      float2 bv = make_float2(0.f, 0.f);  // conj(V) as stored
-      if (col < tl.ncol && kc < qb) bv = Bcat[tl.bcat + (int64_t)col * qb + kc];
-      PL::store(B, bpl, PL::off(2 * cl, 2 * kc, KP), bv.x);
-      PL::store(B, bpl, PL::off(2 * cl, 2 * kc + 1, KP), -bv.y);
-      PL::store(B, bpl, PL::off(2 * cl + 1, 2 * kc, KP), bv.y);
-      PL::store(B, bpl, PL::off(2 * cl + 1, 2 * kc + 1, KP), bv.x);
+      float2 b0 = make_float2(0.f, 0.f), b1 = b0;  // conj(V) as stored
+      if (col < tl.ncol) {
+        const float2 *bc = Bcat + tl.bcat + (int64_t)col * qb;
+        if (2 * q < qb) b0 = bc[2 * q];
+        if (2 * q + 1 < qb) b1 = bc[2 * q + 1];
+      }
+      PL::store4(B, bpl, PL::off(2 * cl, 4 * q, KP), make_float4(b0.x, -b0.y, b1.x, -b1.y));
+      PL::store4(B, bpl, PL::off(2 * cl + 1, 4 * q, KP), make_float4(b0.y, b0.x, b1.y, b1.x));
     }
   };
   const uint32_t idesc = PL::idesc(128, 2 * SW_PACK);
@@ -702,23 +746,26 @@ __global__ void __launch_bounds__(256) p0_tc_kernel(const PkTile *__restrict__ t
   uint32_t phase = 0;
   for (int ch = 0; ch < tl.kcn && ok; ++ch) {
     const int kbase = (tl.kc0 + ch) * 16;
-    // A: 128 rows x 16 complex, row r = (tau, P); zero rows beyond `rows`
+    // A: 128 rows x 16 complex, row r = (tau, P); zero rows beyond `rows`.  A lane
+    // loads two complex (16 B) and writes one K quad; a warp covers 8 rows x 4 quads.
 #pragma unroll 4
-    for (int e = tid; e < 128 * 16; e += 256) {
-      const int r = e >> 4, kk = e & 15;
-      const float2 z = r < rows ? Zb[(int64_t)r * tl.zld + kbase + kk] : make_float2(0.f, 0.f);
-      PL::store(A, apl, PL::off(r, 2 * kk, KP), z.x);
-      PL::store(A, apl, PL::off(r, 2 * kk + 1, KP), z.y);
+    for (int e = tid; e < 128 * 8; e += 256) {
+      const int r = (e >> 6) * 8 + (e & 7), q = (e >> 3) & 7;
+      float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r < rows) z = *reinterpret_cast<const float4 *>(Zb + (int64_t)r * tl.zld + kbase + 2 * q);
+      PL::store4(A, apl, PL::off(r, 4 * q, KP), z);
     }
-    // B: rows (Q, d) of the real embedding of V^T: d=0 -> (Vr, -Vi), d=1 -> (Vi, Vr)
+    // B: rows (Q, d) of the real embedding of V^T: d=0 -> (Vr, -Vi), d=1 -> (Vi, Vr);
+    // a lane writes one K quad of both rows of one Q
 #pragma unroll 2
-    for (int e = tid; e < (NP / 2) * 16; e += 256) {
-      const int Q = e >> 4, kk = e & 15;
-      const float2 v = Q < qb ? Vb[(int64_t)Q * tl.zld + kbase + kk] : make_float2(0.f, 0.f);
-      PL::store(B, bpl, PL::off(2 * Q, 2 * kk, KP), v.x);
-      PL::store(B, bpl, PL::off(2 * Q, 2 * kk + 1, KP), -v.y);
-      PL::store(B, bpl, PL::off(2 * Q + 1, 2 * kk, KP), v.y);
-      PL::store(B, bpl, PL::off(2 * Q + 1, 2 * kk + 1, KP), v.x);
+    for (int e = tid; e < (NP / 2) * 8; e += 256) {
+      const int Q = (e >> 5) * 4 + (e & 3), q = (e >> 2) & 7;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (Q < qb) v = *reinterpret_cast<const float4 *>(Vb + (int64_t)Q * tl.zld + kbase + 2 * q);
+      if (Q < NP / 2) {
+        PL::store4(B, bpl, PL::off(2 * Q, 4 * q, KP), make_float4(v.x, -v.y, v.z, -v.w));
+        PL::store4(B, bpl, PL::off(2 * Q + 1, 4 * q, KP), make_float4(v.y, v.x, v.w, v.z));
+      }
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
