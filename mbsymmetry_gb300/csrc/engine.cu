@@ -351,7 +351,9 @@ class Engine {
   std::vector<char> uv_blocked_host_;
   // tau chunks of the tensor-core operands (W for Sigma, Zcat for P0), each
   // buffer sized to tc_chunk_bytes_: [t0, t1) and the work items of the chunk
-  struct SigChunk { int t0, t1, uv0, nuv_blocked, nuv, w0, nw; };
+  struct SigChunk { int t0, t1, uv0, nuv_blocked, nuv, w0, nw, red0, nred; };
+  DBuf<RedTask> uv_red_;     // ordered sums of the FP32-stage slices, per chunk
+  int64_t uv_part_need_ = 0;
   struct P0Chunk { int t0, t1, k0, nk; };
   std::vector<SigChunk> sig_chunks_;
   std::vector<P0Chunk> p0_chunks_;
@@ -525,7 +527,7 @@ Engine::~Engine() {
   if (mu_host_) cudaFreeHost(mu_host_);
   DBuf<double2> *bufs[] = {&V_, &Gall_, &Pall_, &Sig_, &Pw_, &Ww_, &F_, &S_, &orep_, &auxrep_,
                            &Tnt_, &Ttn_, &TntBF_, &TtnFB_};
-  sw_tiles_.free(); bc_tasks_.free(); sig_wref_.free(); Wbuf_.free(); Bcat_.free();
+  sw_tiles_.free(); bc_tasks_.free(); sig_wref_.free(); Wbuf_.free(); Bcat_.free(); uv_red_.free();
   pz_tasks_.free(); vc_tasks_.free(); pk_tiles_.free(); pr_tiles_.free(); Zbuf_.free(); Vcat_.free(); Ppart_.free();
   for (auto *b : bufs) b->free();
   tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
@@ -813,29 +815,53 @@ void Engine::build_work_lists() {
     check_range(cb.pq, (int64_t)(nts_ - 1) * cb.pstride + (int64_t)cb.qb * cb.qb, po, "Sigma P(q) block");
   }
   sig_contribs_.upload(sc, st_);
-  {  // tcgen05 path, U/Sigma stage: (owner, range of nt tau) tiles, about six waves of two CTAs per SM,
-     // grouped by the tau chunks of the W buffer (tch_w_ values each)
+  {  // tcgen05 path, U/Sigma stage: (owner, tau range, contribution slice) tiles, cost-balanced to
+     // about six waves per chunk of the W buffer (tch_w_ tau each); each tile writes an FP64
+     // partial block, summed in order per chunk (reduce_slices_kernel)
     int64_t wrow = 0;  // W elements per tau: sum over contributions of q_b k1_b k2_b
     for (size_t c = 0; c < sc.size(); ++c) wrow += (int64_t)sc[c].qb * sig_b1_[c] * sc[c].b2;
     tch_w_ = chunk_len(wrow, nts_);
-    const int nt_uv = std::max(1, std::min(8, (int)((int64_t)sig_own.size() * nts_ / (12 * std::max(1, nsm_)))));
+    std::vector<double> ucost(sc.size());  // FP32-stage flops per contribution and tau
+    double utotal = 0;
+    for (size_t c = 0; c < sc.size(); ++c) {
+      ucost[c] = 8.0 * sc[c].qb * sig_b1_[c] * sc[c].b2 * (sig_b1_[c] + sc[c].b2);
+      utotal += ucost[c];
+    }
+    // Slices depend on the per-tau cost only (about one wave of slices per tau), never on
+    // the chunk length: the order of the FP64 sums, hence every result bit, is the same
+    // for any chunking.  Tiles span at most 4 tau.
+    const double target = utotal * ns_ / (double)std::max(1, nsm_);
+    std::vector<std::vector<std::pair<int, int>>> oslices(sig_own.size());
+    for (size_t i = 0; i < sig_own.size(); ++i)
+      oslices[i] = split_slices(ucost, sig_own[i].c0, sig_own[i].c1, target);
     std::vector<SigTile> all;
+    std::vector<RedTask> ured;
     uv_blocked_host_.clear();
     sig_chunks_.clear();
+    uv_part_need_ = 0;
     for (int c0 = 0; c0 < nts_; c0 += tch_w_) {
       const int c1 = std::min(nts_, c0 + tch_w_);
       std::vector<SigTile> stl;
-      for (const Owner &o : sig_own) {
-        int nt = std::max(1, std::min(nt_uv, (smem_bytes_ / 4) / (24 * o.n * o.n)));
-        double f = 0;
-        for (int c = o.c0; c < o.c1; ++c) f += scost[c];
+      int64_t part = 0;
+      const int r0 = (int)ured.size();
+      for (size_t oi = 0; oi < sig_own.size(); ++oi) {
+        const Owner &o = sig_own[oi];
+        const int bb = o.n * o.n;
+        const int nt = std::max(1, std::min(std::min(4, c1 - c0), (smem_bytes_ / 4) / (24 * bb)));
         for (int t0 = c0; t0 < c1; t0 += nt) {
           const int n = std::min(nt, c1 - t0);
-          stl.push_back({o.out, 0, o.ostride, o.n, o.c0, o.c1, t0, n, o.s, (int32_t)std::min(f * n / 1e3, 2e9)});
+          const auto &sl = oslices[oi];
+          ured.push_back({part, o.out, o.ostride, bb, t0, n, (int32_t)sl.size(), 0});
+          for (const auto &r : sl) {
+            stl.push_back({o.out, part, o.ostride, o.n, r.first, r.second, t0, n, o.s,
+                           (int32_t)std::min(slice_cost(ucost, r) * n / 1e3, 2e9)});
+            part += (int64_t)n * bb;
+          }
         }
       }
+      uv_part_need_ = std::max(uv_part_need_, part);
       std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
-      // owners whose contributions average fewer than 200 (Q, m) terms take the
+      // slices whose contributions average fewer than 200 (Q, m) terms take the
       // unblocked variant (barriers dominate there); each chunk = [blocked | small]
       std::vector<SigTile> big, small;
       for (const SigTile &t : stl) {
@@ -844,14 +870,23 @@ void Engine::build_work_lists() {
         const bool sm = t.c1 > t.c0 && k < 200.0 * (t.c1 - t.c0);
         (sm ? small : big).push_back(t);
       }
-      SigChunk ch{c0, c1, (int)all.size(), (int)big.size(), (int)(big.size() + small.size()), 0, 0};
+      SigChunk ch{c0, c1, (int)all.size(), (int)big.size(), (int)(big.size() + small.size()), 0, 0, r0,
+                  (int)ured.size() - r0};
       for (const SigTile &t : big) { all.push_back(t); uv_blocked_host_.push_back(1); }
       for (const SigTile &t : small) { all.push_back(t); uv_blocked_host_.push_back(0); }
       sig_chunks_.push_back(ch);
     }
+    for (const SigTile &t : all) check_range(t.part, (int64_t)t.nt * t.b1 * t.b1, uv_part_need_, "Sigma FP32-stage partials");
+    for (const RedTask &r : ured) {
+      check_range(r.part, (int64_t)r.nslice * r.nt * r.elems, uv_part_need_, "Sigma FP32-stage slice sum");
+      check_range(r.out, (int64_t)(r.t0 + r.nt - 1) * r.ostride + r.elems, (int64_t)nts_ * ns_ * fa,
+                  "Sigma output block");
+    }
     sig_tiles1_.upload(all, st_);
     sig_tiles1_host_ = all;
+    uv_red_.upload(ured, st_);
   }
+
 
 
   // --- FP64 tiles of both contractions and their partial-sum buffer
@@ -910,7 +945,7 @@ void Engine::build_work_lists() {
     sig_tiles_.upload(st, st_);
     p0_red_.upload(pr, st_);
     sig_red_.upload(sr, st_);
-    const int64_t npart = std::max<int64_t>(1, std::max(part0, part1));
+    const int64_t npart = std::max<int64_t>(1, std::max(std::max(part0, part1), uv_part_need_));
     for (const P0Tile &t : pt) check_range(t.part, (int64_t)t.nt * t.qb * t.qb, npart, "P0 partial slice");
     for (const SigTile &t : st) check_range(t.part, (int64_t)t.nt * t.b1 * t.b1, npart, "Sigma partial slice");
     for (const RedTask &r : pr) {
@@ -1211,10 +1246,12 @@ void Engine::k_rotate_P() {
 void Engine::k_sigma() {
   if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
-    for (const SigChunk &ch : sig_chunks_)
+    for (const SigChunk &ch : sig_chunks_) {
       launch_sigma_tc(prec_ == GWGB_PREC_BF16X3, sw_tiles_.p + ch.w0, ch.nw, sw_smem_, Bcat_.p,
                       sig_tiles1_.p + ch.uv0, ch.nuv, sig_contribs_.p, sig_wref_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p,
-                      Sig_.p, ns_, -1.0 / l_.nk, uv_smem_, ch.nuv_blocked, uv_smem_small_, ch.t0, bad_.p + 2, st_);
+                      Part_.p, ns_, uv_smem_, ch.nuv_blocked, uv_smem_small_, ch.t0, bad_.p + 2, st_);
+      launch_reduce_slices(uv_red_.p + ch.red0, ch.nred, Part_.p, Sig_.p, nts_, -1.0 / l_.nk, 0, st_);
+    }
   } else {
     launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Part_.p,
                       ns_, fp64_smem_, st_);
@@ -1272,7 +1309,7 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
     const bool tc = prec_ != GWGB_PREC_FP64;
     int64_t sgt = 0, p0t = 0;
     for (const SigChunk &ch : sig_chunks_)
-      sgt += (ch.nw ? 1 : 0) + (ch.nuv_blocked ? 1 : 0) + (ch.nuv > ch.nuv_blocked ? 1 : 0);
+      sgt += (ch.nw ? 1 : 0) + (ch.nuv_blocked ? 1 : 0) + (ch.nuv > ch.nuv_blocked ? 1 : 0) + (ch.nred ? 1 : 0);
     for (const P0Chunk &ch : p0_chunks_) p0t += (pz_tasks_.n ? 1 : 0) + (ch.nk ? 1 : 0);
     const int64_t p0 = tc ? p0t + (pr_tiles_.n ? 1 : 0)
                           : (p0_tiles_.n ? 1 : 0) + (p0_red_.n ? 1 : 0);

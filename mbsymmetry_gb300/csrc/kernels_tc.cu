@@ -268,7 +268,7 @@ void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat
 __device__ __forceinline__ void sigma_uv_small(const SigTile &tile, const SigContrib *__restrict__ contribs,
                                                const WRef *__restrict__ wref, const double2 *__restrict__ V,
                                                const double2 *__restrict__ G, const float2 *__restrict__ W,
-                                               double2 *__restrict__ Sig, int ns, double scale, int smem_bytes,
+                                               double2 *__restrict__ Part, int ns, int smem_bytes,
     int tau0) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const int b1 = tile.b1, s = tile.s, nt = tile.nt, bb = b1 * b1;
@@ -379,10 +379,7 @@ __device__ __forceinline__ void sigma_uv_small(const SigTile &tile, const SigCon
     }
   }
   __syncthreads();
-  for (int e = tid; e < nt * bb; e += 256) {
-    const int it = e / bb, r = e - it * bb;
-    Sig[tile.sig + (int64_t)(tile.t0 + it) * tile.sstride + r] = make_double2(acc64[e].x * scale, acc64[e].y * scale);
-  }
+  for (int e = tid; e < nt * bb; e += 256) Part[tile.part + e] = acc64[e];  // [nt][b1][b1], summed by slices
 }
 
 // ---------------------------------------------------------------------------
@@ -401,7 +398,7 @@ constexpr int UV_MB = 8;   // U-stage outputs per thread
 __device__ __forceinline__ void sigma_uv_blocked(const SigTile &tile, const SigContrib *__restrict__ contribs,
                                                  const WRef *__restrict__ wref, const double2 *__restrict__ V,
                                                  const double2 *__restrict__ G, const float2 *__restrict__ W,
-                                                 double2 *__restrict__ Sig, int ns, double scale, int smem_bytes,
+                                                 double2 *__restrict__ Part, int ns, int smem_bytes,
     int tau0) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const int b1 = tile.b1, s = tile.s, nt = tile.nt, bb = b1 * b1;
@@ -532,10 +529,7 @@ __device__ __forceinline__ void sigma_uv_blocked(const SigTile &tile, const SigC
     }
   }
   __syncthreads();
-  for (int e = tid; e < nt * bb; e += 256) {
-    const int it = e / bb, r = e - it * bb;
-    Sig[tile.sig + (int64_t)(tile.t0 + it) * tile.sstride + r] = make_double2(acc64[e].x * scale, acc64[e].y * scale);
-  }
+  for (int e = tid; e < nt * bb; e += 256) Part[tile.part + e] = acc64[e];  // [nt][b1][b1], summed by slices
 }
 
 // The two variants as separate kernels (each launch gets its own shared
@@ -548,10 +542,10 @@ __global__ void __launch_bounds__(256) sigma_uv_blocked_kernel(const SigTile *__
                                                                const double2 *__restrict__ V,
                                                                const double2 *__restrict__ G,
                                                                const float2 *__restrict__ W,
-                                                               double2 *__restrict__ Sig, int ns, double scale,
+                                                               double2 *__restrict__ Part, int ns,
                                                                int smem_bytes, int tau0) {
   const SigTile tile = tiles[blockIdx.x];
-  sigma_uv_blocked(tile, contribs, wref, V, G, W, Sig, ns, scale, smem_bytes, tau0);
+  sigma_uv_blocked(tile, contribs, wref, V, G, W, Part, ns, smem_bytes, tau0);
 }
 
 __global__ void __launch_bounds__(256) sigma_uv_small_kernel(const SigTile *__restrict__ tiles,
@@ -560,16 +554,16 @@ __global__ void __launch_bounds__(256) sigma_uv_small_kernel(const SigTile *__re
                                                              const double2 *__restrict__ V,
                                                              const double2 *__restrict__ G,
                                                              const float2 *__restrict__ W,
-                                                             double2 *__restrict__ Sig, int ns, double scale,
+                                                             double2 *__restrict__ Part, int ns,
                                                              int smem_bytes, int tau0) {
   const SigTile tile = tiles[blockIdx.x];
-  sigma_uv_small(tile, contribs, wref, V, G, W, Sig, ns, scale, smem_bytes, tau0);
+  sigma_uv_small(tile, contribs, wref, V, G, W, Part, ns, smem_bytes, tau0);
 }
 
 void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
                      int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
-                     const double2 *G, const double2 *P, float2 *W, double2 *Sig, int ns, double scale,
-                     int uv_smem, int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st) {
+                     const double2 *G, const double2 *P, float2 *W, double2 *Part, int ns, int uv_smem,
+                     int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st) {
   if (nwtiles > 0) {
     if (bf16)
       sigma_w_tc_kernel<true><<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, tau0, err);
@@ -579,13 +573,13 @@ void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, co
   }
   // tiles1 = [blocked tiles (nblocked) | small tiles]
   if (nblocked > 0) {
-    sigma_uv_blocked_kernel<<<nblocked, 256, uv_smem, st>>>(tiles1, contribs, wref, V, G, W, Sig, ns, scale,
-                                                             uv_smem, tau0);
+    sigma_uv_blocked_kernel<<<nblocked, 256, uv_smem, st>>>(tiles1, contribs, wref, V, G, W, Part, ns, uv_smem,
+                                                             tau0);
     GWGB_CUDA(cudaGetLastError());
   }
   if (ntiles1 > nblocked) {
     sigma_uv_small_kernel<<<ntiles1 - nblocked, 256, uv_smem_small, st>>>(tiles1 + nblocked, contribs, wref, V, G, W,
-                                                                          Sig, ns, scale, uv_smem_small, tau0);
+                                                                          Part, ns, uv_smem_small, tau0);
     GWGB_CUDA(cudaGetLastError());
   }
 }

@@ -40,8 +40,8 @@ struct WRef {
 
 void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
                      int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
-                     const double2 *G, const double2 *P, float2 *W, double2 *Sig, int ns, double scale,
-                     int uv_smem, int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st);
+                     const double2 *G, const double2 *P, float2 *W, double2 *Part, int ns, int uv_smem,
+                     int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st);
 
 void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat, cudaStream_t st);
 
