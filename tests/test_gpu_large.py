@@ -1,7 +1,11 @@
-"""C3 scale (Fm-3m 4x4x4: 64 k, 8 irreducible; nao=52, naux=250, nts=120;
-AO blocks up to 16, aux blocks up to 64; V 12.2 GB): the FP64 drop-in against
-the oracle on sampled tau points (the full CPU oracle would take hours), the
-full W~ solve against the oracle, and the TF32x3 path against FP64."""
+"""Large configurations: the FP64 drop-in against the oracle on sampled tau
+points (the full CPU oracle would take hours), the full W~ solve against the
+oracle, and the TF32x3 path against FP64.
+
+* C3: Fm-3m 4x4x4 (64 k, 8 irreducible), nao=52, naux=250, nts=120; AO blocks
+  up to 16, aux blocks up to 64; V 12.2 GB.
+* C4: P6_3mc-like hexagonal 4x4x3 (48 k, 8 irreducible), nao=72, naux=350,
+  nts=120, beta=200; AO and aux blocks up to 30; V 17.1 GB."""
 import numpy as np
 import pytest
 
@@ -11,12 +15,13 @@ from oracle import Oracle
 pytestmark = pytest.mark.gpu
 
 
-def test_c3_fp64_matches_oracle_and_tf32x3_bounded():
+@pytest.mark.parametrize("name,max_block", [("C3", 64), ("C4", 30)])
+def test_large_fp64_matches_oracle_and_tf32x3_bounded(name, max_block):
     from mbsymmetry_gb300.solver import GWSolver
-    cr, tr = crystal("C3")
+    cr, tr = crystal(name)
     L = cr.layout
     nts = tr.nts
-    assert L.max_block() == 64 and L.ink == 8
+    assert L.max_block() == max_block and L.ink == 8
     s = GWSolver(L, 1, tr)
     s.set_shared_Coulomb(cr.V)
     s.set_fock(cr.F, cr.S)
@@ -44,5 +49,5 @@ def test_c3_fp64_matches_oracle_and_tf32x3_bounded():
     assert np.abs(Sig.reshape(nts, -1)[:2] - Sr.reshape(nts, -1)[:2]).max() < 1e-10
 
     err = np.abs(Sig32 - Sig).max()
-    print(f"C3: max|Sigma_tf32x3 - Sigma_fp64| = {err:.3e} (max|Sigma| = {np.abs(Sig).max():.3e})")
+    print(f"{name}: max|Sigma_tf32x3 - Sigma_fp64| = {err:.3e} (max|Sigma| = {np.abs(Sig).max():.3e})")
     assert err < 1e-5 * max(1.0, np.abs(Sig).max())
