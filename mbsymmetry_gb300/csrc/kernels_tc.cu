@@ -9,10 +9,12 @@
 // right operand conj(V_c) does not depend on tau, all tau points and all
 // contributions c that share the aux block (q, iq) form ONE GEMM:
 //   rows (tau, Q) x columns (c, j, n), K = P.
-// (1) runs here as a tcgen05 kind::tf32 GEMM (3-pass split hi*hi + hi*lo +
-// lo*hi, FP32 accumulation in TMEM) writing W to HBM in FP32; (2) and (3) run
-// in a per-(owner, tau) kernel in FP32 with FP64 accumulation across
-// contributions.
+// (1) runs here as a tcgen05 GEMM on split operands (TF32x3: kind::tf32, two
+// planes, three products; BF16x3: kind::f16, three BF16 planes, six products;
+// FP32 accumulation in TMEM) writing W to HBM in FP32, one tau chunk at a time;
+// (2) and (3) run per (owner, tau range, slice of contributions) in FP32 with
+// FP64 accumulation across contributions, writing FP64 partial blocks that
+// reduce_slices_kernel sums in order.
 #include "common.h"
 #include "kernels.h"
 #include "kernels_tc.h"

@@ -6,9 +6,10 @@
 namespace gwgb {
 
 // One CTA of the Sigma W-GEMM: rows (tau, Q) of one aux block (q, iq), all
-// columns (c, j, n) of the block in packs of 64 complex columns.
+// columns (c, j, n) of the block in packs of npk complex columns.
 //   A = P(tau)[Q][P] (FP64, staged once), B = Bcat[col][P] = conj(V_c[P][j][n])
-//   (FP32, built once per V upload), W = Wcat[(tau*qb + Q)*ncol + col] (FP32).
+//   (FP32, built once per V upload), W = Wcat[((tau - t_chunk)*qb + Q)*ncol + col]
+//   (FP32; the W buffer holds one tau chunk starting at t_chunk).
 struct SwTile {
   int64_t pa;       // P(q) block base at tau = 0
   int64_t bcat;     // Bcat base of the block: Bcat[col*qb + P]
@@ -17,7 +18,7 @@ struct SwTile {
   int32_t qb;
   int32_t t0, nt;   // tau range; nt * qb <= 128
   int32_t ncol;     // complex columns of the block
-  int32_t kp;       // pad8(2 qb)
+  int32_t kp;       // K = 2 qb padded to 8 (the BF16 kernel pads it to 16)
   int32_t npk;      // complex columns per pack (16, 32 or 64)
   int32_t pad;
 };
@@ -32,12 +33,16 @@ struct BcTask {
 void set_tc_kernel_attributes(int smem_bytes);
 void set_tc_p0_kernel_attributes(int smem_bytes);
 
-// W reference of one Sigma contribution: W_c(tau)[Q][(j,n)] = W[base + (tau*qb + Q)*ld + j*b2 + n]
+// W reference of one Sigma contribution:
+//   W_c(tau)[Q][(j,n)] = W[base + ((tau - t_chunk)*qb + Q)*ld + j*b2 + n]
 struct WRef {
   int64_t base;
   int64_t ld;
 };
 
+// One tau chunk (starting at tau0) of the Sigma stages: the W GEMM tiles, then the
+// FP32 U/Sigma tiles (tiles1 = [nblocked register-blocked | the rest]) writing
+// FP64 partial blocks to Part.
 void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
                      int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
                      const double2 *G, const double2 *P, float2 *W, double2 *Part, int ns, int uv_smem,
@@ -49,14 +54,14 @@ void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat
 
 namespace gwgb {
 
-// P0, stage Z: one CTA per (contribution, spin) over all tau < nts/2.  Z of
-// the aux block is one matrix Zcat[(tau, P)][K] with K concatenating the
-// (p, m) columns of every (contribution, spin); this task writes columns
-// [zcol, zcol + b1*b2).
+// P0, stage Z: one CTA per (contribution, spin) over one tau chunk of
+// [0, nts/2).  Z of the aux block is one matrix Zcat[(tau - t_chunk, P)][K] with
+// K concatenating the (p, m) columns of every (contribution, spin); this task
+// writes columns [zcol, zcol + b1*b2).
 struct PzTask {
   int64_t v;       // V block [qb][b1][b2]
   int64_t ga, gb;  // G^{k1}, G^{k2} block bases
-  int64_t z;       // Zcat base of the aux block: Zcat[(tau*qb + P)*zld + zcol + p*b2 + m]
+  int64_t z;       // Zcat base of the aux block: Zcat[((tau - t_chunk)*qb + P)*zld + zcol + p*b2 + m]
   int32_t sa, sb;  // (t, s) strides of the G slices
   int32_t b1, b2, qb, s;
   int32_t zld, zcol;
@@ -93,6 +98,8 @@ struct PrTile {
   int32_t pad;
 };
 
+// One tau chunk [tau0, tau1) of the P0 stages: Z tasks, then the GEMM tiles of
+// the chunk; the slice sums (rtiles, nr > 0) are launched after the last chunk.
 void launch_p0_tc(bool bf16, const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
                   int nr, const double2 *V, const double2 *G, float2 *Z, const float2 *Vcat, double2 *Ppart,
                   double2 *P0, int ns, int nts, int tau0, int tau1, double pref, int mirror, int *err,
