@@ -60,12 +60,24 @@ struct P0Tile {
 
 // One V block of one (k1, k2 = k1 - q) pair feeding a Sigma output block.
 struct SigContrib {
-  int64_t v;        // V block [qb][b1][b2]
+  int64_t v;        // pre-rotated V block Vt [qb][b1][b2] (in the Vt buffer)
   int64_t gb;       // G^{k2} block base
-  int64_t pq;       // P(q) block base at t = 0
+  int64_t pq;       // block of P~ of the irreducible q' at t = 0
   int32_t sb;       // (t,s) stride of the G^{k2} slice
-  int32_t pstride;  // per-t stride of P(q)
+  int32_t pstride;  // per-t stride of P~(q')
   int32_t b2, qb;
+  int32_t pconj;    // read conj(P~(q')) (q is a time-reversal partner)
+  int32_t pad;
+};
+
+// Vt = op(O)^T V over the aux index of one Sigma contribution: Vt[Q'][x] =
+// sum_Q op(O[Q][Q']) V[Q][x], op = conj for a time-reversal partner; o < 0:
+// Vt = V.  With it, V P~(q) V^H = Vt P~(q') Vt^H for P~(q) = O P~(q') O^H.
+struct VrTask {
+  int64_t v, vt;    // source V block, target Vt block
+  int64_t o;        // auxrep block (qb x qb) or -1
+  int32_t qb, b1b2;
+  int32_t conj, pad;
 };
 
 // One Sigma output block Sigma[t][s][k_irr block ik1] for a tau range.

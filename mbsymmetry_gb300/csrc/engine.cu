@@ -276,7 +276,6 @@ class Engine {
       GWGB_CUDA(cudaMemsetAsync(Zbuf_.p, 0, Zbuf_.n * sizeof(float2), st_));   // K padding stays zero
       GWGB_CUDA(cudaMemsetAsync(Vcat_.p, 0, Vcat_.n * sizeof(float2), st_));
     }
-    if (prec_ != GWGB_PREC_FP64 && !vcat_ready_) build_vcat();
   }
   void upload_V(const double *V, int64_t n);
   void set_reps(const double *orep, int64_t no, const double *auxrep, int64_t na);
@@ -335,7 +334,10 @@ class Engine {
   DBuf<RedTask> p0_red_, sig_red_;       // FP64: ordered sums of the slices
   DBuf<double2> Part_;                   // FP64: partial sums of the slices
   DBuf<SigContrib> sig_contribs_;
-  DBuf<RotTask> rotG_, rotP_;
+  DBuf<RotTask> rotG_;
+  DBuf<VrTask> vr_tasks_;  // Vt = op(O)^T V for every Sigma contribution
+  DBuf<double2> Vt_;
+  bool vt_ready_ = false;
   DBuf<TSlab> slab_p_fwd_, slab_p_bwd_, slab_s_fwd_, slab_g_bwd_;
   DBuf<InvTask> inv_w_, inv_d_;
   int p0_maxo_ = 8, sig_maxo_ = 8, rot_smem_ = 0;
@@ -374,19 +376,33 @@ class Engine {
   int64_t zbuf_elems_ = 0, vcat_elems_ = 0, ppart_elems_ = 0;
   int pz_smem_ = 0;
   bool vcat_ready_ = false;
-  void build_vcat() {  // tau-independent tensor-core operands derived from V
-    if (prec_ == GWGB_PREC_FP64 || !have_V_) return;
-    launch_vcat(vc_tasks_.p, (int)vc_tasks_.n, V_.p, Vcat_.p, st_);
-    launch_bcat(bc_tasks_.p, (int)bc_tasks_.n, V_.p, Bcat_.p, st_);
-    GWGB_CUDA(cudaStreamSynchronize(st_));
-    vcat_ready_ = true;
+  // tau-independent operands derived from V and the rotations, built outside any
+  // graph capture before a solve: Vt for Sigma (all precisions), and for the
+  // tensor-core paths Vcat (P0, from V) and Bcat = conj(Vt) (Sigma)
+  void prepare_operands() {
+    require_ready(false);
+    bool built = false;
+    if (!vt_ready_) {
+      launch_vrot(vr_tasks_.p, (int)vr_tasks_.n, V_.p, auxrep_.p, Vt_.p, st_);
+      vt_ready_ = true;
+      vcat_ready_ = false;
+      built = true;
+    }
+    if (prec_ != GWGB_PREC_FP64 && !vcat_ready_) {
+      launch_vcat(vc_tasks_.p, (int)vc_tasks_.n, V_.p, Vcat_.p, st_);
+      launch_bcat(bc_tasks_.p, (int)bc_tasks_.n, Vt_.p, Bcat_.p, st_);
+      vcat_ready_ = true;
+      built = true;
+    }
+    if (built) GWGB_CUDA(cudaStreamSynchronize(st_));
   }
   struct P0Group { int64_t pout; int32_t pstride, qb, c0, c1; };
   std::vector<P0Group> p0_groups_;                            // host: P0 output blocks
   std::vector<int> sig_b1_;                                  // host: b1 of every Sigma contribution
-  std::map<std::pair<int, int>, std::vector<int>> sig_groups_;  // host: (q, iq) -> contributions
+  // host: (P~ block of the irreducible q', conj) -> Sigma contributions reading it
+  std::map<std::pair<int64_t, int>, std::vector<int>> sig_groups_;
   int max_cols_p_ = 0, max_cols_g_ = 0;
-  int64_t g_rot_off_ = 0, p_rot_off_ = 0;  // start of the rotated parts
+  int64_t g_rot_off_ = 0;  // start of the rotated G copies
   double p0_flops_ = 0, sig_flops_ = 0;
   bool has_tct_ = false;
   // self-consistent loop: mu search state, G(i w) scratch of the search, G(beta),
@@ -431,7 +447,6 @@ class Engine {
   void k_rotate_G();
   void k_p0(int mirror);
   void k_pq(bool mirror_first);
-  void k_rotate_P();
   void k_sigma();
   void k_dyson();
   // During stream capture an external record keeps the event a timing event
@@ -534,7 +549,7 @@ Engine::~Engine() {
   qoff_irr_.free(); qsz_irr_.free();
   p0_tiles_.free(); p0_contribs_.free(); sig_tiles_.free(); sig_tiles1_.free(); sig_contribs_.free();
   p0_red_.free(); sig_red_.free(); Part_.free();
-  rotG_.free(); rotP_.free(); slab_p_fwd_.free(); slab_p_bwd_.free(); slab_s_fwd_.free(); slab_g_bwd_.free();
+  rotG_.free(); vr_tasks_.free(); Vt_.free(); slab_p_fwd_.free(); slab_p_bwd_.free(); slab_s_fwd_.free(); slab_g_bwd_.free();
   inv_w_.free(); inv_d_.free();
   if (st_) cudaStreamDestroy(st_);
 }
@@ -584,40 +599,43 @@ void Engine::build_work_lists() {
   }
   Gall_.alloc((size_t)go);
 
-  // --- P references: irreducible q in place, others rotated [q'][t][qslice]
-  std::vector<GRef> pref(nk);
-  std::vector<RotTask> rp;
-  p_rot_off_ = (int64_t)nts_ * fq;
-  int64_t po = p_rot_off_;
+  // --- P sources.  Sigma reads P~(q) only as V P~(q) V^H.  With P~(q) =
+  //     O P~(q') O^H for the irreducible q' (conjugated for a time-reversal
+  //     partner; cugw_qkpt_block.cu:288-340), that is Vt P~(q') Vt^H with
+  //     Vt = op(O)^T V, so every q reads the block of its q' directly, the
+  //     Sigma contributions use pre-rotated V (built once per V / rep upload)
+  //     and no rotated copy of P~ exists.
+  struct PSrc { int64_t base; int32_t stride; int64_t o; int32_t conj; };
+  std::vector<std::vector<PSrc>> psrc(nk);
   for (int q = 0; q < nk; ++q) {
     const int cq = l.conj_index[q];
     const int q_ir = l.irre_index[q];  // cugw_qkpt_block.cu:147
     const int qq = l.irre_list[q_ir];
-    if (l.index[cq] == cq && q == cq && qq == q) {
-      pref[q] = {(int64_t)nts_ * l.qaux_off_irre[q_ir], (int32_t)l.qaux_sz[q]};
-      continue;
-    }
-    pref[q] = {po, (int32_t)l.qaux_sz[q]};
     const int64_t src = (int64_t)nts_ * l.qaux_off_irre[q_ir];
-    if (l.index[cq] == cq) {
-      GWGB_REQUIRE(l.qaux_sz[q] == l.qaux_sz[qq], GWGB_E_INVALID, "q slice size differs from its representative");
-      rp.push_back({po, src, 0, (int32_t)l.qaux_sz[q], (int32_t)l.qaux_sz[qq], (int32_t)l.qaux_sz[q], 0, 0,
-                    (int32_t)(q != cq)});
+    const int32_t stride = (int32_t)l.qaux_sz[qq];
+    psrc[q].assign(l.naux_blocks(q), PSrc{-1, 0, -1, 0});
+    if (l.index[cq] == cq && q == cq && qq == q) {
+      for (int iq = 0; iq < l.naux_blocks(q); ++iq) psrc[q][iq] = {src + l.auxoff(q, iq), stride, -1, 0};
+    } else if (l.index[cq] == cq) {  // the same slice, conjugated for q != cq
+      GWGB_REQUIRE(l.qaux_sz[q] == l.qaux_sz[qq] && l.naux_blocks(q) == l.naux_blocks(qq), GWGB_E_INVALID,
+                   "q slice differs from its representative");
+      for (int iq = 0; iq < l.naux_blocks(q); ++iq) {
+        GWGB_REQUIRE(l.auxsz(q, iq) == l.auxsz(qq, iq), GWGB_E_INVALID, "q block differs from its representative");
+        psrc[q][iq] = {src + l.auxoff(qq, iq), stride, -1, (int32_t)(q != cq)};
+      }
     } else {
       std::vector<int> covered(l.naux_blocks(cq), 0);
       for (int b = l.ar_ptr[cq]; b < l.ar_ptr[cq + 1]; ++b) {
-        int i1 = l.ar_ir[2 * b], i2 = l.ar_ir[2 * b + 1];
-        int m = l.auxsz(cq, i1), n = l.auxsz(qq, i2);
-        GWGB_REQUIRE(m == n, GWGB_E_INVALID, "auxrep block must be square");
+        const int i1 = l.ar_ir[2 * b], i2 = l.ar_ir[2 * b + 1];
+        GWGB_REQUIRE(l.auxsz(cq, i1) == l.auxsz(qq, i2) && l.auxsz(q, i1) == l.auxsz(cq, i1), GWGB_E_INVALID,
+                     "auxrep block must be square");
         covered[i1]++;
-        rp.push_back({po + l.auxoff(cq, i1), src + l.auxoff(qq, i2), l.kar_off[cq] + l.ar_off[b],
-                      (int32_t)l.qaux_sz[q], (int32_t)l.qaux_sz[qq], m, n, 1, (int32_t)(q != cq)});
-        rot_smem_ = std::max(rot_smem_, (int)((2 * m * n + n * n) * sizeof(double2)));
+        psrc[q][i1] = {src + l.auxoff(qq, i2), stride, l.kar_off[cq] + l.ar_off[b], (int32_t)(q != cq)};
       }
       for (int c : covered) GWGB_REQUIRE(c == 1, GWGB_E_INVALID, "auxrep must map every block of q exactly once");
     }
-    po += (int64_t)nts_ * l.qaux_sz[q];
   }
+  const int64_t po = (int64_t)nts_ * fq;
   Pall_.alloc((size_t)po);
   for (const RotTask &t : rg) {  // G rotations: batch = nts * ns
     const int64_t nb = (int64_t)nts_ * ns_;
@@ -625,13 +643,7 @@ void Engine::build_work_lists() {
     check_range(t.src, (nb - 1) * t.sstride + (t.rotate ? (int64_t)t.n * t.n : t.m), go, "G rotation source");
     if (t.rotate) check_range(t.o, (int64_t)t.m * t.n, l.flat_orep, "orep block");
   }
-  for (const RotTask &t : rp) {  // P rotations: batch = nts
-    check_range(t.dst, (int64_t)(nts_ - 1) * t.dstride + (t.rotate ? (int64_t)t.m * t.m : t.m), po, "P rotation target");
-    check_range(t.src, (int64_t)(nts_ - 1) * t.sstride + (t.rotate ? (int64_t)t.n * t.n : t.m), po, "P rotation source");
-    if (t.rotate) check_range(t.o, (int64_t)t.m * t.n, l.flat_auxrep, "auxrep block");
-  }
   rotG_.upload(rg, st_);
-  rotP_.upload(rp, st_);
 
   // --- P0: owner = (q_irr, aux block iq); the FP64 tiles are (owner, tau
   //     range, slice of the owner's contributions), see make_fp64_tiles.
@@ -773,6 +785,8 @@ void Engine::build_work_lists() {
 
   // --- Sigma: owner = (k_irr, AO block i1, spin)
   std::vector<SigContrib> sc;
+  std::vector<VrTask> vr;
+  int64_t vt_elems = 0;
   std::vector<double> scost;  // flops per contribution and tau
   std::vector<Owner> sig_own;
   std::vector<SigTile> stl;   // (owner, tau range) tiles of the tcgen05 path
@@ -790,10 +804,14 @@ void Engine::build_work_lists() {
           if (l.ti[3 * b + 1] != i1) continue;
           const int iq = l.ti[3 * b], i2 = l.ti[3 * b + 2];
           const int qb = l.auxsz(q, iq), b2 = l.aosz(k2, i2);
-          sc.push_back({l.kp_off[p] + l.t_off[b], gref[k2].base + l.aooff(k2, i2), pref[q].base + l.auxoff(q, iq),
-                        gref[k2].stride, pref[q].stride, b2, qb});
+          const PSrc &ps = psrc[q][iq];
+          GWGB_REQUIRE(ps.base >= 0, GWGB_E_INVALID, "aux block without a source in the irreducible q");
+          vr.push_back({l.kp_off[p] + l.t_off[b], vt_elems, ps.o, qb, b1 * b2, ps.conj, 0});
+          sc.push_back({vt_elems, gref[k2].base + l.aooff(k2, i2), ps.base, gref[k2].stride, ps.stride, b2, qb,
+                        ps.conj, 0});
+          vt_elems += (int64_t)qb * b1 * b2;
           sig_b1_.push_back(b1);
-          sig_groups_[std::make_pair(q, iq)].push_back((int)sc.size() - 1);
+          sig_groups_[std::make_pair(ps.base, (int)ps.conj)].push_back((int)sc.size() - 1);
           const double f = 8.0 * ((double)qb * b1 * b2 * b2 + (double)b1 * b2 * qb * qb + (double)b1 * b1 * b2 * qb);
           scost.push_back(f);
           sig_flops_ += f * ns_ * nts_;
@@ -807,9 +825,16 @@ void Engine::build_work_lists() {
       }
     }
   }
+  for (const VrTask &t : vr) {
+    check_range(t.v, (int64_t)t.qb * t.b1b2, l.flat_V, "Sigma V block");
+    check_range(t.vt, (int64_t)t.qb * t.b1b2, vt_elems, "Sigma Vt block");
+    if (t.o >= 0) check_range(t.o, (int64_t)t.qb * t.qb, l.flat_auxrep, "auxrep block");
+  }
+  vr_tasks_.upload(vr, st_);
+  Vt_.alloc((size_t)std::max<int64_t>(1, vt_elems));
   for (size_t c = 0; c < sc.size(); ++c) {
     const SigContrib &cb = sc[c];
-    check_range(cb.v, (int64_t)cb.qb * sig_b1_[c] * cb.b2, l.flat_V, "Sigma V block");
+    check_range(cb.v, (int64_t)cb.qb * sig_b1_[c] * cb.b2, vt_elems, "Sigma Vt block");
     check_range(cb.gb, ((int64_t)(nts_ - 1) * ns_ + (ns_ - 1)) * cb.sb + (int64_t)cb.b2 * cb.b2, go,
                 "Sigma G(k2) block");
     check_range(cb.pq, (int64_t)(nts_ - 1) * cb.pstride + (int64_t)cb.qb * cb.qb, po, "Sigma P(q) block");
@@ -970,6 +995,7 @@ void Engine::build_work_lists() {
       const int qb = sc[cs[0]].qb;
       const int64_t pa = sc[cs[0]].pq;
       const int pstride = sc[cs[0]].pstride;
+      const int pconj = sc[cs[0]].pconj;
       int ncol = 0;
       for (int c : cs) {
         const int b1b2 = sig_b1_[c] * sc[c].b2;
@@ -988,7 +1014,7 @@ void Engine::build_work_lists() {
       const int nt = std::max(1, std::min(tch_w_, 128 / qb));
       for (const SigChunk &ch : sig_chunks_)
         for (int t0 = ch.t0; t0 < ch.t1; t0 += nt)
-          swt.push_back({pa, boff, woff, pstride, qb, t0, std::min(nt, ch.t1 - t0), ncol, KP, npk, 0});
+          swt.push_back({pa, boff, woff, pstride, qb, t0, std::min(nt, ch.t1 - t0), ncol, KP, npk, pconj, 0, ncol});
       boff += (int64_t)ncol * qb;
       woff += (int64_t)tch_w_ * qb * ncol;
     }
@@ -1010,10 +1036,28 @@ void Engine::build_work_lists() {
       if (fixed + 24 * t.b1 * b2max > uv_cap) uv_cap = smem_bytes_;
     }
     uv_smem_small_ = std::min(uv_cap, std::max(16 * 1024, ((uvneed_small + 1023) / 1024) * 1024));
+    // Columns split into ranges of whole packs so that each chunk has about four
+    // waves of CTAs (a CTA computes whole W entries, so the split changes no bit)
+    {
+      std::vector<int64_t> packs_in_chunk(sig_chunks_.size(), 0);
+      for (const SwTile &t : swt) packs_in_chunk[t.t0 / tch_w_] += (t.ncol + t.npk - 1) / t.npk;
+      std::vector<SwTile> split;
+      for (const SwTile &t : swt) {
+        const int64_t per = std::max<int64_t>(1, (packs_in_chunk[t.t0 / tch_w_] + 4 * nsm_ - 1) / (4 * std::max(1, nsm_)));
+        const int64_t range = per * t.npk;
+        for (int64_t c0 = 0; c0 < t.ncol; c0 += range) {
+          SwTile u = t;
+          u.c0 = (int32_t)c0;
+          u.c1 = (int32_t)std::min<int64_t>(t.ncol, c0 + range);
+          split.push_back(u);
+        }
+      }
+      swt.swap(split);
+    }
     // tiles grouped by W chunk, widest first within a chunk
     std::stable_sort(swt.begin(), swt.end(), [&](const SwTile &a, const SwTile &b) {
       const int ca = a.t0 / tch_w_, cb = b.t0 / tch_w_;
-      return ca != cb ? ca < cb : a.ncol > b.ncol;
+      return ca != cb ? ca < cb : (a.c1 - a.c0) > (b.c1 - b.c0);
     });
     for (SigChunk &ch : sig_chunks_) {
       ch.w0 = (int)(std::lower_bound(swt.begin(), swt.end(), ch.t0,
@@ -1026,12 +1070,14 @@ void Engine::build_work_lists() {
     for (const SwTile &t : swt) {
       const int t0c = (t.t0 / tch_w_) * tch_w_;  // chunk start
       check_range(t.wcat, (int64_t)(t.t0 - t0c + t.nt) * t.qb * t.ncol, woff, "W rows");
+      GWGB_REQUIRE(0 <= t.c0 && t.c0 < t.c1 && t.c1 <= t.ncol, GWGB_E_INVALID,
+                   "internal work list out of bounds: W column range");
       check_range(t.bcat, (int64_t)t.ncol * t.qb, boff, "conj(V) operand");
       GWGB_REQUIRE(t.nt * t.qb <= 128 && 2 * t.npk <= 128, GWGB_E_INVALID,
                    "internal work list out of bounds: Sigma tensor-core tile shape");
     }
     for (const BcTask &t : bt) {
-      check_range(t.v, (int64_t)t.qb * t.b1b2, l.flat_V, "conj(V) source");
+      check_range(t.v, (int64_t)t.qb * t.b1b2, vt_elems, "conj(Vt) source");
       check_range(t.bcat + (int64_t)t.col0 * t.qb, (int64_t)t.b1b2 * t.qb, boff, "conj(V) target");
     }
     sw_tiles_.upload(swt, st_);
@@ -1138,8 +1184,7 @@ void Engine::upload_V(const double *V, int64_t n) {
   h2d(V_.p, V, (size_t)n * sizeof(double2), st_);
   GWGB_CUDA(cudaStreamSynchronize(st_));
   have_V_ = true;
-  vcat_ready_ = false;
-  build_vcat();
+  vt_ready_ = vcat_ready_ = false;  // rebuilt before the next solve
 }
 
 void Engine::set_reps(const double *orep, int64_t no, const double *auxrep, int64_t na) {
@@ -1148,6 +1193,7 @@ void Engine::set_reps(const double *orep, int64_t no, const double *auxrep, int6
   h2d(auxrep_.p, auxrep, (size_t)na * sizeof(double2), st_);
   GWGB_CUDA(cudaStreamSynchronize(st_));
   have_reps_ = true;
+  vt_ready_ = vcat_ready_ = false;  // rebuilt before the next solve
 }
 
 void Engine::set_transforms(const double *Tnt, const double *Ttn, const double *TntBF, const double *TtnFB,
@@ -1217,7 +1263,7 @@ void Engine::k_rotate_G() {
 void Engine::k_p0(int mirror) {
   const double pref = -1.0 / l_.nk * (ns_ == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
   if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
-    GWGB_REQUIRE((Zbuf_.p || !zbuf_elems_) && vcat_ready_, GWGB_E_STATE, "mixed-precision work buffers missing");
+    GWGB_REQUIRE((Zbuf_.p || !zbuf_elems_) && vcat_ready_, GWGB_E_STATE, "mixed-precision operands not prepared");
     for (size_t i = 0; i < p0_chunks_.size(); ++i) {
       const P0Chunk &ch = p0_chunks_[i];
       const bool last = i + 1 == p0_chunks_.size();  // the slice sums run once, after the last chunk
@@ -1239,21 +1285,18 @@ void Engine::k_pq(bool mirror_first) {
   launch_transform(slab_p_bwd_.p, (int)slab_p_bwd_.n, max_cols_p_, TtnFB_.p, nts_, nw_b_, 0, Pw_.p, Pall_.p, st_);
 }
 
-void Engine::k_rotate_P() {
-  launch_rotate(rotP_.p, (int)rotP_.n, nts_, rot_smem_, Pall_.p, auxrep_.p, Pall_.p, st_);
-}
 
 void Engine::k_sigma() {
   if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
     for (const SigChunk &ch : sig_chunks_) {
       launch_sigma_tc(prec_ == GWGB_PREC_BF16X3, sw_tiles_.p + ch.w0, ch.nw, sw_smem_, Bcat_.p,
-                      sig_tiles1_.p + ch.uv0, ch.nuv, sig_contribs_.p, sig_wref_.p, V_.p, Gall_.p, Pall_.p, Wbuf_.p,
+                      sig_tiles1_.p + ch.uv0, ch.nuv, sig_contribs_.p, sig_wref_.p, Vt_.p, Gall_.p, Pall_.p, Wbuf_.p,
                       Part_.p, ns_, uv_smem_, ch.nuv_blocked, uv_smem_small_, ch.t0, bad_.p + 2, st_);
       launch_reduce_slices(uv_red_.p + ch.red0, ch.nred, Part_.p, Sig_.p, nts_, -1.0 / l_.nk, 0, st_);
     }
   } else {
-    launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, V_.p, Gall_.p, Pall_.p, Part_.p,
+    launch_sigma_fp64(sig_tiles_.p, (int)sig_tiles_.n, sig_maxo_, sig_contribs_.p, Vt_.p, Gall_.p, Pall_.p, Part_.p,
                       ns_, fp64_smem_, st_);
     launch_reduce_slices(sig_red_.p, (int)sig_red_.n, Part_.p, Sig_.p, nts_, -1.0 / l_.nk, 0, st_);
   }
@@ -1315,7 +1358,7 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
                           : (p0_tiles_.n ? 1 : 0) + (p0_red_.n ? 1 : 0);
     const int64_t sg = tc ? sgt
                           : (sig_tiles_.n ? 1 : 0) + (sig_red_.n ? 1 : 0);
-    launches += (rotG_.n ? 1 : 0) + p0 + 3 + (rotP_.n ? 1 : 0) + sg;
+    launches += (rotG_.n ? 1 : 0) + p0 + 3 + sg;
   }
   if (with_dyson) launches += 3 + (has_tct_ ? 1 : 0);
   s.kernel_launches = launches;
@@ -1324,6 +1367,7 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
 
 void Engine::solve_P0() {
   require_ready(false);
+  prepare_operands();
   record(0);
   k_rotate_G();
   record(1);
@@ -1343,13 +1387,13 @@ void Engine::solve_Pq() {
 
 void Engine::solve_sigma() {
   require_ready(false);
+  prepare_operands();
   record(0);
   k_rotate_G();
   record(1);
   k_p0(1);
   record(2);
   record(3);
-  k_rotate_P();
   record(4);
   k_sigma();
   record(5);
@@ -1359,6 +1403,7 @@ void Engine::solve_sigma() {
 
 void Engine::solve() {
   require_ready(true);
+  prepare_operands();
   record(0);
   k_rotate_G();
   record(1);
@@ -1366,7 +1411,6 @@ void Engine::solve() {
   record(2);
   k_pq(false);
   record(3);
-  k_rotate_P();
   record(4);
   k_sigma();
   record(5);
@@ -1392,6 +1436,7 @@ void Engine::dyson(double mu) {
 
 void Engine::iteration(double mu) {
   require_ready(true);
+  prepare_operands();
   GWGB_REQUIRE(have_F_, GWGB_E_STATE, "F and S have not been set");
   // The graph holds mu by value; rebuild when it changes.
   if (!graph_exec_ || *mu_host_ != mu) {
@@ -1411,7 +1456,6 @@ void Engine::iteration(double mu) {
     record(2);
     k_pq(false);
     record(3);
-    k_rotate_P();
     record(4);
     k_sigma();
     record(5);
@@ -1540,7 +1584,6 @@ void Engine::k_sc_iteration(double alpha, const gwgb_mu_search &ms) {
   k_rotate_G();
   k_p0(1);
   k_pq(false);
-  k_rotate_P();
   k_sigma();
   launch_mix(Sig_.p, Sold_.p, (int64_t)Sig_.n, alpha, st_);
   launch_transform(slab_s_fwd_.p, (int)slab_s_fwd_.n, max_cols_g_, Tnt_.p, nw_, ncheb_, 1, Sig_.p, Ww_.p, st_);
@@ -1613,6 +1656,7 @@ void Engine::sc_loop(int niter, double alpha, const gwgb_mu_search &ms, int fina
   GWGB_REQUIRE(niter >= 1 && niter <= 100000, GWGB_E_INVALID, "niter must be in [1, 100000]");
   GWGB_REQUIRE(alpha > 0.0 && alpha <= 1.0, GWGB_E_INVALID, "mixing alpha must be in (0, 1]");
   check_mu_search(ms);
+  prepare_operands();
   if ((int)recs_.n < niter) {  // the graph records through recs_.p
     drop_graphs();
     recs_.alloc((size_t)niter);

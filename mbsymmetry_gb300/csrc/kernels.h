@@ -38,6 +38,9 @@ void launch_reduce_slices(const RedTask *tasks, int ntasks, const double2 *part,
 void launch_rotate(const RotTask *tasks, int ntasks, int nbatch, int smem_bytes, const double2 *src,
                    const double2 *O, double2 *dst, cudaStream_t st);
 
+// Vt = op(O)^T V for every Sigma contribution (VrTask).
+void launch_vrot(const VrTask *tasks, int ntasks, const double2 *V, const double2 *O, double2 *Vt, cudaStream_t st);
+
 void launch_mirror(double2 *P, const int64_t *qoff, const int32_t *qsz, int nq, int nts, cudaStream_t st);
 void launch_zero_upper(double2 *P, const int64_t *qoff, const int32_t *qsz, int nq, int nts, cudaStream_t st);
 

@@ -180,7 +180,10 @@ __global__ void __launch_bounds__(256, 2) sigma_fp64_kernel(const SigTile *__res
         const double2 *Pt = P + cb.pq + (size_t)tau * cb.pstride + Pi;
         const double2 *y1 = Y1 + ((size_t)it * qb * b1 + i) * nn_n + nn;
         double2 a = make_double2(0.0, 0.0);
-        for (int Q = 0; Q < qb; ++Q) a = cfma(y1[(size_t)Q * b1 * nn_n], Pt[(size_t)Q * qb], a);
+        if (cb.pconj)  // P~(q) of a time-reversal partner: conj(P~(q'))
+          for (int Q = 0; Q < qb; ++Q) a = cfma(y1[(size_t)Q * b1 * nn_n], cconj(Pt[(size_t)Q * qb]), a);
+        else
+          for (int Q = 0; Q < qb; ++Q) a = cfma(y1[(size_t)Q * b1 * nn_n], Pt[(size_t)Q * qb], a);
         Y2[e] = a;
       }
       __syncthreads();
@@ -223,6 +226,33 @@ __global__ void reduce_slices_kernel(const RedTask *__restrict__ tasks, const do
     const double2 v = cscale(a, scale);
     out[tk.out + (int64_t)tau * tk.ostride + e] = v;
     if (mirror) out[tk.out + (int64_t)(nts - 1 - tau) * tk.ostride + e] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pre-rotated V of the Sigma contributions: Vt[Q'][x] = sum_Q op(O[Q][Q']) V[Q][x]
+// (op = conj for a time-reversal partner; o < 0: a copy), once per V / rep
+// upload.  One CTA per contribution block.
+// ---------------------------------------------------------------------------
+__global__ void vrot_kernel(const VrTask *__restrict__ tasks, const double2 *__restrict__ V,
+                            const double2 *__restrict__ O, double2 *__restrict__ Vt) {
+  const VrTask t = tasks[blockIdx.x];
+  const int qb = t.qb, n = t.b1b2;
+  const double2 *v = V + t.v;
+  double2 *out = Vt + t.vt;
+  if (t.o < 0) {
+    for (int e = threadIdx.x; e < qb * n; e += blockDim.x) out[e] = v[e];
+    return;
+  }
+  const double2 *o = O + t.o;
+  for (int e = threadIdx.x; e < qb * n; e += blockDim.x) {
+    const int Qp = e / n, x = e - Qp * n;
+    double2 a = make_double2(0.0, 0.0);
+    if (t.conj)
+      for (int Q = 0; Q < qb; ++Q) a = cfma(cconj(o[Q * qb + Qp]), v[(size_t)Q * n + x], a);
+    else
+      for (int Q = 0; Q < qb; ++Q) a = cfma(o[Q * qb + Qp], v[(size_t)Q * n + x], a);
+    out[e] = a;
   }
 }
 
@@ -692,6 +722,12 @@ void launch_rotate(const RotTask *tasks, int ntasks, int nbatch, int smem_bytes,
                    const double2 *O, double2 *dst, cudaStream_t st) {
   if (ntasks == 0 || nbatch == 0) return;
   rotate_kernel<<<dim3(ntasks, nbatch), 128, smem_bytes, st>>>(tasks, src, O, dst);
+  GWGB_CUDA(cudaGetLastError());
+}
+
+void launch_vrot(const VrTask *tasks, int ntasks, const double2 *V, const double2 *O, double2 *Vt, cudaStream_t st) {
+  if (ntasks == 0) return;
+  vrot_kernel<<<ntasks, 256, 0, st>>>(tasks, V, O, Vt);
   GWGB_CUDA(cudaGetLastError());
 }
 

@@ -157,13 +157,14 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
       const double2 *row = P + tl.pa + (int64_t)(tl.t0 + it) * tl.pstride + (int64_t)Q * qb;
       if (2 * q < qb) v0 = __ldg(row + 2 * q);
       if (2 * q + 1 < qb) v1 = __ldg(row + 2 * q + 1);
+      if (tl.pconj) { v0.y = -v0.y; v1.y = -v1.y; }
     }
     PL::store4(A, apl, PL::off(r, 4 * q, KP), make_float4((float)v0.x, (float)v0.y, (float)v1.x, (float)v1.y));
   }
-  const int npacks = (tl.ncol + SW_PACK - 1) / SW_PACK;
+  const int npacks = (tl.c1 - tl.c0 + SW_PACK - 1) / SW_PACK;
   auto stage_b = [&](int pk) {
     unsigned char *B = Bb + (pk & 1) * PL::N * bpl;
-    const int c0 = pk * SW_PACK;
+    const int c0 = tl.c0 + pk * SW_PACK;
     // rows (col, d) of the real embedding of B = conj(V): d=0 -> (Br, -Bi), d=1 -> (Bi, Br), Br = Vr, Bi = -Vi;
     // a lane writes one K quad (two complex) of both rows of one column
     for (int e = tid; e < SW_PACK * nq; e += 256) {
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
       const int q = rest % nq, cl = (rest / nq) * 4 + cll;
       const int col = c0 + cl;
       float2 b0 = make_float2(0.f, 0.f), b1 = b0;  // conj(V) as stored
-      if (col < tl.ncol) {
+      if (col < tl.c1) {
         const float2 *bc = Bcat + tl.bcat + (int64_t)col * qb;
         if (2 * q < qb) b0 = bc[2 * q];
         if (2 * q + 1 < qb) b1 = bc[2 * q + 1];
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
     tc::fence_after_sync();
     if (ok && warp < 4) {
       const uint32_t acc = tmem + (uint32_t)((pk & 1) * 2 * SW_PACK) + ((uint32_t)(warp * 32) << 16);
-      const int c0 = pk * SW_PACK;
+      const int c0 = tl.c0 + pk * SW_PACK;
       for (int j0 = 0; j0 < 2 * SW_PACK; j0 += 8) {
         float v[8];
         tc::tmem_ld8(acc + (uint32_t)j0, v);
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
 #pragma unroll
           for (int j = 0; j < 8; j += 2) {
             const int col = c0 + ((j0 + j) >> 1);
-            if (col < tl.ncol) wrow[col] = make_float2(v[j], v[j + 1]);
+            if (col < tl.c1) wrow[col] = make_float2(v[j], v[j + 1]);
           }
         }
       }

@@ -17,10 +17,11 @@ struct SwTile {
   int32_t pstride;  // per-tau stride of P(q)
   int32_t qb;
   int32_t t0, nt;   // tau range; nt * qb <= 128
-  int32_t ncol;     // complex columns of the block
+  int32_t ncol;     // complex columns of the block (the row length of W)
   int32_t kp;       // K = 2 qb padded to 8 (the BF16 kernel pads it to 16)
   int32_t npk;      // complex columns per pack (16, 32 or 64)
-  int32_t pad;
+  int32_t pconj;    // A = conj(P~(q')) (time-reversal partner)
+  int32_t c0, c1;   // the columns [c0, c1) this CTA computes
 };
 
 // Bcat entries: one per Sigma contribution.
