@@ -197,9 +197,18 @@ def _rand_unitary(rng, n):
     return q * (np.diag(r) / np.abs(np.diag(r)))[None, :]
 
 
-def make_crystal(spec: CrystalSpec, rotate: bool = True) -> Crystal:
+def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool = False,
+                 with_V: bool = True) -> Crystal:
     """Build the crystal.  ``rotate=False`` keeps every k point (ink = nk,
-    identity rotations), the reference's no-symmetry mode."""
+    identity rotations), the reference's no-symmetry mode.
+
+    ``used_pairs_only=True`` stores V blocks only for the k pairs a GW
+    iteration reads -- (k1, k1 + q) for irreducible q (P0) and (k1, k2) for
+    irreducible k1 (Sigma), with their Hermitian partners -- and leaves the
+    other pair slices empty; the stored blocks are identical to the full
+    crystal's (every pair draws from its own random stream).  ``with_V=False``
+    skips V (an empty array): the layout and one-body data only, e.g. to size
+    a configuration before generating it."""
     rng = np.random.default_rng(spec.seed)
     ops, inversion = _fcc_ops() if spec.lattice == "fcc" else _hex_ops()
     kmesh = _kmesh(spec.mesh)
@@ -262,11 +271,24 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True) -> Crystal:
     tmp_layout = BlockLayout(nk=nk, kmesh=kmesh, ao_sizes=ao_sizes, aux_sizes=aux_sizes,
                              tensor_irreps=[np.zeros((0, 3), int)] * (nk * nk),
                              irre_list=irre_list, index=idx, irre_index=irre_index, conj_index=cidx)
+    used = None
+    if used_pairs_only:
+        used = set()
+        for q in irre_list:
+            for k1 in range(nk):
+                k2 = tmp_layout.mom_cons(k1, 0, int(q))
+                used.update({(k1, k2), (k2, k1)})
+        for k1 in irre_list:
+            for k2 in range(nk):
+                used.update({(int(k1), k2), (k2, int(k1))})
     ti = []
     for k1 in range(nk):
         for k2 in range(nk):
             q = tmp_layout.pair_q(k1, k2)
             blocks = []
+            if used is not None and (k1, k2) not in used:
+                ti.append(np.zeros((0, 3), dtype=np.int32))
+                continue
             for iq, lq in enumerate(aux_lab[q]):
                 for i1, l1 in enumerate(ao_lab[k1]):
                     for i2, l2 in enumerate(ao_lab[k2]):
@@ -292,13 +314,15 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True) -> Crystal:
                          auxrep=np.concatenate(auxrep_blocks).astype(np.complex128), auxrep_irreps=auxrep_irreps)
 
     # --- V with the Hermitian pair relation V(k2,k1)_{Q,j,i} = conj(V(k1,k2)_{Q,i,j})
-    V = np.zeros(layout.flat_V_size, dtype=np.complex128)
+    V = np.zeros(layout.flat_V_size if with_V else 0, dtype=np.complex128)
     sigma = spec.v_scale / np.sqrt(spec.nao)
-    vrng = np.random.default_rng(spec.seed + 7)
-    for k1 in range(nk):
+    for k1 in (range(nk) if with_V else ()):
         for k2 in range(k1, nk):
             p = k1 * nk + k2
             pr = k2 * nk + k1
+            if len(layout.tensor_irreps[p]) == 0:
+                continue
+            vrng = np.random.default_rng((spec.seed + 7, p))  # one stream per pair
             q = layout.pair_q(k1, k2)
             qr = layout.pair_q(k2, k1)
             base, baser = layout.kpair_slice_offsets[p], layout.kpair_slice_offsets[pr]

@@ -107,3 +107,28 @@ def test_mixed_tau_chunks_are_exact(kind, monkeypatch):
     (s1, p1, n1), (s2, p2, n2) = out
     assert n2 > n1                      # the chunked run really launched per chunk
     assert np.array_equal(p1, p2) and np.array_equal(s1, s2)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32x3"])
+def test_used_pairs_only_storage_is_exact(precision):
+    """V stored only for the k pairs an iteration reads (the other pair slices
+    empty) gives bitwise the same P~ and Sigma as the full storage."""
+    from mbsymmetry_gb300.crystal import CONFIGS, load_ir, make_crystal
+    from mbsymmetry_gb300.solver import GWSolver
+    from mbsymmetry_gb300.transformer import build_transforms
+    spec = CONFIGS["C1"]
+    tr = build_transforms(load_ir(spec.nts), spec.beta)
+    out = []
+    for used in (False, True):
+        cr = make_crystal(spec, used_pairs_only=used)
+        s = GWSolver(cr.layout, cr.ns, tr, precision=precision)
+        s.set_shared_Coulomb(cr.V)
+        s.set_fock(cr.F, cr.S)
+        s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+        s.dyson(cr.mu)
+        s.solve()
+        out.append((s.P0_q_t_QP(), s.Selfenergy(), cr.layout.flat_V_size))
+        s.close()
+    (p1, s1, n1), (p2, s2, n2) = out
+    assert n2 < n1
+    assert np.array_equal(p1, p2) and np.array_equal(s1, s2)
