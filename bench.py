@@ -36,6 +36,8 @@ WORKLOADS = {
            "ns=1, V stored for all 729 k pairs, irrep blocks 1-8 (AO) / 2-40 (aux)"),
     "C3": ("C3: Fm-3m 4x4x4 k mesh (64 k, 8 irreducible), nao=52, naux=250, nts=120, beta=100, "
            "ns=1, V stored for all 4096 k pairs (12.2 GB), irrep blocks 2-16 (AO) / 4-64 (aux)"),
+    "C3m": ("C3m (profiling case): C3's nao=52, naux=250, nts=120, beta=100 and block sizes 2-16 / 4-64 "
+            "on the Fm-3m 3x3x3 mesh (27 k)"),
 }
 WORKLOAD = WORKLOADS[CONFIG]
 METRIC = "s/GW iteration (FP64 drop-in, P0 -> W~ -> Sigma -> Dyson)"
@@ -383,7 +385,7 @@ def run_profile(args):
     s.set_G(G0)
     s.iteration(cr.mu)
     st = s.stats()
-    if CONFIG == "C2":
+    if CONFIG == "C2":  # the SC loop only on the benchmark workload
         s.single_prec_run(False)
         s.set_G(G0)
         s.set_Selfenergy(np.zeros(s.g_size, np.complex128))

@@ -356,7 +356,7 @@ class Engine {
   struct SigChunk { int t0, t1, uv0, nuv_blocked, nuv, w0, nw, red0, nred; };
   DBuf<RedTask> uv_red_;     // ordered sums of the FP32-stage slices, per chunk
   int64_t uv_part_need_ = 0;
-  struct P0Chunk { int t0, t1, k0, nk; };
+  struct P0Chunk { int t0, t1, k0, nk, r0, nr; };
   std::vector<SigChunk> sig_chunks_;
   std::vector<P0Chunk> p0_chunks_;
   int tch_w_ = 1, tch_z_ = 1;
@@ -697,7 +697,6 @@ void Engine::build_work_lists() {
     std::vector<PkTile> kt;
     std::vector<PrTile> rt;
     int zneed = 0;
-    const int SL = 8;  // K slice: 8 chunks of 16 complex columns
     int zcap = 110 * 1024;  // two CTAs per SM when the one-row minimum of every task fits
     struct ZGroup { int qb, zld; int64_t zoff, voff; };
     std::vector<ZGroup> zg;
@@ -710,7 +709,16 @@ void Engine::build_work_lists() {
       zrow += (int64_t)g.qb * zld;
       voff += (int64_t)g.qb * zld;
     }
-    tch_z_ = chunk_len(zrow, half);
+    // K slices of 8 chunks of 16 complex columns: FP32 (TMEM) accumulation stays
+    // within about one contribution, FP64 across slices.  The tau chunk is sized so
+    // that both Zcat and the FP64 slice partials of one chunk fit the budget.
+    const int SL = 8;
+    int64_t ppart_per_tau = 0;
+    for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {
+      const int nchunks = zg[gi].zld / 16;
+      ppart_per_tau += (int64_t)p0_groups_[gi].qb * p0_groups_[gi].qb * std::max(1, (nchunks + SL - 1) / SL);
+    }
+    tch_z_ = chunk_len(zrow + 2 * ppart_per_tau, half);
     for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {
       const auto &g = p0_groups_[gi];
       const int qb = g.qb, zld = zg[gi].zld;
@@ -732,11 +740,12 @@ void Engine::build_work_lists() {
       GWGB_REQUIRE(NP <= 128, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 P0 kernel");
     }
     const int64_t zbuf = zrow * tch_z_;
-    int64_t poff = 0;
+    int64_t ppart_max = 0;
     p0_chunks_.clear();
     for (int c0 = 0; c0 < half; c0 += tch_z_) {
       const int c1 = std::min(half, c0 + tch_z_);
-      const size_t k0 = kt.size();
+      const size_t k0 = kt.size(), r0 = rt.size();
+      int64_t poff = 0;  // the partial sums of one chunk, summed before the next chunk
       for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {
         const auto &g = p0_groups_[gi];
         const int qb = g.qb, zld = zg[gi].zld;
@@ -760,9 +769,11 @@ void Engine::build_work_lists() {
           poff += nslice * slice;
         }
       }
+      ppart_max = std::max(ppart_max, poff);
       std::stable_sort(kt.begin() + k0, kt.end(), [](const PkTile &a, const PkTile &b) { return a.kcn > b.kcn; });
-      p0_chunks_.push_back({c0, c1, (int)k0, (int)(kt.size() - k0)});
+      p0_chunks_.push_back({c0, c1, (int)k0, (int)(kt.size() - k0), (int)r0, (int)(rt.size() - r0)});
     }
+    const int64_t poff = ppart_max;
     for (const PzTask &t : zt)
       check_range(t.z + t.zcol, ((int64_t)(tch_z_ - 1) * t.qb + (t.qb - 1)) * t.zld + (int64_t)t.b1 * t.b2, zbuf,
                   "Z operand rows");
@@ -1264,13 +1275,10 @@ void Engine::k_p0(int mirror) {
   const double pref = -1.0 / l_.nk * (ns_ == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
   if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE((Zbuf_.p || !zbuf_elems_) && vcat_ready_, GWGB_E_STATE, "mixed-precision operands not prepared");
-    for (size_t i = 0; i < p0_chunks_.size(); ++i) {
-      const P0Chunk &ch = p0_chunks_[i];
-      const bool last = i + 1 == p0_chunks_.size();  // the slice sums run once, after the last chunk
+    for (const P0Chunk &ch : p0_chunks_)  // each chunk's slices are summed before the next chunk
       launch_p0_tc(prec_ == GWGB_PREC_BF16X3, pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pk_tiles_.p + ch.k0, ch.nk,
-                   pr_tiles_.p, last ? (int)pr_tiles_.n : 0, V_.p, Gall_.p, Zbuf_.p, Vcat_.p, Ppart_.p, Pall_.p, ns_,
-                   nts_, ch.t0, ch.t1, pref, mirror, bad_.p + 2, st_);
-    }
+                   pr_tiles_.p + ch.r0, ch.nr, V_.p, Gall_.p, Zbuf_.p, Vcat_.p, Ppart_.p, Pall_.p, ns_, nts_,
+                   ch.t0, ch.t1, pref, mirror, bad_.p + 2, st_);
   } else {
     launch_p0_fp64(p0_tiles_.p, (int)p0_tiles_.n, p0_maxo_, p0_contribs_.p, V_.p, Gall_.p, Part_.p, ns_, nts_,
                    fp64_smem_, st_);
@@ -1353,8 +1361,8 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
     int64_t sgt = 0, p0t = 0;
     for (const SigChunk &ch : sig_chunks_)
       sgt += (ch.nw ? 1 : 0) + (ch.nuv_blocked ? 1 : 0) + (ch.nuv > ch.nuv_blocked ? 1 : 0) + (ch.nred ? 1 : 0);
-    for (const P0Chunk &ch : p0_chunks_) p0t += (pz_tasks_.n ? 1 : 0) + (ch.nk ? 1 : 0);
-    const int64_t p0 = tc ? p0t + (pr_tiles_.n ? 1 : 0)
+    for (const P0Chunk &ch : p0_chunks_) p0t += (pz_tasks_.n ? 1 : 0) + (ch.nk ? 1 : 0) + (ch.nr ? 1 : 0);
+    const int64_t p0 = tc ? p0t
                           : (p0_tiles_.n ? 1 : 0) + (p0_red_.n ? 1 : 0);
     const int64_t sg = tc ? sgt
                           : (sig_tiles_.n ? 1 : 0) + (sig_red_.n ? 1 : 0);

@@ -99,8 +99,8 @@ struct PrTile {
   int32_t pad;
 };
 
-// One tau chunk [tau0, tau1) of the P0 stages: Z tasks, then the GEMM tiles of
-// the chunk; the slice sums (rtiles, nr > 0) are launched after the last chunk.
+// One tau chunk [tau0, tau1) of the P0 stages: Z tasks, the GEMM tiles of the
+// chunk, then the ordered sums of the chunk's slices (rtiles).
 void launch_p0_tc(bool bf16, const PzTask *ztasks, int nz, int zsmem, const PkTile *ktiles, int nk, const PrTile *rtiles,
                   int nr, const double2 *V, const double2 *G, float2 *Z, const float2 *Vcat, double2 *Ppart,
                   double2 *P0, int ns, int nts, int tau0, int tau1, double pref, int mirror, int *err,
