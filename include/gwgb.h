@@ -104,6 +104,7 @@ typedef struct gwgb_stats {
   double sigma_flops;     /* algorithmic FLOPs of the Sigma stage */
   double leakage;         /* max|c_{n-1}| / max|c_0| of G after the last Dyson */
   int64_t kernel_launches;/* kernels launched by the last solve/iteration */
+  int64_t device_bytes;   /* device memory held by the buffers of all live handles of this process */
 } gwgb_stats;
 
 /* Library version string. */

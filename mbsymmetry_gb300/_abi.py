@@ -56,6 +56,7 @@ class GwgbStats(ctypes.Structure):
         ("rotate_P_ms", c_double), ("sigma_ms", c_double), ("dyson_ms", c_double),
         ("total_ms", c_double), ("p0_flops", c_double), ("sigma_flops", c_double),
         ("leakage", c_double), ("kernel_launches", c_int64),
+        ("device_bytes", c_int64),
     ]
 
 

@@ -7,6 +7,7 @@
 // kernels.  An iteration is a fixed sequence of kernel launches over static
 // work lists, so it is captured once as a CUDA graph and replayed.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <cstdlib>
@@ -187,14 +188,18 @@ static Lay derive_layout(const gwgb_layout &L) {
 // ---------------------------------------------------------------------------
 // device buffer helper
 // ---------------------------------------------------------------------------
+// Device bytes held by the buffers of every live handle in this process.
+static std::atomic<int64_t> g_device_bytes{0};
+
 template <typename T>
 struct DBuf {
   T *p = nullptr;
   size_t n = 0;
   void alloc(size_t count) {
     free();
-    n = count;
     if (count) GWGB_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+    g_device_bytes += (int64_t)(n * sizeof(T));
   }
   void upload(const std::vector<T> &v, cudaStream_t st) {
     alloc(v.size());
@@ -202,6 +207,7 @@ struct DBuf {
   }
   void free() {
     if (p) cudaFree(p);
+    g_device_bytes -= (int64_t)(n * sizeof(T));
     p = nullptr;
     n = 0;
   }
@@ -299,7 +305,10 @@ class Engine {
   void find_mu(const gwgb_mu_search &ms, double *mu_out, double *n_out);
   void energy(double *e_corr, double *e_one);
   void sc_loop(int niter, double alpha, const gwgb_mu_search &ms, int final_fp64, gwgb_sc_record *out);
-  void stats(gwgb_stats *out) const { *out = stats_; }
+  void stats(gwgb_stats *out) const {
+    *out = stats_;
+    out->device_bytes = g_device_bytes.load();
+  }
   void test_raise_status(int which) {
     GWGB_REQUIRE(which >= 0 && which <= 2, GWGB_E_INVALID, "status word must be 0, 1 or 2");
     const int one = 1;
