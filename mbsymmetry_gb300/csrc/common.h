@@ -89,6 +89,9 @@ struct SigTile {
   int32_t c0, c1;
   int32_t t0, nt;
   int32_t s, cost;
+  int32_t ntq;        // tcgen05 U/Sigma tiles: the tau count the aux-row chunks are sized
+                      // for (the owner's, so the K steps never depend on the tau chunking)
+  int32_t pad;
 };
 
 // Rotation task: dst = O * src * O^H per (batch index), optionally conjugated;

@@ -362,7 +362,9 @@ class Engine {
   std::vector<char> uv_blocked_host_;
   // tau chunks of the tensor-core operands (W for Sigma, Zcat for P0), each
   // buffer sized to tc_chunk_bytes_: [t0, t1) and the work items of the chunk
-  struct SigChunk { int t0, t1, uv0, nuv_blocked, nuv, w0, nw, red0, nred; };
+  // tiles [uv0, uv0 + nuv): nuvt tcgen05 U/Sigma tiles, then nuv_blocked and the rest SIMT tiles
+  struct SigChunk { int t0, t1, uv0, nuvt, nuv_blocked, nuv, w0, nw, red0, nred; };
+  int uvt_smem_ = 0;
   DBuf<RedTask> uv_red_;     // ordered sums of the FP32-stage slices, per chunk
   int64_t uv_part_need_ = 0;
   struct P0Chunk { int t0, t1, k0, nk, r0, nr; };
@@ -872,10 +874,35 @@ void Engine::build_work_lists() {
       ucost[c] = 8.0 * sc[c].qb * sig_b1_[c] * sc[c].b2 * (sig_b1_[c] + sc[c].b2);
       utotal += ucost[c];
     }
-    // Slices depend on the per-tau cost only (about one wave of slices per tau), never on
-    // the chunk length: the order of the FP64 sums, hence every result bit, is the same
-    // for any chunking.  Tiles span at most 4 tau.
-    const double target = utotal * ns_ / (double)std::max(1, nsm_);
+    // Slices depend on the per-tau cost only (about four waves of slices per tau), never
+    // on the chunk length: the order of the FP64 sums, hence every result bit, is the
+    // same for any chunking.  tcgen05 tiles span up to 128 / b1 tau, SIMT tiles 4.
+    const double target = utotal * ns_ / (4.0 * std::max(1, nsm_));
+    // tcgen05 U/Sigma tiles (AO blocks up to 64): tau per tile such that one aux row
+    // of the largest contribution fits the shared-memory budget (two CTAs per SM when
+    // possible; measured against one CTA with longer aux-row chunks (slower on both
+    // workloads) and three (3% faster on C3, 25% slower on C2); GWGB_UVT_SMEM_KB
+    // overrides the budget)
+    int uvt_budget = 110 * 1024;
+    if (const char *e = std::getenv("GWGB_UVT_SMEM_KB")) uvt_budget = std::max(60, std::min(227, std::atoi(e))) * 1024;  // <= 4 CTAs x 128 TMEM columns
+    uvt_budget = std::min(uvt_budget, smem_bytes_);
+    std::vector<int> own_nt(sig_own.size(), 0);  // 0: SIMT tiles
+    uvt_smem_ = 0;
+    for (size_t oi = 0; oi < sig_own.size(); ++oi) {
+      const Owner &o = sig_own[oi];
+      if (o.n > 64) continue;
+      int b2max = 1;
+      for (int c = o.c0; c < o.c1; ++c) b2max = std::max(b2max, sc[c].b2);
+      auto need = [&](int nt) {
+        return (int)std::max(uvt_smem(1, nt, o.n, b2max, false), uvt_smem(1, nt, o.n, b2max, true));
+      };
+      int nt = std::max(1, std::min(nts_, 128 / o.n));
+      while (nt > 1 && need(nt) > uvt_budget) --nt;
+      if (need(nt) > smem_bytes_) continue;
+      own_nt[oi] = nt;
+      uvt_smem_ = std::max(uvt_smem_, std::max(uvt_budget, need(nt)));
+    }
+    uvt_smem_ = std::min(smem_bytes_, ((uvt_smem_ + 1023) / 1024) * 1024);
     std::vector<std::vector<std::pair<int, int>>> oslices(sig_own.size());
     for (size_t i = 0; i < sig_own.size(); ++i)
       oslices[i] = split_slices(ucost, sig_own[i].c0, sig_own[i].c1, target);
@@ -886,26 +913,29 @@ void Engine::build_work_lists() {
     uv_part_need_ = 0;
     for (int c0 = 0; c0 < nts_; c0 += tch_w_) {
       const int c1 = std::min(nts_, c0 + tch_w_);
-      std::vector<SigTile> stl;
+      std::vector<SigTile> stl, utl;
       int64_t part = 0;
       const int r0 = (int)ured.size();
       for (size_t oi = 0; oi < sig_own.size(); ++oi) {
         const Owner &o = sig_own[oi];
         const int bb = o.n * o.n;
-        const int nt = std::max(1, std::min(std::min(4, c1 - c0), (smem_bytes_ / 4) / (24 * bb)));
+        const bool tcu = own_nt[oi] > 0;
+        const int nt = tcu ? std::min(own_nt[oi], c1 - c0)
+                           : std::max(1, std::min(std::min(4, c1 - c0), (smem_bytes_ / 4) / (24 * bb)));
         for (int t0 = c0; t0 < c1; t0 += nt) {
           const int n = std::min(nt, c1 - t0);
           const auto &sl = oslices[oi];
           ured.push_back({part, o.out, o.ostride, bb, t0, n, (int32_t)sl.size(), 0});
           for (const auto &r : sl) {
-            stl.push_back({o.out, part, o.ostride, o.n, r.first, r.second, t0, n, o.s,
-                           (int32_t)std::min(slice_cost(ucost, r) * n / 1e3, 2e9)});
+            (tcu ? utl : stl).push_back({o.out, part, o.ostride, o.n, r.first, r.second, t0, n, o.s,
+                                         (int32_t)std::min(slice_cost(ucost, r) * n / 1e3, 2e9), own_nt[oi], 0});
             part += (int64_t)n * bb;
           }
         }
       }
       uv_part_need_ = std::max(uv_part_need_, part);
       std::stable_sort(stl.begin(), stl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
+      std::stable_sort(utl.begin(), utl.end(), [](const SigTile &a, const SigTile &b) { return a.cost > b.cost; });
       // slices whose contributions average fewer than 200 (Q, m) terms take the
       // unblocked variant (barriers dominate there); each chunk = [blocked | small]
       std::vector<SigTile> big, small;
@@ -915,8 +945,14 @@ void Engine::build_work_lists() {
         const bool sm = t.c1 > t.c0 && k < 200.0 * (t.c1 - t.c0);
         (sm ? small : big).push_back(t);
       }
-      SigChunk ch{c0, c1, (int)all.size(), (int)big.size(), (int)(big.size() + small.size()), 0, 0, r0,
-                  (int)ured.size() - r0};
+      SigChunk ch{c0, c1, (int)all.size(), (int)utl.size(), (int)big.size(),
+                  (int)(utl.size() + big.size() + small.size()), 0, 0, r0, (int)ured.size() - r0};
+      for (const SigTile &t : utl) {
+        GWGB_REQUIRE(t.nt * t.b1 <= 128 && t.b1 <= 64 && t.nt <= t.ntq, GWGB_E_INVALID,
+                     "internal work list out of bounds: tcgen05 U/Sigma tile shape");
+        all.push_back(t);
+        uv_blocked_host_.push_back(2);
+      }
       for (const SigTile &t : big) { all.push_back(t); uv_blocked_host_.push_back(1); }
       for (const SigTile &t : small) { all.push_back(t); uv_blocked_host_.push_back(0); }
       sig_chunks_.push_back(ch);
@@ -1044,7 +1080,8 @@ void Engine::build_work_lists() {
     int uv_cap = smem_bytes_;
     for (size_t n = 0; n < sig_tiles1_host_.size(); ++n) {
       const SigTile &t = sig_tiles1_host_[n];
-      const bool blocked = uv_blocked_host_[n] != 0;
+      if (uv_blocked_host_[n] == 2) continue;  // tcgen05 U/Sigma tile (sized above)
+      const bool blocked = uv_blocked_host_[n] == 1;
       int b2max = 1, qbmax = 1;
       for (int c = t.c0; c < t.c1; ++c) { b2max = std::max(b2max, sc[c].b2); qbmax = std::max(qbmax, sc[c].qb); }
       // acc64, acc32, red (blocked variant only), G2
@@ -1308,8 +1345,9 @@ void Engine::k_sigma() {
     GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
     for (const SigChunk &ch : sig_chunks_) {
       launch_sigma_tc(prec_ == GWGB_PREC_BF16X3, sw_tiles_.p + ch.w0, ch.nw, sw_smem_, Bcat_.p,
-                      sig_tiles1_.p + ch.uv0, ch.nuv, sig_contribs_.p, sig_wref_.p, Vt_.p, Gall_.p, Pall_.p, Wbuf_.p,
-                      Part_.p, ns_, uv_smem_, ch.nuv_blocked, uv_smem_small_, ch.t0, bad_.p + 2, st_);
+                      sig_tiles1_.p + ch.uv0, ch.nuvt, uvt_smem_, sig_tiles1_.p + ch.uv0 + ch.nuvt, ch.nuv - ch.nuvt,
+                      sig_contribs_.p, sig_wref_.p, Vt_.p, Gall_.p, Pall_.p, Wbuf_.p, Part_.p, ns_, uv_smem_,
+                      ch.nuv_blocked, uv_smem_small_, ch.t0, bad_.p + 2, st_);
       launch_reduce_slices(uv_red_.p + ch.red0, ch.nred, Part_.p, Sig_.p, nts_, -1.0 / l_.nk, 0, st_);
     }
   } else {
@@ -1369,7 +1407,8 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
     const bool tc = prec_ != GWGB_PREC_FP64;
     int64_t sgt = 0, p0t = 0;
     for (const SigChunk &ch : sig_chunks_)
-      sgt += (ch.nw ? 1 : 0) + (ch.nuv_blocked ? 1 : 0) + (ch.nuv > ch.nuv_blocked ? 1 : 0) + (ch.nred ? 1 : 0);
+      sgt += (ch.nw ? 1 : 0) + (ch.nuvt ? 1 : 0) + (ch.nuv_blocked ? 1 : 0) +
+             (ch.nuv - ch.nuvt > ch.nuv_blocked ? 1 : 0) + (ch.nred ? 1 : 0);
     for (const P0Chunk &ch : p0_chunks_) p0t += (pz_tasks_.n ? 1 : 0) + (ch.nk ? 1 : 0) + (ch.nr ? 1 : 0);
     const int64_t p0 = tc ? p0t
                           : (p0_tiles_.n ? 1 : 0) + (p0_red_.n ? 1 : 0);

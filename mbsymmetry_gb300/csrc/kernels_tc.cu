@@ -563,10 +563,226 @@ __global__ void __launch_bounds__(256) sigma_uv_small_kernel(const SigTile *__re
   sigma_uv_small(tile, contribs, wref, V, G, W, Part, ns, smem_bytes, tau0);
 }
 
-void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
-                     int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
-                     const double2 *G, const double2 *P, float2 *W, double2 *Part, int ns, int uv_smem,
-                     int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st) {
+// ---------------------------------------------------------------------------
+// (2) on CUDA cores feeding (3) on tcgen05: one CTA per (owner, range of nt tau
+// with nt * b1 <= 128, slice of contributions).  Per contribution and chunk of
+// qn aux rows Q:
+//   U[(tau, Q, j)][m] = sum_n W(tau)[Q][j][n] G2(tau)[m][n]   FP32 SIMT: a thread owns
+//       8 m of one row and stores them, split, straight into the operand planes of
+//   S[(tau, j)][(i, re/im)] += sum_K A[(tau, j)][K] Bv[(i, re/im)][K]   tcgen05, M = 128,
+//       N = 2 b1 padded to 16, K = (Q, m, re/im), FP32 accumulation in TMEM over
+//       the whole contribution,
+// with Bv the real embedding of Vt[Q][i][m] (row 2i: (Vr, -Vi), row 2i+1: (Vi, Vr)).
+// After every chunk the TMEM accumulator (a short K) is added to an FP64
+// accumulator in shared memory, written to the tile's partial block
+// Part[tile.part + (it * b1 + i) * b1 + j] at the end; FP32 holds partial sums
+// over one chunk of aux rows, FP64 everything above.
+// Shared: FP64 acc [(tau, j)][b1|1] | A planes (128 x ks) | Bv planes (nsp x ks) |
+// W [nt][qn][b1][b2|1] | G2^T [nt][b2][m8] (float2), ks = qn * kq padded to the
+// MMA K step, kq = 2 b2 padded to 4, m8 = b2 padded to 8.
+// ---------------------------------------------------------------------------
+template <bool BF>
+__global__ void __launch_bounds__(256) sigma_uvt_kernel(const SigTile *__restrict__ tiles,
+                                                        const SigContrib *__restrict__ contribs,
+                                                        const WRef *__restrict__ wref, const double2 *__restrict__ V,
+                                                        const double2 *__restrict__ G, const float2 *__restrict__ W,
+                                                        double2 *__restrict__ Part, int ns, int smem_bytes, int tau0,
+                                                        int *__restrict__ err) {
+  using PL = Planes<BF>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ uint32_t tmem_slot;
+  __shared__ __align__(8) uint64_t mbar;
+  const SigTile tile = tiles[blockIdx.x];
+  const int b1 = tile.b1, nt = tile.nt, s = tile.s;
+  const int rows = nt * b1;             // <= 128 (host-checked)
+  const int nsp = uvt_nsp(b1);          // <= 128
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tile.c0 == tile.c1) {  // an owner without contributions: a zero block
+    for (int e = tid; e < nt * b1 * b1; e += 256) Part[tile.part + e] = make_double2(0.0, 0.0);
+    return;
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 128);
+  if (tid == 0) tc::mbar_init(&mbar, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  uint32_t phase = 0;
+  bool ok = true, pending = false;
+  const int ald = b1 | 1;
+  double2 *acc = reinterpret_cast<double2 *>(smem_raw);
+  unsigned char *const opnd = smem_raw + uvt_acc_bytes(nt, b1);
+  for (int e = tid; e < rows * ald; e += 256) acc[e] = make_double2(0.0, 0.0);
+  const uint32_t idesc = PL::idesc(128, nsp);
+  // Wait for the MMA group in flight and add its accumulator (one chunk of aux
+  // rows: a short K, so FP32 holds only a short sum) to the FP64 partial block;
+  // warps w and w+4 share TMEM lanes 32 (w % 4) .. +31 and split the columns.
+  auto flush = [&]() {
+    const bool done = tc::mbar_wait(&mbar, phase);
+    if (done) phase ^= 1u;
+    if (!done && tid == 0) atomicExch(err, 1);
+    ok = __syncthreads_and(done) != 0;
+    tc::fence_after_sync();
+    pending = !done;
+    if (!ok) return;
+    const int r = (warp & 3) * 32 + lane;
+    const int cbeg = (warp < 4) ? 0 : (nsp >> 1), cend = (warp < 4) ? (nsp >> 1) : nsp;
+    for (int c8 = cbeg; c8 < cend; c8 += 8) {
+      float v[8];
+      tc::tmem_ld8(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c8, v);
+      if (r < rows) {
+#pragma unroll
+        for (int h = 0; h < 8; h += 2) {
+          const int i = (c8 + h) >> 1;
+          if (i < b1) {
+            double2 &a = acc[r * ald + i];
+            a.x += (double)v[h];
+            a.y += (double)v[h + 1];
+          }
+        }
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();  // accumulator drained before the next group overwrites it
+    tc::fence_after_sync();
+  };
+  for (int c = tile.c0; c < tile.c1 && ok; ++c) {
+    if (pending) flush();  // the previous group reads shared memory laid out for its contribution
+    if (!ok) break;
+    const SigContrib cb = contribs[c];
+    const int qb = cb.qb, b2 = cb.b2;
+    const int kq = uvt_kq(b2), wld = uvt_wld(b2), m8 = uvt_m8(b2);
+    // aux rows per chunk: sized for the owner's tau count, not this tile's, so that
+    // the K steps (the rounding) are the same for every tau chunking
+    int qc = qb;
+    while (qc > 1 && uvt_smem(qc, tile.ntq, b1, b2, BF) > smem_bytes) --qc;
+    const int ksm = uvt_ks(qc, kq, BF);
+    unsigned char *A = opnd;
+    unsigned char *Bv = A + PL::N * 128u * ksm * PL::EB;
+    float2 *Ws = reinterpret_cast<float2 *>(Bv + PL::N * (uint32_t)nsp * ksm * PL::EB);
+    float2 *G2t = Ws + uvt_ws_elems(qc, nt, b1, b2);  // 16-byte aligned (float4 reads)
+    const double2 *Vb = V + cb.v;
+    const WRef wr = wref[c];
+    // G2^T for every tau of the range (no MMA of this CTA is in flight here)
+    for (int e = tid; e < nt * b2 * m8; e += 256) {
+      const int it = e / (b2 * m8), r = e - it * (b2 * m8), n = r / m8, m = r - n * m8;
+      float2 g = make_float2(0.f, 0.f);
+      if (m < b2) {
+        const double2 v = __ldg(G + cb.gb + ((int64_t)(tile.t0 + it) * ns + s) * cb.sb + m * b2 + n);
+        g = make_float2((float)v.x, (float)v.y);
+      }
+      G2t[e] = g;
+    }
+    for (int q0 = 0; q0 < qb; q0 += qc) {
+      const int qn = min(qc, qb - q0);
+      const int ks = uvt_ks(qn, kq, BF);
+      const uint32_t apl = 128u * ks * PL::EB, bpl = (uint32_t)nsp * ks * PL::EB;
+      // W rows (tau, Q) of the chunk (b1*b2 contiguous complex each); within a
+      // contribution they are loaded while the previous chunk's MMAs run (the MMAs
+      // read only A and Bv)
+      const int wrow = b1 * b2;
+      auto stage_w = [&]() {
+        for (int e = tid; e < nt * qn * wrow; e += 256) {
+          const int r = e / wrow, x = e - r * wrow, it = r / qn, Q = r - it * qn, j = x / b2, n = x - j * b2;
+          Ws[(r * b1 + j) * wld + n] = W[wr.base + ((int64_t)(tile.t0 + it - tau0) * qb + q0 + Q) * wr.ld + x];
+        }
+      };
+      const bool early = pending;
+      if (early) stage_w();
+      if (pending) flush();
+      if (!ok) break;
+      if (!early) stage_w();
+      // Bv: m pairs of Vt rows; zero rows >= 2 b1 and K columns >= qn * kq
+      const int mp = kq >> 2;
+      for (int e = tid; e < qn * b1 * mp; e += 256) {
+        const int p = e % mp, r = e / mp, i = r % b1, Q = r / b1, m = 2 * p;
+        const double2 *vr = Vb + ((int64_t)(q0 + Q) * b1 + i) * b2;
+        double2 v0 = make_double2(0.0, 0.0), v1 = v0;
+        if (m < b2) v0 = __ldg(vr + m);
+        if (m + 1 < b2) v1 = __ldg(vr + m + 1);
+        const int k = Q * kq + 4 * p;
+        PL::store4(Bv, bpl, PL::off(2 * i, k, ks),
+                   make_float4((float)v0.x, (float)-v0.y, (float)v1.x, (float)-v1.y));
+        PL::store4(Bv, bpl, PL::off(2 * i + 1, k, ks),
+                   make_float4((float)v0.y, (float)v0.x, (float)v1.y, (float)v1.x));
+      }
+      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int e = tid; e < (nsp - 2 * b1) * (ks >> 2); e += 256) {
+        const int r = 2 * b1 + e / (ks >> 2), k = 4 * (e % (ks >> 2));
+        PL::store4(Bv, bpl, PL::off(r, k, ks), z4);
+      }
+      const int kpad = (ks - qn * kq) >> 2;
+      for (int e = tid; e < 2 * b1 * kpad; e += 256) {
+        const int r = e / kpad, k = qn * kq + 4 * (e % kpad);
+        PL::store4(Bv, bpl, PL::off(r, k, ks), z4);
+      }
+      for (int e = tid; e < rows * kpad; e += 256) {
+        const int r = e / kpad, k = qn * kq + 4 * (e % kpad);
+        PL::store4(A, apl, PL::off(r, k, ks), z4);
+      }
+      __syncthreads();
+      // U, 8 m per thread; lanes of a warp share m (G2 reads are broadcasts)
+      const int nrow = nt * qn * b1, mc_n = m8 >> 3;
+      for (int item = tid; item < mc_n * nrow; item += 256) {
+        const int mc = item / nrow, row = item - mc * nrow;
+        const int it = row / (qn * b1), Q = (row / b1) % qn, j = row % b1;
+        const float2 *w = Ws + row * wld;
+        const float4 *g = reinterpret_cast<const float4 *>(G2t + it * b2 * m8 + 8 * mc);
+        float ur[8], ui[8];
+#pragma unroll
+        for (int x = 0; x < 8; ++x) ur[x] = ui[x] = 0.f;
+        for (int n = 0; n < b2; ++n) {
+          const float2 wv = w[n];
+          const float4 *gn = g + n * (m8 >> 1);
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const float4 gg = gn[h];
+            ur[2 * h] = fmaf(wv.x, gg.x, ur[2 * h]);
+            ur[2 * h] = fmaf(-wv.y, gg.y, ur[2 * h]);
+            ui[2 * h] = fmaf(wv.x, gg.y, ui[2 * h]);
+            ui[2 * h] = fmaf(wv.y, gg.x, ui[2 * h]);
+            ur[2 * h + 1] = fmaf(wv.x, gg.z, ur[2 * h + 1]);
+            ur[2 * h + 1] = fmaf(-wv.y, gg.w, ur[2 * h + 1]);
+            ui[2 * h + 1] = fmaf(wv.x, gg.w, ui[2 * h + 1]);
+            ui[2 * h + 1] = fmaf(wv.y, gg.z, ui[2 * h + 1]);
+          }
+        }
+        const int ra = it * b1 + j, kend = (Q + 1) * kq;
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int k = Q * kq + 16 * mc + 4 * h;
+          if (k < kend) PL::store4(A, apl, PL::off(ra, k, ks), make_float4(ur[2 * h], ui[2 * h], ur[2 * h + 1], ui[2 * h + 1]));
+        }
+      }
+      tc::fence_async_smem();
+      tc::fence_before_sync();
+      __syncthreads();
+      tc::fence_after_sync();
+      if (tid == 0) {
+        const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(Bv), sbo = PL::sbo(ks);
+        for (int st = 0; st < ks / PL::KSTEP; ++st)
+          PL::mma_step(tmem, a, apl, b, bpl, (uint32_t)st * 256, sbo, sbo, idesc, st > 0 ? 1u : 0u);
+        tc::commit(&mbar);
+      }
+      pending = true;
+    }
+  }
+  if (pending && ok) flush();  // the last group
+  if (pending) tc::mbar_wait(&mbar, phase, 100000);  // MMAs still in flight after a timeout (bounded)
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 128);
+  if (ok)
+    for (int e = tid; e < nt * b1 * b1; e += 256) {
+      const int it = e / (b1 * b1), x = e - it * (b1 * b1), i = x / b1, j = x - i * b1;
+      Part[tile.part + e] = acc[(it * b1 + j) * ald + i];
+    }
+}
+
+void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *uvt,
+                     int nuvt, int uvt_smem, const SigTile *tiles1, int ntiles1, const SigContrib *contribs,
+                     const WRef *wref, const double2 *V, const double2 *G, const double2 *P, float2 *W, double2 *Part,
+                     int ns, int uv_smem, int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st) {
   if (nwtiles > 0) {
     if (bf16)
       sigma_w_tc_kernel<true><<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, tau0, err);
@@ -574,7 +790,14 @@ void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, co
       sigma_w_tc_kernel<false><<<nwtiles, 256, wsmem, st>>>(wtiles, Bcat, P, W, tau0, err);
     GWGB_CUDA(cudaGetLastError());
   }
-  // tiles1 = [blocked tiles (nblocked) | small tiles]
+  if (nuvt > 0) {
+    if (bf16)
+      sigma_uvt_kernel<true><<<nuvt, 256, uvt_smem, st>>>(uvt, contribs, wref, V, G, W, Part, ns, uvt_smem, tau0, err);
+    else
+      sigma_uvt_kernel<false><<<nuvt, 256, uvt_smem, st>>>(uvt, contribs, wref, V, G, W, Part, ns, uvt_smem, tau0, err);
+    GWGB_CUDA(cudaGetLastError());
+  }
+  // tiles1 = [blocked tiles (nblocked) | small tiles]: owners with AO blocks above 64
   if (nblocked > 0) {
     sigma_uv_blocked_kernel<<<nblocked, 256, uv_smem, st>>>(tiles1, contribs, wref, V, G, W, Part, ns, uv_smem,
                                                              tau0);
@@ -592,6 +815,8 @@ void set_tc_kernel_attributes(int smem_bytes) {
   GWGB_CUDA(cudaFuncSetAttribute(sigma_w_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(sigma_uv_blocked_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(sigma_uv_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_uvt_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_uvt_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
 }
 
 }  // namespace gwgb
@@ -810,7 +1035,9 @@ __global__ void p0_reduce_kernel(const PrTile *__restrict__ tiles, const double2
   const PrTile tl = tiles[blockIdx.x];
   const int qb = tl.qb, rows = tl.nt * qb;
   const int64_t slice = (int64_t)rows * qb;
-  for (int e = threadIdx.x; e < rows * qb; e += blockDim.x) {
+  // gridDim.y CTAs share a tile (one tau chunk has few tiles); each element sums its
+  // slices in order
+  for (int e = blockIdx.y * blockDim.x + threadIdx.x; e < rows * qb; e += gridDim.y * blockDim.x) {
     const int r = e / qb, Q = e - r * qb;
     double2 acc = make_double2(0.0, 0.0);
     for (int sl = 0; sl < tl.nslice; ++sl) {
@@ -858,7 +1085,7 @@ void launch_p0_tc(bool bf16, const PzTask *ztasks, int nz, int zsmem, const PkTi
     GWGB_CUDA(cudaGetLastError());
   }
   if (nr > 0) {
-    p0_reduce_kernel<<<nr, 256, 0, st>>>(rtiles, Ppart, P0, nts, pref, mirror);
+    p0_reduce_kernel<<<dim3(nr, 4), 256, 0, st>>>(rtiles, Ppart, P0, nts, pref, mirror);
     GWGB_CUDA(cudaGetLastError());
   }
 }

@@ -41,13 +41,38 @@ struct WRef {
   int64_t ld;
 };
 
-// One tau chunk (starting at tau0) of the Sigma stages: the W GEMM tiles, then the
-// FP32 U/Sigma tiles (tiles1 = [nblocked register-blocked | the rest]) writing
-// FP64 partial blocks to Part.
-void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *tiles1,
-                     int ntiles1, const SigContrib *contribs, const WRef *wref, const double2 *V,
-                     const double2 *G, const double2 *P, float2 *W, double2 *Part, int ns, int uv_smem,
-                     int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st);
+// Geometry of sigma_uvt_kernel (U on CUDA cores feeding the Sigma GEMM on
+// tcgen05), shared by the kernel and the host's tile planning: K elements per
+// aux row (2 b2 padded to 4), the W row stride in shared memory (odd: no bank
+// conflicts), m padded to 8, N = 2 b1 padded to 16, K of a chunk of qn aux rows
+// padded to the MMA K step, and the shared memory of such a chunk.
+__host__ __device__ inline int uvt_kq(int b2) { return (2 * b2 + 3) & ~3; }
+__host__ __device__ inline int uvt_wld(int b2) { return b2 | 1; }
+__host__ __device__ inline int uvt_m8(int b2) { return (b2 + 7) & ~7; }
+__host__ __device__ inline int uvt_nsp(int b1) { return (2 * b1 + 15) & ~15; }
+__host__ __device__ inline int uvt_ks(int qn, int kq, bool bf) {
+  const int st = bf ? 16 : 8;
+  return (qn * kq + st - 1) / st * st;
+}
+__host__ __device__ inline int uvt_ws_elems(int qn, int nt, int b1, int b2) {
+  return (nt * qn * b1 * uvt_wld(b2) + 1) & ~1;
+}
+// FP64 accumulator rows (tau, j) x b1 with an odd row stride
+__host__ __device__ inline int uvt_acc_bytes(int nt, int b1) { return 16 * nt * b1 * (b1 | 1); }
+__host__ __device__ inline int64_t uvt_smem(int qn, int nt, int b1, int b2, bool bf) {
+  const int ks = uvt_ks(qn, uvt_kq(b2), bf);
+  return (int64_t)uvt_acc_bytes(nt, b1) + (int64_t)(bf ? 6 : 8) * (128 + uvt_nsp(b1)) * ks +
+         8ll * uvt_ws_elems(qn, nt, b1, b2) + 8ll * nt * b2 * uvt_m8(b2);
+}
+
+// One tau chunk (starting at tau0) of the Sigma stages: the W GEMM tiles, the
+// U/Sigma tiles of owners with AO blocks up to 64 (uvt: U on CUDA cores, Sigma
+// on tcgen05), then the FP32 U/Sigma tiles of larger owners (tiles1 =
+// [nblocked register-blocked | the rest]); all write FP64 partial blocks to Part.
+void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, const float2 *Bcat, const SigTile *uvt,
+                     int nuvt, int uvt_smem, const SigTile *tiles1, int ntiles1, const SigContrib *contribs,
+                     const WRef *wref, const double2 *V, const double2 *G, const double2 *P, float2 *W, double2 *Part,
+                     int ns, int uv_smem, int nblocked, int uv_smem_small, int tau0, int *err, cudaStream_t st);
 
 void launch_bcat(const BcTask *tasks, int ntasks, const double2 *V, float2 *Bcat, cudaStream_t st);
 
