@@ -324,7 +324,7 @@ class Engine {
   double beta_;
   Lay l_;
   cudaStream_t st_ = nullptr;
-  int smem_bytes_ = 0;
+  int smem_bytes_ = 0, sw_cap_ = 0;
   bool have_V_ = false, have_T_ = false, have_F_ = false, have_reps_ = false;
 
   // device data
@@ -493,12 +493,13 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
   int optin = 0;
   GWGB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev_));
   smem_bytes_ = std::min(optin, 200 * 1024);
+  sw_cap_ = optin - 2048;  // the W GEMM kernel: all of it but its static shared memory
   int per_sm = 0;
   GWGB_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev_));
   GWGB_CUDA(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_));
   set_fp64_kernel_attributes(smem_bytes_);
   fp64_smem_ = std::min(smem_bytes_, ((per_sm / 2 - 2048) / 1024) * 1024);  // two CTAs per SM
-  set_tc_kernel_attributes(smem_bytes_);
+  set_tc_kernel_attributes(smem_bytes_, sw_cap_);
   set_tc_p0_kernel_attributes(smem_bytes_);
   GWGB_CUDA(cudaMallocHost(&mu_host_, sizeof(double)));
   // device memory for one tau chunk of each tensor-core operand buffer (W, Zcat):
@@ -1059,20 +1060,23 @@ void Engine::build_work_lists() {
         wr[c] = {woff + ncol, 0};  // W rows are (tau - chunk start, Q)
         ncol += b1b2;
       }
-      for (int c : cs) wr[c].ld = ncol;
+      const int ld = (ncol + 1) & ~1;  // even row stride: 16-byte W stores
+      for (int c : cs) wr[c].ld = ld;
       const int KP = ((2 * qb + 7) / 8) * 8, KP16 = ((2 * qb + 15) / 16) * 16;
       // shared memory: TF32x3 2 planes x 4 B, BF16x3 3 planes x 2 B (K padded to 16)
-      auto need = [&](int npk) { return std::max(KP * (1024 + 32 * npk), KP16 * (768 + 24 * npk)); };
+      // (+ 18432 B of drain tiles: 4 warps x 32 rows x 36 floats)
+      auto need = [&](int npk) { return 18432 + std::max(KP * (1024 + 32 * npk), KP16 * (768 + 24 * npk)); };
       int npk = 64;
-      while (npk > 16 && need(npk) > 200 * 1024) npk /= 2;
-      GWGB_REQUIRE(need(npk) <= 200 * 1024, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 Sigma kernel");
+      while (npk > 16 && need(npk) > sw_cap_) npk /= 2;
+      GWGB_REQUIRE(need(npk) <= sw_cap_, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 Sigma kernel");
       wsmem = std::max(wsmem, need(npk));
       const int nt = std::max(1, std::min(tch_w_, 128 / qb));
       for (const SigChunk &ch : sig_chunks_)
         for (int t0 = ch.t0; t0 < ch.t1; t0 += nt)
-          swt.push_back({pa, boff, woff, pstride, qb, t0, std::min(nt, ch.t1 - t0), ncol, KP, npk, pconj, 0, ncol});
+          swt.push_back({pa, boff, woff, pstride, qb, t0, std::min(nt, ch.t1 - t0), ncol, KP, npk, pconj, 0, ncol,
+                         ld, 0});
       boff += (int64_t)ncol * qb;
-      woff += (int64_t)tch_w_ * qb * ncol;
+      woff += (int64_t)tch_w_ * qb * ld;
     }
     int uvneed_small = 0;
     // the U/Sigma stage keeps large Q chunks (one CTA per SM measured faster than two
@@ -1126,7 +1130,9 @@ void Engine::build_work_lists() {
     }
     for (const SwTile &t : swt) {
       const int t0c = (t.t0 / tch_w_) * tch_w_;  // chunk start
-      check_range(t.wcat, (int64_t)(t.t0 - t0c + t.nt) * t.qb * t.ncol, woff, "W rows");
+      check_range(t.wcat, (int64_t)(t.t0 - t0c + t.nt) * t.qb * t.ld, woff, "W rows");
+      GWGB_REQUIRE(t.ld >= t.ncol && (t.ld & 1) == 0 && (t.wcat & 1) == 0 && (t.c0 & 1) == 0, GWGB_E_INVALID,
+                   "internal work list out of bounds: W row alignment");
       GWGB_REQUIRE(0 <= t.c0 && t.c0 < t.c1 && t.c1 <= t.ncol, GWGB_E_INVALID,
                    "internal work list out of bounds: W column range");
       check_range(t.bcat, (int64_t)t.ncol * t.qb, boff, "conj(V) operand");

@@ -115,12 +115,24 @@ struct Planes {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// (1): one CTA = 128 rows (tau, Q) of one aux block x all its columns.  A is
-// staged once; B packs of npk complex columns are double-buffered against two
-// TMEM accumulators (MMA of pack i+1 overlaps the drain of pack i).
-// Shared: A planes (128 x K) | B buffer 0 planes (2 npk x K) | buffer 1 planes;
-// K = 2 q_b padded to the MMA K step.
+// (1): one CTA = 128 rows (tau, Q) of one aux block x a range of its columns
+// in packs of npk complex columns.  A is staged once by all threads; then the
+// warps specialise into a pipeline over the packs:
+//   warps 5-7  stage B packs into a ring of two buffers   (full[b] / empty[b])
+//   warp 4     one lane issues the MMAs of a pack into one of two TMEM
+//              accumulators                               (done[a] / afree[a])
+//   warps 0-3  drain an accumulator (TMEM lanes = rows) through a per-warp
+//              shared tile of 32 rows x 16 complex, written out as whole
+//              128-byte row segments (coalesced)
+// so staging, MMAs and the W stores of consecutive packs overlap.  Every wait
+// is bounded; a wait that runs out sets the error word and an abort flag that
+// ends the other roles' loops, and the TMEM is released only after the MMAs
+// issued so far have completed (bounded wait).
+// Shared: A planes (128 x K) | B buffer 0 planes (2 npk x K) | buffer 1 planes |
+// drain tiles [4][32][36] floats; K = 2 q_b padded to the MMA K step.
 // ---------------------------------------------------------------------------
+constexpr int SW_DRAIN_LD = 36;  // floats per row of a drain tile (32 + 4: spreads the banks)
+static_assert(4 * 32 * SW_DRAIN_LD * 4 == 18432, "the host sizes the drain tiles as 18432 bytes");
 template <bool BF>
 __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restrict__ tiles,
                                                          const float2 *__restrict__ Bcat,
@@ -129,7 +141,8 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
   using PL = Planes<BF>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ uint32_t tmem_slot;
-  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ __align__(8) uint64_t bar[9];  // full[2] | empty[2] | done[2] | afree[2] | last
+  __shared__ int abort_flag, issued;
   const SwTile tl = tiles[blockIdx.x];
   const int qb = tl.qb;
   const int KP = BF ? ((tl.kp + 15) & ~15) : tl.kp;
@@ -138,10 +151,19 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
   const uint32_t apl = 128u * KP * PL::EB, bpl = (uint32_t)BR * KP * PL::EB;  // plane bytes
   unsigned char *A = smem_raw;
   unsigned char *Bb = A + PL::N * apl;  // 2 buffers x N planes
+  uint64_t *full = bar, *empty = bar + 2, *done = bar + 4, *afree = bar + 6, *last = bar + 8;
+  constexpr int NPROD = 96;  // producer threads (warps 5-7)
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 256);
   if (tid == 0) {
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&full[b], NPROD);
+      tc::mbar_init(&empty[b], 1);
+      tc::mbar_init(&done[b], 1);
+      tc::mbar_init(&afree[b], 128);
+    }
+    tc::mbar_init(last, 1);
+    abort_flag = 0;
+    issued = 0;
   }
   const int rows = tl.nt * qb;
   // A: rows (tau, Q) of P(tau), K = (P, re/im); every row is qb contiguous complex.
@@ -161,82 +183,134 @@ __global__ void __launch_bounds__(256) sigma_w_tc_kernel(const SwTile *__restric
     }
     PL::store4(A, apl, PL::off(r, 4 * q, KP), make_float4((float)v0.x, (float)v0.y, (float)v1.x, (float)v1.y));
   }
-  const int npacks = (tl.c1 - tl.c0 + SW_PACK - 1) / SW_PACK;
-  auto stage_b = [&](int pk) {
-    unsigned char *B = Bb + (pk & 1) * PL::N * bpl;
-    const int c0 = tl.c0 + pk * SW_PACK;
-    // rows (col, d) of the real embedding of B = conj(V): d=0 -> (Br, -Bi), d=1 -> (Bi, Br), Br = Vr, Bi = -Vi;
-    // a lane writes one K quad (two complex) of both rows of one column
-    for (int e = tid; e < SW_PACK * nq; e += 256) {
-      const int cll = e & 3, rest = e >> 2;
-      const int q = rest % nq, cl = (rest / nq) * 4 + cll;
-      const int col = c0 + cl;
-      float2 b0 = make_float2(0.f, 0.f), b1 = b0;  // conj(V) as stored
-      if (col < tl.c1) {
-        const float2 *bc = Bcat + tl.bcat + (int64_t)col * qb;
-        if (2 * q < qb) b0 = bc[2 * q];
-        if (2 * q + 1 < qb) b1 = bc[2 * q + 1];
-      }
-      PL::store4(B, bpl, PL::off(2 * cl, 4 * q, KP), make_float4(b0.x, -b0.y, b1.x, -b1.y));
-      PL::store4(B, bpl, PL::off(2 * cl + 1, 4 * q, KP), make_float4(b0.y, b0.x, b1.y, b1.x));
-    }
-  };
-  const uint32_t idesc = PL::idesc(128, 2 * SW_PACK);
-  const uint32_t sbo = PL::sbo(KP);
-  auto issue = [&](int pk, uint32_t tmem) {
-    const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(Bb + (pk & 1) * PL::N * bpl);
-    const uint32_t d = tmem + (uint32_t)((pk & 1) * 2 * SW_PACK);
-    for (int st = 0; st < KP / PL::KSTEP; ++st)
-      PL::mma_step(d, a, apl, b, bpl, (uint32_t)st * 256, sbo, sbo, idesc, st > 0);
-    tc::commit(&mbar[pk & 1]);
-  };
-  if (npacks > 0) stage_b(0);
   tc::fence_async_smem();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
-  if (tid == 0 && npacks > 0) issue(0, tmem);
-  uint32_t ph[2] = {0u, 0u};
-  bool ok = true;
-  const int r = (warp & 3) * 32 + lane;  // warps 0-3 drain (TMEM lanes), warps 4-7 only stage
-  const bool live = warp < 4 && r < rows;
-  const int it = live ? r / qb : 0, Q = live ? r - (r / qb) * qb : 0;
-  float2 *wrow = W + tl.wcat + ((int64_t)(tl.t0 - tau0 + it) * qb + Q) * tl.ncol;  // W holds one tau chunk
-  for (int pk = 0; pk < npacks && ok; ++pk) {
-    if (pk + 1 < npacks) stage_b(pk + 1);  // buffer (pk+1)&1 was read by MMA pk-1, already complete
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0 && pk + 1 < npacks) issue(pk + 1, tmem);
-    bool done = tc::mbar_wait(&mbar[pk & 1], ph[pk & 1]);
-    if (done) ph[pk & 1] ^= 1u;  // a phase that timed out is waited for again below
-    if (!done && lane == 0) atomicExch(err, 1);
-    ok = __syncthreads_and(done);
-    tc::fence_after_sync();
-    if (ok && warp < 4) {
-      const uint32_t acc = tmem + (uint32_t)((pk & 1) * 2 * SW_PACK) + ((uint32_t)(warp * 32) << 16);
+  const int npacks = (tl.c1 - tl.c0 + SW_PACK - 1) / SW_PACK;
+  // bounded wait; false when it ran out (error word and abort flag set) or another role aborted
+  auto bwait = [&](uint64_t *b, uint32_t par) -> bool {
+    for (int rep = 0; rep < 64; ++rep) {
+      if (tc::mbar_wait(b, par, 65536)) return true;
+      if (*(volatile int *)&abort_flag) return false;
+    }
+    atomicExch(err, 1);
+    *(volatile int *)&abort_flag = 1;
+    return false;
+  };
+  if (warp >= 5) {
+    // producers: rows (col, d) of the real embedding of B = conj(V): d=0 -> (Br, -Bi),
+    // d=1 -> (Bi, Br), Br = Vr, Bi = -Vi; a thread writes one K quad (two complex) of
+    // both rows of one column
+    const int ptid = tid - (256 - NPROD);
+    for (int pk = 0; pk < npacks; ++pk) {
+      const int b = pk & 1;
+      if (pk >= 2 && !bwait(&empty[b], ((pk >> 1) - 1) & 1)) break;
+      unsigned char *B = Bb + b * PL::N * bpl;
       const int c0 = tl.c0 + pk * SW_PACK;
-      for (int j0 = 0; j0 < 2 * SW_PACK; j0 += 8) {
-        float v[8];
-        tc::tmem_ld8(acc + (uint32_t)j0, v);
-        if (live) {
+      // batches of 8 items: their 16 loads are in flight together (the pack comes
+      // from HBM; one load at a time per thread left the producers latency-bound)
+      constexpr int BU = 8;
+      for (int e0 = ptid; e0 < SW_PACK * nq; e0 += BU * NPROD) {
+        float2 b0[BU], b1[BU];  // conj(V) as stored
 #pragma unroll
-          for (int j = 0; j < 8; j += 2) {
-            const int col = c0 + ((j0 + j) >> 1);
-            if (col < tl.c1) wrow[col] = make_float2(v[j], v[j + 1]);
+        for (int u = 0; u < BU; ++u) {
+          const int e = e0 + u * NPROD;
+          const int cll = e & 3, rest = e >> 2;
+          const int q = rest % nq, col = c0 + (rest / nq) * 4 + cll;
+          b0[u] = b1[u] = make_float2(0.f, 0.f);
+          if (e < SW_PACK * nq && col < tl.c1) {
+            const float2 *bc = Bcat + tl.bcat + (int64_t)col * qb;
+            if (2 * q < qb) b0[u] = __ldg(bc + 2 * q);
+            if (2 * q + 1 < qb) b1[u] = __ldg(bc + 2 * q + 1);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < BU; ++u) {
+          const int e = e0 + u * NPROD;
+          if (e < SW_PACK * nq) {
+            const int cll = e & 3, rest = e >> 2;
+            const int q = rest % nq, cl = (rest / nq) * 4 + cll;
+            PL::store4(B, bpl, PL::off(2 * cl, 4 * q, KP), make_float4(b0[u].x, -b0[u].y, b1[u].x, -b1[u].y));
+            PL::store4(B, bpl, PL::off(2 * cl + 1, 4 * q, KP), make_float4(b0[u].y, b0[u].x, b1[u].y, b1[u].x));
           }
         }
       }
+      tc::fence_async_smem();
+      tc::mbar_arrive(&full[b]);
     }
-    tc::fence_before_sync();
-    __syncthreads();  // accumulator pk&1 drained before MMA pk+2 reuses it
-    tc::fence_after_sync();
+  } else if (warp == 4) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idesc = PL::idesc(128, 2 * SW_PACK);
+      const uint32_t sbo = PL::sbo(KP);
+      int n = 0;
+      for (int pk = 0; pk < npacks; ++pk) {
+        const int b = pk & 1;
+        if (!bwait(&full[b], (pk >> 1) & 1)) break;
+        if (pk >= 2 && !bwait(&afree[b], ((pk >> 1) - 1) & 1)) break;
+        tc::fence_after_sync();
+        const uint32_t a = tc::smem_u32(A), bb = tc::smem_u32(Bb + b * PL::N * bpl);
+        const uint32_t d = tmem + (uint32_t)(b * 2 * SW_PACK);
+        for (int st = 0; st < KP / PL::KSTEP; ++st)
+          PL::mma_step(d, a, apl, bb, bpl, (uint32_t)st * 256, sbo, sbo, idesc, st > 0);
+        tc::commit(&empty[b]);
+        tc::commit(&done[b]);
+        ++n;
+      }
+      if (n > 0) tc::commit(last);  // arrives when every MMA issued above has completed
+      issued = n;
+    }
+    __syncwarp();
+  } else {
+    // drain: warp w owns TMEM lanes (rows) 32 w .. 32 w + 31; a lane reads its row's
+    // 16 complex columns into the warp's tile, then 8 lanes write one row's 128 bytes
+    float *tile = reinterpret_cast<float *>(Bb + 2 * PL::N * bpl) + warp * 32 * SW_DRAIN_LD;
+    const int seg = lane & 7, rsub = lane >> 3;
+    for (int pk = 0; pk < npacks; ++pk) {
+      const int a = pk & 1;
+      const bool okw = __all_sync(0xffffffffu, bwait(&done[a], (pk >> 1) & 1));
+      if (!okw) break;
+      tc::fence_after_sync();
+      const uint32_t acc = tmem + (uint32_t)(a * 2 * SW_PACK) + ((uint32_t)(warp * 32) << 16);
+      const int c0 = tl.c0 + pk * SW_PACK;
+      for (int j0 = 0; j0 < 2 * SW_PACK; j0 += 32) {
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          float v[8];
+          tc::tmem_ld8(acc + (uint32_t)(j0 + 8 * h), v);
+          float4 *t = reinterpret_cast<float4 *>(tile + lane * SW_DRAIN_LD + 8 * h);
+          t[0] = make_float4(v[0], v[1], v[2], v[3]);
+          t[1] = make_float4(v[4], v[5], v[6], v[7]);
+        }
+        __syncwarp();
+        const int col = c0 + (j0 >> 1) + 2 * seg;  // even: packs start at even columns, ld is even
+#pragma unroll
+        for (int rr = 0; rr < 32; rr += 4) {
+          const int rl = rr + rsub, r = warp * 32 + rl;
+          if (r < rows) {
+            const int it = r / qb, Q = r - it * qb;
+            float2 *wrow = W + tl.wcat + ((int64_t)(tl.t0 - tau0 + it) * qb + Q) * tl.ld;  // one tau chunk
+            const float4 x = *reinterpret_cast<const float4 *>(tile + rl * SW_DRAIN_LD + 4 * seg);
+            if (col + 1 < tl.c1) *reinterpret_cast<float4 *>(wrow + col) = x;
+            else if (col < tl.c1) wrow[col] = make_float2(x.x, x.y);
+          }
+        }
+        __syncwarp();
+      }
+      tc::fence_before_sync();
+      tc::mbar_arrive(&afree[a]);
+    }
   }
-  if (!ok) {  // let MMAs still in flight finish before the TMEM is released (bounded)
-    if (npacks > 0) tc::mbar_wait(&mbar[0], ph[0], 100000);
-    if (npacks > 1) tc::mbar_wait(&mbar[1], ph[1], 100000);
+  __syncthreads();
+  if (tid == 0) {  // every commit's arrive has landed (and every MMA completed) before the CTA ends
+    const int n = issued;
+    for (int b = 0; b < 2 && b < n; ++b) {
+      const int pl = ((n - 1 - b) >> 1) * 2 + b;  // the last pack that used buffer / accumulator b
+      tc::mbar_wait(&empty[b], (uint32_t)(pl >> 1) & 1u, 4000000);
+      tc::mbar_wait(&done[b], (uint32_t)(pl >> 1) & 1u, 4000000);
+    }
+    if (n > 0) tc::mbar_wait(last, 0u, 4000000);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -581,6 +655,48 @@ __global__ void __launch_bounds__(256) sigma_uv_small_kernel(const SigTile *__re
 // W [nt][qn][b1][b2|1] | G2^T [nt][b2][m8] (float2), ks = qn * kq padded to the
 // MMA K step, kq = 2 b2 padded to 4, m8 = b2 padded to 8.
 // ---------------------------------------------------------------------------
+// U stage of sigma_uvt_kernel: U[(tau, Q, j)][m] = sum_n W[(tau, Q, j)][n] G2^T[tau][n][m]
+// for MB consecutive m per thread, written split into the A planes at
+// row tau*b1 + j, K = Q*kq + 2m (+1 for the imaginary part).
+template <bool BF, int MB>
+__device__ __forceinline__ void uvt_u_phase(int tid, int nrow, int qn, int b1, int b2, int m8, int kq, int ks,
+                                            const float2 *Ws, int wld, const float2 *G2t, unsigned char *A,
+                                            uint32_t apl) {
+  using PL = Planes<BF>;
+  const int mc_n = (MB == 8) ? (m8 >> 3) : (((b2 + 3) & ~3) >> 2);
+  for (int item = tid; item < mc_n * nrow; item += 256) {
+    const int mc = item / nrow, row = item - mc * nrow;
+    const int it = row / (qn * b1), Q = (row / b1) % qn, j = row % b1;
+    const float2 *w = Ws + row * wld;
+    const float4 *g = reinterpret_cast<const float4 *>(G2t + it * b2 * m8 + MB * mc);
+    float ur[MB], ui[MB];
+#pragma unroll
+    for (int x = 0; x < MB; ++x) ur[x] = ui[x] = 0.f;
+    for (int n = 0; n < b2; ++n) {
+      const float2 wv = w[n];
+      const float4 *gn = g + n * (m8 >> 1);
+#pragma unroll
+      for (int h = 0; h < MB / 2; ++h) {
+        const float4 gg = gn[h];
+        ur[2 * h] = fmaf(wv.x, gg.x, ur[2 * h]);
+        ur[2 * h] = fmaf(-wv.y, gg.y, ur[2 * h]);
+        ui[2 * h] = fmaf(wv.x, gg.y, ui[2 * h]);
+        ui[2 * h] = fmaf(wv.y, gg.x, ui[2 * h]);
+        ur[2 * h + 1] = fmaf(wv.x, gg.z, ur[2 * h + 1]);
+        ur[2 * h + 1] = fmaf(-wv.y, gg.w, ur[2 * h + 1]);
+        ui[2 * h + 1] = fmaf(wv.x, gg.w, ui[2 * h + 1]);
+        ui[2 * h + 1] = fmaf(wv.y, gg.z, ui[2 * h + 1]);
+      }
+    }
+    const int ra = it * b1 + j, kend = (Q + 1) * kq;
+#pragma unroll
+    for (int h = 0; h < MB / 2; ++h) {
+      const int k = Q * kq + 2 * MB * mc + 4 * h;
+      if (k < kend) PL::store4(A, apl, PL::off(ra, k, ks), make_float4(ur[2 * h], ui[2 * h], ur[2 * h + 1], ui[2 * h + 1]));
+    }
+  }
+}
+
 template <bool BF>
 __global__ void __launch_bounds__(256) sigma_uvt_kernel(const SigTile *__restrict__ tiles,
                                                         const SigContrib *__restrict__ contribs,
@@ -664,14 +780,18 @@ __global__ void __launch_bounds__(256) sigma_uvt_kernel(const SigTile *__restric
     const double2 *Vb = V + cb.v;
     const WRef wr = wref[c];
     // G2^T for every tau of the range (no MMA of this CTA is in flight here)
-    for (int e = tid; e < nt * b2 * m8; e += 256) {
-      const int it = e / (b2 * m8), r = e - it * (b2 * m8), n = r / m8, m = r - n * m8;
-      float2 g = make_float2(0.f, 0.f);
-      if (m < b2) {
-        const double2 v = __ldg(G + cb.gb + ((int64_t)(tile.t0 + it) * ns + s) * cb.sb + m * b2 + n);
-        g = make_float2((float)v.x, (float)v.y);
+    for (int e0 = tid; e0 < nt * b2 * m8; e0 += 4 * 256) {  // 4 loads in flight per thread
+      double2 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = e0 + u * 256;
+        const int it = e / (b2 * m8), r = e - it * (b2 * m8), n = r / m8, m = r - n * m8;
+        v[u] = make_double2(0.0, 0.0);
+        if (e < nt * b2 * m8 && m < b2) v[u] = __ldg(G + cb.gb + ((int64_t)(tile.t0 + it) * ns + s) * cb.sb + m * b2 + n);
       }
-      G2t[e] = g;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (e0 + u * 256 < nt * b2 * m8) G2t[e0 + u * 256] = make_float2((float)v[u].x, (float)v[u].y);
     }
     for (int q0 = 0; q0 < qb; q0 += qc) {
       const int qn = min(qc, qb - q0);
@@ -681,10 +801,27 @@ __global__ void __launch_bounds__(256) sigma_uvt_kernel(const SigTile *__restric
       // contribution they are loaded while the previous chunk's MMAs run (the MMAs
       // read only A and Bv)
       const int wrow = b1 * b2;
-      auto stage_w = [&]() {
-        for (int e = tid; e < nt * qn * wrow; e += 256) {
-          const int r = e / wrow, x = e - r * wrow, it = r / qn, Q = r - it * qn, j = x / b2, n = x - j * b2;
-          Ws[(r * b1 + j) * wld + n] = W[wr.base + ((int64_t)(tile.t0 + it - tau0) * qb + q0 + Q) * wr.ld + x];
+      auto stage_w = [&]() {  // batches of 8 loads in flight per thread
+        constexpr int BU = 8;
+        const int total = nt * qn * wrow;
+        for (int e0 = tid; e0 < total; e0 += BU * 256) {
+          float2 w[BU];
+#pragma unroll
+          for (int u = 0; u < BU; ++u) {
+            const int e = e0 + u * 256;
+            if (e < total) {
+              const int r = e / wrow, x = e - r * wrow, it = r / qn, Q = r - it * qn;
+              w[u] = W[wr.base + ((int64_t)(tile.t0 + it - tau0) * qb + q0 + Q) * wr.ld + x];
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < BU; ++u) {
+            const int e = e0 + u * 256;
+            if (e < total) {
+              const int r = e / wrow, x = e - r * wrow, j = x / b2, n = x - j * b2;
+              Ws[(r * b1 + j) * wld + n] = w[u];
+            }
+          }
         }
       };
       const bool early = pending;
@@ -721,39 +858,12 @@ __global__ void __launch_bounds__(256) sigma_uvt_kernel(const SigTile *__restric
         PL::store4(A, apl, PL::off(r, k, ks), z4);
       }
       __syncthreads();
-      // U, 8 m per thread; lanes of a warp share m (G2 reads are broadcasts)
-      const int nrow = nt * qn * b1, mc_n = m8 >> 3;
-      for (int item = tid; item < mc_n * nrow; item += 256) {
-        const int mc = item / nrow, row = item - mc * nrow;
-        const int it = row / (qn * b1), Q = (row / b1) % qn, j = row % b1;
-        const float2 *w = Ws + row * wld;
-        const float4 *g = reinterpret_cast<const float4 *>(G2t + it * b2 * m8 + 8 * mc);
-        float ur[8], ui[8];
-#pragma unroll
-        for (int x = 0; x < 8; ++x) ur[x] = ui[x] = 0.f;
-        for (int n = 0; n < b2; ++n) {
-          const float2 wv = w[n];
-          const float4 *gn = g + n * (m8 >> 1);
-#pragma unroll
-          for (int h = 0; h < 4; ++h) {
-            const float4 gg = gn[h];
-            ur[2 * h] = fmaf(wv.x, gg.x, ur[2 * h]);
-            ur[2 * h] = fmaf(-wv.y, gg.y, ur[2 * h]);
-            ui[2 * h] = fmaf(wv.x, gg.y, ui[2 * h]);
-            ui[2 * h] = fmaf(wv.y, gg.x, ui[2 * h]);
-            ur[2 * h + 1] = fmaf(wv.x, gg.z, ur[2 * h + 1]);
-            ur[2 * h + 1] = fmaf(-wv.y, gg.w, ur[2 * h + 1]);
-            ui[2 * h + 1] = fmaf(wv.x, gg.w, ui[2 * h + 1]);
-            ui[2 * h + 1] = fmaf(wv.y, gg.z, ui[2 * h + 1]);
-          }
-        }
-        const int ra = it * b1 + j, kend = (Q + 1) * kq;
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          const int k = Q * kq + 16 * mc + 4 * h;
-          if (k < kend) PL::store4(A, apl, PL::off(ra, k, ks), make_float4(ur[2 * h], ui[2 * h], ur[2 * h + 1], ui[2 * h + 1]));
-        }
-      }
+      // U, MB m per thread (4 when b2 padded to 4 is shorter than padded to 8);
+      // lanes of a warp share m (G2 reads are broadcasts)
+      if (((b2 + 3) & ~3) < m8)
+        uvt_u_phase<BF, 4>(tid, nt * qn * b1, qn, b1, b2, m8, kq, ks, Ws, wld, G2t, A, apl);
+      else
+        uvt_u_phase<BF, 8>(tid, nt * qn * b1, qn, b1, b2, m8, kq, ks, Ws, wld, G2t, A, apl);
       tc::fence_async_smem();
       tc::fence_before_sync();
       __syncthreads();
@@ -810,9 +920,9 @@ void launch_sigma_tc(bool bf16, const SwTile *wtiles, int nwtiles, int wsmem, co
   }
 }
 
-void set_tc_kernel_attributes(int smem_bytes) {
-  GWGB_CUDA(cudaFuncSetAttribute(sigma_w_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
-  GWGB_CUDA(cudaFuncSetAttribute(sigma_w_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+void set_tc_kernel_attributes(int smem_bytes, int sw_smem_bytes) {
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_w_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sw_smem_bytes));
+  GWGB_CUDA(cudaFuncSetAttribute(sigma_w_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sw_smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(sigma_uv_blocked_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(sigma_uv_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(sigma_uvt_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));

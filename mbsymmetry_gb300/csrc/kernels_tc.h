@@ -22,6 +22,8 @@ struct SwTile {
   int32_t npk;      // complex columns per pack (16, 32 or 64)
   int32_t pconj;    // A = conj(P~(q')) (time-reversal partner)
   int32_t c0, c1;   // the columns [c0, c1) this CTA computes
+  int32_t ld;       // W row stride (ncol rounded up to even: 16-byte stores)
+  int32_t pad;
 };
 
 // Bcat entries: one per Sigma contribution.
@@ -31,7 +33,8 @@ struct BcTask {
   int32_t qb, b1b2, col0, pad;
 };
 
-void set_tc_kernel_attributes(int smem_bytes);
+// sw_smem_bytes: the W GEMM kernel (up to the device's opt-in limit)
+void set_tc_kernel_attributes(int smem_bytes, int sw_smem_bytes);
 void set_tc_p0_kernel_attributes(int smem_bytes);
 
 // W reference of one Sigma contribution:

@@ -71,6 +71,11 @@ __device__ __forceinline__ void commit(uint64_t *mbar) {
       smem_u32(mbar)));
 }
 
+// Plain arrive (release, CTA scope) of this thread on the mbarrier.
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
 // Bounded wait for the mbarrier phase `parity`; returns false when the limit ran out.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, int limit = 4000000) {
   uint32_t done = 0;
