@@ -267,7 +267,7 @@ def run_gpu(args):
     # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the same
     # kernel on this workload, from the ncu capture summarised in
     # profiles/c2_contraction_kernels.md; the kernels are FP64-pipe bound.
-    traffic = {"sigma": 1.390e9, "p0": 0.0565e9}[dom]
+    traffic = {"sigma": 0.0703e9, "p0": 0.0563e9}[dom]
     roofline = {"bound": "tensor", "kernel": f"{dom}_fp64_kernel", "achieved": achieved, "peak": fp64_peak,
                 "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": traffic,
                 "traffic_unit": "bytes per launch (ncu)",
