@@ -312,6 +312,25 @@ def run_gpu(args):
     mixed_bf16 = run_mixed("bf16x3", "bf16x3 (tcgen05 kind::f16, 3 BF16 planes, 6 products, FP32 accumulate per "
                                      "contribution, FP64 across)")
 
+    # ---- the reference's cuBLAS call sequence on this GPU (measurement only) --
+    # G rotation + per-pair strided-batched ZGEMM chains of P0 and Sigma, 16
+    # streams, 4 tau per batch (the reference's nqkpt streams and test nt_batch);
+    # P0 from G0, Sigma from G0 and the FP64 P~ of the same solve.
+    s.set_G(G0)
+    s.solve()
+    s.refproxy(nt_batch=4, nstreams=16)  # warm-up: cuBLAS handle and kernel loading
+    px = s.refproxy(nt_batch=4, nstreams=16)
+    _, sig_px = s.refproxy_results()
+    px_s = (px["p0_ms"] + px["sigma_ms"]) / 1e3
+    proxy = {"what": "SymmetryMBPT's cuBLAS call sequence (cugw_routines_block.cu, cugw_qkpt_block.cu) replayed "
+                     "on this GPU: G rotation, per-pair V transposes and ZGEMM_SB chains of P0 and Sigma; "
+                     "V resident in HBM, per-stream accumulators instead of locks",
+             "nt_batch": 4, "streams": 16, "p0_s": px["p0_ms"] / 1e3, "sigma_s": px["sigma_ms"] / 1e3,
+             "contractions_s": px_s, "gemm_calls": int(px["gemm_calls"]), "other_calls": int(px["other_calls"]),
+             "sigma_max_abs_diff_vs_fp64_kernels": float(np.abs(sig_px - sig64).max()),
+             "speedup_fp64_kernels": px_s / ((stages["p0_ms"] + stages["sigma_ms"]) / 1e3),
+             "speedup_tf32x3_kernels": px_s / ((mixed["stages_ms"]["p0_ms"] + mixed["stages_ms"]["sigma_ms"]) / 1e3)}
+
     # replicas: every rank runs the whole iteration, so the job completes `world`
     # iterations per max-over-ranks time
     # ---- self-consistent loop: 10 graph-launched iterations, alpha = 0.5 ----
@@ -352,6 +371,7 @@ def run_gpu(args):
         "clocks": clocks.summary(),
         "mixed": mixed,
         "mixed_bf16x3": mixed_bf16,
+        "reference_gpu_proxy": proxy,
         "sc_loop": sc,
         "peaks": {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops"),
                   "fp64_tflops_measured": fp64_peak},

@@ -203,6 +203,33 @@ int gwgb_get_stats(gwgb_handle h, gwgb_stats *out);
 /* Block until all work of the handle is done. */
 int gwgb_synchronize(gwgb_handle h);
 
+/* ---- reference-GPU proxy (measurement only, not on the drop-in path) ----
+ * Replays the reference's cuBLAS call sequence for the two contractions of one
+ * GW iteration on this GPU, for the comparison "reference call sequence vs
+ * these kernels" on the same hardware: the G rotation and G(-tau) copies
+ * (SymmetryMBPT/src/cuda/cugw_routines_block.cu:164-199), per (q_irr, k) pair
+ * the V transposes and the three strided-batched ZGEMMs of P0 per V block and
+ * tau batch (cugw_qkpt_block.cu:119-130, 195-284), per (k_irr, q) pair the P~
+ * rotation, the V conj-transposes and the three ZGEMMs of Sigma
+ * (cugw_qkpt_block.cu:140-192, 288-436), round-robin over nstreams streams
+ * (the reference's nqkpt streams), nt_batch tau per batch (its nt_batch).
+ * V stays in HBM and the per-pair accumulation locks become per-stream
+ * accumulators (both in the reference's favour).  P0 is computed from the
+ * handle's G, Sigma from its G and its P~ (the state after gwgb_solve).
+ * cuBLAS is loaded when this runs (GWGB_E_UNSUPPORTED if it cannot be). */
+typedef struct gwgb_proxy_stats {
+  double p0_ms;        /* G set-up + P0 pair loop, CUDA events */
+  double sigma_ms;     /* P~ rotation + Sigma pair loop */
+  int64_t gemm_calls;  /* cuBLAS ZGEMM_SB calls */
+  int64_t other_calls; /* GEAM, SCAL, AXPY, memset and D2D copy calls */
+} gwgb_proxy_stats;
+
+int gwgb_refproxy_run(gwgb_handle h, int32_t nt_batch, int32_t nstreams, gwgb_proxy_stats *out);
+
+/* The proxy's P0 ([q_irr][t][qslice], t < nts/2) and Sigma ([t][s][flat_ao]);
+ * either pointer may be NULL. */
+int gwgb_refproxy_get(gwgb_handle h, double *P0, double *Sigma);
+
 /* ---- self-consistent loop ----------------------------------------------
  * No counterpart in the reference: sc_loop_block_t keeps mu fixed
  * (sc_loop_block_t.h:25), never assigns its energy (:123), does not mix and

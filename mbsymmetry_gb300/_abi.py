@@ -60,6 +60,10 @@ class GwgbStats(ctypes.Structure):
     ]
 
 
+class GwgbProxyStats(ctypes.Structure):
+    _fields_ = [("p0_ms", c_double), ("sigma_ms", c_double), ("gemm_calls", c_int64), ("other_calls", c_int64)]
+
+
 class GwgbMuSearch(ctypes.Structure):
     _fields_ = [
         ("n_electrons", c_double), ("mu0", c_double), ("step", c_double), ("tol", c_double),
@@ -100,6 +104,8 @@ SIGNATURES = {
     "gwgb_iteration": (c_int32, [c_void_p, c_double]),
     "gwgb_get_stats": (c_int32, [c_void_p, POINTER(GwgbStats)]),
     "gwgb_synchronize": (c_int32, [c_void_p]),
+    "gwgb_refproxy_run": (c_int32, [c_void_p, c_int32, c_int32, POINTER(GwgbProxyStats)]),
+    "gwgb_refproxy_get": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "gwgb_set_hcore": (c_int32, [c_void_p, c_void_p]),
     "gwgb_set_energy_matrix": (c_int32, [c_void_p, c_void_p, c_int32]),
     "gwgb_find_mu": (c_int32, [c_void_p, POINTER(GwgbMuSearch), POINTER(c_double), POINTER(c_double)]),

@@ -305,6 +305,8 @@ class Engine {
   void find_mu(const gwgb_mu_search &ms, double *mu_out, double *n_out);
   void energy(double *e_corr, double *e_one);
   void sc_loop(int niter, double alpha, const gwgb_mu_search &ms, int final_fp64, gwgb_sc_record *out);
+  void refproxy(int nt_batch, int nstreams, gwgb_proxy_stats *out);
+  void refproxy_get(double *P0, double *S);
   void stats(gwgb_stats *out) const {
     *out = stats_;
     out->device_bytes = g_device_bytes.load();
@@ -326,6 +328,8 @@ class Engine {
   cudaStream_t st_ = nullptr;
   int smem_bytes_ = 0, sw_cap_ = 0;
   bool have_V_ = false, have_T_ = false, have_F_ = false, have_reps_ = false;
+  DBuf<double2> px_p0_, px_sig_;  // results of the reference-GPU proxy
+  bool px_ready_ = false;
 
   // device data
   DBuf<double2> V_, Gall_, Pall_, Sig_, Pw_, Ww_, F_, S_, orep_, auxrep_;
@@ -552,7 +556,7 @@ Engine::~Engine() {
   Wg_.free(); Gb_.free(); Sold_.free(); Hc_.free(); Me_.free(); Hm_.free();
   mus_.free(); recs_.free(); counter_.free(); tr_tasks_.free(); slab_e_.free();
   if (mu_host_) cudaFreeHost(mu_host_);
-  DBuf<double2> *bufs[] = {&V_, &Gall_, &Pall_, &Sig_, &Pw_, &Ww_, &F_, &S_, &orep_, &auxrep_,
+  DBuf<double2> *bufs[] = {&V_, &Gall_, &Pall_, &Sig_, &Pw_, &Ww_, &F_, &S_, &orep_, &auxrep_, &px_p0_, &px_sig_,
                            &Tnt_, &Ttn_, &TntBF_, &TtnFB_};
   sw_tiles_.free(); bc_tasks_.free(); sig_wref_.free(); Wbuf_.free(); Bcat_.free(); uv_red_.free();
   pz_tasks_.free(); vc_tasks_.free(); pk_tiles_.free(); pr_tiles_.free(); Zbuf_.free(); Vcat_.free(); Ppart_.free();
@@ -1767,6 +1771,8 @@ void Engine::sc_loop(int niter, double alpha, const gwgb_mu_search &ms, int fina
 
 }  // namespace gwgb
 
+#include "refproxy.cuh"
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
@@ -1878,6 +1884,9 @@ int gwgb_test_wait_timeout(int32_t device, int32_t polls) {
 }
 
 GWGB_FORWARD(gwgb_set_hcore, (gwgb_handle h, const double *H), e.set_hcore(H))
+GWGB_FORWARD(gwgb_refproxy_run, (gwgb_handle h, int32_t nt_batch, int32_t nstreams, gwgb_proxy_stats *out),
+             e.refproxy(nt_batch, nstreams, out))
+GWGB_FORWARD(gwgb_refproxy_get, (gwgb_handle h, double *P0, double *Sigma), e.refproxy_get(P0, Sigma))
 GWGB_FORWARD(gwgb_set_energy_matrix, (gwgb_handle h, const double *M, int32_t n), e.set_energy_matrix(M, n))
 GWGB_FORWARD(gwgb_find_mu, (gwgb_handle h, const gwgb_mu_search *ms, double *mu_out, double *n_out),
              GWGB_REQUIRE(ms, GWGB_E_INVALID, "NULL mu search"); e.find_mu(*ms, mu_out, n_out))

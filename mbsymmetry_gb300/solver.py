@@ -212,6 +212,21 @@ class GWSolver:
     def synchronize(self):
         _abi.check(self.lib.gwgb_synchronize(self.h))
 
+    def refproxy(self, nt_batch: int = 4, nstreams: int = 16) -> dict:
+        """Run the reference's cuBLAS call sequence for P0 and Sigma on this
+        GPU (measurement only; gwgb_refproxy_run).  P0 comes from the current G,
+        Sigma from G and the P~ of the last solve()."""
+        st = _abi.GwgbProxyStats()
+        _abi.check(self.lib.gwgb_refproxy_run(self.h, nt_batch, nstreams, ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in _abi.GwgbProxyStats._fields_}
+
+    def refproxy_results(self):
+        """(P0 [q_irr][t][qslice], Sigma [t][s][flat_ao]) of the last refproxy()."""
+        P = np.zeros(self.p_size, np.complex128)
+        S = np.zeros(self.g_size, np.complex128)
+        _abi.check(self.lib.gwgb_refproxy_get(self.h, P.ctypes.data, S.ctypes.data))
+        return P, S
+
     def stats(self) -> dict:
         s = _abi.GwgbStats()
         _abi.check(self.lib.gwgb_get_stats(self.h, ctypes.byref(s)))
