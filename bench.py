@@ -214,7 +214,8 @@ def run_gpu(args):
             s.iteration(cr.mu)              # events inside the engine's graph
             st = s.stats()
             times.append(st["total_ms"])
-            for k in ("rotate_G_ms", "p0_ms", "pq_ms", "rotate_P_ms", "sigma_ms", "dyson_ms"):
+            for k in ("rotate_G_ms", "p0_ms", "pq_ms", "rotate_P_ms", "sigma_ms", "dyson_ms", "transform_ms",
+                      "solve_ms"):
                 stage_tot[k] = stage_tot.get(k, 0.0) + st[k]
         barrier()
     launches = int(st["kernel_launches"]) * args.steps
@@ -312,6 +313,10 @@ def run_gpu(args):
     mixed_bf16 = run_mixed("bf16x3", "bf16x3 (tcgen05 kind::f16, 3 BF16 planes, 6 products, FP32 accumulate per "
                                      "contribution, FP64 across)")
 
+    # ---- tile-shape autotuner (mbsymmetry_gb300/autotune.py) on this workload ---
+    from mbsymmetry_gb300 import autotune as _autotune
+    tune = _autotune.autotune(L, cr.ns, tr, cr.V, cr.F, cr.S, cr.mu, G=G0, precision="tf32x3", reps=2)
+
     # ---- the reference's cuBLAS call sequence on this GPU (measurement only) --
     # G rotation + per-pair strided-batched ZGEMM chains of P0 and Sigma, 16
     # streams, 4 tau per batch (the reference's nqkpt streams and test nt_batch);
@@ -368,10 +373,21 @@ def run_gpu(args):
         "contraction_tflops": {"p0": st["p0_flops"] / (stages["p0_ms"] * 1e-3) / 1e12,
                                "sigma": st["sigma_flops"] / (stages["sigma_ms"] * 1e-3) / 1e12},
         "roofline": roofline,
+        # the four tau <-> omega transforms of an iteration (HBM-bound) and the block solves
+        # (FP64 latency-bound, no roofline claim), from events inside the iteration's graph
+        "transforms": {"ms": stages["transform_ms"], "bytes_alg": st["transform_bytes"],
+                       "achieved_gbs": st["transform_bytes"] / (stages["transform_ms"] * 1e-3) / 1e9,
+                       "peak_gbs": peaks.get("hbm_gbs"),
+                       "frac": (st["transform_bytes"] / (stages["transform_ms"] * 1e-3) / 1e9 / peaks["hbm_gbs"])
+                               if peaks.get("hbm_gbs") else None},
+        "solves": {"ms": stages["solve_ms"], "flops": st["solve_flops"],
+                   "gflops": st["solve_flops"] / (stages["solve_ms"] * 1e-3) / 1e9},
         "clocks": clocks.summary(),
         "mixed": mixed,
         "mixed_bf16x3": mixed_bf16,
         "reference_gpu_proxy": proxy,
+        "autotune": {"best": tune["best"], "default": _autotune.DEFAULT_CANDIDATES[0],
+                     "trials": tune["trials"]},
         "sc_loop": sc,
         "peaks": {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops"),
                   "fp64_tflops_measured": fp64_peak},

@@ -60,6 +60,12 @@ typedef struct gwgb_params {
   int32_t device;    /* CUDA device ordinal */
   int32_t nt_batch;  /* accepted for params_t compatibility; the kernels choose their own tau tiles */
   int32_t flags;     /* reserved, 0 */
+  /* Tile-shape settings of the tcgen05 Sigma path, 0 = the built-in choice;
+   * mbsymmetry_gb300/autotune.py picks them by timing a workload. */
+  int32_t uvt_smem_kb; /* shared memory per U/Sigma CTA (60..227 KB; sets tau per tile and aux rows per chunk) */
+  int32_t sw_npk_max;  /* widest W-GEMM column pack (16, 32 or 64 complex columns) */
+  int32_t uv_waves;    /* U/Sigma contribution slices per tau, in units of the SM count (1..16; default 8) */
+  int32_t tune_pad;
 } gwgb_params;
 
 /* Block layout: the arrays symmetry_utils_t reads from symmetry_info.h5,
@@ -105,6 +111,10 @@ typedef struct gwgb_stats {
   double leakage;         /* max|c_{n-1}| / max|c_0| of G after the last Dyson */
   int64_t kernel_launches;/* kernels launched by the last solve/iteration */
   int64_t device_bytes;   /* device memory held by the buffers of all live handles of this process */
+  double transform_ms;    /* tau <-> omega transforms of the W~ solve and Dyson that ran */
+  double transform_bytes; /* their algorithmic bytes: 16 (n_in + n_out) per column + the matrix */
+  double solve_ms;        /* block solves: W~ (inverse + product) and Dyson (inverse) */
+  double solve_flops;     /* 16 n^3 per W~ block, 8 n^3 per Dyson block */
 } gwgb_stats;
 
 /* Library version string. */

@@ -34,6 +34,7 @@ class GwgbParams(ctypes.Structure):
         ("ns", c_int32), ("nts", c_int32), ("nw", c_int32), ("nw_b", c_int32),
         ("beta", c_double), ("precision", c_int32), ("device", c_int32),
         ("nt_batch", c_int32), ("flags", c_int32),
+        ("uvt_smem_kb", c_int32), ("sw_npk_max", c_int32), ("uv_waves", c_int32), ("tune_pad", c_int32),
     ]
 
 
@@ -56,7 +57,8 @@ class GwgbStats(ctypes.Structure):
         ("rotate_P_ms", c_double), ("sigma_ms", c_double), ("dyson_ms", c_double),
         ("total_ms", c_double), ("p0_flops", c_double), ("sigma_flops", c_double),
         ("leakage", c_double), ("kernel_launches", c_int64),
-        ("device_bytes", c_int64),
+        ("device_bytes", c_int64), ("transform_ms", c_double), ("transform_bytes", c_double),
+        ("solve_ms", c_double), ("solve_flops", c_double),
     ]
 
 

@@ -1,0 +1,91 @@
+"""Empirical tile-shape tuning of the tcgen05 Sigma path for one workload.
+
+The engine picks tile shapes per irrep-block size class by rule (tau per
+U/Sigma tile from 128 / k1_b and the shared-memory budget, aux rows per chunk
+from what fits, W-GEMM pack width from the aux block size, slices from the
+per-tau cost).  Three global settings of those rules trade occupancy against
+chunk length and load balance, and the best values depend on the block-size
+distribution: gwgb_params.uvt_smem_kb (shared memory per U/Sigma CTA),
+sw_npk_max (widest W-GEMM pack) and uv_waves (contribution slices per tau).
+``autotune`` times a small candidate set on the caller's own layout and data
+(one handle per candidate, CUDA-event timing of the Sigma stage of full
+iterations) and returns the fastest; ``cache`` stores results keyed by a
+fingerprint of the layout's block sizes, nts and precision.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+
+from .solver import GWSolver
+
+DEFAULT_CANDIDATES = (
+    {"uvt_smem_kb": 110, "sw_npk_max": 64, "uv_waves": 8},   # the built-in choice
+    {"uvt_smem_kb": 110, "sw_npk_max": 64, "uv_waves": 4},
+    {"uvt_smem_kb": 110, "sw_npk_max": 64, "uv_waves": 16},
+    {"uvt_smem_kb": 72, "sw_npk_max": 64, "uv_waves": 8},
+    {"uvt_smem_kb": 150, "sw_npk_max": 64, "uv_waves": 8},
+    {"uvt_smem_kb": 110, "sw_npk_max": 32, "uv_waves": 8},
+)
+
+
+def fingerprint(layout, nts: int, precision: str) -> str:
+    """Hash of what the tile rules see: block sizes per k / q, the V block list, nts, precision."""
+    h = hashlib.sha256()
+    for arrs in (layout.ao_sizes, layout.aux_sizes, layout.tensor_irreps):
+        for a in arrs:
+            h.update(np.ascontiguousarray(a, dtype=np.int64).tobytes())
+            h.update(b"|")
+    h.update(np.asarray(layout.irre_list, dtype=np.int64).tobytes())
+    h.update(f"{nts}:{precision}".encode())
+    return h.hexdigest()[:16]
+
+
+def autotune(layout, ns, transforms, V, F, S, mu, G=None, precision="tf32x3", candidates=DEFAULT_CANDIDATES,
+             warmup=1, reps=2, cache=None, device=0):
+    """Time each candidate on this workload; return {"best": settings, "trials": [...]}.
+
+    G: the Green's function to iterate from (default: Dyson of Sigma = 0 at mu).
+    The metric is the Sigma stage (the stage the settings shape) of `reps`
+    iterations after `warmup`; each trial also records the whole iteration.
+    With ``cache`` (a JSON file path) an earlier result for the same
+    fingerprint is returned without timing, and new results are added."""
+    key = fingerprint(layout, transforms.nts, precision)
+    store = {}
+    if cache and os.path.exists(cache):
+        with open(cache) as f:
+            store = json.load(f)
+        if key in store:
+            return store[key]
+    trials = []
+    for cand in candidates:
+        s = GWSolver(layout, ns, transforms, precision=precision, device=device, tune=cand)
+        try:
+            s.set_shared_Coulomb(V)
+            s.set_fock(F, S)
+            if G is None:
+                s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+                s.dyson(mu)
+                G0 = s.G_tau()
+            else:
+                G0 = G
+            sig, tot = [], []
+            for r in range(warmup + reps):
+                s.set_G(G0)
+                s.iteration(mu)
+                st = s.stats()
+                if r >= warmup:
+                    sig.append(st["sigma_ms"])
+                    tot.append(st["total_ms"])
+            trials.append({"settings": dict(cand), "sigma_ms": float(np.median(sig)),
+                           "iteration_ms": float(np.median(tot))})
+        finally:
+            s.close()
+    best = min(trials, key=lambda t: t["sigma_ms"])
+    out = {"fingerprint": key, "precision": precision, "best": best["settings"], "trials": trials}
+    if cache:
+        store[key] = out
+        with open(cache, "w") as f:
+            json.dump(store, f, indent=1)
+    return out

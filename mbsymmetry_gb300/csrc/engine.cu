@@ -327,6 +327,7 @@ class Engine {
   Lay l_;
   cudaStream_t st_ = nullptr;
   int smem_bytes_ = 0, sw_cap_ = 0;
+  int tune_uvt_kb_ = 0, tune_npk_ = 64, tune_waves_ = 8;  // tile-shape settings (gwgb_params)
   bool have_V_ = false, have_T_ = false, have_F_ = false, have_reps_ = false;
   DBuf<double2> px_p0_, px_sig_;  // results of the reference-GPU proxy
   bool px_ready_ = false;
@@ -448,7 +449,7 @@ class Engine {
   gwgb_sc_record read_record(int i);
   // graph
   cudaGraphExec_t graph_exec_ = nullptr;
-  cudaEvent_t ev_[8];
+  cudaEvent_t ev_[16];  // 0-6 stage boundaries; 8-11 inside the W~ solve, 12-14 inside Dyson
   double *mu_host_ = nullptr;
   gwgb_stats stats_{};
 
@@ -479,7 +480,9 @@ class Engine {
     return ms;
   }
   void check_device_flags();
-  void finish_stats(bool with_dyson, bool with_gw);
+  // with_pq / with_dy: the W~ solve / Dyson of this call ran with events 8-11 / 12-14
+  void finish_stats(bool with_dyson, bool with_gw, bool with_pq = false, bool with_dy = false);
+  double tr_bytes_pq_ = 0, tr_bytes_dy_ = 0, solve_flops_pq_ = 0, solve_flops_dy_ = 0;
 };
 
 Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
@@ -489,6 +492,14 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
                "tau/frequency grids are limited to 160 points");
   GWGB_REQUIRE(p.beta > 0.0, GWGB_E_INVALID, "beta must be positive");
   ns_ = p.ns; nts_ = p.nts; nw_ = p.nw; nw_b_ = p.nw_b; ncheb_ = p.nts - 2;
+  GWGB_REQUIRE(p.uvt_smem_kb == 0 || (p.uvt_smem_kb >= 60 && p.uvt_smem_kb <= 227), GWGB_E_INVALID,
+               "uvt_smem_kb must be 0 or in [60, 227]");
+  GWGB_REQUIRE(p.sw_npk_max == 0 || p.sw_npk_max == 16 || p.sw_npk_max == 32 || p.sw_npk_max == 64, GWGB_E_INVALID,
+               "sw_npk_max must be 0, 16, 32 or 64");
+  GWGB_REQUIRE(p.uv_waves >= 0 && p.uv_waves <= 16, GWGB_E_INVALID, "uv_waves must be in [0, 16]");
+  tune_uvt_kb_ = p.uvt_smem_kb;
+  if (p.sw_npk_max) tune_npk_ = p.sw_npk_max;
+  if (p.uv_waves) tune_waves_ = p.uv_waves;
   beta_ = p.beta; prec_ = GWGB_PREC_FP64; dev_ = p.device;
   l_ = derive_layout(L);
   GWGB_CUDA(cudaSetDevice(dev_));
@@ -879,10 +890,10 @@ void Engine::build_work_lists() {
       ucost[c] = 8.0 * sc[c].qb * sig_b1_[c] * sc[c].b2 * (sig_b1_[c] + sc[c].b2);
       utotal += ucost[c];
     }
-    // Slices depend on the per-tau cost only (about four waves of slices per tau), never
+    // Slices depend on the per-tau cost only (tune_waves_ waves of slices per tau), never
     // on the chunk length: the order of the FP64 sums, hence every result bit, is the
     // same for any chunking.  tcgen05 tiles span up to 128 / b1 tau, SIMT tiles 4.
-    const double target = utotal * ns_ / (4.0 * std::max(1, nsm_));
+    const double target = utotal * ns_ / ((double)tune_waves_ * std::max(1, nsm_));
     // tcgen05 U/Sigma tiles (AO blocks up to 64): tau per tile such that one aux row
     // of the largest contribution fits the shared-memory budget (two CTAs per SM when
     // possible; measured against one CTA with longer aux-row chunks (slower on both
@@ -890,6 +901,7 @@ void Engine::build_work_lists() {
     // overrides the budget)
     int uvt_budget = 110 * 1024;
     if (const char *e = std::getenv("GWGB_UVT_SMEM_KB")) uvt_budget = std::max(60, std::min(227, std::atoi(e))) * 1024;  // <= 4 CTAs x 128 TMEM columns
+    if (tune_uvt_kb_) uvt_budget = tune_uvt_kb_ * 1024;
     uvt_budget = std::min(uvt_budget, smem_bytes_);
     std::vector<int> own_nt(sig_own.size(), 0);  // 0: SIMT tiles
     uvt_smem_ = 0;
@@ -1070,7 +1082,7 @@ void Engine::build_work_lists() {
       // shared memory: TF32x3 2 planes x 4 B, BF16x3 3 planes x 2 B (K padded to 16)
       // (+ 18432 B of drain tiles: 4 warps x 32 rows x 36 floats)
       auto need = [&](int npk) { return 18432 + std::max(KP * (1024 + 32 * npk), KP16 * (768 + 24 * npk)); };
-      int npk = 64;
+      int npk = tune_npk_;
       while (npk > 16 && need(npk) > sw_cap_) npk /= 2;
       GWGB_REQUIRE(need(npk) <= sw_cap_, GWGB_E_UNSUPPORTED, "aux block too large for the tcgen05 Sigma kernel");
       wsmem = std::max(wsmem, need(npk));
@@ -1228,6 +1240,19 @@ void Engine::build_work_lists() {
   }
   inv_w_.upload(iw, st_);
   inv_d_.upload(id, st_);
+  {  // algorithmic work of the transforms (16 (n_in + n_out) B per column + T once per launch) and
+     // of the block solves (W~: inverse + product, 16 n^3 flop; Dyson: inverse, 8 n^3)
+    auto tb = [](const std::vector<TSlab> &v, int nin, int nout) {
+      double b = 16.0 * nin * nout;
+      for (const TSlab &t : v) b += 16.0 * (nin + nout) * t.ncols;
+      return b;
+    };
+    tr_bytes_pq_ = tb(pf, ncheb_, nw_b_) + tb(pb, nw_b_, nts_);
+    tr_bytes_dy_ = tb(sf, ncheb_, nw_) + tb(gb, nw_, nts_);
+    solve_flops_pq_ = solve_flops_dy_ = 0;
+    for (const InvTask &t : iw) solve_flops_pq_ += 16.0 * t.n * t.n * t.n;
+    for (const InvTask &t : id) solve_flops_dy_ += 8.0 * t.n * t.n * t.n;
+  }
   qoff_irr_.upload(qo, st_);
   qsz_irr_.upload(qs, st_);
   GWGB_CUDA(cudaStreamSynchronize(st_));
@@ -1344,9 +1369,13 @@ void Engine::k_p0(int mirror) {
 
 void Engine::k_pq(bool mirror_first) {
   if (mirror_first) launch_mirror(Pall_.p, qoff_irr_.p, qsz_irr_.p, l_.ink, nts_, st_);
+  record(8);
   launch_transform(slab_p_fwd_.p, (int)slab_p_fwd_.n, max_cols_p_, TntBF_.p, nw_b_, ncheb_, 1, Pall_.p, Pw_.p, st_);
+  record(9);
   launch_inverse(inv_w_.p, (int)inv_w_.n, l_.max_aux, Pw_.p, nullptr, nullptr, nullptr, beta_, 0.0, 0, bad_.p, st_);
+  record(10);
   launch_transform(slab_p_bwd_.p, (int)slab_p_bwd_.n, max_cols_p_, TtnFB_.p, nts_, nw_b_, 0, Pw_.p, Pall_.p, st_);
+  record(11);
 }
 
 
@@ -1387,7 +1416,7 @@ void Engine::check_device_flags() {
   }
 }
 
-void Engine::finish_stats(bool with_dyson, bool with_gw) {
+void Engine::finish_stats(bool with_dyson, bool with_gw, bool with_pq, bool with_dy) {
   GWGB_CUDA(cudaStreamSynchronize(st_));
   check_device_flags();
   gwgb_stats s{};
@@ -1412,6 +1441,18 @@ void Engine::finish_stats(bool with_dyson, bool with_gw) {
     }
   }
   s.total_ms = elapsed(with_gw ? 0 : 5, with_dyson ? 6 : 5);
+  if (with_pq) {
+    s.transform_ms += elapsed(8, 9) + elapsed(10, 11);
+    s.transform_bytes += tr_bytes_pq_;
+    s.solve_ms += elapsed(9, 10);
+    s.solve_flops += solve_flops_pq_;
+  }
+  if (with_dy) {
+    s.transform_ms += elapsed(5, 12) + elapsed(13, 14);
+    s.transform_bytes += tr_bytes_dy_;
+    s.solve_ms += elapsed(12, 13);
+    s.solve_flops += solve_flops_dy_;
+  }
   int64_t launches = 0;
   if (with_gw) {
     const bool tc = prec_ != GWGB_PREC_FP64;
@@ -1448,7 +1489,7 @@ void Engine::solve_Pq() {
   record(0); record(1); record(2);
   k_pq(true);
   for (int i = 3; i <= 6; ++i) record(i);
-  finish_stats(false, true);
+  finish_stats(false, true, true);
 }
 
 void Engine::solve_sigma() {
@@ -1481,7 +1522,7 @@ void Engine::solve() {
   k_sigma();
   record(5);
   record(6);
-  finish_stats(false, true);
+  finish_stats(false, true, true);
 }
 
 void Engine::dyson(double mu) {
@@ -1490,14 +1531,17 @@ void Engine::dyson(double mu) {
   // mu enters the inverse kernel by value here (no graph)
   record(5);
   launch_transform(slab_s_fwd_.p, (int)slab_s_fwd_.n, max_cols_g_, Tnt_.p, nw_, ncheb_, 1, Sig_.p, Ww_.p, st_);
+  record(12);
   launch_inverse(inv_d_.p, (int)inv_d_.n, l_.max_ao, Ww_.p, S_.p, F_.p, ws_.p, beta_, mu, 1, bad_.p + 1, st_);
+  record(13);
   launch_transform(slab_g_bwd_.p, (int)slab_g_bwd_.n, max_cols_g_, Ttn_.p, nts_, nw_, 0, Ww_.p, Gall_.p, st_);
+  record(14);
   if (has_tct_) {
     GWGB_CUDA(cudaMemsetAsync(leak_.p, 0, 2 * sizeof(unsigned long long), st_));
     launch_leakage(slab_g_bwd_.p, (int)slab_g_bwd_.n, Gall_.p, tct_f_.p, tct_l_.p, ncheb_, leak_.p, st_);
   }
   record(6);
-  finish_stats(true, false);
+  finish_stats(true, false, false, true);
 }
 
 void Engine::iteration(double mu) {
@@ -1526,8 +1570,11 @@ void Engine::iteration(double mu) {
     k_sigma();
     record(5);
     launch_transform(slab_s_fwd_.p, (int)slab_s_fwd_.n, max_cols_g_, Tnt_.p, nw_, ncheb_, 1, Sig_.p, Ww_.p, st_);
+    record(12);
     launch_inverse(inv_d_.p, (int)inv_d_.n, l_.max_ao, Ww_.p, S_.p, F_.p, ws_.p, beta_, mu, 1, bad_.p + 1, st_);
+    record(13);
     launch_transform(slab_g_bwd_.p, (int)slab_g_bwd_.n, max_cols_g_, Ttn_.p, nts_, nw_, 0, Ww_.p, Gall_.p, st_);
+    record(14);
     if (has_tct_) {
       GWGB_CUDA(cudaMemsetAsync(leak_.p, 0, 2 * sizeof(unsigned long long), st_));
       launch_leakage(slab_g_bwd_.p, (int)slab_g_bwd_.n, Gall_.p, tct_f_.p, tct_l_.p, ncheb_, leak_.p, st_);
@@ -1547,7 +1594,7 @@ void Engine::iteration(double mu) {
     cudaGraphDestroy(g);
   }
   GWGB_CUDA(cudaGraphLaunch(graph_exec_, st_));
-  finish_stats(true, true);
+  finish_stats(true, true, true, true);
 }
 
 

@@ -31,7 +31,10 @@ def _ptr(a: np.ndarray):
 
 class GWSolver:
     def __init__(self, layout: BlockLayout, ns: int, transforms: IRTransforms,
-                 precision: str = "fp64", device: int = 0):
+                 precision: str = "fp64", device: int = 0, tune: dict = None):
+        """tune: optional tile-shape settings of the tcgen05 Sigma path
+        (uvt_smem_kb, sw_npk_max, uv_waves; see gwgb_params), e.g. the
+        "best" entry returned by autotune.autotune()."""
         self.lib = _abi.load()
         self.layout = layout
         self.ns = ns
@@ -39,7 +42,7 @@ class GWSolver:
         self.nts = transforms.nts
         p = _abi.GwgbParams(ns=ns, nts=transforms.nts, nw=transforms.nw, nw_b=transforms.nw_b,
                             beta=transforms.beta, precision=_abi.PREC_NAMES[precision], device=device,
-                            nt_batch=0, flags=0)
+                            nt_batch=0, flags=0, **{k: int(v) for k, v in (tune or {}).items()})
         self._lay_c, self._keep = layout.to_c()
         h = ctypes.c_void_p()
         _abi.check(self.lib.gwgb_create(ctypes.byref(p), ctypes.byref(self._lay_c), ctypes.byref(h)))
