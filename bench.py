@@ -375,11 +375,16 @@ def run_gpu(args):
         "roofline": roofline,
         # the four tau <-> omega transforms of an iteration (HBM-bound) and the block solves
         # (FP64 latency-bound, no roofline claim), from events inside the iteration's graph
+        # (bound: FP64 FMA, about 25 flop per byte at n ~ 100; the HBM figure is given too)
         "transforms": {"ms": stages["transform_ms"], "bytes_alg": st["transform_bytes"],
                        "achieved_gbs": st["transform_bytes"] / (stages["transform_ms"] * 1e-3) / 1e9,
                        "peak_gbs": peaks.get("hbm_gbs"),
-                       "frac": (st["transform_bytes"] / (stages["transform_ms"] * 1e-3) / 1e9 / peaks["hbm_gbs"])
-                               if peaks.get("hbm_gbs") else None},
+                       "frac_hbm": (st["transform_bytes"] / (stages["transform_ms"] * 1e-3) / 1e9 / peaks["hbm_gbs"])
+                                   if peaks.get("hbm_gbs") else None,
+                       "flops_alg": st["transform_flops"], "bound": "fp64",
+                       "achieved_tflops": st["transform_flops"] / (stages["transform_ms"] * 1e-3) / 1e12,
+                       "frac_fp64": st["transform_flops"] / (stages["transform_ms"] * 1e-3) / 1e12 / fp64_peak
+                                    if fp64_peak > 0 else None},
         "solves": {"ms": stages["solve_ms"], "flops": st["solve_flops"],
                    "gflops": st["solve_flops"] / (stages["solve_ms"] * 1e-3) / 1e9},
         "clocks": clocks.summary(),

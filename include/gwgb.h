@@ -115,6 +115,8 @@ typedef struct gwgb_stats {
   double transform_bytes; /* their algorithmic bytes: 16 (n_in + n_out) per column + the matrix */
   double solve_ms;        /* block solves: W~ (inverse + product) and Dyson (inverse) */
   double solve_flops;     /* 16 n^3 per W~ block, 8 n^3 per Dyson block */
+  double transform_flops; /* 8 n_in n_out per complex column (FP64: with n ~ 100 the transforms are
+                             bound by the FP64 pipe, not by HBM) */
 } gwgb_stats;
 
 /* Library version string. */

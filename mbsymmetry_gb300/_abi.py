@@ -58,7 +58,7 @@ class GwgbStats(ctypes.Structure):
         ("total_ms", c_double), ("p0_flops", c_double), ("sigma_flops", c_double),
         ("leakage", c_double), ("kernel_launches", c_int64),
         ("device_bytes", c_int64), ("transform_ms", c_double), ("transform_bytes", c_double),
-        ("solve_ms", c_double), ("solve_flops", c_double),
+        ("solve_ms", c_double), ("solve_flops", c_double), ("transform_flops", c_double),
     ]
 
 

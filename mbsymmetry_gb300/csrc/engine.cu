@@ -482,7 +482,7 @@ class Engine {
   void check_device_flags();
   // with_pq / with_dy: the W~ solve / Dyson of this call ran with events 8-11 / 12-14
   void finish_stats(bool with_dyson, bool with_gw, bool with_pq = false, bool with_dy = false);
-  double tr_bytes_pq_ = 0, tr_bytes_dy_ = 0, solve_flops_pq_ = 0, solve_flops_dy_ = 0;
+  double tr_bytes_pq_ = 0, tr_bytes_dy_ = 0, tr_flops_pq_ = 0, tr_flops_dy_ = 0, solve_flops_pq_ = 0, solve_flops_dy_ = 0;
 };
 
 Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
@@ -1249,6 +1249,13 @@ void Engine::build_work_lists() {
     };
     tr_bytes_pq_ = tb(pf, ncheb_, nw_b_) + tb(pb, nw_b_, nts_);
     tr_bytes_dy_ = tb(sf, ncheb_, nw_) + tb(gb, nw_, nts_);
+    auto tf = [](const std::vector<TSlab> &v, int nin, int nout) {  // 8 n_in n_out flop per complex column
+      double f = 0;
+      for (const TSlab &t : v) f += 8.0 * nin * nout * t.ncols;
+      return f;
+    };
+    tr_flops_pq_ = tf(pf, ncheb_, nw_b_) + tf(pb, nw_b_, nts_);
+    tr_flops_dy_ = tf(sf, ncheb_, nw_) + tf(gb, nw_, nts_);
     solve_flops_pq_ = solve_flops_dy_ = 0;
     for (const InvTask &t : iw) solve_flops_pq_ += 16.0 * t.n * t.n * t.n;
     for (const InvTask &t : id) solve_flops_dy_ += 8.0 * t.n * t.n * t.n;
@@ -1444,12 +1451,14 @@ void Engine::finish_stats(bool with_dyson, bool with_gw, bool with_pq, bool with
   if (with_pq) {
     s.transform_ms += elapsed(8, 9) + elapsed(10, 11);
     s.transform_bytes += tr_bytes_pq_;
+    s.transform_flops += tr_flops_pq_;
     s.solve_ms += elapsed(9, 10);
     s.solve_flops += solve_flops_pq_;
   }
   if (with_dy) {
     s.transform_ms += elapsed(5, 12) + elapsed(13, 14);
     s.transform_bytes += tr_bytes_dy_;
+    s.transform_flops += tr_flops_dy_;
     s.solve_ms += elapsed(12, 13);
     s.solve_flops += solve_flops_dy_;
   }
