@@ -21,11 +21,13 @@ import numpy as np
 from .solver import GWSolver
 
 DEFAULT_CANDIDATES = (
-    {"uvt_smem_kb": 110, "sw_npk_max": 64, "uv_waves": 8},   # the built-in choice
+    {"uvt_smem_kb": 0, "sw_npk_max": 0, "uv_waves": 0},      # the built-in choice (0: engine rules)
+    {"uvt_smem_kb": 110, "sw_npk_max": 64, "uv_waves": 8},
     {"uvt_smem_kb": 110, "sw_npk_max": 64, "uv_waves": 4},
     {"uvt_smem_kb": 110, "sw_npk_max": 64, "uv_waves": 16},
     {"uvt_smem_kb": 72, "sw_npk_max": 64, "uv_waves": 8},
     {"uvt_smem_kb": 150, "sw_npk_max": 64, "uv_waves": 8},
+    {"uvt_smem_kb": 200, "sw_npk_max": 64, "uv_waves": 8},
     {"uvt_smem_kb": 110, "sw_npk_max": 32, "uv_waves": 8},
 )
 

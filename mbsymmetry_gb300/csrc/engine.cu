@@ -899,7 +899,19 @@ void Engine::build_work_lists() {
     // possible; measured against one CTA with longer aux-row chunks (slower on both
     // workloads) and three (3% faster on C3, 25% slower on C2); GWGB_UVT_SMEM_KB
     // overrides the budget)
+    // Default: 110 KB (two CTAs per SM), raised (to at most 200 KB) until every owner's
+    // tiles keep the full 128 / k1_b tau rows: with AO blocks near 30 the 110 KB
+    // tiles hold 1-2 tau and most of the 128 MMA rows idle (C4: 1.81 s vs 1.24 s at
+    // 150 KB for the Sigma stage); with blocks up to 16 the default already fits.
     int uvt_budget = 110 * 1024;
+    for (const Owner &o : sig_own) {
+      if (o.n > 64) continue;
+      int b2max = 1;
+      for (int c = o.c0; c < o.c1; ++c) b2max = std::max(b2max, sc[c].b2);
+      const int ntf = std::max(1, std::min(nts_, 128 / o.n));
+      const int64_t nd = std::max(uvt_smem(1, ntf, o.n, b2max, false), uvt_smem(1, ntf, o.n, b2max, true));
+      uvt_budget = (int)std::max<int64_t>(uvt_budget, std::min<int64_t>(nd, 200 * 1024));
+    }
     if (const char *e = std::getenv("GWGB_UVT_SMEM_KB")) uvt_budget = std::max(60, std::min(227, std::atoi(e))) * 1024;  // <= 4 CTAs x 128 TMEM columns
     if (tune_uvt_kb_) uvt_budget = tune_uvt_kb_ * 1024;
     uvt_budget = std::min(uvt_budget, smem_bytes_);
