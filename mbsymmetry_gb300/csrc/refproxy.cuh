@@ -73,6 +73,28 @@ const CublasApi &cublas_api() {
                                        std::to_string((int)s_) + "): " #x);                \
   } while (0)
 
+// Streams, events and the cuBLAS handle of one proxy run, released on every exit.
+struct ProxyResources {
+  const CublasApi &cb;
+  cublasHandle_t h = nullptr;
+  std::vector<cudaStream_t> ss;
+  std::vector<cudaEvent_t> ev;
+  explicit ProxyResources(const CublasApi &api) : cb(api) {}
+  ~ProxyResources() {
+    if (h) cb.destroy(h);
+    for (cudaStream_t s : ss)
+      if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  cudaEvent_t event(unsigned flags) {
+    cudaEvent_t e = nullptr;
+    GWGB_CUDA(cudaEventCreateWithFlags(&e, flags));
+    ev.push_back(e);
+    return e;
+  }
+};
+
 inline cuDoubleComplex cz(double re, double im = 0.0) { return make_cuDoubleComplex(re, im); }
 inline cuDoubleComplex *zc(double2 *p) { return reinterpret_cast<cuDoubleComplex *>(p); }
 inline const cuDoubleComplex *zc(const double2 *p) { return reinterpret_cast<const cuDoubleComplex *>(p); }
@@ -83,6 +105,7 @@ void Engine::refproxy(int nt_batch, int nstreams, gwgb_proxy_stats *out) {
   GWGB_REQUIRE(have_V_, GWGB_E_STATE, "V has not been uploaded");
   GWGB_REQUIRE(nt_batch >= 1 && nt_batch <= nts_ && nstreams >= 1 && nstreams <= 64, GWGB_E_INVALID,
                "nt_batch must be in [1, nts] and nstreams in [1, 64]");
+  px_ready_ = false;  // until this run has completed
   const CublasApi &cb = cublas_api();
   GWGB_REQUIRE(cb.ok, GWGB_E_UNSUPPORTED, "libcublas could not be loaded for the reference-GPU proxy");
   const Lay &l = l_;
@@ -103,6 +126,11 @@ void Engine::refproxy(int nt_batch, int nstreams, gwgb_proxy_stats *out) {
   }
   for (int q = 0; q < nk; ++q) max_qs = std::max<int64_t>(max_qs, l.qaux_sz[q]);
   for (int k = 0; k < nk; ++k) max_ks = std::max<int64_t>(max_ks, l.kao_sz[k]);
+  // cuBLAS takes 32-bit counts (AXPY / SCAL lengths, matrix sizes)
+  const int64_t imax = 2147483647;
+  GWGB_REQUIRE((int64_t)nts * fq <= imax && (int64_t)nts * ns * fa <= imax && max_pair <= imax &&
+                   (int64_t)nts * ns * max_ks <= imax,
+               GWGB_E_UNSUPPORTED, "layout too large for the 32-bit cuBLAS calls of the reference-GPU proxy");
   const int S = nstreams;
   DBuf<double2> gfull, grev, vt, vc, x1, x2, plocal, prot, slocal, pacc, sacc, rt;
   const int64_t max_rt = std::max<int64_t>((int64_t)nts * ns * l.max_ao * l.max_ao, (int64_t)nts * l.max_aux * l.max_aux);
@@ -118,17 +146,16 @@ void Engine::refproxy(int nt_batch, int nstreams, gwgb_proxy_stats *out) {
   slocal.alloc((size_t)(S * nts * ns * max_ks));
   pacc.alloc((size_t)(S * nts * fq));
   sacc.alloc((size_t)(S * nts * ns * fa));
-  std::vector<cudaStream_t> ss(S);
-  for (auto &s : ss) GWGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  cublasHandle_t h = nullptr;
-  GWGB_CUBLAS(cb.create(&h));
-  cudaEvent_t e0, e1, e2, ef;
+  ProxyResources res(cb);
+  res.ss.assign(S, nullptr);
+  for (auto &s : res.ss) GWGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  const std::vector<cudaStream_t> &ss = res.ss;
+  GWGB_CUBLAS(cb.create(&res.h));
+  cublasHandle_t h = res.h;
+  cudaEvent_t ef = res.event(cudaEventDisableTiming);
+  cudaEvent_t e0 = res.event(cudaEventDefault), e1 = res.event(cudaEventDefault), e2 = res.event(cudaEventDefault);
   std::vector<cudaEvent_t> es(S);
-  GWGB_CUDA(cudaEventCreateWithFlags(&ef, cudaEventDisableTiming));
-  GWGB_CUDA(cudaEventCreate(&e0));
-  GWGB_CUDA(cudaEventCreate(&e1));
-  GWGB_CUDA(cudaEventCreate(&e2));
-  for (auto &e : es) GWGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  for (auto &e : es) e = res.event(cudaEventDisableTiming);
   int64_t ngemm = 0, nother = 0;
   const cuDoubleComplex one = cz(1.0), zero = cz(0.0);
   auto on = [&](int s) { GWGB_CUBLAS(cb.set_stream(h, ss[s])); };
@@ -349,13 +376,6 @@ void Engine::refproxy(int nt_batch, int nstreams, gwgb_proxy_stats *out) {
   GWGB_CUDA(cudaMemcpyAsync(px_p0_.p, pacc.p, px_p0_.n * sizeof(double2), cudaMemcpyDeviceToDevice, st_));
   GWGB_CUDA(cudaMemcpyAsync(px_sig_.p, sacc.p, px_sig_.n * sizeof(double2), cudaMemcpyDeviceToDevice, st_));
   GWGB_CUDA(cudaStreamSynchronize(st_));
-  GWGB_CUBLAS(cb.destroy(h));
-  for (auto &s : ss) cudaStreamDestroy(s);
-  for (auto &e : es) cudaEventDestroy(e);
-  cudaEventDestroy(ef);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaEventDestroy(e2);
   px_ready_ = true;
   if (out) {
     out->p0_ms = ms_p0;
