@@ -65,7 +65,7 @@ typedef struct gwgb_params {
   int32_t uvt_smem_kb; /* shared memory per U/Sigma CTA (60..227 KB; sets tau per tile and aux rows per chunk) */
   int32_t sw_npk_max;  /* widest W-GEMM column pack (16, 32 or 64 complex columns) */
   int32_t uv_waves;    /* U/Sigma contribution slices per tau, in units of the SM count (1..16; default 8) */
-  int32_t tune_pad;
+  int32_t uv_simt;     /* 1: all U/Sigma tiles on the FP32 SIMT kernels (the path for AO blocks above 64) */
 } gwgb_params;
 
 /* Block layout: the arrays symmetry_utils_t reads from symmetry_info.h5,

@@ -34,7 +34,7 @@ class GwgbParams(ctypes.Structure):
         ("ns", c_int32), ("nts", c_int32), ("nw", c_int32), ("nw_b", c_int32),
         ("beta", c_double), ("precision", c_int32), ("device", c_int32),
         ("nt_batch", c_int32), ("flags", c_int32),
-        ("uvt_smem_kb", c_int32), ("sw_npk_max", c_int32), ("uv_waves", c_int32), ("tune_pad", c_int32),
+        ("uvt_smem_kb", c_int32), ("sw_npk_max", c_int32), ("uv_waves", c_int32), ("uv_simt", c_int32),
     ]
 
 

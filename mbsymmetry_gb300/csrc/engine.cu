@@ -327,7 +327,7 @@ class Engine {
   Lay l_;
   cudaStream_t st_ = nullptr;
   int smem_bytes_ = 0, sw_cap_ = 0;
-  int tune_uvt_kb_ = 0, tune_npk_ = 64, tune_waves_ = 8;  // tile-shape settings (gwgb_params)
+  int tune_uvt_kb_ = 0, tune_npk_ = 64, tune_waves_ = 8, tune_simt_ = 0;  // tile-shape settings (gwgb_params)
   bool have_V_ = false, have_T_ = false, have_F_ = false, have_reps_ = false;
   DBuf<double2> px_p0_, px_sig_;  // results of the reference-GPU proxy
   bool px_ready_ = false;
@@ -497,7 +497,9 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
   GWGB_REQUIRE(p.sw_npk_max == 0 || p.sw_npk_max == 16 || p.sw_npk_max == 32 || p.sw_npk_max == 64, GWGB_E_INVALID,
                "sw_npk_max must be 0, 16, 32 or 64");
   GWGB_REQUIRE(p.uv_waves >= 0 && p.uv_waves <= 16, GWGB_E_INVALID, "uv_waves must be in [0, 16]");
+  GWGB_REQUIRE(p.uv_simt == 0 || p.uv_simt == 1, GWGB_E_INVALID, "uv_simt must be 0 or 1");
   tune_uvt_kb_ = p.uvt_smem_kb;
+  tune_simt_ = p.uv_simt;
   if (p.sw_npk_max) tune_npk_ = p.sw_npk_max;
   if (p.uv_waves) tune_waves_ = p.uv_waves;
   beta_ = p.beta; prec_ = GWGB_PREC_FP64; dev_ = p.device;
@@ -894,15 +896,14 @@ void Engine::build_work_lists() {
     // on the chunk length: the order of the FP64 sums, hence every result bit, is the
     // same for any chunking.  tcgen05 tiles span up to 128 / b1 tau, SIMT tiles 4.
     const double target = utotal * ns_ / ((double)tune_waves_ * std::max(1, nsm_));
-    // tcgen05 U/Sigma tiles (AO blocks up to 64): tau per tile such that one aux row
-    // of the largest contribution fits the shared-memory budget (two CTAs per SM when
-    // possible; measured against one CTA with longer aux-row chunks (slower on both
-    // workloads) and three (3% faster on C3, 25% slower on C2); GWGB_UVT_SMEM_KB
-    // overrides the budget)
-    // Default: 110 KB (two CTAs per SM), raised (to at most 200 KB) until every owner's
-    // tiles keep the full 128 / k1_b tau rows: with AO blocks near 30 the 110 KB
-    // tiles hold 1-2 tau and most of the 128 MMA rows idle (C4: 1.81 s vs 1.24 s at
-    // 150 KB for the Sigma stage); with blocks up to 16 the default already fits.
+    // tcgen05 U/Sigma tiles (AO blocks up to 64; uv_simt routes every owner to the
+    // SIMT kernels): tau per tile such that one aux row of the owner's largest
+    // contribution fits the shared-memory budget.  Default budget 110 KB (two CTAs per
+    // SM), raised (to at most 200 KB) until every owner's tiles keep the full
+    // 128 / k1_b tau rows: with AO blocks near 30 the 110 KB tiles hold 1-2 tau and
+    // most of the 128 MMA rows idle (C4 Sigma stage 1.81 s at 110 KB, 0.99 s at
+    // 200 KB); with blocks up to 16 the default already fits.  gwgb_params.uvt_smem_kb
+    // (or GWGB_UVT_SMEM_KB) sets it.
     int uvt_budget = 110 * 1024;
     for (const Owner &o : sig_own) {
       if (o.n > 64) continue;
@@ -919,7 +920,7 @@ void Engine::build_work_lists() {
     uvt_smem_ = 0;
     for (size_t oi = 0; oi < sig_own.size(); ++oi) {
       const Owner &o = sig_own[oi];
-      if (o.n > 64) continue;
+      if (o.n > 64 || tune_simt_) continue;
       int b2max = 1;
       for (int c = o.c0; c < o.c1; ++c) b2max = std::max(b2max, sc[c].b2);
       auto need = [&](int nt) {

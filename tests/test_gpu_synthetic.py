@@ -132,3 +132,33 @@ def test_used_pairs_only_storage_is_exact(precision):
     (p1, s1, n1), (p2, s2, n2) = out
     assert n2 < n1
     assert np.array_equal(p1, p2) and np.array_equal(s1, s2)
+
+
+@pytest.mark.parametrize("ns", [1, 2])
+def test_uv_simt_path_and_tcgen05_path_agree(ns):
+    """The FP32 SIMT U/Sigma kernels (the path of AO blocks above 64, forced here
+    with uv_simt) and the tcgen05 Sigma GEMM path both keep the mixed-precision
+    bound against FP64, at ns = 1 and 2."""
+    from mbsymmetry_gb300.solver import GWSolver
+    cr, tr = crystal("C1", ns=ns)
+    ref = GWSolver(cr.layout, cr.ns, tr)
+    ref.set_shared_Coulomb(cr.V)
+    ref.set_fock(cr.F, cr.S)
+    ref.set_Selfenergy(np.zeros(ref.g_size, np.complex128))
+    ref.dyson(cr.mu)
+    G0 = ref.G_tau()
+    ref.solve()
+    S64 = ref.Selfenergy()
+    ref.close()
+    out = []
+    for simt in (0, 1):
+        s = GWSolver(cr.layout, cr.ns, tr, precision="tf32x3", tune={"uv_simt": simt})
+        s.set_shared_Coulomb(cr.V)
+        s.set_fock(cr.F, cr.S)
+        s.set_G(G0)
+        s.solve()
+        out.append(s.Selfenergy())
+        s.close()
+    bound = 1e-5 * max(1.0, np.abs(S64).max())
+    assert np.abs(out[0] - S64).max() < bound and np.abs(out[1] - S64).max() < bound
+    assert np.abs(out[0] - out[1]).max() > 0          # two different kernels ran
