@@ -899,14 +899,15 @@ void Engine::build_work_lists() {
     // tcgen05 U/Sigma tiles (AO blocks up to 64; uv_simt routes every owner to the
     // SIMT kernels): tau per tile such that one aux row of the owner's largest
     // contribution fits the shared-memory budget.  Default budget 110 KB (two CTAs per
-    // SM), raised (to at most 200 KB) until every owner's tiles keep the full
-    // 128 / k1_b tau rows: with AO blocks near 30 the 110 KB tiles hold 1-2 tau and
+    // SM), raised (to at most 200 KB) until the tiles of owners with AO blocks of 24 and
+    // more keep the full 128 / k1_b tau rows: there the 110 KB tiles hold 1-2 tau and
     // most of the 128 MMA rows idle (C4 Sigma stage 1.81 s at 110 KB, 0.99 s at
-    // 200 KB); with blocks up to 16 the default already fits.  gwgb_params.uvt_smem_kb
-    // (or GWGB_UVT_SMEM_KB) sets it.
+    // 200 KB).  Owners with small blocks do not raise it: their full-tau tiles (up to
+    // 64 tau of G2) would take one CTA per SM for every tile (C3 iteration 0.56 s at
+    // 110 KB, 0.64 s at 200 KB).  gwgb_params.uvt_smem_kb (or GWGB_UVT_SMEM_KB) sets it.
     int uvt_budget = 110 * 1024;
     for (const Owner &o : sig_own) {
-      if (o.n > 64) continue;
+      if (o.n > 64 || o.n < 24) continue;
       int b2max = 1;
       for (int c = o.c0; c < o.c1; ++c) b2max = std::max(b2max, sc[c].b2);
       const int ntf = std::max(1, std::min(nts_, 128 / o.n));
