@@ -45,8 +45,8 @@ L2_BYTES = 129 * 1024 * 1024
 
 
 def _rank_info():
-    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
-            int(os.environ.get("LOCAL_RANK", 0)))
+    from mbsymmetry_gb300.replicas import rank_info
+    return rank_info()
 
 
 def _load_peaks():
@@ -176,11 +176,10 @@ def run_reference(args):
 def run_gpu(args):
     rank, world, local = _rank_info()
     import torch
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from mbsymmetry_gb300.replicas import Replicas
     dev = local
     torch.cuda.set_device(dev)
+    reps = Replicas(device=f"cuda:{dev}")  # independent replicas: max-over-ranks timing, rank 0 reports
     from mbsymmetry_gb300.solver import GWSolver
     from mbsymmetry_gb300 import _abi
     import ctypes
@@ -195,10 +194,7 @@ def run_gpu(args):
     G0 = s.G_tau()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
 
-    def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
+    barrier = reps.barrier
 
     for _ in range(args.warmup):
         s.set_G(G0)
@@ -219,11 +215,7 @@ def run_gpu(args):
                 stage_tot[k] = stage_tot.get(k, 0.0) + st[k]
         barrier()
     launches = int(st["kernel_launches"]) * args.steps
-    ms = float(np.mean(times))
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reps.max_over_ranks(float(np.mean(times)))
     stages = {k: v / args.steps for k, v in stage_tot.items()}
 
     # ---- e2e through the C ABI with pinned host buffers ------------------
@@ -248,11 +240,7 @@ def run_gpu(args):
         _abi.check(lib.gwgb_get_G(h, vp(g_out.data_ptr())))
         e2e.append(time.perf_counter() - t0)
     barrier()
-    e2e_s = float(np.mean(e2e))
-    if world > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reps.max_over_ranks(float(np.mean(e2e)))
     gbytes = s.g_size * 16
 
     # ---- roofline of the dominant kernel ---------------------------------
@@ -362,7 +350,8 @@ def run_gpu(args):
     sc["speedup"] = sc["fp64"]["s_per_iteration"] / sc["tf32x3_final_fp64"]["s_per_iteration"]
 
     line = {
-        "metric": METRIC, "value": ms / 1e3 / world, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": reps.job_seconds_per_iteration(ms), "unit": "s", "n_gpus": world,
+        "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "precision": "fp64", "l2": "flushed (256 MiB write) before each step",
@@ -398,13 +387,12 @@ def run_gpu(args):
                   "fp64_tflops_measured": fp64_peak},
     }
     s.close()
-    if rank == 0 and not args.no_cpu_baseline:
+    if reps.reports and not args.no_cpu_baseline:
         v, cores, sample = _cpu_reference(cr, tr, 1)
         line["cpu_baseline"] = {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample}
-    if rank == 0:
+    if reps.reports:
         print(json.dumps(line))
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    reps.close()
 
 
 def run_profile(args):
