@@ -87,7 +87,7 @@ class CrystalSpec:
     v_scale: float = 0.5
 
 
-#: The five benchmark crystals (shapes of the BASELINE configurations).
+#: The five benchmark crystals C1-C5 (their shapes, block-size ranges and V storage).
 CONFIGS: Dict[str, CrystalSpec] = {
     "C1": CrystalSpec("C1", "fcc", (3, 3, 3), 8, 36, 62, 50.0, ao_block=(1, 4), aux_block=(2, 12), seed=20260101),
     "C2": CrystalSpec("C2", "fcc", (3, 3, 3), 26, 120, 100, 100.0, ao_block=(1, 8), aux_block=(2, 40), seed=20260102),
