@@ -85,19 +85,20 @@ class CrystalSpec:
     aux_block: Tuple[int, int] = (2, 40)
     seed: int = 20260101
     v_scale: float = 0.5
+    atoms: int = 2               # atoms per cell (physical block sizes, fcc only)
 
 
 #: The five benchmark crystals C1-C5 (their shapes, block-size ranges and V storage).
 CONFIGS: Dict[str, CrystalSpec] = {
     "C1": CrystalSpec("C1", "fcc", (3, 3, 3), 8, 36, 62, 50.0, ao_block=(1, 4), aux_block=(2, 12), seed=20260101),
     "C2": CrystalSpec("C2", "fcc", (3, 3, 3), 26, 120, 100, 100.0, ao_block=(1, 8), aux_block=(2, 40), seed=20260102),
-    "C3": CrystalSpec("C3", "fcc", (4, 4, 4), 52, 250, 120, 100.0, ao_block=(2, 16), aux_block=(4, 64), seed=20260103),
+    "C3": CrystalSpec("C3", "fcc", (4, 4, 4), 52, 250, 120, 100.0, ao_block=(2, 16), aux_block=(4, 64), seed=20260103, atoms=4),
     "C4": CrystalSpec("C4", "hex", (4, 4, 3), 72, 350, 120, 200.0, ao_block=(2, 30), aux_block=(2, 30), seed=20260104),
-    "C5": CrystalSpec("C5", "fcc", (5, 5, 5), 100, 500, 150, 200.0, ao_block=(4, 40), aux_block=(8, 64), seed=20260105),
+    "C5": CrystalSpec("C5", "fcc", (5, 5, 5), 100, 500, 150, 200.0, ao_block=(4, 40), aux_block=(8, 64), seed=20260105, atoms=4),
     # profiling case: C3's orbitals, grid and block sizes on the 3x3x3 mesh (V ~2 GB
     # instead of 12 GB), small enough for multi-pass kernel captures
     "C3m": CrystalSpec("C3m", "fcc", (3, 3, 3), 52, 250, 120, 100.0, ao_block=(2, 16), aux_block=(4, 64),
-                       seed=20260106),
+                       seed=20260106, atoms=4),
 }
 
 
@@ -198,7 +199,7 @@ def _rand_unitary(rng, n):
 
 
 def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool = False,
-                 with_V: bool = True) -> Crystal:
+                 with_V: bool = True, physical: bool = False) -> Crystal:
     """Build the crystal.  ``rotate=False`` keeps every k point (ink = nk,
     identity rotations), the reference's no-symmetry mode.
 
@@ -208,7 +209,12 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
     other pair slices empty; the stored blocks are identical to the full
     crystal's (every pair draws from its own random stream).  ``with_V=False``
     skips V (an empty array): the layout and one-body data only, e.g. to size
-    a configuration before generating it."""
+    a configuration before generating it.  ``physical=True`` (fcc) takes the
+    AO and aux block sizes of every star from the O_h irreps at its
+    representative k (:mod:`symmetry`: d blocks of size m per irrep of
+    dimension d and multiplicity m, for spec.atoms atoms with s/p/d shells)
+    instead of drawing them in the spec's ranges; block labels and the V
+    selection rule stay the labelled ones."""
     rng = np.random.default_rng(spec.seed)
     ops, inversion = _fcc_ops() if spec.lattice == "fcc" else _hex_ops()
     kmesh = _kmesh(spec.mesh)
@@ -224,12 +230,22 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
 
     # --- blocks per star (AO) and per {star(q), star(-q)} (aux)
     ao_sizes_star, ao_labels_star, aux_sizes_star, aux_labels_star = {}, {}, {}, {}
+    phys = None
+    if physical:
+        if spec.lattice != "fcc":
+            raise ValueError("physical block sizes are built for the fcc (O_h) crystals only")
+        from . import symmetry
+        Bt = np.linalg.inv(0.5 * np.array([[0, 1, 1], [1, 0, 1], [1, 1, 0]], dtype=float))
+        ops_c = symmetry.oh_operations()
+        bao, baux = symmetry.fcc_basis(spec.nao, spec.atoms), symmetry.fcc_basis(spec.naux, spec.atoms)
+        phys = {s: (np.array(symmetry.block_sizes(Bt @ kmesh[k], bao, ops_c)),
+                    np.array(symmetry.block_sizes(Bt @ kmesh[k], baux, ops_c))) for s, k in enumerate(reps)}
     for s, k in enumerate(reps):
         g = little[s]
         shrink = 1.0 / np.sqrt(max(1.0, g / 2.0))
         t_ao = spec.ao_block[0] + (spec.ao_block[1] - spec.ao_block[0]) * shrink
         t_aux = spec.aux_block[0] + (spec.aux_block[1] - spec.aux_block[0]) * shrink
-        sz = _partition(rng, spec.nao, spec.ao_block[0], spec.ao_block[1], t_ao)
+        sz = _partition(rng, spec.nao, spec.ao_block[0], spec.ao_block[1], t_ao) if phys is None else phys[s][0]
         ao_sizes_star[s] = np.array(sz)
         ao_labels_star[s] = rng.integers(0, 4, size=len(sz))
     for s, k in enumerate(reps):
@@ -239,7 +255,8 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
         g = little[s]
         shrink = 1.0 / np.sqrt(max(1.0, g / 2.0))
         t_aux = spec.aux_block[0] + (spec.aux_block[1] - spec.aux_block[0]) * shrink
-        sz = np.array(_partition(rng, spec.naux, spec.aux_block[0], spec.aux_block[1], t_aux))
+        sz = (np.array(_partition(rng, spec.naux, spec.aux_block[0], spec.aux_block[1], t_aux)) if phys is None
+              else phys[s][1])
         if ms == s:   # self-conjugate star: labels in {0, 2}
             lab = 2 * rng.integers(0, 2, size=len(sz))
             aux_sizes_star[s], aux_labels_star[s] = sz, lab

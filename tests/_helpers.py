@@ -47,12 +47,12 @@ def p_slices(layout, nts, P, t_list):
 
 
 @lru_cache(maxsize=8)
-def crystal(name, rotate=True, ns=None):
+def crystal(name, rotate=True, ns=None, physical=False):
     from mbsymmetry_gb300.crystal import CONFIGS, load_ir, make_crystal
     import dataclasses
     spec = CONFIGS[name]
     if ns is not None:
         spec = dataclasses.replace(spec, ns=ns)
-    cr = make_crystal(spec, rotate=rotate)
+    cr = make_crystal(spec, rotate=rotate, physical=physical)
     tr = build_transforms(load_ir(spec.nts), spec.beta)
     return cr, tr

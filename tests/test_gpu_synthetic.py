@@ -10,10 +10,13 @@ from oracle import Oracle
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name,rotate,ns", [("C1", True, 1), ("C1", True, 2), ("C1", False, 1)])
-def test_iteration_matches_oracle(name, rotate, ns):
+@pytest.mark.parametrize("name,rotate,ns,physical", [("C1", True, 1, False), ("C1", True, 2, False),
+                                                   ("C1", False, 1, False), ("C1", True, 1, True),
+                                                   ("C2", True, 1, True)])
+def test_iteration_matches_oracle(name, rotate, ns, physical):
+    """physical: block sizes from the O_h irreps (mbsymmetry_gb300.symmetry)."""
     from mbsymmetry_gb300.solver import GWSolver
-    cr, tr = crystal(name, rotate=rotate, ns=ns)
+    cr, tr = crystal(name, rotate=rotate, ns=ns, physical=physical)
     L = cr.layout
     s = GWSolver(L, ns, tr)
     s.set_shared_Coulomb(cr.V)

@@ -1,6 +1,7 @@
 """The C oracle against an independent numpy restatement on a rotated crystal
 (irreducible k only stored: exercises orep/auxrep rotations and conj)."""
 import numpy as np
+import pytest
 
 from _helpers import crystal
 from oracle import Oracle
@@ -31,8 +32,9 @@ def _rot_numpy(L, ns, nts, G_irr, blocks_of, rep, slice_sz, slice_off_irre, off_
     return out
 
 
-def test_rotated_p0_sigma_against_numpy():
-    cr, tr = crystal("C1")
+@pytest.mark.parametrize("physical", [False, True])
+def test_rotated_p0_sigma_against_numpy(physical):
+    cr, tr = crystal("C1", physical=physical)
     L, ns, nts = cr.layout, cr.ns, tr.nts
     assert L.ink < L.nk
     orc = Oracle(L, ns, nts)
