@@ -296,10 +296,10 @@ def run_gpu(args):
                 "contraction_tflops_alg": {"p0": stm["p0_flops"] / (mstage["p0_ms"] * 1e-3) / 1e12,
                                            "sigma": stm["sigma_flops"] / (mstage["sigma_ms"] * 1e-3) / 1e12}}
 
-    mixed = run_mixed("tf32x3", "tf32x3 (tcgen05 kind::tf32, 2 planes, 3 products, FP32 accumulate per "
-                                "contribution, FP64 across)")
-    mixed_bf16 = run_mixed("bf16x3", "bf16x3 (tcgen05 kind::f16, 3 BF16 planes, 6 products, FP32 accumulate per "
-                                     "contribution, FP64 across)")
+    mixed = run_mixed("tf32x3", "tf32x3 (tcgen05 kind::tf32, 2 planes, 3 products, FP32 accumulate within an aux "
+                                "block or aux-row chunk, FP64 across)")
+    mixed_bf16 = run_mixed("bf16x3", "bf16x3 (tcgen05 kind::f16, 3 BF16 planes, 6 products, FP32 accumulate within "
+                                     "an aux block or aux-row chunk, FP64 across)")
 
     # ---- tile-shape autotuner (mbsymmetry_gb300/autotune.py) on this workload ---
     from mbsymmetry_gb300 import autotune as _autotune
