@@ -12,9 +12,12 @@
 // (1) runs here as a tcgen05 GEMM on split operands (TF32x3: kind::tf32, two
 // planes, three products; BF16x3: kind::f16, three BF16 planes, six products;
 // FP32 accumulation in TMEM) writing W to HBM in FP32, one tau chunk at a time;
-// (2) and (3) run per (owner, tau range, slice of contributions) in FP32 with
-// FP64 accumulation across contributions, writing FP64 partial blocks that
-// reduce_slices_kernel sums in order.
+// (2) and (3) run per (owner, tau range, slice of contributions): (2) on CUDA
+// cores in FP32, written split into the operand planes of (3), which runs as a
+// tcgen05 GEMM with rows (tau, j) and K = (Q, m) (sigma_uvt_kernel; the FP32
+// SIMT kernels sigma_uv_{blocked,small} take AO blocks above 64).  FP32
+// accumulates within an aux-row chunk, FP64 above; every tile writes an FP64
+// partial block that reduce_slices_kernel sums in order.
 #include "common.h"
 #include "kernels.h"
 #include "kernels_tc.h"
