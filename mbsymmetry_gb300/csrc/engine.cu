@@ -1884,7 +1884,7 @@ static int on_handle(gwgb_handle h, F &&f) {
 
 extern "C" {
 
-const char *gwgb_version(void) { return "gwgb 0.3 (sm_103a, FP64, TF32x3 and BF16x3 contraction paths)"; }
+const char *gwgb_version(void) { return "gwgb 0.4 (sm_103a; FP64, TF32x3 and BF16x3 contraction paths)"; }
 
 const char *gwgb_last_error(void) { return gwgb::g_last_error.c_str(); }
 
