@@ -120,10 +120,21 @@ def _setup():
     return cr, tr
 
 
-def _cpu_reference(cr, tr, steps, threads=0):
+def _host_cores():
+    """Cores this process may run on (torchrun sets OMP_NUM_THREADS=1 for its
+    ranks; the CPU timings use every core they have)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def _cpu_reference(cr, tr, steps, threads=None):
     """Time the FP64 CPU oracle on a bounded sample: G rotation, P0 and Sigma
     for a subset of tau points, the full W~ solve and the full Dyson step;
-    contraction times are scaled to all tau points."""
+    contraction times are scaled to all tau points.  threads: all host cores
+    by default."""
+    threads = _host_cores() if threads is None else threads
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle  # the CPU baseline (restatement of the reference's CPU path)
     L, nts, ns = cr.layout, tr.nts, cr.ns
@@ -387,7 +398,7 @@ def run_gpu(args):
                   "fp64_tflops_measured": fp64_peak},
     }
     s.close()
-    if reps.reports and not args.no_cpu_baseline:
+    if reps.reports and world == 1 and not args.no_cpu_baseline:  # rank 0 at N = 1 only
         v, cores, sample = _cpu_reference(cr, tr, 1)
         line["cpu_baseline"] = {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample}
     if reps.reports:
