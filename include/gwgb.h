@@ -197,6 +197,14 @@ int gwgb_solve_Pq(gwgb_handle h);
  * Replaces cugw_solver_block_t::solve_sigma (cugw_solver_block.cpp:86-112, 192-252). */
 int gwgb_solve_sigma(gwgb_handle h);
 
+/* The Sigma contraction alone, from the handle's G and its P buffer as it is
+ * (gwgb_set_P0 or the last gwgb_solve_Pq), without recomputing P0: the Sigma
+ * half of cugw_solver_block_t::solve (cugw_solver_block.cpp:192-252).  With
+ * P = identity at tau = 0 and G = a density matrix at tau = 0, Sigma(tau = 0)
+ * is the Hartree-Fock exchange on the block engine (mbsymmetry_gb300
+ * solver.hf_exchange). */
+int gwgb_solve_sigma_from_P(gwgb_handle h);
+
 /* Full GW self-energy: P0 -> P~ -> Sigma.  Replaces
  * cugw_solver_block_t::solve (cugw_solver_block.cpp:34-65, 254-315). */
 int gwgb_solve(gwgb_handle h);

@@ -297,6 +297,7 @@ class Engine {
   void solve_P0();
   void solve_Pq();
   void solve_sigma();
+  void solve_sigma_from_P();
   void solve();
   void dyson(double mu);
   void iteration(double mu);
@@ -1531,6 +1532,19 @@ void Engine::solve_sigma() {
   finish_stats(false, true);
 }
 
+// The Sigma stage alone on the handle's G and P buffers (P0 is not recomputed).
+void Engine::solve_sigma_from_P() {
+  require_ready(false);
+  prepare_operands();
+  record(0);
+  k_rotate_G();
+  for (int i = 1; i <= 4; ++i) record(i);
+  k_sigma();
+  record(5);
+  record(6);
+  finish_stats(false, true);
+}
+
 void Engine::solve() {
   require_ready(true);
   prepare_operands();
@@ -1931,6 +1945,7 @@ GWGB_FORWARD(gwgb_get_P0, (gwgb_handle h, double *P), e.get_P0(P))
 GWGB_FORWARD(gwgb_solve_P0, (gwgb_handle h), e.solve_P0())
 GWGB_FORWARD(gwgb_solve_Pq, (gwgb_handle h), e.solve_Pq())
 GWGB_FORWARD(gwgb_solve_sigma, (gwgb_handle h), e.solve_sigma())
+GWGB_FORWARD(gwgb_solve_sigma_from_P, (gwgb_handle h), e.solve_sigma_from_P())
 GWGB_FORWARD(gwgb_solve, (gwgb_handle h), e.solve())
 GWGB_FORWARD(gwgb_dyson, (gwgb_handle h, double mu), e.dyson(mu))
 GWGB_FORWARD(gwgb_iteration, (gwgb_handle h, double mu), e.iteration(mu))

@@ -215,6 +215,32 @@ class GWSolver:
     def synchronize(self):
         _abi.check(self.lib.gwgb_synchronize(self.h))
 
+    def solve_sigma_from_P(self):
+        """The Sigma contraction from the current G and P buffers (P0 is not recomputed)."""
+        _abi.check(self.lib.gwgb_solve_sigma_from_P(self.h))
+
+    def hf_exchange(self, rho: np.ndarray) -> np.ndarray:
+        """Hartree-Fock exchange on the block engine,
+            K(k) = -(1/nk) sum_k2 sum_Q V^Q(k, k2) rho(k2) V^Q(k, k2)^H,
+        as the Sigma contraction with P = identity and G = rho at tau = 0 (the
+        reference's HF solver is a stub, cuhf_solver_block.h:36-39).  rho and the
+        result: [s][flat_ao] over the stored k.  Overwrites the handle's G, P and Sigma."""
+        L = self.layout
+        fa = L.flat_ao_size
+        rho = np.ascontiguousarray(rho, dtype=np.complex128).reshape(self.ns, fa)
+        G = np.zeros(self.g_size, np.complex128)
+        G[:self.ns * fa] = rho.ravel()
+        P = np.zeros(self.p_size, np.complex128)
+        for r, q in enumerate(L.irre_list):
+            base = self.nts * L.qaux_slice_offsets_irre[r]
+            for iq, qb in enumerate(L.aux_sizes[q]):
+                o = base + L.aux_offsets[q][iq]
+                P[o:o + qb * qb] = np.eye(qb).ravel()
+        self.set_G(G)
+        self.set_P0(P)
+        self.solve_sigma_from_P()
+        return self.Selfenergy()[:self.ns * fa].reshape(self.ns, fa).copy()
+
     def refproxy(self, nt_batch: int = 4, nstreams: int = 16) -> dict:
         """Run the reference's cuBLAS call sequence for P0 and Sigma on this
         GPU (measurement only; gwgb_refproxy_run).  P0 comes from the current G,
