@@ -205,6 +205,15 @@ int gwgb_solve_sigma(gwgb_handle h);
  * solver.hf_exchange). */
 int gwgb_solve_sigma_from_P(gwgb_handle h);
 
+/* Hartree (direct) term of HF from the handle's G at tau = 0 taken as the
+ * density matrix rho: J(k)_ij = sum_Q V^Q_ij(k, k) c_Q with
+ * c_Q = (f / nk) sum_{k', s} sum_ab V^Q_ab(k', k') rho_s(k')_ba over the full
+ * BZ (f = 2 for ns = 1, 1 for ns = 2), for the diagonal AO blocks of the
+ * stored k; J: flat_ao complex (spin independent).  With the exchange of
+ * gwgb_solve_sigma_from_P this is HF on the block layout (the reference's HF
+ * solver is a stub, SymmetryMBPT/include/solver/cuhf_solver_block.h:36-39). */
+int gwgb_hf_hartree(gwgb_handle h, double *J);
+
 /* Full GW self-energy: P0 -> P~ -> Sigma.  Replaces
  * cugw_solver_block_t::solve (cugw_solver_block.cpp:34-65, 254-315). */
 int gwgb_solve(gwgb_handle h);

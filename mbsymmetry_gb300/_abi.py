@@ -102,6 +102,7 @@ SIGNATURES = {
     "gwgb_solve_Pq": (c_int32, [c_void_p]),
     "gwgb_solve_sigma": (c_int32, [c_void_p]),
     "gwgb_solve_sigma_from_P": (c_int32, [c_void_p]),
+    "gwgb_hf_hartree": (c_int32, [c_void_p, c_void_p]),
     "gwgb_solve": (c_int32, [c_void_p]),
     "gwgb_dyson": (c_int32, [c_void_p, c_double]),
     "gwgb_iteration": (c_int32, [c_void_p, c_double]),

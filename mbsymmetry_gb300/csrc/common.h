@@ -137,4 +137,27 @@ struct InvTask {
   int32_t w;       // frequency index (Dyson) or -1
 };
 
+// Hartree (direct) term of HF on the block layout, from q = 0 V blocks:
+//   c[Q] = scale sum_{k', s} sum_{a,b} V^Q_ab(k', k') rho_s(k')_ba,
+//   J(k)_ij = sum_Q V^Q_ij(k, k) c[Q]   (diagonal AO blocks, i1 = i2).
+struct HcItem {    // one V block of pair (k', k') and rho(k') of its AO block
+  int64_t v;       // V block [qb][b][b]
+  int64_t g;       // rho block at spin 0 (G at tau = 0)
+  int32_t gstride; // spin stride of G
+  int32_t b;
+};
+struct HcTask {    // c over one aux block of q = 0: items [i0, i1) summed in order
+  int64_t cout;
+  int32_t qb, i0, i1, pad;
+};
+struct HjItem {    // one V block of pair (k, k) and its aux block's c
+  int64_t v;
+  int64_t c;
+  int32_t qb, pad;
+};
+struct HjTask {    // J over one AO block of a stored k: items [i0, i1) summed in order
+  int64_t out;
+  int32_t b, i0, i1, pad;
+};
+
 }  // namespace gwgb

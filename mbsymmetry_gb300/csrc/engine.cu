@@ -307,6 +307,7 @@ class Engine {
   void energy(double *e_corr, double *e_one);
   void sc_loop(int niter, double alpha, const gwgb_mu_search &ms, int final_fp64, gwgb_sc_record *out);
   void refproxy(int nt_batch, int nstreams, gwgb_proxy_stats *out);
+  void hf_hartree(double *J);
   void refproxy_get(double *P0, double *S);
   void stats(gwgb_stats *out) const {
     *out = stats_;
@@ -331,6 +332,12 @@ class Engine {
   int tune_uvt_kb_ = 0, tune_npk_ = 64, tune_waves_ = 8, tune_simt_ = 0;  // tile-shape settings (gwgb_params)
   bool have_V_ = false, have_T_ = false, have_F_ = false, have_reps_ = false;
   DBuf<double2> px_p0_, px_sig_;  // results of the reference-GPU proxy
+  // Hartree term of HF: work lists, c over the q = 0 aux slice, J over the stored k
+  DBuf<HcTask> hart_ct_;
+  DBuf<HcItem> hart_ci_;
+  DBuf<HjTask> hart_jt_;
+  DBuf<HjItem> hart_ji_;
+  DBuf<double2> hart_c_, hart_J_;
   bool px_ready_ = false;
 
   // device data
@@ -667,6 +674,64 @@ void Engine::build_work_lists() {
   }
   const int64_t po = (int64_t)nts_ * fq;
   Pall_.alloc((size_t)po);
+
+  {  // Hartree term: q = 0 V blocks with equal AO blocks on both sides
+    int q0 = -1;
+    for (int q = 0; q < nk && q0 < 0; ++q)
+      if (l.mom_cons(0, 0, q) == 0) q0 = q;
+    GWGB_REQUIRE(q0 >= 0, GWGB_E_INVALID, "the k mesh has no zero-momentum point");
+    std::vector<HcTask> ct;
+    std::vector<HcItem> ci;
+    std::vector<HjTask> jt;
+    std::vector<HjItem> ji;
+    for (int iq = 0; iq < l.naux_blocks(q0); ++iq) {
+      const int i0 = (int)ci.size();
+      for (int k = 0; k < nk; ++k) {
+        const int p = k * nk + k;
+        for (int b = l.kp_ptr[p]; b < l.kp_ptr[p + 1]; ++b) {
+          if (l.ti[3 * b] != iq || l.ti[3 * b + 1] != l.ti[3 * b + 2]) continue;
+          const int i1 = l.ti[3 * b + 1];
+          ci.push_back({l.kp_off[p] + l.t_off[b], gref[k].base + l.aooff(k, i1), gref[k].stride, l.aosz(k, i1)});
+        }
+      }
+      ct.push_back({l.auxoff(q0, iq), l.auxsz(q0, iq), i0, (int)ci.size(), 0});
+    }
+    for (int ik = 0; ik < ink; ++ik) {
+      const int k = l.irre_list[ik], p = k * nk + k;
+      for (int i1 = 0; i1 < l.nao_blocks(k); ++i1) {
+        const int i0 = (int)ji.size();
+        for (int b = l.kp_ptr[p]; b < l.kp_ptr[p + 1]; ++b) {
+          if (l.ti[3 * b + 1] != i1 || l.ti[3 * b + 2] != i1) continue;
+          const int iq = l.ti[3 * b];
+          ji.push_back({l.kp_off[p] + l.t_off[b], l.auxoff(q0, iq), l.auxsz(q0, iq), 0});
+        }
+        jt.push_back({l.kao_off_irre[ik] + l.aooff(k, i1), l.aosz(k, i1), i0, (int)ji.size(), 0});
+      }
+    }
+    const int64_t qs0 = l.qaux_sz[q0];
+    for (const HcTask &t : ct) {
+      check_range(t.cout, t.qb, qs0, "Hartree c block");
+      for (int i = t.i0; i < t.i1; ++i) {
+        const HcItem &x = ci[i];
+        check_range(x.v, (int64_t)t.qb * x.b * x.b, l.flat_V, "Hartree V block");
+        check_range(x.g, (int64_t)(ns_ - 1) * x.gstride + (int64_t)x.b * x.b, go, "Hartree rho block");
+      }
+    }
+    for (const HjTask &t : jt) {
+      check_range(t.out, (int64_t)t.b * t.b, fa, "Hartree J block");
+      for (int i = t.i0; i < t.i1; ++i) {
+        const HjItem &x = ji[i];
+        check_range(x.v, (int64_t)x.qb * t.b * t.b, l.flat_V, "Hartree V block");
+        check_range(x.c, x.qb, qs0, "Hartree c block");
+      }
+    }
+    hart_ct_.upload(ct, st_);
+    hart_ci_.upload(ci, st_);
+    hart_jt_.upload(jt, st_);
+    hart_ji_.upload(ji, st_);
+    hart_c_.alloc((size_t)std::max<int64_t>(1, qs0));
+    hart_J_.alloc((size_t)std::max<int64_t>(1, fa));
+  }
   for (const RotTask &t : rg) {  // G rotations: batch = nts * ns
     const int64_t nb = (int64_t)nts_ * ns_;
     check_range(t.dst, (nb - 1) * t.dstride + (t.rotate ? (int64_t)t.m * t.m : t.m), go, "G rotation target");
@@ -1532,6 +1597,19 @@ void Engine::solve_sigma() {
   finish_stats(false, true);
 }
 
+// Hartree term of HF from the handle's G at tau = 0 (a density matrix): J over
+// the stored k, [flat_ao].  Closed-shell factor 2 for ns = 1.
+void Engine::hf_hartree(double *J) {
+  GWGB_REQUIRE(J, GWGB_E_INVALID, "NULL J");
+  require_ready(false);
+  k_rotate_G();
+  launch_hartree(hart_ct_.p, (int)hart_ct_.n, hart_ci_.p, hart_jt_.p, (int)hart_jt_.n, hart_ji_.p, V_.p, Gall_.p,
+                 ns_, (ns_ == 1 ? 2.0 : 1.0) / l_.nk, hart_c_.p, hart_J_.p, st_);
+  GWGB_CUDA(cudaMemcpyAsync(J, hart_J_.p, (size_t)l_.flat_ao * sizeof(double2), cudaMemcpyDeviceToHost, st_));
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  check_device_flags();
+}
+
 // The Sigma stage alone on the handle's G and P buffers (P0 is not recomputed).
 void Engine::solve_sigma_from_P() {
   require_ready(false);
@@ -1946,6 +2024,7 @@ GWGB_FORWARD(gwgb_solve_P0, (gwgb_handle h), e.solve_P0())
 GWGB_FORWARD(gwgb_solve_Pq, (gwgb_handle h), e.solve_Pq())
 GWGB_FORWARD(gwgb_solve_sigma, (gwgb_handle h), e.solve_sigma())
 GWGB_FORWARD(gwgb_solve_sigma_from_P, (gwgb_handle h), e.solve_sigma_from_P())
+GWGB_FORWARD(gwgb_hf_hartree, (gwgb_handle h, double *J), e.hf_hartree(J))
 GWGB_FORWARD(gwgb_solve, (gwgb_handle h), e.solve())
 GWGB_FORWARD(gwgb_dyson, (gwgb_handle h, double mu), e.dyson(mu))
 GWGB_FORWARD(gwgb_iteration, (gwgb_handle h, double mu), e.iteration(mu))

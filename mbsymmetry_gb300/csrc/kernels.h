@@ -58,4 +58,9 @@ void launch_inverse(const InvTask *tasks, int ntasks, int nmax, double2 *W, cons
 void launch_leakage(const TSlab *slabs, int nslabs, const double2 *G, const double *tf, const double *tl,
                     int ncheb, unsigned long long *out, cudaStream_t st);
 
+// Hartree term: c over the aux blocks of q = 0, then J over the AO blocks of the stored k.
+void launch_hartree(const HcTask *ct, int nct, const HcItem *ci, const HjTask *jt, int njt, const HjItem *ji,
+                    const double2 *V, const double2 *G, int ns, double scale, double2 *c, double2 *J,
+                    cudaStream_t st);
+
 }  // namespace gwgb

@@ -698,6 +698,56 @@ void launch_p0_fp64(const P0Tile *tiles, int ntiles, int maxo, const P0Contrib *
   GWGB_CUDA(cudaGetLastError());
 }
 
+// Hartree term (HF on the block layout; the reference's HF solver is a stub,
+// cuhf_solver_block.h:36-39).  One thread per aux index Q (c) or per element of
+// an AO block (J); every sum runs over its items in list order (deterministic).
+__global__ void hartree_c_kernel(const HcTask *__restrict__ tasks, const HcItem *__restrict__ items,
+                                 const double2 *__restrict__ V, const double2 *__restrict__ G, int ns,
+                                 double scale, double2 *__restrict__ c) {
+  const HcTask t = tasks[blockIdx.x];
+  for (int Q = threadIdx.x; Q < t.qb; Q += blockDim.x) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int it = t.i0; it < t.i1; ++it) {
+      const HcItem x = items[it];
+      const double2 *vq = V + x.v + (int64_t)Q * x.b * x.b;
+      for (int s = 0; s < ns; ++s) {
+        const double2 *r = G + x.g + (int64_t)s * x.gstride;
+        for (int a = 0; a < x.b; ++a)
+          for (int b = 0; b < x.b; ++b) acc = cfma(vq[a * x.b + b], r[b * x.b + a], acc);
+      }
+    }
+    c[t.cout + Q] = make_double2(acc.x * scale, acc.y * scale);
+  }
+}
+
+__global__ void hartree_j_kernel(const HjTask *__restrict__ tasks, const HjItem *__restrict__ items,
+                                 const double2 *__restrict__ V, const double2 *__restrict__ c,
+                                 double2 *__restrict__ J) {
+  const HjTask t = tasks[blockIdx.x];
+  const int bb = t.b * t.b;
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int it = t.i0; it < t.i1; ++it) {
+      const HjItem x = items[it];
+      for (int Q = 0; Q < x.qb; ++Q) acc = cfma(V[x.v + (int64_t)Q * bb + e], c[x.c + Q], acc);
+    }
+    J[t.out + e] = acc;
+  }
+}
+
+void launch_hartree(const HcTask *ct, int nct, const HcItem *ci, const HjTask *jt, int njt, const HjItem *ji,
+                    const double2 *V, const double2 *G, int ns, double scale, double2 *c, double2 *J,
+                    cudaStream_t st) {
+  if (nct > 0) {
+    hartree_c_kernel<<<nct, 128, 0, st>>>(ct, ci, V, G, ns, scale, c);
+    GWGB_CUDA(cudaGetLastError());
+  }
+  if (njt > 0) {
+    hartree_j_kernel<<<njt, 128, 0, st>>>(jt, ji, V, c, J);
+    GWGB_CUDA(cudaGetLastError());
+  }
+}
+
 void launch_reduce_slices(const RedTask *tasks, int ntasks, const double2 *part, double2 *out, int nts,
                           double scale, int mirror, cudaStream_t st) {
   if (ntasks == 0) return;

@@ -241,6 +241,20 @@ class GWSolver:
         self.solve_sigma_from_P()
         return self.Selfenergy()[:self.ns * fa].reshape(self.ns, fa).copy()
 
+    def hf_hartree(self, rho: np.ndarray) -> np.ndarray:
+        """Hartree (direct) term J(k) = sum_Q V^Q(k, k) c_Q, c_Q = (f/nk) sum_{k', s}
+        Tr[V^Q(k', k') rho_s(k')] (f = 2 for ns = 1), on the diagonal AO blocks of the
+        stored k (gwgb_hf_hartree).  rho: [s][flat_ao]; returns [s][flat_ao] (the same J
+        for every spin).  Overwrites the handle's G."""
+        fa = self.layout.flat_ao_size
+        rho = np.ascontiguousarray(rho, dtype=np.complex128).reshape(self.ns, fa)
+        G = np.zeros(self.g_size, np.complex128)
+        G[:self.ns * fa] = rho.ravel()
+        self.set_G(G)
+        J = np.zeros(fa, np.complex128)
+        _abi.check(self.lib.gwgb_hf_hartree(self.h, J.ctypes.data))
+        return np.tile(J, (self.ns, 1))
+
     def refproxy(self, nt_batch: int = 4, nstreams: int = 16) -> dict:
         """Run the reference's cuBLAS call sequence for P0 and Sigma on this
         GPU (measurement only; gwgb_refproxy_run).  P0 comes from the current G,

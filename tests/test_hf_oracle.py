@@ -60,3 +60,56 @@ def test_oracle_exchange_equals_direct_formula():
                     Kd[s, o1:o1 + b1 * b1] -= np.einsum("qim,mn,qjn->ij", V, R, V.conj()).ravel() / L.nk
     assert np.abs(K - Kd).max() < 1e-12 * max(1.0, np.abs(Kd).max())
     assert np.abs(Kd).max() > 1e-3
+
+
+def hf_hartree_numpy(cr, tr, rho):
+    """J(k) = sum_Q V^Q(k, k) c_Q, c_Q = (f/nk) sum_{k', s} Tr[V^Q(k', k') rho_s(k')]
+    (f = 2 for ns = 1) on the diagonal AO blocks; rho of every k' from the oracle's
+    rotation.  Returns (J [flat_ao], c)."""
+    L, ns, nts = cr.layout, cr.ns, tr.nts
+    fa, nk = L.flat_ao_size, L.nk
+    orc = Oracle(L, ns, nts)
+    G = np.zeros(nts * ns * fa, np.complex128)
+    G[:ns * fa] = rho.ravel()
+    Gf = orc.rotate_G(G)
+    q0 = next(q for q in range(nk) if L.mom_cons(0, 0, q) == 0)
+    f = (2.0 if ns == 1 else 1.0) / nk
+    c = np.zeros(L.qaux_slice_sizes[q0], np.complex128)
+    for k in range(nk):
+        p = k * nk + k
+        for b, (iq, i1, i2) in enumerate(L.tensor_irreps[p]):
+            if i1 != i2:
+                continue
+            qb, bs = L.aux_sizes[q0][iq], L.ao_sizes[k][i1]
+            o = L.kpair_slice_offsets[p] + L.tensor_offsets[p][b]
+            V = cr.V[o:o + qb * bs * bs].reshape(qb, bs, bs)
+            for s in range(ns):
+                og = L.kao_slice_offsets[k] * ns * nts + s * L.kao_slice_sizes[k] + L.ao_offsets[k][i1]
+                R = Gf[og:og + bs * bs].reshape(bs, bs)
+                c[L.aux_offsets[q0][iq]:L.aux_offsets[q0][iq] + qb] += f * np.einsum("qab,ba->q", V, R)
+    J = np.zeros(fa, np.complex128)
+    for ik, k in enumerate(L.irre_list):
+        p = k * nk + k
+        for b, (iq, i1, i2) in enumerate(L.tensor_irreps[p]):
+            if i1 != i2:
+                continue
+            qb, bs = L.aux_sizes[q0][iq], L.ao_sizes[k][i1]
+            o = L.kpair_slice_offsets[p] + L.tensor_offsets[p][b]
+            V = cr.V[o:o + qb * bs * bs].reshape(qb, bs, bs)
+            oj = L.kao_slice_offsets_irre[ik] + L.ao_offsets[k][i1]
+            J[oj:oj + bs * bs] += np.einsum("qij,q->ij", V, c[L.aux_offsets[q0][iq]:L.aux_offsets[q0][iq] + qb]).ravel()
+    return J, c
+
+
+def test_hartree_is_hermitian_with_real_density_coefficients():
+    """V(k, k) is Hermitian for every Q and rho is Hermitian, so c_Q is real and every J block Hermitian."""
+    cr, tr = crystal("C1")
+    rho = density(cr)
+    J, c = hf_hartree_numpy(cr, tr, rho)
+    L = cr.layout
+    assert np.abs(c.imag).max() < 1e-12 * max(1.0, np.abs(c).max()) and np.abs(c).max() > 1e-3
+    for ik, k in enumerate(L.irre_list):
+        for ib, bs in enumerate(L.ao_sizes[k]):
+            o = L.kao_slice_offsets_irre[ik] + L.ao_offsets[k][ib]
+            B = J[o:o + bs * bs].reshape(bs, bs)
+            assert np.abs(B - B.conj().T).max() < 1e-12 * max(1.0, np.abs(J).max())
