@@ -52,7 +52,10 @@ def autotune(layout, ns, transforms, V, F, S, mu, G=None, precision="tf32x3", ca
     The metric is the Sigma stage (the stage the settings shape) of `reps`
     iterations after `warmup`; each trial also records the whole iteration.
     With ``cache`` (a JSON file path) an earlier result for the same
-    fingerprint is returned without timing, and new results are added."""
+    fingerprint is returned without timing, and new results are added.
+    Each candidate is a full handle with V in device memory, built and closed
+    in turn: the device needs room for one such handle besides any the caller
+    holds (at C5 scale, 180 GB, tune before creating the working handle)."""
     key = fingerprint(layout, transforms.nts, precision)
     store = {}
     if cache and os.path.exists(cache):
