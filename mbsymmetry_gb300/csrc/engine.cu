@@ -635,6 +635,7 @@ void Engine::build_work_lists() {
     go += (int64_t)nts_ * ns_ * l.kao_sz[k];
   }
   Gall_.alloc((size_t)go);
+  GWGB_CUDA(cudaMemsetAsync(Gall_.p, 0, Gall_.n * sizeof(double2), st_));  // defined (zero) before set_G
 
   // --- P sources.  Sigma reads P~(q) only as V P~(q) V^H.  With P~(q) =
   //     O P~(q') O^H for the irreducible q' (conjugated for a time-reversal
@@ -674,6 +675,7 @@ void Engine::build_work_lists() {
   }
   const int64_t po = (int64_t)nts_ * fq;
   Pall_.alloc((size_t)po);
+  GWGB_CUDA(cudaMemsetAsync(Pall_.p, 0, Pall_.n * sizeof(double2), st_));
 
   {  // Hartree term: q = 0 V blocks with equal AO blocks on both sides
     int q0 = -1;
