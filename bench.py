@@ -23,6 +23,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -67,7 +68,7 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"gwgb_clocks_{os.getpid()}_dev{device}.csv")
 
     def __enter__(self):
         try:
@@ -256,17 +257,22 @@ def run_gpu(args):
 
     # ---- roofline of the dominant kernel ---------------------------------
     peaks = _load_peaks()
-    probe = ctypes.CDLL(os.path.join(ROOT, "mbsymmetry_gb300", "csrc", "probe", "libgwgb_probe.so"))
-    probe.gwgb_probe_fp64_tflops.restype = ctypes.c_double
-    probe.gwgb_probe_fp64_tflops.argtypes = [ctypes.c_int]
+    probe = ctypes.CDLL(os.path.join(ROOT, "peaks", "libgwgb_peaks.so"))
+    for fn in ("gwgb_probe_fp64_tflops", "gwgb_probe_dmma_tflops"):
+        getattr(probe, fn).restype = ctypes.c_double
+        getattr(probe, fn).argtypes = [ctypes.c_int]
+    probe.gwgb_probe_tc_tflops.restype = ctypes.c_double
+    probe.gwgb_probe_tc_tflops.argtypes = [ctypes.c_int, ctypes.c_int]
     fp64_peak = probe.gwgb_probe_fp64_tflops(dev)
+    dmma_peak = probe.gwgb_probe_dmma_tflops(dev)
+    tf32_peak = probe.gwgb_probe_tc_tflops(dev, 0)
+    bf16_tc_peak = probe.gwgb_probe_tc_tflops(dev, 1)
     dom = "sigma" if stages["sigma_ms"] >= stages["p0_ms"] else "p0"
     flops = st[f"{dom}_flops"]
     dom_ms = stages[f"{dom}_ms"]
     achieved = flops / (dom_ms * 1e-3) / 1e12
     # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the same
-    # kernel on this workload, from the ncu capture summarised in
-    # profiles/c2_contraction_kernels.md; the kernels are FP64-pipe bound.
+    # kernel on this workload from one ncu capture; the kernels are FP64-pipe bound.
     traffic = {"sigma": 0.0703e9, "p0": 0.0563e9}[dom]
     roofline = {"bound": "tensor", "kernel": f"{dom}_fp64_kernel", "achieved": achieved, "peak": fp64_peak,
                 "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": traffic,
@@ -335,8 +341,6 @@ def run_gpu(args):
              "speedup_fp64_kernels": px_s / ((stages["p0_ms"] + stages["sigma_ms"]) / 1e3),
              "speedup_tf32x3_kernels": px_s / ((mixed["stages_ms"]["p0_ms"] + mixed["stages_ms"]["sigma_ms"]) / 1e3)}
 
-    # replicas: every rank runs the whole iteration, so the job completes `world`
-    # iterations per max-over-ranks time
     # ---- self-consistent loop: 10 graph-launched iterations, alpha = 0.5 ----
     # Each iteration: GW Sigma, linear mixing, device-side mu search (half
     # filling, N = nao), Dyson, energies.  FP64 throughout, and TF32x3 with the
@@ -361,7 +365,7 @@ def run_gpu(args):
     sc["speedup"] = sc["fp64"]["s_per_iteration"] / sc["tf32x3_final_fp64"]["s_per_iteration"]
 
     line = {
-        "metric": METRIC, "value": reps.job_seconds_per_iteration(ms), "unit": "s", "n_gpus": world,
+        "metric": METRIC, "value": reps.seconds_per_iteration(ms), "unit": "s", "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",

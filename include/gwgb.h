@@ -338,9 +338,12 @@ int gwgb_test_wait_timeout(int32_t device, int32_t polls);
  * P(i Omega) buffer and the task lists) lives in one static device array of
  * GWGB_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
  * exit; the call allocates nothing.  The first call on a device performs the
- * set-up (looks up the array's device address, sets kernel limits): make it
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race, so serialise them.  The call synchronises `stream`.
+ * set-up (looks up the array's device address, sets the block-inverse kernels'
+ * shared-memory limits).  All calls share the array: calls that overlap on
+ * the GPU race, so serialise them.  Every call reads a status word back to
+ * the host and synchronises `stream`, so no call (first or later) can be
+ * recorded into a CUDA graph.  The host thread's current device is restored
+ * before the call returns.
  *   P0_t   device, [nts][qslice] complex: P0(tau) of the q slice, all nts rows
  *          (mirrored, as after gwgb_solve); may alias P_t
  *   P_t    device, [nts][qslice] complex output P~(tau)

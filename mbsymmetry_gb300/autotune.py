@@ -10,7 +10,8 @@ sw_npk_max (widest W-GEMM pack) and uv_waves (contribution slices per tau).
 ``autotune`` times a small candidate set on the caller's own layout and data
 (one handle per candidate, CUDA-event timing of the Sigma stage of full
 iterations) and returns the fastest; ``cache`` stores results keyed by a
-fingerprint of the layout's block sizes, nts and precision.
+fingerprint of the layout's block sizes, nts, precision, the library version
+and the GPU model.
 """
 import hashlib
 import json
@@ -32,9 +33,26 @@ DEFAULT_CANDIDATES = (
 )
 
 
-def fingerprint(layout, nts: int, precision: str) -> str:
-    """Hash of what the tile rules see: block sizes per k / q, the V block list, nts, precision."""
+def _device_key(device: int) -> str:
+    """Library version plus the GPU's name, SM count and shared memory per block:
+    a cached setting is reused only with the same kernels on the same kind of GPU."""
+    from . import _abi
+    key = _abi.load().gwgb_version().decode()
+    try:
+        import torch
+        if torch.cuda.is_available():
+            p = torch.cuda.get_device_properties(device)
+            key += f"|{p.name}|{p.multi_processor_count}|{getattr(p, 'shared_memory_per_block_optin', 0)}"
+    except Exception:  # noqa: BLE001 - no device information: the key holds the library version only
+        pass
+    return key
+
+
+def fingerprint(layout, nts: int, precision: str, device: int = 0) -> str:
+    """Hash of what the tile rules see (block sizes per k / q, the V block list,
+    nts, precision) and of the kernels and GPU that were timed."""
     h = hashlib.sha256()
+    h.update(_device_key(device).encode())
     for arrs in (layout.ao_sizes, layout.aux_sizes, layout.tensor_irreps):
         for a in arrs:
             h.update(np.ascontiguousarray(a, dtype=np.int64).tobytes())
@@ -56,7 +74,7 @@ def autotune(layout, ns, transforms, V, F, S, mu, G=None, precision="tf32x3", ca
     Each candidate is a full handle with V in device memory, built and closed
     in turn: the device needs room for one such handle besides any the caller
     holds (at C5 scale, 180 GB, tune before creating the working handle)."""
-    key = fingerprint(layout, transforms.nts, precision)
+    key = fingerprint(layout, transforms.nts, precision, device)
     store = {}
     if cache and os.path.exists(cache):
         with open(cache) as f:

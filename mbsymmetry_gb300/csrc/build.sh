@@ -16,5 +16,4 @@ for src in "$HERE"/*.cu; do
 done
 for p in $pids; do wait $p; done
 $NVCC -gencode arch=compute_103a,code=sm_103a -shared -o "$OUT" "$BUILD"/*.o -lcudart_static -lrt -lpthread -ldl
-$NVCC $FLAGS -shared -o "$HERE/probe/libgwgb_probe.so" "$HERE/probe/peaks.cu" -lcudart_static -lrt -lpthread -ldl
 echo "built $OUT"

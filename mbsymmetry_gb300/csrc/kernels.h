@@ -21,6 +21,8 @@ __host__ __device__ constexpr int inv_smem_bytes(int nmax) {
 __host__ __device__ constexpr int rotate_smem_bytes(int nmax) { return 3 * nmax * nmax * 16; }
 
 void set_fp64_kernel_attributes(int smem_bytes);
+// The shared-memory limits of the two block-inverse kernels only (sizes fixed by MAX_BLOCK).
+void set_inverse_kernel_attributes();
 
 // FP64 contractions: each tile writes its partial block to Part[tile.part];
 // launch_reduce_slices then sums the slices in order into P0 / Sigma.

@@ -836,6 +836,10 @@ void set_fp64_kernel_attributes(int smem_bytes) {
   GWGB_CUDA(cudaFuncSetAttribute(sigma_fp64_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(sigma_fp64_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
   GWGB_CUDA(cudaFuncSetAttribute(rotate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rotate_smem_bytes(MAX_BLOCK)));
+  set_inverse_kernel_attributes();
+}
+
+void set_inverse_kernel_attributes() {
   GWGB_CUDA(cudaFuncSetAttribute(inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, inv_smem_bytes(MAX_BLOCK)));
   GWGB_CUDA(cudaFuncSetAttribute(inverse_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  inv_cta_smem_bytes(MAX_BLOCK)));

@@ -13,12 +13,15 @@
 // loads the library, for the life of the process.
 //
 // Set-up: the first call on a device looks up the array's device address
-// with cudaGetSymbolAddress (with that device current) and sets the kernels'
-// shared-memory limits; make that first call before any stream capture.
+// with cudaGetSymbolAddress (with that device current) and sets the
+// shared-memory limits of the two block-inverse kernels it launches.
 // Every call shares the one array and finds the previous call's contents in
 // it; the status word is cleared at the start of each call and the rest is
 // fully overwritten before it is read.  Calls that overlap on the GPU (two
-// streams, two host threads) race on the array: serialise them.
+// streams, two host threads) race on the array: serialise them.  Every call
+// copies the status word to the host and synchronises `stream`, so no call
+// can be recorded into a CUDA graph.  The caller's current device is the
+// same after the call as before it.
 #include <mutex>
 
 #include "common.h"
@@ -60,6 +63,20 @@ __global__ void wsolve_setup_kernel(WsolveDesc d, TSlab *slabs, InvTask *tasks, 
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Makes `device` current for the life of the guard and then restores the
+// device that was current before (the caller's host thread state).
+struct DeviceGuard {
+  int saved = -1;
+  explicit DeviceGuard(int device) {
+    GWGB_CUDA(cudaGetDevice(&saved));
+    if (saved != device) GWGB_CUDA(cudaSetDevice(device));
+  }
+  ~DeviceGuard() {
+    int now = -1;
+    if (saved >= 0 && cudaGetDevice(&now) == cudaSuccess && now != saved) cudaSetDevice(saved);
+  }
+};
+
 }  // namespace
 }  // namespace gwgb
 
@@ -98,7 +115,7 @@ extern "C" int gwgb_wsolve_noalloc(int32_t device, const double *P0_t, double *P
                  "gwgb_wsolve_noalloc: nw_b * qslice needs " + std::to_string(head + task_bytes + pw_bytes) +
                      " bytes of scratch; the limit is " + std::to_string((size_t)GWGB_NOALLOC_SCRATCH_BYTES));
 
-    GWGB_CUDA(cudaSetDevice(device));
+    DeviceGuard guard(device);
     void *base = nullptr;
     {
       std::lock_guard<std::mutex> lk(g_setup_mu);
@@ -107,7 +124,7 @@ extern "C" int gwgb_wsolve_noalloc(int32_t device, const double *P0_t, double *P
         cudaError_t e = cudaGetSymbolAddress(&p, g_wsolve_scratch);
         if (e != cudaSuccess)
           throw Error(GWGB_E_CUDA, std::string("cudaGetSymbolAddress(g_wsolve_scratch): ") + cudaGetErrorString(e));
-        set_fp64_kernel_attributes(200 * 1024);
+        set_inverse_kernel_attributes();
         g_scratch_ptr[device] = p;
       }
       base = g_scratch_ptr[device];

@@ -2,8 +2,9 @@
 
 The GW iteration is timed per replica (every rank runs the whole iteration on
 its own GPU; the contractions are not sharded, no data-path collective), so
-the job's time is the maximum over ranks and the job completes ``world``
-iterations in it.  This module holds that logic for ``bench.py`` so that it
+the time of one iteration is the maximum over ranks; the job completes
+``world`` independent iterations in that time, reported separately as a
+throughput.  This module holds that logic for ``bench.py`` so that it
 runs, and is tested, the same way on CPU ranks (``gloo``) as on GPUs
 (``nccl``)."""
 import os
@@ -39,9 +40,15 @@ class Replicas:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    def job_seconds_per_iteration(self, ms_max: float) -> float:
-        """Whole-job seconds per iteration: `world` iterations in the slowest replica's time."""
-        return ms_max / 1e3 / self.world
+    def seconds_per_iteration(self, ms_max: float) -> float:
+        """Seconds per GW iteration of one crystal: the slowest replica's time.
+        Replicas do not shard an iteration, so adding ranks does not shorten it."""
+        return ms_max / 1e3
+
+    def replica_throughput(self, ms_max: float) -> float:
+        """Independent iterations the whole job completes per second (`world` in
+        the slowest replica's time): throughput of copies, not a faster iteration."""
+        return self.world / (ms_max / 1e3)
 
     @property
     def reports(self) -> bool:

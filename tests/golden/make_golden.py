@@ -1,9 +1,10 @@
 """Generate the LiH golden fixtures from the reference's own data files.
 
 Run in a checkout where the reference tree is available (it reads
-``SymmetryMBPT/data`` under ``--ref``):
+``SymmetryMBPT/data`` under ``--ref``, or under $MBSYMMETRY_REF when the
+option is not given):
 
-    python tests/golden/make_golden.py --ref /root/reference
+    python tests/golden/make_golden.py --ref <path of the reference tree>
 
 Outputs (committed; the GPU tests read only these):
 
@@ -102,8 +103,11 @@ def numpy_sigma(L, G_full_fn, P_full_fn, V, ns, nts, nt_max):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("MBSYMMETRY_REF"),
+                    help="path of the reference tree (default: $MBSYMMETRY_REF)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref or set MBSYMMETRY_REF to the reference tree")
     from oracle import Oracle
     D = os.path.join(args.ref, "SymmetryMBPT", "data")
     blk = os.path.join(D, "LiH", "integral", "nk2", "block")

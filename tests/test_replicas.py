@@ -21,7 +21,7 @@ def _rank_main(rank, world, port, q):
     r.barrier()
     ms = 10.0 + 5.0 * rank                     # each replica's own time
     ms_max = r.max_over_ranks(ms)
-    q.put((rank, ms_max, r.job_seconds_per_iteration(ms_max), r.reports))
+    q.put((rank, ms_max, r.seconds_per_iteration(ms_max), r.replica_throughput(ms_max), r.reports))
     r.close()
 
 
@@ -37,8 +37,9 @@ def test_two_gloo_ranks():
         assert p.exitcode == 0
     out = sorted(q.get(timeout=10) for _ in range(world))
     assert [o[1] for o in out] == [15.0, 15.0]                 # both ranks see the slowest replica
-    assert [o[2] for o in out] == [15.0 / 1e3 / 2] * 2         # two iterations in that time
-    assert [o[3] for o in out] == [True, False]                # rank 0 reports
+    assert [o[2] for o in out] == [15.0 / 1e3] * 2             # one iteration takes the slowest time
+    assert [o[3] for o in out] == [2 / 15e-3] * 2              # two independent iterations in it
+    assert [o[4] for o in out] == [True, False]                # rank 0 reports
 
 
 def test_single_process_defaults(monkeypatch):
@@ -47,4 +48,5 @@ def test_single_process_defaults(monkeypatch):
     from mbsymmetry_gb300.replicas import Replicas
     r = Replicas()
     assert (r.rank, r.world) == (0, 1) and r.reports
-    assert r.max_over_ranks(3.5) == 3.5 and r.job_seconds_per_iteration(100.0) == 0.1
+    assert r.max_over_ranks(3.5) == 3.5 and r.seconds_per_iteration(100.0) == 0.1
+    assert r.replica_throughput(100.0) == 10.0
