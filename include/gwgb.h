@@ -45,6 +45,9 @@ extern "C" {
 #define GWGB_PREC_FP64       0  /* complex128 everywhere: the drop-in path */
 #define GWGB_PREC_TF32X3     1  /* P0/Sigma on tcgen05 kind::tf32, 3-pass split, FP32 accumulate */
 #define GWGB_PREC_BF16X3     2  /* P0/Sigma on tcgen05 kind::f16 (BF16), 3-way split, 6 products, FP32 accumulate */
+#define GWGB_PREC_OZAKI      3  /* P0/Sigma on tcgen05 kind::f16 (BF16): four fixed-point slices per operand row
+                                   (Ozaki scheme), 10 products, exact FP32 partial sums, float-float accumulation
+                                   and intermediates; Sigma error about 1e-9 of the FP64 path */
 
 typedef struct gwgb_handle_s *gwgb_handle;
 

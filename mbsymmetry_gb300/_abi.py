@@ -25,8 +25,9 @@ GWGB_E_UNSUPPORTED = 7
 PREC_FP64 = 0
 PREC_TF32X3 = 1
 PREC_BF16X3 = 2
+PREC_OZAKI = 3
 
-PREC_NAMES = {"fp64": PREC_FP64, "tf32x3": PREC_TF32X3, "bf16x3": PREC_BF16X3}
+PREC_NAMES = {"fp64": PREC_FP64, "tf32x3": PREC_TF32X3, "bf16x3": PREC_BF16X3, "ozaki": PREC_OZAKI}
 
 
 class GwgbParams(ctypes.Structure):

@@ -22,6 +22,7 @@
 #include "kernels.h"
 #include "kernels_tc.h"
 #include "kernels_sc.h"
+#include "kernels_oz.h"
 
 namespace gwgb {
 
@@ -267,10 +268,27 @@ class Engine {
   ~Engine();
 
   void set_precision(int prec) {
-    GWGB_REQUIRE(prec == GWGB_PREC_FP64 || prec == GWGB_PREC_TF32X3 || prec == GWGB_PREC_BF16X3, GWGB_E_INVALID,
-                 "unknown precision");
+    GWGB_REQUIRE(prec == GWGB_PREC_FP64 || prec == GWGB_PREC_TF32X3 || prec == GWGB_PREC_BF16X3 ||
+                     prec == GWGB_PREC_OZAKI,
+                 GWGB_E_INVALID, "unknown precision");
     if (prec != prec_) drop_graphs();  // the captured graphs hold the old kernels
     prec_ = prec;
+    if (prec_ == GWGB_PREC_OZAKI) {
+      if (!oz_built_) build_oz_lists();
+      if (!ozVcat_.p) {
+        ozVcat_.alloc((size_t)oz_vcat_elems_);
+        ozBcat_.alloc((size_t)oz_bcat_elems_);
+        ozVcatS_.alloc((size_t)oz_vcats_elems_);
+        ozZ1_.alloc((size_t)oz_z1_elems_);
+        ozZcat_.alloc((size_t)oz_zcat_elems_);
+        ozW_.alloc((size_t)oz_w_elems_);
+        ozU_.alloc((size_t)oz_u_elems_);
+        Gff_.alloc(Gall_.n);
+        Pff_.alloc(Pall_.n);
+        oz_ready_ = false;
+      }
+      return;
+    }
     if (prec_ != GWGB_PREC_FP64 && !Wbuf_.p && wbuf_elems_) {
       Wbuf_.alloc((size_t)wbuf_elems_);
       Bcat_.alloc((size_t)bcat_elems_);
@@ -412,13 +430,60 @@ class Engine {
       vcat_ready_ = false;
       built = true;
     }
-    if (prec_ != GWGB_PREC_FP64 && !vcat_ready_) {
+    if (prec_ == GWGB_PREC_OZAKI && !oz_ready_) {
+      launch_oz_perm(oz_perm_v_.p, (int)oz_perm_v_.n, V_.p, ozVcat_.p, st_);
+      launch_oz_perm(oz_perm_b_.p, (int)oz_perm_b_.n, Vt_.p, ozBcat_.p, st_);
+      launch_oz_perm(oz_perm_s_.p, (int)oz_perm_s_.n, Vt_.p, ozVcatS_.p, st_);
+      oz_ready_ = true;
+      built = true;
+    }
+    if (tc_split() && !vcat_ready_) {
       launch_vcat(vc_tasks_.p, (int)vc_tasks_.n, V_.p, Vcat_.p, st_);
       launch_bcat(bc_tasks_.p, (int)bc_tasks_.n, Vt_.p, Bcat_.p, st_);
       vcat_ready_ = true;
       built = true;
     }
     if (built) GWGB_CUDA(cudaStreamSynchronize(st_));
+  }
+  bool tc_split() const { return prec_ == GWGB_PREC_TF32X3 || prec_ == GWGB_PREC_BF16X3; }
+  // Sliced (Ozaki) path: descriptors and tasks of the six GEMM stages per tau
+  // chunk, the float-float operand buffers and the copies that build the
+  // tau-independent ones from V / Vt.
+  enum OzBufId { OZB_GFF, OZB_PFF, OZB_VCAT, OZB_BCAT, OZB_VCATS, OZB_Z1, OZB_ZCAT, OZB_W, OZB_U, OZB_P0, OZB_SIG };
+  struct OzLaunch { int64_t t0, n; int a, b, c; };
+  bool oz_built_ = false, oz_ready_ = false;
+  DBuf<OzDesc> oz_descs_;
+  DBuf<OzTask> oz_tasks_;
+  DBuf<OzPerm> oz_perm_v_, oz_perm_b_, oz_perm_s_;
+  DBuf<float4> Gff_, Pff_, ozVcat_, ozBcat_, ozVcatS_, ozZ1_, ozZcat_, ozW_, ozU_;
+  int64_t oz_vcat_elems_ = 0, oz_bcat_elems_ = 0, oz_vcats_elems_ = 0, oz_z1_elems_ = 0, oz_zcat_elems_ = 0,
+          oz_w_elems_ = 0, oz_u_elems_ = 0;
+  std::vector<OzLaunch> oz_p0_, oz_sig_;
+  int oz_tch_p0_ = 1, oz_tch_sig_ = 1;
+  std::vector<P0Contrib> pc_host_;
+  std::vector<SigContrib> sc_host_;
+  std::vector<Owner> sig_own_host_;
+  void build_oz_lists();
+  const void *oz_ptr(int id) const {
+    switch (id) {
+      case OZB_GFF: return Gff_.p;
+      case OZB_PFF: return Pff_.p;
+      case OZB_VCAT: return ozVcat_.p;
+      case OZB_BCAT: return ozBcat_.p;
+      case OZB_VCATS: return ozVcatS_.p;
+      case OZB_Z1: return ozZ1_.p;
+      case OZB_ZCAT: return ozZcat_.p;
+      case OZB_W: return ozW_.p;
+      case OZB_U: return ozU_.p;
+      case OZB_P0: return Pall_.p;
+      default: return Sig_.p;
+    }
+  }
+  void oz_run(const std::vector<OzLaunch> &ls) {
+    for (const OzLaunch &x : ls)
+      launch_oz_gemm(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, static_cast<const float4 *>(oz_ptr(x.a)),
+                     static_cast<const float4 *>(oz_ptr(x.b)), const_cast<void *>(oz_ptr(x.c)), nsm_, bad_.p + 2,
+                     st_);
   }
   struct P0Group { int64_t pout; int32_t pstride, qb, c0, c1; };
   std::vector<P0Group> p0_groups_;                            // host: P0 output blocks
@@ -526,6 +591,7 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
   fp64_smem_ = std::min(smem_bytes_, ((per_sm / 2 - 2048) / 1024) * 1024);  // two CTAs per SM
   set_tc_kernel_attributes(smem_bytes_, sw_cap_);
   set_tc_p0_kernel_attributes(smem_bytes_);
+  set_oz_kernel_attributes();
   GWGB_CUDA(cudaMallocHost(&mu_host_, sizeof(double)));
   // device memory for one tau chunk of each tensor-core operand buffer (W, Zcat):
   // an eighth of the free memory, 1 to 16 GiB, unless GWGB_TC_CHUNK_MB says otherwise
@@ -581,6 +647,8 @@ Engine::~Engine() {
                            &Tnt_, &Ttn_, &TntBF_, &TtnFB_};
   sw_tiles_.free(); bc_tasks_.free(); sig_wref_.free(); Wbuf_.free(); Bcat_.free(); uv_red_.free();
   pz_tasks_.free(); vc_tasks_.free(); pk_tiles_.free(); pr_tiles_.free(); Zbuf_.free(); Vcat_.free(); Ppart_.free();
+  oz_descs_.free(); oz_tasks_.free(); oz_perm_v_.free(); oz_perm_b_.free(); oz_perm_s_.free();
+  for (DBuf<float4> *b : {&Gff_, &Pff_, &ozVcat_, &ozBcat_, &ozVcatS_, &ozZ1_, &ozZcat_, &ozW_, &ozU_}) b->free();
   for (auto *b : bufs) b->free();
   tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
   qoff_irr_.free(); qsz_irr_.free();
@@ -1344,7 +1412,331 @@ void Engine::build_work_lists() {
   }
   qoff_irr_.upload(qo, st_);
   qsz_irr_.upload(qs, st_);
+  pc_host_ = pc;
+  sc_host_ = sc;
+  sig_own_host_ = sig_own;
   GWGB_CUDA(cudaStreamSynchronize(st_));
+}
+
+// ---------------------------------------------------------------------------
+// sliced (Ozaki) path: work lists of the six GEMM stages
+// ---------------------------------------------------------------------------
+namespace {
+
+// Inclusive extent of the offsets of rows [0, M) of a row map.
+void oz_rows_extent(const OzRows &m, int M, int64_t &lo, int64_t &hi) {
+  const int64_t qmax = (M - 1) / m.d, rmax = std::min<int64_t>(m.d, M) - 1;
+  lo = m.base + std::min<int64_t>(0, qmax * m.s1) + std::min<int64_t>(0, rmax * m.s0);
+  hi = m.base + std::max<int64_t>(0, qmax * m.s1) + std::max<int64_t>(0, rmax * m.s0);
+}
+
+void oz_widen(int64_t &lo, int64_t &hi, int64_t step, int64_t count) {
+  const int64_t e = (count - 1) * step;
+  lo += std::min<int64_t>(0, e);
+  hi += std::max<int64_t>(0, e);
+}
+
+// Every element that the tasks of descriptor d (nrep repetitions) read or
+// write lies inside its buffers of na, nb, nc elements.
+void oz_check(const OzDesc &d, int nrep, int64_t na, int64_t nb, int64_t nc, const char *what) {
+  GWGB_REQUIRE(d.M >= 1 && d.N >= 1 && d.K >= 1 && nrep >= 1 && d.a.d >= 1 && d.b.d >= 1 && d.c.d >= 1 &&
+                   d.cnd >= 1,
+               GWGB_E_INVALID, std::string("internal work list out of bounds: empty sliced GEMM in ") + what);
+  int64_t lo, hi;
+  oz_rows_extent(d.a, d.M, lo, hi);
+  oz_widen(lo, hi, d.aks, d.K);
+  oz_widen(lo, hi, d.ra, nrep);
+  check_range(lo, hi - lo + 1, na, what);
+  oz_rows_extent(d.b, d.N, lo, hi);
+  oz_widen(lo, hi, d.bks, d.K);
+  oz_widen(lo, hi, d.rb, nrep);
+  check_range(lo, hi - lo + 1, nb, what);
+  oz_rows_extent(d.c, d.M, lo, hi);
+  const int64_t qmax = (d.N - 1) / d.cnd, rmax = std::min<int64_t>(d.cnd, d.N) - 1;
+  lo += std::min<int64_t>(0, qmax * d.cn1) + std::min<int64_t>(0, rmax * d.cn0);
+  hi += std::max<int64_t>(0, qmax * d.cn1) + std::max<int64_t>(0, rmax * d.cn0);
+  oz_widen(lo, hi, d.rc, nrep);
+  check_range(lo, hi - lo + 1, nc, what);
+}
+
+}  // namespace
+
+void Engine::build_oz_lists() {
+  const Lay &l = l_;
+  const int ns = ns_, nts = nts_, half = nts / 2;
+  const std::vector<P0Contrib> &pc = pc_host_;
+  const std::vector<SigContrib> &sc = sc_host_;
+  std::vector<OzDesc> ds;
+  std::vector<OzTask> ts;
+  std::vector<int> dsrep;
+  constexpr int REPG = 8;  // tau per task in the per-tau stages (Z, U)
+  auto add = [&](const OzDesc &d, int nrep, int repg) {
+    const int id = (int)ds.size();
+    ds.push_back(d);
+    dsrep.push_back(nrep);
+    const int mtn = (d.M + OZ_M - 1) / OZ_M, ntn = (d.N + OZ_NC - 1) / OZ_NC;
+    GWGB_REQUIRE(mtn < 65536 && ntn < 65536, GWGB_E_UNSUPPORTED, "sliced GEMM too large");
+    for (int r0 = 0; r0 < nrep; r0 += repg)
+      for (int mt = 0; mt < mtn; ++mt)
+        for (int nt = 0; nt < ntn; ++nt) ts.push_back({id, r0, std::min(repg, nrep - r0), (mt << 16) | nt});
+  };
+  // tasks of one stage (appended since t0): heaviest first, then one launch
+  auto stage = [&](std::vector<OzLaunch> &v, size_t t0, int a, int b, int c) {
+    auto cost = [&](const OzTask &t) { return (int64_t)t.nrep * ((ds[t.desc].K + OZ_KR - 1) / OZ_KR); };
+    std::stable_sort(ts.begin() + t0, ts.end(), [&](const OzTask &x, const OzTask &y) { return cost(x) > cost(y); });
+    v.push_back({(int64_t)t0, (int64_t)(ts.size() - t0), a, b, c});
+  };
+  oz_p0_.clear();
+  oz_sig_.clear();
+  const int64_t gsz = (int64_t)Gall_.n, psz = (int64_t)Pall_.n, ssz = (int64_t)nts * ns * l.flat_ao;
+
+  // ---- P0: per output block g = (q_irr, iq), K over (contribution, spin) ----
+  std::vector<OzPerm> pv;
+  struct PG { int64_t voff, zc; int zld; };
+  std::vector<PG> pg;
+  std::vector<int> zcol(pc.size() * ns);
+  std::vector<int64_t> z1c(pc.size() * ns);
+  int64_t voff = 0, zct = 0, z1t = 0;  // Vcat elements; Zcat and Z1 elements per tau
+  for (const P0Group &g : p0_groups_) {
+    int zld = 0;
+    for (int c = g.c0; c < g.c1; ++c)
+      for (int sp = 0; sp < ns; ++sp) {
+        zcol[c * ns + sp] = zld;
+        zld += pc[c].b1 * pc[c].b2;
+        z1c[c * ns + sp] = z1t;
+        z1t += (int64_t)g.qb * pc[c].b1 * pc[c].b2;
+      }
+    pg.push_back({voff, zct, zld});
+    for (int c = g.c0; c < g.c1; ++c)
+      for (int sp = 0; sp < ns; ++sp)
+        pv.push_back({pc[c].v, voff + zcol[c * ns + sp], zld, pc[c].b2, 1, g.qb, pc[c].b1, pc[c].b2, 0});
+    voff += (int64_t)g.qb * zld;
+    zct += (int64_t)g.qb * zld;
+  }
+  oz_vcat_elems_ = voff;
+  const int64_t p0_tau_bytes = 16 * std::max<int64_t>(1, zct + z1t);
+  const int tp = (int)std::max<int64_t>(1, std::min<int64_t>(half, tc_chunk_bytes_ / p0_tau_bytes));
+  oz_tch_p0_ = tp;
+  oz_z1_elems_ = z1t * tp;
+  oz_zcat_elems_ = zct * tp;
+  const double pref = -1.0 / l.nk * (ns == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
+  for (int t0 = 0; t0 < half; t0 += tp) {
+    const int ntc = std::min(tp, half - t0);
+    size_t s0 = ts.size();
+    for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {  // Z1[P][t][tau][m] = sum_n conj(V[P][t][n]) G2(tau)[m][n]
+      const P0Group &g = p0_groups_[gi];
+      for (int c = g.c0; c < g.c1; ++c)
+        for (int sp = 0; sp < ns; ++sp) {
+          const P0Contrib &cb = pc[c];
+          const int qb = g.qb, b1 = cb.b1, b2 = cb.b2;
+          OzDesc d{};
+          d.a = {pg[gi].voff + zcol[c * ns + sp], pg[gi].zld, b2, b1};
+          d.b = {cb.gb + ((int64_t)t0 * ns + sp) * cb.sb, (int64_t)ns * cb.sb, b2, b2};
+          d.c = {z1c[c * ns + sp] * tp, (int64_t)b2 * b1, 1, b1};
+          d.cn1 = (int64_t)qb * b2 * b1;
+          d.cn0 = b1;
+          d.cnd = b2;
+          d.aks = d.bks = 1;
+          d.M = qb * b1;
+          d.N = ntc * b2;
+          d.K = b2;
+          d.flags = OZ_CONJ_A;
+          oz_check(d, 1, oz_vcat_elems_, gsz, oz_z1_elems_, "P0 stage Z1");
+          add(d, 1, 1);
+        }
+    }
+    stage(oz_p0_, s0, OZB_VCAT, OZB_GFF, OZB_Z1);
+    s0 = ts.size();
+    for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {  // Z[(tau,P)][(p,m)] = sum_t G1(beta-tau)[t][p] Z1[P][t][tau][m]
+      const P0Group &g = p0_groups_[gi];
+      for (int c = g.c0; c < g.c1; ++c)
+        for (int sp = 0; sp < ns; ++sp) {
+          const P0Contrib &cb = pc[c];
+          const int qb = g.qb, b1 = cb.b1, b2 = cb.b2;
+          OzDesc d{};
+          d.a = {z1c[c * ns + sp] * tp, b1, 0, 1};
+          d.ra = (int64_t)qb * b2 * b1;
+          d.b = {cb.ga + ((int64_t)(nts - 1 - t0) * ns + sp) * cb.sa, 1, 0, 1};
+          d.bks = b1;
+          d.rb = -(int64_t)ns * cb.sa;
+          d.c = {pg[gi].zc * tp + zcol[c * ns + sp], pg[gi].zld, 1, b2};
+          d.cn1 = b2;
+          d.cnd = 1;
+          d.rc = (int64_t)qb * pg[gi].zld;
+          d.aks = 1;
+          d.M = qb * b2;
+          d.N = b1;
+          d.K = b1;
+          oz_check(d, ntc, oz_z1_elems_, gsz, oz_zcat_elems_, "P0 stage Z");
+          add(d, ntc, REPG);
+        }
+    }
+    stage(oz_p0_, s0, OZB_Z1, OZB_GFF, OZB_ZCAT);
+    s0 = ts.size();
+    for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {  // P0[Q][P] = sum_K Zcat[(tau,P)][K] Vcat[Q][K]
+      const P0Group &g = p0_groups_[gi];
+      if (g.c1 == g.c0) continue;
+      OzDesc d{};
+      d.a = {pg[gi].zc * tp, pg[gi].zld, 0, 1};
+      d.b = {pg[gi].voff, pg[gi].zld, 0, 1};
+      d.c = {g.pout + (int64_t)t0 * g.pstride, g.pstride, 1, g.qb};
+      d.cn1 = g.qb;
+      d.cnd = 1;
+      d.aks = d.bks = 1;
+      d.M = ntc * g.qb;
+      d.N = g.qb;
+      d.K = pg[gi].zld;
+      d.flags = OZ_OUT_F64;
+      d.alpha = pref;
+      oz_check(d, 1, oz_zcat_elems_, oz_vcat_elems_, psz, "P0 stage P0");
+      add(d, 1, 1);
+    }
+    stage(oz_p0_, s0, OZB_ZCAT, OZB_VCAT, OZB_P0);
+  }
+
+  // ---- Sigma: W per P~ block group, U per contribution, Sigma per owner ----
+  std::vector<OzPerm> pb, psg;
+  struct SG { int64_t boff, wc; int ncol; };
+  std::vector<SG> sg;
+  std::vector<int> cgroup(sc.size(), -1), ccol(sc.size(), 0);
+  int64_t boff = 0, wct = 0;
+  for (const auto &grp : sig_groups_) {
+    const std::vector<int> &cs = grp.second;
+    const int qb = sc[cs[0]].qb;
+    int ncol = 0;
+    for (int c : cs) {
+      cgroup[c] = (int)sg.size();
+      ccol[c] = ncol;
+      pb.push_back({sc[c].v, boff + (int64_t)ncol * qb, 1, (int64_t)sc[c].b2 * qb, qb, qb, sig_b1_[c], sc[c].b2, 1});
+      ncol += sig_b1_[c] * sc[c].b2;
+    }
+    sg.push_back({boff, wct, ncol});
+    boff += (int64_t)ncol * qb;
+    wct += (int64_t)qb * ncol;
+  }
+  oz_bcat_elems_ = boff;
+  // U columns per owner (the same for both spins of an AO block), Vcat of Sigma per AO block
+  std::vector<int> ucol(sc.size(), 0);
+  std::map<std::pair<int, int>, std::pair<int64_t, int>> vs;  // (c0, c1) -> (VcatS offset, uld)
+  int64_t vsoff = 0, uct = 0;
+  std::vector<int64_t> uoff(sig_own_host_.size());
+  for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {
+    const Owner &o = sig_own_host_[oi];
+    int uld = 0;
+    for (int c = o.c0; c < o.c1; ++c) {
+      ucol[c] = uld;
+      uld += sc[c].qb * sc[c].b2;
+    }
+    const auto key = std::make_pair(o.c0, o.c1);
+    if (!vs.count(key)) {
+      vs[key] = {vsoff, uld};
+      for (int c = o.c0; c < o.c1; ++c)
+        psg.push_back({sc[c].v, vsoff + ucol[c], sc[c].b2, uld, 1, sc[c].qb, sig_b1_[c], sc[c].b2, 0});
+      vsoff += (int64_t)o.n * uld;
+    }
+    uoff[oi] = uct;
+    uct += (int64_t)o.n * uld;
+  }
+  oz_vcats_elems_ = vsoff;
+  const int64_t sig_tau_bytes = 16 * std::max<int64_t>(1, wct + uct);
+  const int tsg = (int)std::max<int64_t>(1, std::min<int64_t>(nts, tc_chunk_bytes_ / sig_tau_bytes));
+  oz_tch_sig_ = tsg;
+  oz_w_elems_ = wct * tsg;
+  oz_u_elems_ = uct * tsg;
+  for (int t0 = 0; t0 < nts; t0 += tsg) {
+    const int ntc = std::min(tsg, nts - t0);
+    size_t s0 = ts.size();
+    {  // W[(tau,Q)][(c,j,n)] = sum_P op(P~(tau))[Q][P] conj(Vt_c[P][j][n])
+      size_t gi = 0;
+      for (const auto &grp : sig_groups_) {
+        const SigContrib &c0 = sc[grp.second[0]];
+        const int qb = c0.qb;
+        OzDesc d{};
+        d.a = {c0.pq + (int64_t)t0 * c0.pstride, c0.pstride, qb, qb};
+        d.b = {sg[gi].boff, qb, 0, 1};
+        d.c = {sg[gi].wc * tsg, sg[gi].ncol, 0, 1};
+        d.cn1 = 1;
+        d.cnd = 1;
+        d.aks = d.bks = 1;
+        d.M = ntc * qb;
+        d.N = sg[gi].ncol;
+        d.K = qb;
+        d.flags = c0.pconj ? OZ_CONJ_A : 0;
+        oz_check(d, 1, psz, oz_bcat_elems_, oz_w_elems_, "Sigma stage W");
+        add(d, 1, 1);
+        ++gi;
+      }
+    }
+    stage(oz_sig_, s0, OZB_PFF, OZB_BCAT, OZB_W);
+    s0 = ts.size();
+    for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {  // U_c[Q][j][m] = sum_n W[Q][(c,j,n)] G2(tau)[m][n]
+      const Owner &o = sig_own_host_[oi];
+      const int uld = vs[std::make_pair(o.c0, o.c1)].second, b1 = o.n;
+      for (int c = o.c0; c < o.c1; ++c) {
+        const SigContrib &cb = sc[c];
+        const SG &g = sg[cgroup[c]];
+        const int qb = cb.qb, b2 = cb.b2;
+        OzDesc d{};
+        d.a = {g.wc * tsg + ccol[c], g.ncol, b2, b1};
+        d.ra = (int64_t)qb * g.ncol;
+        d.b = {cb.gb + ((int64_t)t0 * ns + o.s) * cb.sb, b2, 0, 1};
+        d.rb = (int64_t)ns * cb.sb;
+        d.c = {uoff[oi] * tsg + ucol[c], b2, uld, b1};
+        d.cn1 = 1;
+        d.cnd = 1;
+        d.rc = (int64_t)b1 * uld;
+        d.aks = d.bks = 1;
+        d.M = qb * b1;
+        d.N = b2;
+        d.K = b2;
+        oz_check(d, ntc, oz_w_elems_, gsz, oz_u_elems_, "Sigma stage U");
+        add(d, ntc, REPG);
+      }
+    }
+    stage(oz_sig_, s0, OZB_W, OZB_GFF, OZB_U);
+    s0 = ts.size();
+    for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {  // Sigma[i][j] = sum_K U[(tau,j)][K] VcatS[i][K]
+      const Owner &o = sig_own_host_[oi];
+      const auto &v = vs[std::make_pair(o.c0, o.c1)];
+      if (v.second == 0) continue;
+      OzDesc d{};
+      d.a = {uoff[oi] * tsg, v.second, 0, 1};
+      d.b = {v.first, v.second, 0, 1};
+      d.c = {o.out + (int64_t)t0 * o.ostride, o.ostride, 1, o.n};
+      d.cn1 = o.n;
+      d.cnd = 1;
+      d.aks = d.bks = 1;
+      d.M = ntc * o.n;
+      d.N = o.n;
+      d.K = v.second;
+      d.flags = OZ_OUT_F64;
+      d.alpha = -1.0 / l.nk;
+      oz_check(d, 1, oz_u_elems_, oz_vcats_elems_, ssz, "Sigma stage Sigma");
+      add(d, 1, 1);
+    }
+    stage(oz_sig_, s0, OZB_U, OZB_VCATS, OZB_SIG);
+  }
+  for (const OzPerm &t : pv) {
+    check_range(t.src, (int64_t)t.X * t.Y * t.Z, l.flat_V, "sliced Vcat source");
+    check_range(t.dst, (t.X - 1) * t.dx + (t.Y - 1) * t.dy + (t.Z - 1) * t.dz + 1, oz_vcat_elems_, "sliced Vcat");
+  }
+  for (const OzPerm &t : pb) {
+    check_range(t.src, (int64_t)t.X * t.Y * t.Z, (int64_t)Vt_.n, "sliced Bcat source");
+    check_range(t.dst, (t.X - 1) * t.dx + (t.Y - 1) * t.dy + (t.Z - 1) * t.dz + 1, oz_bcat_elems_, "sliced Bcat");
+  }
+  for (const OzPerm &t : psg) {
+    check_range(t.src, (int64_t)t.X * t.Y * t.Z, (int64_t)Vt_.n, "sliced Sigma Vcat source");
+    check_range(t.dst, (t.X - 1) * t.dx + (t.Y - 1) * t.dy + (t.Z - 1) * t.dz + 1, oz_vcats_elems_,
+                "sliced Sigma Vcat");
+  }
+  GWGB_REQUIRE(ts.size() < (size_t)INT32_MAX, GWGB_E_UNSUPPORTED, "too many sliced GEMM tasks");
+  oz_descs_.upload(ds, st_);
+  oz_tasks_.upload(ts, st_);
+  oz_perm_v_.upload(pv, st_);
+  oz_perm_b_.upload(pb, st_);
+  oz_perm_s_.upload(psg, st_);
+  GWGB_CUDA(cudaStreamSynchronize(st_));
+  oz_built_ = true;
 }
 
 // ---------------------------------------------------------------------------
@@ -1365,7 +1757,7 @@ void Engine::upload_V(const double *V, int64_t n) {
   h2d(V_.p, V, (size_t)n * sizeof(double2), st_);
   GWGB_CUDA(cudaStreamSynchronize(st_));
   have_V_ = true;
-  vt_ready_ = vcat_ready_ = false;  // rebuilt before the next solve
+  vt_ready_ = vcat_ready_ = oz_ready_ = false;  // rebuilt before the next solve
 }
 
 void Engine::set_reps(const double *orep, int64_t no, const double *auxrep, int64_t na) {
@@ -1374,7 +1766,7 @@ void Engine::set_reps(const double *orep, int64_t no, const double *auxrep, int6
   h2d(auxrep_.p, auxrep, (size_t)na * sizeof(double2), st_);
   GWGB_CUDA(cudaStreamSynchronize(st_));
   have_reps_ = true;
-  vt_ready_ = vcat_ready_ = false;  // rebuilt before the next solve
+  vt_ready_ = vcat_ready_ = oz_ready_ = false;  // rebuilt before the next solve
 }
 
 void Engine::set_transforms(const double *Tnt, const double *Ttn, const double *TntBF, const double *TtnFB,
@@ -1443,7 +1835,13 @@ void Engine::k_rotate_G() {
 
 void Engine::k_p0(int mirror) {
   const double pref = -1.0 / l_.nk * (ns_ == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
-  if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
+  if (prec_ == GWGB_PREC_OZAKI) {  // sliced contractions: Z1 -> Z -> P0 per tau chunk
+    GWGB_REQUIRE(oz_ready_, GWGB_E_STATE, "sliced-precision operands not prepared");
+    launch_to_ffc(Gall_.p, Gff_.p, (int64_t)Gall_.n, st_);
+    GWGB_CUDA(cudaMemsetAsync(Pall_.p, 0, Pall_.n * sizeof(double2), st_));  // blocks without contributions
+    oz_run(oz_p0_);
+    if (mirror) launch_mirror(Pall_.p, qoff_irr_.p, qsz_irr_.p, l_.ink, nts_, st_);
+  } else if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE((Zbuf_.p || !zbuf_elems_) && vcat_ready_, GWGB_E_STATE, "mixed-precision operands not prepared");
     for (const P0Chunk &ch : p0_chunks_)  // each chunk's slices are summed before the next chunk
       launch_p0_tc(prec_ == GWGB_PREC_BF16X3, pz_tasks_.p, (int)pz_tasks_.n, pz_smem_, pk_tiles_.p + ch.k0, ch.nk,
@@ -1469,7 +1867,13 @@ void Engine::k_pq(bool mirror_first) {
 
 
 void Engine::k_sigma() {
-  if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
+  if (prec_ == GWGB_PREC_OZAKI) {  // sliced contractions: W -> U -> Sigma per tau chunk
+    GWGB_REQUIRE(oz_ready_, GWGB_E_STATE, "sliced-precision operands not prepared");
+    launch_to_ffc(Gall_.p, Gff_.p, (int64_t)Gall_.n, st_);
+    launch_to_ffc(Pall_.p, Pff_.p, (int64_t)Pall_.n, st_);
+    GWGB_CUDA(cudaMemsetAsync(Sig_.p, 0, Sig_.n * sizeof(double2), st_));  // blocks without contributions
+    oz_run(oz_sig_);
+  } else if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
     for (const SigChunk &ch : sig_chunks_) {
       launch_sigma_tc(prec_ == GWGB_PREC_BF16X3, sw_tiles_.p + ch.w0, ch.nw, sw_smem_, Bcat_.p,
@@ -1546,7 +1950,7 @@ void Engine::finish_stats(bool with_dyson, bool with_gw, bool with_pq, bool with
   }
   int64_t launches = 0;
   if (with_gw) {
-    const bool tc = prec_ != GWGB_PREC_FP64;
+    const bool tc = tc_split();
     int64_t sgt = 0, p0t = 0;
     for (const SigChunk &ch : sig_chunks_)
       sgt += (ch.nw ? 1 : 0) + (ch.nuvt ? 1 : 0) + (ch.nuv_blocked ? 1 : 0) +
@@ -1556,6 +1960,12 @@ void Engine::finish_stats(bool with_dyson, bool with_gw, bool with_pq, bool with
                           : (p0_tiles_.n ? 1 : 0) + (p0_red_.n ? 1 : 0);
     const int64_t sg = tc ? sgt
                           : (sig_tiles_.n ? 1 : 0) + (sig_red_.n ? 1 : 0);
+    if (prec_ == GWGB_PREC_OZAKI) {
+      int64_t a = 1, b = 2;  // G (and P~) to float-float
+      for (const OzLaunch &x : oz_p0_) a += x.n ? 1 : 0;
+      for (const OzLaunch &x : oz_sig_) b += x.n ? 1 : 0;
+      launches += (rotG_.n ? 1 : 0) + a + 1 + 3 + b;
+    } else
     launches += (rotG_.n ? 1 : 0) + p0 + 3 + sg;
   }
   if (with_dyson) launches += 3 + (has_tct_ ? 1 : 0);
