@@ -285,6 +285,7 @@ class Engine {
         ozU_.alloc((size_t)oz_u_elems_);
         Gff_.alloc(Gall_.n);
         Pff_.alloc(Pall_.n);
+        Vff_.alloc((size_t)l_.flat_V);
         oz_ready_ = false;
       }
       return;
@@ -431,6 +432,7 @@ class Engine {
       built = true;
     }
     if (prec_ == GWGB_PREC_OZAKI && !oz_ready_) {
+      launch_to_ffc(V_.p, Vff_.p, (int64_t)l_.flat_V, st_);
       launch_oz_perm(oz_perm_v_.p, (int)oz_perm_v_.n, V_.p, ozVcat_.p, st_);
       launch_oz_perm(oz_perm_b_.p, (int)oz_perm_b_.n, Vt_.p, ozBcat_.p, st_);
       launch_oz_perm(oz_perm_s_.p, (int)oz_perm_s_.n, Vt_.p, ozVcatS_.p, st_);
@@ -449,13 +451,15 @@ class Engine {
   // Sliced (Ozaki) path: descriptors and tasks of the six GEMM stages per tau
   // chunk, the float-float operand buffers and the copies that build the
   // tau-independent ones from V / Vt.
-  enum OzBufId { OZB_GFF, OZB_PFF, OZB_VCAT, OZB_BCAT, OZB_VCATS, OZB_Z1, OZB_ZCAT, OZB_W, OZB_U, OZB_P0, OZB_SIG };
+  enum OzBufId { OZB_GFF, OZB_PFF, OZB_VFF, OZB_VCAT, OZB_BCAT, OZB_VCATS, OZB_Z1, OZB_ZCAT, OZB_W, OZB_U, OZB_P0,
+                 OZB_SIG };
   struct OzLaunch { int64_t t0, n; int a, b, c; };
   bool oz_built_ = false, oz_ready_ = false;
   DBuf<OzDesc> oz_descs_;
   DBuf<OzTask> oz_tasks_;
   DBuf<OzPerm> oz_perm_v_, oz_perm_b_, oz_perm_s_;
-  DBuf<float4> Gff_, Pff_, ozVcat_, ozBcat_, ozVcatS_, ozZ1_, ozZcat_, ozW_, ozU_;
+  DBuf<int64_t> oz_rowtab_;
+  DBuf<float4> Gff_, Pff_, Vff_, ozVcat_, ozBcat_, ozVcatS_, ozZ1_, ozZcat_, ozW_, ozU_;
   int64_t oz_vcat_elems_ = 0, oz_bcat_elems_ = 0, oz_vcats_elems_ = 0, oz_z1_elems_ = 0, oz_zcat_elems_ = 0,
           oz_w_elems_ = 0, oz_u_elems_ = 0;
   std::vector<OzLaunch> oz_p0_, oz_sig_;
@@ -468,6 +472,7 @@ class Engine {
     switch (id) {
       case OZB_GFF: return Gff_.p;
       case OZB_PFF: return Pff_.p;
+      case OZB_VFF: return Vff_.p;
       case OZB_VCAT: return ozVcat_.p;
       case OZB_BCAT: return ozBcat_.p;
       case OZB_VCATS: return ozVcatS_.p;
@@ -482,8 +487,8 @@ class Engine {
   void oz_run(const std::vector<OzLaunch> &ls) {
     for (const OzLaunch &x : ls)
       launch_oz_gemm(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, static_cast<const float4 *>(oz_ptr(x.a)),
-                     static_cast<const float4 *>(oz_ptr(x.b)), const_cast<void *>(oz_ptr(x.c)), nsm_, bad_.p + 2,
-                     st_);
+                     static_cast<const float4 *>(oz_ptr(x.b)), const_cast<void *>(oz_ptr(x.c)), oz_rowtab_.p, nsm_,
+                     bad_.p + 2, st_);
   }
   struct P0Group { int64_t pout; int32_t pstride, qb, c0, c1; };
   std::vector<P0Group> p0_groups_;                            // host: P0 output blocks
@@ -647,8 +652,8 @@ Engine::~Engine() {
                            &Tnt_, &Ttn_, &TntBF_, &TtnFB_};
   sw_tiles_.free(); bc_tasks_.free(); sig_wref_.free(); Wbuf_.free(); Bcat_.free(); uv_red_.free();
   pz_tasks_.free(); vc_tasks_.free(); pk_tiles_.free(); pr_tiles_.free(); Zbuf_.free(); Vcat_.free(); Ppart_.free();
-  oz_descs_.free(); oz_tasks_.free(); oz_perm_v_.free(); oz_perm_b_.free(); oz_perm_s_.free();
-  for (DBuf<float4> *b : {&Gff_, &Pff_, &ozVcat_, &ozBcat_, &ozVcatS_, &ozZ1_, &ozZcat_, &ozW_, &ozU_}) b->free();
+  oz_descs_.free(); oz_tasks_.free(); oz_perm_v_.free(); oz_perm_b_.free(); oz_perm_s_.free(); oz_rowtab_.free();
+  for (DBuf<float4> *b : {&Gff_, &Pff_, &Vff_, &ozVcat_, &ozBcat_, &ozVcatS_, &ozZ1_, &ozZcat_, &ozW_, &ozU_}) b->free();
   for (auto *b : bufs) b->free();
   tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
   qoff_irr_.free(); qsz_irr_.free();
@@ -1439,18 +1444,22 @@ void oz_widen(int64_t &lo, int64_t &hi, int64_t step, int64_t count) {
 // Every element that the tasks of descriptor d (nrep repetitions) read or
 // write lies inside its buffers of na, nb, nc elements.
 void oz_check(const OzDesc &d, int nrep, int64_t na, int64_t nb, int64_t nc, const char *what) {
-  GWGB_REQUIRE(d.M >= 1 && d.N >= 1 && d.K >= 1 && nrep >= 1 && d.a.d >= 1 && d.b.d >= 1 && d.c.d >= 1 &&
-                   d.cnd >= 1,
+  GWGB_REQUIRE(d.M >= 1 && d.N >= 1 && d.K >= 1 && nrep >= 1 && d.a.d >= 0 && d.b.d >= 0 && d.c.d >= 0 &&
+                   d.cnd >= 1 && (d.a.d != 0 || d.aks == 1),
                GWGB_E_INVALID, std::string("internal work list out of bounds: empty sliced GEMM in ") + what);
   int64_t lo, hi;
-  oz_rows_extent(d.a, d.M, lo, hi);
-  oz_widen(lo, hi, d.aks, d.K);
-  oz_widen(lo, hi, d.ra, nrep);
-  check_range(lo, hi - lo + 1, na, what);
+  if (d.a.d != 0) {  // table-mapped rows are checked entry by entry where the table is built
+    oz_rows_extent(d.a, d.M, lo, hi);
+    oz_widen(lo, hi, d.aks, d.K);
+    oz_widen(lo, hi, d.ra, nrep);
+    check_range(lo, hi - lo + 1, na, what);
+  }
+  GWGB_REQUIRE(d.b.d != 0, GWGB_E_INVALID, std::string("internal work list: B rows must not be table-mapped in ") + what);
   oz_rows_extent(d.b, d.N, lo, hi);
   oz_widen(lo, hi, d.bks, d.K);
   oz_widen(lo, hi, d.rb, nrep);
   check_range(lo, hi - lo + 1, nb, what);
+  if (d.c.d == 0) return;
   oz_rows_extent(d.c, d.M, lo, hi);
   const int64_t qmax = (d.N - 1) / d.cnd, rmax = std::min<int64_t>(d.cnd, d.N) - 1;
   lo += std::min<int64_t>(0, qmax * d.cn1) + std::min<int64_t>(0, rmax * d.cn0);
@@ -1462,18 +1471,28 @@ void oz_check(const OzDesc &d, int nrep, int64_t na, int64_t nb, int64_t nc, con
 }  // namespace
 
 void Engine::build_oz_lists() {
+  // Layouts (float-float, complex elements).  Every tau-dependent buffer is a
+  // sequence of tau slabs with one stride (z1t, zct, wct, uct elements per tau),
+  // so one repetition offset serves every row of a packed GEMM.
+  //   Z1[tau][pack][m][row]      row = (c, P, t) of the contributions sharing G2's block
+  //   Zcat[tau][group][P][K]     K = (c, s, m, p) of the P0 output block (q_irr, iq)
+  //   Vcat[group][Q][K]          = V_c[Q][p][m] at the same K
+  //   W[tau][group][Q][col]      col = (c, j, n) of the P~ block group
+  //   U[tau][owner][j][K]        K = (c, Q, m) of the Sigma owner (k_irr, i1, s)
+  //   VcatS[owner][i][K]         = Vt_c[Q][i][m] at the same K
+  // Per-tau stages (Z1, Z, U) pack all contributions that share their
+  // G-block operand (same block and spin) into one GEMM with a row table.
   const Lay &l = l_;
   const int ns = ns_, nts = nts_, half = nts / 2;
   const std::vector<P0Contrib> &pc = pc_host_;
   const std::vector<SigContrib> &sc = sc_host_;
   std::vector<OzDesc> ds;
   std::vector<OzTask> ts;
-  std::vector<int> dsrep;
-  constexpr int REPG = 8;  // tau per task in the per-tau stages (Z, U)
+  std::vector<int64_t> rt;  // row table
+  constexpr int REPG = 8;   // tau per task in the per-tau stages (Z, U)
   auto add = [&](const OzDesc &d, int nrep, int repg) {
     const int id = (int)ds.size();
     ds.push_back(d);
-    dsrep.push_back(nrep);
     const int mtn = (d.M + OZ_M - 1) / OZ_M, ntn = (d.N + OZ_NC - 1) / OZ_NC;
     GWGB_REQUIRE(mtn < 65536 && ntn < 65536, GWGB_E_UNSUPPORTED, "sliced GEMM too large");
     for (int r0 = 0; r0 < nrep; r0 += repg)
@@ -1486,34 +1505,65 @@ void Engine::build_oz_lists() {
     std::stable_sort(ts.begin() + t0, ts.end(), [&](const OzTask &x, const OzTask &y) { return cost(x) > cost(y); });
     v.push_back({(int64_t)t0, (int64_t)(ts.size() - t0), a, b, c});
   };
+  // Row-table checks: every entry (plus the row's K extent and reps) inside the buffer.
+  auto check_tab = [&](int64_t base, int M, int64_t klen, int64_t rep, int nrep, int64_t size, const char *what) {
+    for (int r = 0; r < M; ++r) {
+      int64_t lo = rt[base + r], hi = lo + klen - 1;
+      oz_widen(lo, hi, rep, nrep);
+      check_range(lo, hi - lo + 1, size, what);
+    }
+  };
   oz_p0_.clear();
   oz_sig_.clear();
   const int64_t gsz = (int64_t)Gall_.n, psz = (int64_t)Pall_.n, ssz = (int64_t)nts * ns * l.flat_ao;
 
-  // ---- P0: per output block g = (q_irr, iq), K over (contribution, spin) ----
+  // ---- P0 -------------------------------------------------------------------
   std::vector<OzPerm> pv;
   struct PG { int64_t voff, zc; int zld; };
   std::vector<PG> pg;
-  std::vector<int> zcol(pc.size() * ns);
-  std::vector<int64_t> z1c(pc.size() * ns);
-  int64_t voff = 0, zct = 0, z1t = 0;  // Vcat elements; Zcat and Z1 elements per tau
-  for (const P0Group &g : p0_groups_) {
+  std::vector<int> zcol(pc.size() * ns), cgrp(pc.size());
+  int64_t voff = 0, zct = 0;
+  for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {
+    const P0Group &g = p0_groups_[gi];
     int zld = 0;
-    for (int c = g.c0; c < g.c1; ++c)
+    for (int c = g.c0; c < g.c1; ++c) {
+      cgrp[c] = (int)gi;
       for (int sp = 0; sp < ns; ++sp) {
         zcol[c * ns + sp] = zld;
         zld += pc[c].b1 * pc[c].b2;
-        z1c[c * ns + sp] = z1t;
-        z1t += (int64_t)g.qb * pc[c].b1 * pc[c].b2;
       }
+    }
     pg.push_back({voff, zct, zld});
     for (int c = g.c0; c < g.c1; ++c)
-      for (int sp = 0; sp < ns; ++sp)
-        pv.push_back({pc[c].v, voff + zcol[c * ns + sp], zld, pc[c].b2, 1, g.qb, pc[c].b1, pc[c].b2, 0});
+      for (int sp = 0; sp < ns; ++sp)  // Vcat[Q][zcol + m b1 + p] = V_c[Q][p][m]
+        pv.push_back({pc[c].v, voff + zcol[c * ns + sp], zld, 1, pc[c].b1, g.qb, pc[c].b1, pc[c].b2, 0});
     voff += (int64_t)g.qb * zld;
     zct += (int64_t)g.qb * zld;
   }
   oz_vcat_elems_ = voff;
+  // Z1 packs: (G2 block, spin) -> [(contribution, row position in the pack)]
+  struct PackRow { int c; int64_t pos; };
+  std::map<std::pair<int64_t, int>, std::vector<PackRow>> z1p, zp;
+  std::vector<int64_t> z1pack(pc.size() * ns), z1mp(pc.size() * ns), z1pos(pc.size() * ns);
+  for (size_t c = 0; c < pc.size(); ++c)
+    for (int sp = 0; sp < ns; ++sp) {
+      auto &v = z1p[{pc[c].gb, sp}];
+      const int64_t pos = v.empty() ? 0 : v.back().pos + (int64_t)p0_groups_[cgrp[v.back().c]].qb * pc[v.back().c].b1;
+      v.push_back({(int)c, pos});
+      zp[{pc[c].ga, sp}].push_back({(int)c, 0});
+    }
+  int64_t z1t = 0;
+  for (auto &kv : z1p) {
+    const auto &v = kv.second;
+    const int64_t mp = v.back().pos + (int64_t)p0_groups_[cgrp[v.back().c]].qb * pc[v.back().c].b1;
+    const int b2 = pc[v[0].c].b2;
+    for (const PackRow &x : v) {
+      z1pack[x.c * ns + kv.first.second] = z1t;
+      z1mp[x.c * ns + kv.first.second] = mp;
+      z1pos[x.c * ns + kv.first.second] = x.pos;
+    }
+    z1t += mp * b2;
+  }
   const int64_t p0_tau_bytes = 16 * std::max<int64_t>(1, zct + z1t);
   const int tp = (int)std::max<int64_t>(1, std::min<int64_t>(half, tc_chunk_bytes_ / p0_tau_bytes));
   oz_tch_p0_ = tp;
@@ -1523,53 +1573,74 @@ void Engine::build_oz_lists() {
   for (int t0 = 0; t0 < half; t0 += tp) {
     const int ntc = std::min(tp, half - t0);
     size_t s0 = ts.size();
-    for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {  // Z1[P][t][tau][m] = sum_n conj(V[P][t][n]) G2(tau)[m][n]
-      const P0Group &g = p0_groups_[gi];
-      for (int c = g.c0; c < g.c1; ++c)
-        for (int sp = 0; sp < ns; ++sp) {
-          const P0Contrib &cb = pc[c];
-          const int qb = g.qb, b1 = cb.b1, b2 = cb.b2;
-          OzDesc d{};
-          d.a = {pg[gi].voff + zcol[c * ns + sp], pg[gi].zld, b2, b1};
-          d.b = {cb.gb + ((int64_t)t0 * ns + sp) * cb.sb, (int64_t)ns * cb.sb, b2, b2};
-          d.c = {z1c[c * ns + sp] * tp, (int64_t)b2 * b1, 1, b1};
-          d.cn1 = (int64_t)qb * b2 * b1;
-          d.cn0 = b1;
-          d.cnd = b2;
-          d.aks = d.bks = 1;
-          d.M = qb * b1;
-          d.N = ntc * b2;
-          d.K = b2;
-          d.flags = OZ_CONJ_A;
-          oz_check(d, 1, oz_vcat_elems_, gsz, oz_z1_elems_, "P0 stage Z1");
-          add(d, 1, 1);
-        }
+    for (auto &kv : z1p) {  // Z1[tau][m][(c,P,t)] = sum_n conj(V_c[P][t][n]) G2(tau)[m][n]
+      const int sp = kv.first.second;
+      const auto &v = kv.second;
+      const P0Contrib &c0 = pc[v[0].c];
+      const int b2 = c0.b2;
+      const int64_t tab = (int64_t)rt.size();
+      for (const PackRow &x : v) {
+        const P0Contrib &cb = pc[x.c];
+        const int qb = p0_groups_[cgrp[x.c]].qb;
+        for (int P = 0; P < qb; ++P)
+          for (int t = 0; t < cb.b1; ++t) rt.push_back(cb.v + ((int64_t)P * cb.b1 + t) * b2);
+      }
+      OzDesc d{};
+      d.M = (int)(rt.size() - tab);
+      d.a = {tab, 0, 0, 0};
+      d.b = {c0.gb + ((int64_t)t0 * ns + sp) * c0.sb, (int64_t)ns * c0.sb, b2, b2};
+      d.c = {z1pack[v[0].c * ns + sp], 1, 0, 1};
+      d.cn1 = z1t;
+      d.cn0 = (int32_t)z1mp[v[0].c * ns + sp];
+      d.cnd = b2;
+      d.aks = d.bks = 1;
+      d.N = ntc * b2;
+      d.K = b2;
+      d.flags = OZ_CONJ_A;
+      check_tab(tab, d.M, b2, 0, 1, l.flat_V, "P0 stage Z1 (V rows)");
+      oz_check(d, 1, l.flat_V, gsz, oz_z1_elems_, "P0 stage Z1");
+      add(d, 1, 1);
     }
-    stage(oz_p0_, s0, OZB_VCAT, OZB_GFF, OZB_Z1);
+    stage(oz_p0_, s0, OZB_VFF, OZB_GFF, OZB_Z1);
     s0 = ts.size();
-    for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {  // Z[(tau,P)][(p,m)] = sum_t G1(beta-tau)[t][p] Z1[P][t][tau][m]
-      const P0Group &g = p0_groups_[gi];
-      for (int c = g.c0; c < g.c1; ++c)
-        for (int sp = 0; sp < ns; ++sp) {
-          const P0Contrib &cb = pc[c];
-          const int qb = g.qb, b1 = cb.b1, b2 = cb.b2;
-          OzDesc d{};
-          d.a = {z1c[c * ns + sp] * tp, b1, 0, 1};
-          d.ra = (int64_t)qb * b2 * b1;
-          d.b = {cb.ga + ((int64_t)(nts - 1 - t0) * ns + sp) * cb.sa, 1, 0, 1};
-          d.bks = b1;
-          d.rb = -(int64_t)ns * cb.sa;
-          d.c = {pg[gi].zc * tp + zcol[c * ns + sp], pg[gi].zld, 1, b2};
-          d.cn1 = b2;
-          d.cnd = 1;
-          d.rc = (int64_t)qb * pg[gi].zld;
-          d.aks = 1;
-          d.M = qb * b2;
-          d.N = b1;
-          d.K = b1;
-          oz_check(d, ntc, oz_z1_elems_, gsz, oz_zcat_elems_, "P0 stage Z");
-          add(d, ntc, REPG);
-        }
+    for (auto &kv : zp) {  // Zcat[tau][P][K = (c,s,m,p)] = sum_t G1(beta-tau)[t][p] Z1[tau][m][(c,P,t)]
+      const int sp = kv.first.second;
+      const auto &v = kv.second;
+      const P0Contrib &c0 = pc[v[0].c];
+      const int b1 = c0.b1;
+      const int64_t taba = (int64_t)rt.size();
+      for (const PackRow &x : v) {
+        const P0Contrib &cb = pc[x.c];
+        const int qb = p0_groups_[cgrp[x.c]].qb, k = x.c * ns + sp;
+        for (int P = 0; P < qb; ++P)
+          for (int m = 0; m < cb.b2; ++m) rt.push_back(z1pack[k] + m * z1mp[k] + z1pos[k] + (int64_t)P * b1);
+      }
+      const int64_t tabc = (int64_t)rt.size();
+      for (const PackRow &x : v) {
+        const P0Contrib &cb = pc[x.c];
+        const int gi = cgrp[x.c], qb = p0_groups_[gi].qb, k = x.c * ns + sp;
+        for (int P = 0; P < qb; ++P)
+          for (int m = 0; m < cb.b2; ++m)
+            rt.push_back(pg[gi].zc + (int64_t)P * pg[gi].zld + zcol[k] + (int64_t)m * b1);
+      }
+      OzDesc d{};
+      d.M = (int)(tabc - taba);
+      d.a = {taba, 0, 0, 0};
+      d.ra = z1t;
+      d.b = {c0.ga + ((int64_t)(nts - 1 - t0) * ns + sp) * c0.sa, 1, 0, 1};
+      d.bks = b1;
+      d.rb = -(int64_t)ns * c0.sa;
+      d.c = {tabc, 0, 0, 0};
+      d.rc = zct;
+      d.cn1 = 1;
+      d.cnd = 1;
+      d.aks = 1;
+      d.N = b1;
+      d.K = b1;
+      check_tab(taba, d.M, b1, z1t, ntc, oz_z1_elems_, "P0 stage Z (Z1 rows)");
+      check_tab(tabc, d.M, b1, zct, ntc, oz_zcat_elems_, "P0 stage Z (Zcat rows)");
+      oz_check(d, ntc, oz_z1_elems_, gsz, oz_zcat_elems_, "P0 stage Z");
+      add(d, ntc, REPG);
     }
     stage(oz_p0_, s0, OZB_Z1, OZB_GFF, OZB_ZCAT);
     s0 = ts.size();
@@ -1577,7 +1648,7 @@ void Engine::build_oz_lists() {
       const P0Group &g = p0_groups_[gi];
       if (g.c1 == g.c0) continue;
       OzDesc d{};
-      d.a = {pg[gi].zc * tp, pg[gi].zld, 0, 1};
+      d.a = {pg[gi].zc, zct, pg[gi].zld, g.qb};
       d.b = {pg[gi].voff, pg[gi].zld, 0, 1};
       d.c = {g.pout + (int64_t)t0 * g.pstride, g.pstride, 1, g.qb};
       d.cn1 = g.qb;
@@ -1594,7 +1665,7 @@ void Engine::build_oz_lists() {
     stage(oz_p0_, s0, OZB_ZCAT, OZB_VCAT, OZB_P0);
   }
 
-  // ---- Sigma: W per P~ block group, U per contribution, Sigma per owner ----
+  // ---- Sigma ----------------------------------------------------------------
   std::vector<OzPerm> pb, psg;
   struct SG { int64_t boff, wc; int ncol; };
   std::vector<SG> sg;
@@ -1615,7 +1686,6 @@ void Engine::build_oz_lists() {
     wct += (int64_t)qb * ncol;
   }
   oz_bcat_elems_ = boff;
-  // U columns per owner (the same for both spins of an AO block), Vcat of Sigma per AO block
   std::vector<int> ucol(sc.size(), 0);
   std::map<std::pair<int, int>, std::pair<int64_t, int>> vs;  // (c0, c1) -> (VcatS offset, uld)
   int64_t vsoff = 0, uct = 0;
@@ -1638,6 +1708,12 @@ void Engine::build_oz_lists() {
     uct += (int64_t)o.n * uld;
   }
   oz_vcats_elems_ = vsoff;
+  // U packs: (G2 block, spin) -> [(owner, contribution)]
+  std::map<std::pair<int64_t, int>, std::vector<std::pair<int, int>>> up;
+  for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {
+    const Owner &o = sig_own_host_[oi];
+    for (int c = o.c0; c < o.c1; ++c) up[{sc[c].gb, o.s}].push_back({(int)oi, c});
+  }
   const int64_t sig_tau_bytes = 16 * std::max<int64_t>(1, wct + uct);
   const int tsg = (int)std::max<int64_t>(1, std::min<int64_t>(nts, tc_chunk_bytes_ / sig_tau_bytes));
   oz_tch_sig_ = tsg;
@@ -1646,7 +1722,7 @@ void Engine::build_oz_lists() {
   for (int t0 = 0; t0 < nts; t0 += tsg) {
     const int ntc = std::min(tsg, nts - t0);
     size_t s0 = ts.size();
-    {  // W[(tau,Q)][(c,j,n)] = sum_P op(P~(tau))[Q][P] conj(Vt_c[P][j][n])
+    {  // W[tau][Q][(c,j,n)] = sum_P op(P~(tau))[Q][P] conj(Vt_c[P][j][n])
       size_t gi = 0;
       for (const auto &grp : sig_groups_) {
         const SigContrib &c0 = sc[grp.second[0]];
@@ -1654,7 +1730,7 @@ void Engine::build_oz_lists() {
         OzDesc d{};
         d.a = {c0.pq + (int64_t)t0 * c0.pstride, c0.pstride, qb, qb};
         d.b = {sg[gi].boff, qb, 0, 1};
-        d.c = {sg[gi].wc * tsg, sg[gi].ncol, 0, 1};
+        d.c = {sg[gi].wc, wct, sg[gi].ncol, qb};
         d.cn1 = 1;
         d.cnd = 1;
         d.aks = d.bks = 1;
@@ -1669,29 +1745,43 @@ void Engine::build_oz_lists() {
     }
     stage(oz_sig_, s0, OZB_PFF, OZB_BCAT, OZB_W);
     s0 = ts.size();
-    for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {  // U_c[Q][j][m] = sum_n W[Q][(c,j,n)] G2(tau)[m][n]
-      const Owner &o = sig_own_host_[oi];
-      const int uld = vs[std::make_pair(o.c0, o.c1)].second, b1 = o.n;
-      for (int c = o.c0; c < o.c1; ++c) {
-        const SigContrib &cb = sc[c];
+    for (auto &kv : up) {  // U[tau][j][(c,Q,m)] = sum_n W[tau][Q][(c,j,n)] G2(tau)[m][n]
+      const int sp = kv.first.second;
+      const auto &v = kv.second;
+      const SigContrib &c0 = sc[v[0].second];
+      const int b2 = c0.b2;
+      const int64_t taba = (int64_t)rt.size();
+      for (const auto &x : v) {
+        const int c = x.second, b1 = sig_b1_[c];
         const SG &g = sg[cgroup[c]];
-        const int qb = cb.qb, b2 = cb.b2;
-        OzDesc d{};
-        d.a = {g.wc * tsg + ccol[c], g.ncol, b2, b1};
-        d.ra = (int64_t)qb * g.ncol;
-        d.b = {cb.gb + ((int64_t)t0 * ns + o.s) * cb.sb, b2, 0, 1};
-        d.rb = (int64_t)ns * cb.sb;
-        d.c = {uoff[oi] * tsg + ucol[c], b2, uld, b1};
-        d.cn1 = 1;
-        d.cnd = 1;
-        d.rc = (int64_t)b1 * uld;
-        d.aks = d.bks = 1;
-        d.M = qb * b1;
-        d.N = b2;
-        d.K = b2;
-        oz_check(d, ntc, oz_w_elems_, gsz, oz_u_elems_, "Sigma stage U");
-        add(d, ntc, REPG);
+        for (int Q = 0; Q < sc[c].qb; ++Q)
+          for (int j = 0; j < b1; ++j) rt.push_back(g.wc + (int64_t)Q * g.ncol + ccol[c] + (int64_t)j * b2);
       }
+      const int64_t tabc = (int64_t)rt.size();
+      for (const auto &x : v) {
+        const int c = x.second, b1 = sig_b1_[c];
+        const Owner &o = sig_own_host_[x.first];
+        const int uld = vs[std::make_pair(o.c0, o.c1)].second;
+        for (int Q = 0; Q < sc[c].qb; ++Q)
+          for (int j = 0; j < b1; ++j) rt.push_back(uoff[x.first] + ucol[c] + (int64_t)Q * b2 + (int64_t)j * uld);
+      }
+      OzDesc d{};
+      d.M = (int)(tabc - taba);
+      d.a = {taba, 0, 0, 0};
+      d.ra = wct;
+      d.b = {c0.gb + ((int64_t)t0 * ns + sp) * c0.sb, b2, 0, 1};
+      d.rb = (int64_t)ns * c0.sb;
+      d.c = {tabc, 0, 0, 0};
+      d.rc = uct;
+      d.cn1 = 1;
+      d.cnd = 1;
+      d.aks = d.bks = 1;
+      d.N = b2;
+      d.K = b2;
+      check_tab(taba, d.M, b2, wct, ntc, oz_w_elems_, "Sigma stage U (W rows)");
+      check_tab(tabc, d.M, b2, uct, ntc, oz_u_elems_, "Sigma stage U (U rows)");
+      oz_check(d, ntc, oz_w_elems_, gsz, oz_u_elems_, "Sigma stage U");
+      add(d, ntc, REPG);
     }
     stage(oz_sig_, s0, OZB_W, OZB_GFF, OZB_U);
     s0 = ts.size();
@@ -1700,7 +1790,7 @@ void Engine::build_oz_lists() {
       const auto &v = vs[std::make_pair(o.c0, o.c1)];
       if (v.second == 0) continue;
       OzDesc d{};
-      d.a = {uoff[oi] * tsg, v.second, 0, 1};
+      d.a = {uoff[oi], uct, v.second, o.n};
       d.b = {v.first, v.second, 0, 1};
       d.c = {o.out + (int64_t)t0 * o.ostride, o.ostride, 1, o.n};
       d.cn1 = o.n;
@@ -1732,6 +1822,7 @@ void Engine::build_oz_lists() {
   GWGB_REQUIRE(ts.size() < (size_t)INT32_MAX, GWGB_E_UNSUPPORTED, "too many sliced GEMM tasks");
   oz_descs_.upload(ds, st_);
   oz_tasks_.upload(ts, st_);
+  oz_rowtab_.upload(rt.empty() ? std::vector<int64_t>(1, 0) : rt, st_);
   oz_perm_v_.upload(pv, st_);
   oz_perm_b_.upload(pb, st_);
   oz_perm_s_.upload(psg, st_);

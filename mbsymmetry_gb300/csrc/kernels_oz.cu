@@ -47,12 +47,7 @@ constexpr int OZ_KP = 2 * OZ_KR;            // real K per round (BF16 elements p
 constexpr int OZ_SBO = (OZ_KP / 8) * 128;   // bytes between 8-row groups of core matrices
 constexpr int OZ_PA = OZ_M * OZ_KP * 2;     // bytes of one A slice plane
 constexpr int OZ_PB = OZ_NR * OZ_KP * 2;    // bytes of one B slice plane
-constexpr int OZ_TILES = 4 * OZ_PA + 4 * OZ_PB;
-constexpr int OZ_SMEM = 80 * 1024;          // requested per CTA: at most two CTAs per SM
-constexpr int OZ_TMEM = 256;                // D0 | D1 | D2, OZ_NR columns each
 constexpr int OZ_EMIN = -100, OZ_EMAX = 100;
-static_assert(OZ_TILES + 1024 <= OZ_SMEM, "slice planes must fit the requested shared memory");
-static_assert(3 * OZ_NR <= OZ_TMEM, "three accumulators must fit the TMEM allocation");
 static_assert(OZ_KP % 16 == 0, "a round is a whole number of BF16 MMA K steps");
 
 // E with |x| < 2^E for every |x| <= m (m >= 0), clamped to [OZ_EMIN, OZ_EMAX].
@@ -114,212 +109,334 @@ __device__ __forceinline__ uint32_t seg_off(int r, int k8) {
   return (uint32_t)((r >> 3) * OZ_SBO + (k8 >> 3) * 128 + (r & 7) * 16);
 }
 
-__device__ __forceinline__ int64_t row_off(const OzRows &m, int r) {
+// Offset of local row r of a row map (d == 0: from the row table).
+__device__ __forceinline__ int64_t row_off(const OzRows &m, int r, const int64_t *__restrict__ rowtab) {
+  if (m.d == 0) return __ldg(rowtab + m.base + r);
+  if (m.d == 1) return m.base + (int64_t)r * m.s1;
   return m.base + (int64_t)(r / m.d) * m.s1 + (int64_t)(r % m.d) * m.s0;
 }
 
-__global__ void __launch_bounds__(128, 2)
+// 32 lanes x 8 consecutive 32-bit columns from registers into TMEM (this warp's lane quarter).
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+               "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+constexpr int OZ_THREADS = 256;         // warps 0-3 drain (TMEM lanes), 4-7 stage; lane 0 of warp 4 issues MMAs
+constexpr int OZ_ACC = 3 * OZ_NR;       // TMEM columns of one accumulator set D0 | D1 | D2
+constexpr int OZ_TMEM_WS = 512;         // two accumulator sets, then the float-float sums (hi | lo)
+constexpr int OZ_SUM = 2 * OZ_ACC;      // TMEM column of the running sums of multi-round GEMMs
+constexpr int OZ_BUF = 4 * OZ_PA + 4 * OZ_PB;
+constexpr int OZ_SMEM_WS = 120 * 1024;  // two tile buffers (96 KB); more than half an SM: one CTA per SM
+static_assert(2 * OZ_BUF + 1024 <= OZ_SMEM_WS, "two tile buffers must fit the requested shared memory");
+static_assert(2 * OZ_ACC + 2 * OZ_NR <= OZ_TMEM_WS, "two accumulator sets and the sums must fit the TMEM allocation");
+
+// Combined, scaled value of one accumulator column: (D0 + D1 + D2) * sc as a
+// float-float pair (D0, D1 exact; D2 small).
+__device__ __forceinline__ void oz_combine(float x0, float x1, float x2, float sc, float &h, float &l) {
+  float vh, vl;
+  two_sum(x0, x1, vh, vl);
+  vl += x2;
+  h = vh + vl;
+  l = (vl - (h - vh)) * sc;
+  h *= sc;
+}
+
+__device__ __forceinline__ void oz_store(void *Cg, int64_t o, bool f64, double alpha, float rh, float ih, float rl,
+                                         float il) {
+  if (f64)
+    reinterpret_cast<double2 *>(Cg)[o] =
+        make_double2(alpha * ((double)rh + (double)rl), alpha * ((double)ih + (double)il));
+  else
+    reinterpret_cast<float4 *>(Cg)[o] = make_float4(rh, ih, rl, il);
+}
+
+// Persistent warp-specialised sliced GEMM.  Every role walks the same work
+// sequence (tasks of this CTA with a grid stride, repetitions, rounds of
+// OZ_KR complex K), counting rounds i.  Rings: 2 shared tile buffers
+// (full / empty), 2 TMEM accumulator sets (done / afree), 4 exponent slots
+// (eready / efree).  Every wait is bounded; a wait that runs out sets the error
+// word and an abort flag that ends every role's loop, and TMEM is released only
+// after the MMAs issued so far have completed (bounded wait on `last`).
+__global__ void __launch_bounds__(OZ_THREADS, 1)
     oz_gemm_kernel(const OzDesc *__restrict__ descs, const OzTask *__restrict__ tasks, int ntasks,
                    const float4 *__restrict__ Ag, const float4 *__restrict__ Bg, void *__restrict__ Cg,
-                   int *__restrict__ err) {
+                   const int64_t *__restrict__ rowtab, int *__restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint32_t tslot;
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ int ebs[OZ_NC];
-  __shared__ int abort_flag;
-  unsigned char *As = smem, *Bs = smem + 4 * OZ_PA;
+  __shared__ __align__(8) uint64_t full[2], empty[2], done[2], afree[2], eready[4], efree[4], last;
+  __shared__ int ea_s[4][OZ_M], eb_s[4][OZ_NC];
+  __shared__ int abort_flag, issued;
   const int tid = threadIdx.x, warp = tid >> 5;
-  if (warp == 0) tc::tmem_alloc(&tslot, OZ_TMEM);
+  if (warp == 0) tc::tmem_alloc(&tslot, OZ_TMEM_WS);
   if (tid == 0) {
-    tc::mbar_init(&bar, 1);
+    for (int j = 0; j < 2; ++j) {
+      tc::mbar_init(&full[j], 128);
+      tc::mbar_init(&empty[j], 1);
+      tc::mbar_init(&done[j], 1);
+      tc::mbar_init(&afree[j], 128);
+    }
+    for (int j = 0; j < 4; ++j) {
+      tc::mbar_init(&eready[j], 128);
+      tc::mbar_init(&efree[j], 128);
+    }
+    tc::mbar_init(&last, 1);
     abort_flag = 0;
+    issued = 0;
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tm = tslot;
-  const uint32_t tlane = tm + ((uint32_t)(warp * 32) << 16);
-  uint32_t phase = 0;
-  bool pending = false;  // a commit whose completion nobody observed (abort path)
+  // bounded wait; false when it ran out (error word and abort flag set) or another role aborted
+  auto bwait = [&](uint64_t *b, uint32_t par) -> bool {
+    for (int rep = 0; rep < 64; ++rep) {
+      if (tc::mbar_wait(b, par, 65536)) return true;
+      if (*(volatile int *)&abort_flag) return false;
+    }
+    atomicExch(err, 1);
+    *(volatile int *)&abort_flag = 1;
+    return false;
+  };
+  auto aborted = [&]() { return *(volatile int *)&abort_flag != 0; };
 
-  for (int ti = blockIdx.x; ti < ntasks && !abort_flag; ti += gridDim.x) {
-   const OzTask tk = tasks[ti];
-   for (int rr = 0; rr < tk.nrep && !abort_flag; ++rr) {
-    const int rep = tk.rep0 + rr, mt = tk.mtnt >> 16, nt = tk.mtnt & 0xffff;
-    const OzDesc &dg = descs[tk.desc];
-    const int M = dg.M, N = dg.N, K = dg.K, flags = dg.flags;
-    const int Mt = min(OZ_M, M - mt * OZ_M), Nt = min(OZ_NC, N - nt * OZ_NC);
-    const int aks = dg.aks, bks = dg.bks;
-    // this thread's A row and (with qd) B row
+  if (warp >= 4) {
+    // ------------------------------ producers (and the MMA issuer) ------------------------------
+    const int pt = tid - 128;
+    const int bn = pt >> 2, qd = pt & 3;
+    int i = 0, nissued = 0;
+    bool stop = false;
+    for (int ti = blockIdx.x; ti < ntasks && !stop; ti += gridDim.x) {
+      const OzTask tk = tasks[ti];
+      const OzDesc dg = descs[tk.desc];
+      const int mt = tk.mtnt >> 16, nt = tk.mtnt & 0xffff;
+      const int Mt = min(OZ_M, dg.M - mt * OZ_M), Nt = min(OZ_NC, dg.N - nt * OZ_NC);
+      const int ngrp = (Nt + 7) >> 3;
+      const bool rv = pt < Mt, bv = bn < Nt, bw = bn < 8 * ngrp;
+      const int64_t arow0 = rv ? row_off(dg.a, mt * OZ_M + pt, rowtab) : 0;
+      const int64_t brow0 = bv ? row_off(dg.b, nt * OZ_NC + bn, rowtab) : 0;
+      const bool ca = dg.flags & OZ_CONJ_A, cb = dg.flags & OZ_CONJ_B;
+      for (int rr = 0; rr < tk.nrep && !stop; ++rr) {
+        const int rep = tk.rep0 + rr;
+        const float4 *arow = Ag + arow0 + (int64_t)rep * dg.ra;
+        const float4 *brow = Bg + brow0 + (int64_t)rep * dg.rb;
+        for (int k0 = 0; k0 < dg.K; k0 += OZ_KR, ++i) {
+          if (aborted()) { stop = true; break; }
+          const int b = i & 1, e = i & 3;
+          if (i >= 2 && !bwait(&empty[b], ((i >> 1) - 1) & 1)) { stop = true; break; }
+          if (i >= 4 && !bwait(&efree[e], ((i >> 2) - 1) & 1)) { stop = true; break; }
+          const int kn = min(OZ_KR, dg.K - k0);
+          const int nks = (kn + 7) >> 3;  // MMA K steps this round (8 complex each)
+          unsigned char *As = smem + b * OZ_BUF, *Bs = As + 4 * OZ_PA;
+          {  // A: row pt (rows past Mt stage zeros)
+            float4 v[OZ_KR];
+            float m = 0.f;
+#pragma unroll
+            for (int k = 0; k < OZ_KR; ++k) {
+              v[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+              if (rv && k < kn) v[k] = __ldg(arow + (int64_t)(k0 + k) * dg.aks);
+              m = fmaxf(m, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
+            }
+            const int ea = oz_exponent(m);
+            const float f = oz_pow2(7 - ea);
+#pragma unroll
+            for (int g = 0; g < OZ_KR / 4; ++g) {
+              if (g < 2 * nks) {
+                uint32_t w[4][4];
+                if (rv) {
+#pragma unroll
+                  for (int j = 0; j < 4; ++j) {
+                    float4 x = v[g * 4 + j];
+                    if (ca) { x.y = -x.y; x.w = -x.w; }
+                    float sr[4], si[4];
+                    oz_slice(x.x, x.z, f, sr);
+                    oz_slice(x.y, x.w, f, si);
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) w[p][j] = bf2(sr[p], si[p]);
+                  }
+                } else {
+#pragma unroll
+                  for (int p = 0; p < 4; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0u;
+                }
+                const uint32_t o = seg_off(pt, 8 * g);
+#pragma unroll
+                for (int p = 0; p < 4; ++p)
+                  *reinterpret_cast<uint4 *>(As + p * OZ_PA + o) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+              }
+            }
+            ea_s[e][pt] = ea;
+          }
+          {  // B: four threads per complex row; rows (n,0) = [Br -Bi], (n,1) = [Bi Br]
+            float4 v[4];
+            float mb = 0.f;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const int k = 4 * qd + j;
+              v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+              if (bv && k < kn) v[j] = __ldg(brow + (int64_t)(k0 + k) * dg.bks);
+              if (cb) { v[j].y = -v[j].y; v[j].w = -v[j].w; }
+              mb = fmaxf(mb, fmaxf(fabsf(v[j].x), fabsf(v[j].y)));
+            }
+            mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, 1));
+            mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, 2));
+            const int eb = oz_exponent(mb);
+            if (qd == 0) eb_s[e][bn] = eb;
+            if (bw && qd < 2 * nks) {
+              uint32_t w0[4][4], w1[4][4];
+              if (bv) {
+                const float f = oz_pow2(7 - eb);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                  float sr[4], si[4];
+                  oz_slice(v[j].x, v[j].z, f, sr);
+                  oz_slice(v[j].y, v[j].w, f, si);
+#pragma unroll
+                  for (int p = 0; p < 4; ++p) {
+                    w0[p][j] = bf2(sr[p], -si[p]);
+                    w1[p][j] = bf2(si[p], sr[p]);
+                  }
+                }
+              } else {
+#pragma unroll
+                for (int p = 0; p < 4; ++p)
+#pragma unroll
+                  for (int j = 0; j < 4; ++j) w0[p][j] = w1[p][j] = 0u;
+              }
+              const uint32_t o0 = seg_off(2 * bn, 8 * qd), o1 = seg_off(2 * bn + 1, 8 * qd);
+#pragma unroll
+              for (int p = 0; p < 4; ++p) {
+                *reinterpret_cast<uint4 *>(Bs + p * OZ_PB + o0) = make_uint4(w0[p][0], w0[p][1], w0[p][2], w0[p][3]);
+                *reinterpret_cast<uint4 *>(Bs + p * OZ_PB + o1) = make_uint4(w1[p][0], w1[p][1], w1[p][2], w1[p][3]);
+              }
+            }
+          }
+          tc::fence_async_smem();
+          tc::mbar_arrive(&eready[e]);
+          tc::mbar_arrive(&full[b]);
+          if (pt == 0) {  // MMA issue for this round once all producers have staged it
+            const int a = i & 1;
+            bool ok = bwait(&full[b], (i >> 1) & 1);
+            if (ok && i >= 2) ok = bwait(&afree[a], ((i >> 1) - 1) & 1);
+            if (ok) {
+              tc::fence_after_sync();
+              const uint32_t id = tc::idesc_bf16(OZ_M, 16 * ngrp);
+              const uint32_t a0 = tc::smem_u32(As), b0 = a0 + 4 * OZ_PA;
+              const uint32_t d0 = tm + (uint32_t)(a * OZ_ACC), d1 = d0 + OZ_NR, d2 = d0 + 2 * OZ_NR;
+              for (int ks = 0; ks < nks; ++ks) {
+                auto da = [&](int p) { return tc::make_desc(a0 + p * OZ_PA + ks * 256, 128, OZ_SBO); };
+                auto db = [&](int p) { return tc::make_desc(b0 + p * OZ_PB + ks * 256, 128, OZ_SBO); };
+                const uint32_t acc = ks > 0 ? 1u : 0u;
+                tc::mma_bf16(d0, da(0), db(0), id, acc);
+                tc::mma_bf16(d1, da(0), db(1), id, acc);
+                tc::mma_bf16(d1, da(1), db(0), id, 1u);
+                tc::mma_bf16(d2, da(0), db(2), id, acc);
+                tc::mma_bf16(d2, da(1), db(1), id, 1u);
+                tc::mma_bf16(d2, da(2), db(0), id, 1u);
+                tc::mma_bf16(d2, da(0), db(3), id, 1u);
+                tc::mma_bf16(d2, da(1), db(2), id, 1u);
+                tc::mma_bf16(d2, da(2), db(1), id, 1u);
+                tc::mma_bf16(d2, da(3), db(0), id, 1u);
+              }
+              tc::commit(&empty[b]);
+              tc::commit(&done[a]);
+              ++nissued;
+            }
+          }
+          __syncwarp();
+        }
+      }
+    }
+    if (pt == 0) {
+      if (nissued > 0) tc::commit(&last);  // arrives when every MMA issued above has completed
+      issued = nissued;
+    }
+  } else {
+    // ------------------------------ drain (row = TMEM lane = tid) ------------------------------
     const int r = tid;
-    const bool rv = r < Mt;
-    const float4 *arow = Ag + (rv ? row_off(dg.a, mt * OZ_M + r) + (int64_t)rep * dg.ra : 0);
-    const int bn = tid >> 2, qd = tid & 3;
-    const bool bv = bn < Nt;
-    const float4 *brow = Bg + (bv ? row_off(dg.b, nt * OZ_NC + bn) + (int64_t)rep * dg.rb : 0);
-    const bool ca = flags & OZ_CONJ_A, cb = flags & OZ_CONJ_B;
-    float acc_h[OZ_NR], acc_l[OZ_NR];
+    const uint32_t tlane = tm + ((uint32_t)(warp * 32) << 16);
+    const uint32_t sum_h = tlane + OZ_SUM, sum_l = sum_h + OZ_NR;
+    int i = 0;
+    bool stop = false;
+    for (int ti = blockIdx.x; ti < ntasks && !stop; ti += gridDim.x) {
+      const OzTask tk = tasks[ti];
+      const OzDesc dg = descs[tk.desc];
+      const int mt = tk.mtnt >> 16, nt = tk.mtnt & 0xffff;
+      const int Mt = min(OZ_M, dg.M - mt * OZ_M), Nt = min(OZ_NC, dg.N - nt * OZ_NC);
+      const int ngrp = (Nt + 7) >> 3;
+      const bool rv = r < Mt, f64 = dg.flags & OZ_OUT_F64;
+      const int64_t crow0 = rv ? row_off(dg.c, mt * OZ_M + r, rowtab) : 0;
+      const int ng0 = nt * OZ_NC;
+      const int nq0 = ng0 / dg.cnd, nr0 = ng0 - nq0 * dg.cnd;  // column ng0 = nq0 * cnd + nr0
+      for (int rr = 0; rr < tk.nrep && !stop; ++rr) {
+        const int64_t co = crow0 + (int64_t)(tk.rep0 + rr) * dg.rc;
+        for (int k0 = 0; k0 < dg.K; k0 += OZ_KR, ++i) {
+          if (aborted()) { stop = true; break; }
+          const int a = i & 1, e = i & 3;
+          if (!bwait(&done[a], (i >> 1) & 1) || !bwait(&eready[e], (i >> 2) & 1)) { stop = true; break; }
+          tc::fence_after_sync();
+          const bool first = k0 == 0, lastr = k0 + OZ_KR >= dg.K;
+          const int ea = ea_s[e][r];
+          const uint32_t base = tlane + (uint32_t)(a * OZ_ACC);
+          int nq = nq0, nrr = nr0;  // output column cursor
 #pragma unroll
-    for (int j = 0; j < OZ_NR; ++j) acc_h[j] = acc_l[j] = 0.f;
-
-    for (int k0 = 0; k0 < K; k0 += OZ_KR) {
-      const int kn = min(OZ_KR, K - k0);
-      // ---- A: one row per thread; exponent from the row's largest hi part ----
-      float m = 0.f;
-      if (rv)
-        for (int k = 0; k < kn; ++k) {
-          const float4 v = __ldg(arow + (int64_t)(k0 + k) * aks);
-          m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
-        }
-      const int ea = oz_exponent(m);
-      {
-        const float f = oz_pow2(7 - ea);
+          for (int g = 0; g < OZ_NR / 8; ++g) {  // groups of 8 real columns (4 complex)
+            if (g < 2 * ngrp) {
+              float x0[8], x1[8], x2[8], sh[8], sl[8];
+              tc::tmem_ld8(base + (uint32_t)(8 * g), x0);
+              tc::tmem_ld8(base + (uint32_t)(OZ_NR + 8 * g), x1);
+              tc::tmem_ld8(base + (uint32_t)(2 * OZ_NR + 8 * g), x2);
+              if (!first) {
+                tc::tmem_ld8(sum_h + (uint32_t)(8 * g), sh);
+                tc::tmem_ld8(sum_l + (uint32_t)(8 * g), sl);
+              }
 #pragma unroll
-        for (int g = 0; g < OZ_KR / 4; ++g) {
-          uint32_t w[4][4];
+              for (int j = 0; j < 8; ++j) {
+                const float sc = oz_pow2(ea + eb_s[e][4 * g + (j >> 1)] - 14);
+                float vh, vl;
+                oz_combine(x0[j], x1[j], x2[j], sc, vh, vl);
+                if (first) {
+                  sh[j] = vh;
+                  sl[j] = vl;
+                } else {
+                  ff_add(sh[j], sl[j], vh, vl);
+                }
+              }
+              if (lastr) {
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int k = g * 4 + j;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (rv && k < kn) v = __ldg(arow + (int64_t)(k0 + k) * aks);
-            if (ca) { v.y = -v.y; v.w = -v.w; }
-            float sr[4], si[4];
-            oz_slice(v.x, v.z, f, sr);
-            oz_slice(v.y, v.w, f, si);
-#pragma unroll
-            for (int p = 0; p < 4; ++p) w[p][j] = bf2(sr[p], si[p]);
+                for (int j = 0; j < 8; j += 2) {
+                  const int n = 4 * g + (j >> 1);
+                  if (rv && n < Nt) {
+                    oz_store(Cg, co + nq * dg.cn1 + nrr * dg.cn0, f64, dg.alpha, sh[j], sh[j + 1], sl[j], sl[j + 1]);
+                    if (++nrr == dg.cnd) {
+                      nrr = 0;
+                      ++nq;
+                    }
+                  }
+                }
+              } else {
+                tmem_st8(sum_h + (uint32_t)(8 * g), sh);
+                tmem_st8(sum_l + (uint32_t)(8 * g), sl);
+              }
+            }
           }
-          const uint32_t o = seg_off(r, 8 * g);
-#pragma unroll
-          for (int p = 0; p < 4; ++p)
-            *reinterpret_cast<uint4 *>(As + p * OZ_PA + o) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
-        }
-      }
-      // ---- B: four threads per complex row (4 complex K each); rows (n,0) = [Br -Bi], (n,1) = [Bi Br] ----
-      {
-        float4 v[4];
-        float mb = 0.f;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int k = 4 * qd + j;
-          v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (bv && k < kn) v[j] = __ldg(brow + (int64_t)(k0 + k) * bks);
-          if (cb) { v[j].y = -v[j].y; v[j].w = -v[j].w; }
-          mb = fmaxf(mb, fmaxf(fabsf(v[j].x), fabsf(v[j].y)));
-        }
-        mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, 1));
-        mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, 2));
-        const int eb = oz_exponent(mb);
-        if (qd == 0) ebs[bn] = eb;
-        const float f = oz_pow2(7 - eb);
-        uint32_t w0[4][4], w1[4][4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          float sr[4], si[4];
-          oz_slice(v[j].x, v[j].z, f, sr);
-          oz_slice(v[j].y, v[j].w, f, si);
-#pragma unroll
-          for (int p = 0; p < 4; ++p) {
-            w0[p][j] = bf2(sr[p], -si[p]);
-            w1[p][j] = bf2(si[p], sr[p]);
-          }
-        }
-        const uint32_t o0 = seg_off(2 * bn, 8 * qd), o1 = seg_off(2 * bn + 1, 8 * qd);
-#pragma unroll
-        for (int p = 0; p < 4; ++p) {
-          *reinterpret_cast<uint4 *>(Bs + p * OZ_PB + o0) = make_uint4(w0[p][0], w0[p][1], w0[p][2], w0[p][3]);
-          *reinterpret_cast<uint4 *>(Bs + p * OZ_PB + o1) = make_uint4(w1[p][0], w1[p][1], w1[p][2], w1[p][3]);
-        }
-      }
-      tc::fence_async_smem();
-      tc::fence_before_sync();
-      __syncthreads();
-      tc::fence_after_sync();
-      // ---- MMAs: classes 0 | 1 | 2-3 into D0 | D1 | D2 ----
-      if (tid == 0) {
-        const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs);
-        const uint32_t id = tc::idesc_bf16(OZ_M, OZ_NR);
-        const uint32_t d0 = tm, d1 = tm + OZ_NR, d2 = tm + 2 * OZ_NR;
-#pragma unroll
-        for (int ks = 0; ks < OZ_KP / 16; ++ks) {
-          auto da = [&](int p) { return tc::make_desc(a0 + p * OZ_PA + ks * 256, 128, OZ_SBO); };
-          auto db = [&](int p) { return tc::make_desc(b0 + p * OZ_PB + ks * 256, 128, OZ_SBO); };
-          const uint32_t acc = ks > 0 ? 1u : 0u;
-          tc::mma_bf16(d0, da(0), db(0), id, acc);
-          tc::mma_bf16(d1, da(0), db(1), id, acc);
-          tc::mma_bf16(d1, da(1), db(0), id, 1u);
-          tc::mma_bf16(d2, da(0), db(2), id, acc);
-          tc::mma_bf16(d2, da(1), db(1), id, 1u);
-          tc::mma_bf16(d2, da(2), db(0), id, 1u);
-          tc::mma_bf16(d2, da(0), db(3), id, 1u);
-          tc::mma_bf16(d2, da(1), db(2), id, 1u);
-          tc::mma_bf16(d2, da(2), db(1), id, 1u);
-          tc::mma_bf16(d2, da(3), db(0), id, 1u);
-        }
-        tc::commit(&bar);
-      }
-      const bool ok = tc::mbar_wait(&bar, phase);
-      phase ^= 1u;
-      if (__syncthreads_or(!ok)) {
-        if (tid == 0) {
-          atomicExch(err, 1);
-          abort_flag = 1;
-        }
-        pending = true;
-        break;
-      }
-      tc::fence_after_sync();
-      // ---- drain: combine the classes, scale, add to the float-float accumulator ----
-#pragma unroll
-      for (int j0 = 0; j0 < OZ_NR; j0 += 8) {
-        float x0[8], x1[8], x2[8];
-        tc::tmem_ld8(tlane + (uint32_t)j0, x0);
-        tc::tmem_ld8(tlane + (uint32_t)(OZ_NR + j0), x1);
-        tc::tmem_ld8(tlane + (uint32_t)(2 * OZ_NR + j0), x2);
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const float sc = oz_pow2(ea + ebs[(j0 + j) >> 1] - 14);
-          float vh, vl;
-          two_sum(x0[j], x1[j], vh, vl);
-          vl += x2[j];
-          const float s = vh + vl;
-          vl -= s - vh;
-          ff_add(acc_h[j0 + j], acc_l[j0 + j], s * sc, vl * sc);
-        }
-      }
-      tc::fence_before_sync();
-      __syncthreads();  // shared tiles, ebs and TMEM free for the next round
-    }
-    __syncthreads();
-    if (abort_flag) break;
-    // ---- output ----
-    if (rv) {
-      const int64_t co = row_off(dg.c, mt * OZ_M + r) + (int64_t)rep * dg.rc;
-#pragma unroll
-      for (int n = 0; n < OZ_NC; ++n) {
-        if (n < Nt) {
-          const int ng = nt * OZ_NC + n;
-          const int64_t o = co + (int64_t)(ng / dg.cnd) * dg.cn1 + (int64_t)(ng % dg.cnd) * dg.cn0;
-          if (flags & OZ_OUT_F64) {
-            const double al = dg.alpha;
-            reinterpret_cast<double2 *>(Cg)[o] =
-                make_double2(al * ((double)acc_h[2 * n] + (double)acc_l[2 * n]),
-                             al * ((double)acc_h[2 * n + 1] + (double)acc_l[2 * n + 1]));
-          } else {
-            reinterpret_cast<float4 *>(Cg)[o] =
-                make_float4(acc_h[2 * n], acc_h[2 * n + 1], acc_l[2 * n], acc_l[2 * n + 1]);
-          }
+          if (!lastr) tmem_wait_st();
+          tc::fence_before_sync();
+          tc::mbar_arrive(&afree[a]);
+          tc::mbar_arrive(&efree[e]);
         }
       }
     }
-   }
   }
   __syncthreads();
-  if (tid == 0 && pending) tc::mbar_wait(&bar, phase ^ 1u, 4000000);  // the MMAs of the aborted round
+  if (tid == 0 && issued > 0) tc::mbar_wait(&last, 0u, 4000000);  // every issued MMA has completed
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tm, OZ_TMEM);
+  if (warp == 0) tc::tmem_dealloc(tm, OZ_TMEM_WS);
 }
 
 __global__ void to_ffc_kernel(const double2 *__restrict__ x, float4 *__restrict__ y, int64_t n) {
@@ -347,14 +464,14 @@ __global__ void oz_perm_kernel(const OzPerm *__restrict__ tasks, const double2 *
 }  // namespace
 
 void set_oz_kernel_attributes() {
-  GWGB_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
+  GWGB_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM_WS));
 }
 
 void launch_oz_gemm(const OzDesc *descs, const OzTask *tasks, int ntasks, const float4 *A, const float4 *B, void *C,
-                    int nsm, int *err, cudaStream_t st) {
+                    const int64_t *rowtab, int nsm, int *err, cudaStream_t st) {
   if (ntasks == 0) return;
-  const int grid = std::min(ntasks, 2 * std::max(1, nsm));
-  oz_gemm_kernel<<<grid, 128, OZ_SMEM, st>>>(descs, tasks, ntasks, A, B, C, err);
+  const int grid = std::min(ntasks, std::max(1, nsm));
+  oz_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM_WS, st>>>(descs, tasks, ntasks, A, B, C, rowtab, err);
   GWGB_CUDA(cudaGetLastError());
 }
 

@@ -14,7 +14,8 @@
 namespace gwgb {
 
 // Row map of an operand or of the output: local row r (of the whole descriptor,
-// not of a tile) -> base + (r / d) * s1 + (r % d) * s0 (complex elements).
+// not of a tile) -> base + (r / d) * s1 + (r % d) * s0 (complex elements), or,
+// with d == 0, -> rowtab[base + r] (a table of row offsets).
 struct OzRows {
   int64_t base;
   int64_t s1;
@@ -71,7 +72,7 @@ void set_oz_kernel_attributes();
 // taken in list order with a stride of the grid size).  err: set to 1 when a
 // bounded tensor-core completion wait ran out.
 void launch_oz_gemm(const OzDesc *descs, const OzTask *tasks, int ntasks, const float4 *A, const float4 *B, void *C,
-                    int nsm, int *err, cudaStream_t st);
+                    const int64_t *rowtab, int nsm, int *err, cudaStream_t st);
 
 // y[i] = float-float(x[i]) for n complex elements.
 void launch_to_ffc(const double2 *x, float4 *y, int64_t n, cudaStream_t st);
