@@ -126,7 +126,7 @@ __device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
 }
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
-constexpr int OZ_THREADS = 256;         // warps 0-3 drain (TMEM lanes), 4-7 stage; lane 0 of warp 4 issues MMAs
+constexpr int OZ_THREADS = 512;         // warps 0-7 drain (TMEM lanes), 8-15 stage; lane 0 of warp 8 issues MMAs
 constexpr int OZ_ACC = 3 * OZ_NR;       // TMEM columns of one accumulator set D0 | D1 | D2
 constexpr int OZ_TMEM_WS = 512;         // two accumulator sets, then the float-float sums (hi | lo)
 constexpr int OZ_SUM = 2 * OZ_ACC;      // TMEM column of the running sums of multi-round GEMMs
@@ -170,21 +170,25 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __shared__ uint32_t tslot;
   __shared__ __align__(8) uint64_t full[2], empty[2], done[2], afree[2], eready[4], efree[4], last;
   __shared__ int ea_s[4][OZ_M], eb_s[4][OZ_NC];
+  __shared__ float amax[2][2][OZ_M];  // per tile buffer: partial row maxima of the two A halves
+  __shared__ __align__(8) uint64_t mx[2];
   __shared__ int abort_flag, issued;
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0) tc::tmem_alloc(&tslot, OZ_TMEM_WS);
   if (tid == 0) {
     for (int j = 0; j < 2; ++j) {
-      tc::mbar_init(&full[j], 128);
+      tc::mbar_init(&full[j], 256);
       tc::mbar_init(&empty[j], 1);
       tc::mbar_init(&done[j], 1);
-      tc::mbar_init(&afree[j], 128);
+      tc::mbar_init(&afree[j], 256);
     }
     for (int j = 0; j < 4; ++j) {
-      tc::mbar_init(&eready[j], 128);
-      tc::mbar_init(&efree[j], 128);
+      tc::mbar_init(&eready[j], 256);
+      tc::mbar_init(&efree[j], 256);
     }
     tc::mbar_init(&last, 1);
+    tc::mbar_init(&mx[0], 256);
+    tc::mbar_init(&mx[1], 256);
     abort_flag = 0;
     issued = 0;
   }
@@ -192,10 +196,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tm = tslot;
-  // bounded wait; false when it ran out (error word and abort flag set) or another role aborted
+  // bounded wait; false when it ran out (error word and abort flag set) or another role aborted.
+  // Each poll may suspend the thread for up to 20 us (hint) until the phase completes, so
+  // waiting roles do not take issue slots from the working ones; 2^16 polls bound the wait.
   auto bwait = [&](uint64_t *b, uint32_t par) -> bool {
-    for (int rep = 0; rep < 64; ++rep) {
-      if (tc::mbar_wait(b, par, 65536)) return true;
+    for (int rep = 0; rep < 256; ++rep) {
+      for (int it = 0; it < 256; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.b32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(tc::smem_u32(b)), "r"(par), "r"(20000u)
+            : "memory");
+        if (ok) return true;
+      }
       if (*(volatile int *)&abort_flag) return false;
     }
     atomicExch(err, 1);
@@ -204,10 +218,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   };
   auto aborted = [&]() { return *(volatile int *)&abort_flag != 0; };
 
-  if (warp >= 4) {
+  if (warp >= 8) {
     // ------------------------------ producers (and the MMA issuer) ------------------------------
-    const int pt = tid - 128;
-    const int bn = pt >> 2, qd = pt & 3;
+    // A: two threads per row (h = K half); B: eight threads per complex row (two complex K each).
+    const int pt = tid - 256;
+    const int ar = pt & 127, ah = pt >> 7;
+    const int bn = pt >> 3, bq = pt & 7;
     int i = 0, nissued = 0;
     bool stop = false;
     for (int ti = blockIdx.x; ti < ntasks && !stop; ti += gridDim.x) {
@@ -216,8 +232,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const int mt = tk.mtnt >> 16, nt = tk.mtnt & 0xffff;
       const int Mt = min(OZ_M, dg.M - mt * OZ_M), Nt = min(OZ_NC, dg.N - nt * OZ_NC);
       const int ngrp = (Nt + 7) >> 3;
-      const bool rv = pt < Mt, bv = bn < Nt, bw = bn < 8 * ngrp;
-      const int64_t arow0 = rv ? row_off(dg.a, mt * OZ_M + pt, rowtab) : 0;
+      const bool rv = ar < Mt, bv = bn < Nt, bw = bn < 8 * ngrp;
+      const int64_t arow0 = rv ? row_off(dg.a, mt * OZ_M + ar, rowtab) : 0;
       const int64_t brow0 = bv ? row_off(dg.b, nt * OZ_NC + bn, rowtab) : 0;
       const bool ca = dg.flags & OZ_CONJ_A, cb = dg.flags & OZ_CONJ_B;
       for (int rr = 0; rr < tk.nrep && !stop; ++rr) {
@@ -231,21 +247,26 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           if (i >= 4 && !bwait(&efree[e], ((i >> 2) - 1) & 1)) { stop = true; break; }
           const int kn = min(OZ_KR, dg.K - k0);
           const int nks = (kn + 7) >> 3;  // MMA K steps this round (8 complex each)
+          const int kw = 4 * nks;         // complex K per thread of an A row (4 or 8)
           unsigned char *As = smem + b * OZ_BUF, *Bs = As + 4 * OZ_PA;
-          {  // A: row pt (rows past Mt stage zeros)
-            float4 v[OZ_KR];
+          {  // A: this thread's half [kw h, kw h + kw) of row ar; exponent from both halves
+            float4 v[8];
             float m = 0.f;
 #pragma unroll
-            for (int k = 0; k < OZ_KR; ++k) {
+            for (int k = 0; k < 8; ++k) {
+              const int kk = kw * ah + k;
               v[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-              if (rv && k < kn) v[k] = __ldg(arow + (int64_t)(k0 + k) * dg.aks);
+              if (rv && k < kw && kk < kn) v[k] = __ldg(arow + (int64_t)(k0 + kk) * dg.aks);
               m = fmaxf(m, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
             }
-            const int ea = oz_exponent(m);
+            amax[b][ah][ar] = m;
+            tc::mbar_arrive(&mx[b]);  // both halves' maxima posted (bounded wait, no named barrier)
+            if (!bwait(&mx[b], (i >> 1) & 1)) { stop = true; break; }
+            const int ea = oz_exponent(fmaxf(amax[b][0][ar], amax[b][1][ar]));
             const float f = oz_pow2(7 - ea);
 #pragma unroll
-            for (int g = 0; g < OZ_KR / 4; ++g) {
-              if (g < 2 * nks) {
+            for (int g = 0; g < 2; ++g) {  // segments of 4 complex (8 reals per plane)
+              if (4 * g < kw) {
                 uint32_t w[4][4];
                 if (rv) {
 #pragma unroll
@@ -262,20 +283,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
                   for (int p = 0; p < 4; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0u;
                 }
-                const uint32_t o = seg_off(pt, 8 * g);
+                const uint32_t o = seg_off(ar, 8 * (kw * ah / 4 + g));
 #pragma unroll
                 for (int p = 0; p < 4; ++p)
                   *reinterpret_cast<uint4 *>(As + p * OZ_PA + o) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
               }
             }
-            ea_s[e][pt] = ea;
+            if (ah == 0) ea_s[e][ar] = ea;
           }
-          {  // B: four threads per complex row; rows (n,0) = [Br -Bi], (n,1) = [Bi Br]
-            float4 v[4];
+          {  // B: rows (n,0) = [Br -Bi], (n,1) = [Bi Br]; complex K [2 bq, 2 bq + 2) of row bn
+            float4 v[2];
             float mb = 0.f;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              const int k = 4 * qd + j;
+            for (int j = 0; j < 2; ++j) {
+              const int k = 2 * bq + j;
               v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
               if (bv && k < kn) v[j] = __ldg(brow + (int64_t)(k0 + k) * dg.bks);
               if (cb) { v[j].y = -v[j].y; v[j].w = -v[j].w; }
@@ -283,14 +304,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             }
             mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, 1));
             mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, 2));
+            mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, 4));
             const int eb = oz_exponent(mb);
-            if (qd == 0) eb_s[e][bn] = eb;
-            if (bw && qd < 2 * nks) {
-              uint32_t w0[4][4], w1[4][4];
+            if (bq == 0) eb_s[e][bn] = eb;
+            if (bw && 2 * bq < 8 * nks) {
+              uint32_t w0[4][2], w1[4][2];
               if (bv) {
                 const float f = oz_pow2(7 - eb);
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
+                for (int j = 0; j < 2; ++j) {
                   float sr[4], si[4];
                   oz_slice(v[j].x, v[j].z, f, sr);
                   oz_slice(v[j].y, v[j].w, f, si);
@@ -302,15 +324,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 }
               } else {
 #pragma unroll
-                for (int p = 0; p < 4; ++p)
-#pragma unroll
-                  for (int j = 0; j < 4; ++j) w0[p][j] = w1[p][j] = 0u;
+                for (int p = 0; p < 4; ++p) w0[p][0] = w0[p][1] = w1[p][0] = w1[p][1] = 0u;
               }
-              const uint32_t o0 = seg_off(2 * bn, 8 * qd), o1 = seg_off(2 * bn + 1, 8 * qd);
+              // 8-byte halves of the 16-byte core-matrix row segments of complex K [4 (bq/2), +4)
+              const uint32_t o0 = seg_off(2 * bn, 8 * (bq >> 1)) + 8 * (bq & 1);
+              const uint32_t o1 = seg_off(2 * bn + 1, 8 * (bq >> 1)) + 8 * (bq & 1);
 #pragma unroll
               for (int p = 0; p < 4; ++p) {
-                *reinterpret_cast<uint4 *>(Bs + p * OZ_PB + o0) = make_uint4(w0[p][0], w0[p][1], w0[p][2], w0[p][3]);
-                *reinterpret_cast<uint4 *>(Bs + p * OZ_PB + o1) = make_uint4(w1[p][0], w1[p][1], w1[p][2], w1[p][3]);
+                *reinterpret_cast<uint2 *>(Bs + p * OZ_PB + o0) = make_uint2(w0[p][0], w0[p][1]);
+                *reinterpret_cast<uint2 *>(Bs + p * OZ_PB + o1) = make_uint2(w1[p][0], w1[p][1]);
               }
             }
           }
@@ -355,9 +377,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       issued = nissued;
     }
   } else {
-    // ------------------------------ drain (row = TMEM lane = tid) ------------------------------
-    const int r = tid;
-    const uint32_t tlane = tm + ((uint32_t)(warp * 32) << 16);
+    // ------------------------------ drain ------------------------------
+    // warp w: TMEM lanes (rows) 32 (w & 3) .. + 31, complex columns [16 (w >> 2), + 16)
+    const int r = 32 * (warp & 3) + (tid & 31), ch = warp >> 2;
+    const uint32_t tlane = tm + ((uint32_t)(32 * (warp & 3)) << 16);
     const uint32_t sum_h = tlane + OZ_SUM, sum_l = sum_h + OZ_NR;
     int i = 0;
     bool stop = false;
@@ -369,7 +392,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const int ngrp = (Nt + 7) >> 3;
       const bool rv = r < Mt, f64 = dg.flags & OZ_OUT_F64;
       const int64_t crow0 = rv ? row_off(dg.c, mt * OZ_M + r, rowtab) : 0;
-      const int ng0 = nt * OZ_NC;
+      const int ng0 = nt * OZ_NC + 16 * ch;
       const int nq0 = ng0 / dg.cnd, nr0 = ng0 - nq0 * dg.cnd;  // column ng0 = nq0 * cnd + nr0
       for (int rr = 0; rr < tk.nrep && !stop; ++rr) {
         const int64_t co = crow0 + (int64_t)(tk.rep0 + rr) * dg.rc;
@@ -383,7 +406,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           const uint32_t base = tlane + (uint32_t)(a * OZ_ACC);
           int nq = nq0, nrr = nr0;  // output column cursor
 #pragma unroll
-          for (int g = 0; g < OZ_NR / 8; ++g) {  // groups of 8 real columns (4 complex)
+          for (int gl = 0; gl < 4; ++gl) {  // this warp's groups of 8 real columns (4 complex)
+            const int g = 4 * ch + gl;
             if (g < 2 * ngrp) {
               float x0[8], x1[8], x2[8], sh[8], sl[8];
               tc::tmem_ld8(base + (uint32_t)(8 * g), x0);
