@@ -184,18 +184,36 @@ int64_t gwo_flat_V(const gwo_layout *l) { return l->flat_V; }
 int64_t gwo_flat_orep(const gwo_layout *l) { return l->flat_orep; }
 int64_t gwo_flat_auxrep(const gwo_layout *l) { return l->flat_auxrep; }
 
+/* y[0:n] += a * x[0:n] on interleaved (re, im) doubles: the inner loop of the
+ * GEMMs below, written on real arithmetic so that it vectorises. */
+static inline void zaxpy(int n, cplx a, const cplx *x, cplx *y) {
+  const double ar = creal(a), ai = cimag(a);
+  const double *xd = (const double *)x;
+  double *yd = (double *)y;
+  for (int j = 0; j < n; ++j) {
+    const double xr = xd[2 * j], xi = xd[2 * j + 1];
+    yd[2 * j] += ar * xr - ai * xi;
+    yd[2 * j + 1] += ar * xi + ai * xr;
+  }
+}
+
+/* C(m x n) += A(m x k) * B(k x n), all row-major (i-p-j order: contiguous rows). */
+static void zgemm_nn_acc(int m, int n, int k, const cplx *A, int lda, const cplx *B, int ldb,
+                         cplx *C, int ldc) {
+  for (int i = 0; i < m; ++i) {
+    cplx *c = C + (size_t)i * ldc;
+    for (int p = 0; p < k; ++p) zaxpy(n, A[(size_t)i * lda + p], B + (size_t)p * ldb, c);
+  }
+}
+
 /* C(m x n) = A(m x k) * B(k x n), all row-major, overwrite. */
 static void zgemm_nn(int m, int n, int k, const cplx *A, int lda, const cplx *B, int ldb,
                      cplx *C, int ldc) {
   for (int i = 0; i < m; ++i) {
     cplx *c = C + (size_t)i * ldc;
     for (int j = 0; j < n; ++j) c[j] = 0;
-    for (int p = 0; p < k; ++p) {
-      cplx a = A[(size_t)i * lda + p];
-      const cplx *b = B + (size_t)p * ldb;
-      for (int j = 0; j < n; ++j) c[j] += a * b[j];
-    }
   }
+  zgemm_nn_acc(m, n, k, A, lda, B, ldb, C, ldc);
 }
 
 /* out = O * X * O^H for one (m x n) block O and (n x n) X, row-major. */
@@ -264,7 +282,7 @@ void gwo_p0(const gwo_layout *l, int ns, int nts, int nt_max, const double *G_fu
 #pragma omp parallel num_threads(gwo_get_threads())
   {
     size_t cap = 0;
-    cplx *X1 = NULL, *X2 = NULL;
+    cplx *X1 = NULL, *X2 = NULL, *VT = NULL;
 #pragma omp for collapse(2) schedule(dynamic)
     for (int iq_irr = 0; iq_irr < ink; ++iq_irr)
       for (int t = 0; t < nt_max; ++t) {
@@ -287,45 +305,32 @@ void gwo_p0(const gwo_layout *l, int ns, int nts, int nt_max, const double *G_fu
               const cplx *Gmn = G2 + l->ao_off[l->ao_ptr[k2] + i2];
               size_t need = (size_t)qb * b1 * b2;
               if (need > cap) {
-                free(X1); free(X2);
+                free(X1); free(X2); free(VT);
                 cap = need;
                 X1 = (cplx *)malloc(sizeof(cplx) * cap);
                 X2 = (cplx *)malloc(sizeof(cplx) * cap);
+                VT = (cplx *)malloc(sizeof(cplx) * cap);
               }
-              /* X1[t'][m][Q] = sum_p G^{k1}(beta-t)[t'][p] V[Q][p][m]   (gw_block.cpp:57-62) */
-              for (int tp = 0; tp < b1; ++tp)
-                for (int m = 0; m < b2; ++m)
-                  for (int Q = 0; Q < qb; ++Q) {
-                    cplx acc = 0;
-                    for (int pp = 0; pp < b1; ++pp)
-                      acc += Gtp[tp * b1 + pp] * Vb[((size_t)Q * b1 + pp) * b2 + m];
-                    X1[((size_t)tp * b2 + m) * qb + Q] = acc;
-                  }
-              /* X2[P][t'][m] = sum_n conj(V[P][t'][n]) G^{k2}(t)[m][n]   (gw_block.cpp:67-69) */
+              /* X1[t'][Q][m] = sum_p G^{k1}(beta-t)[t'][p] V[Q][p][m]   (gw_block.cpp:57-62) */
+              for (int Q = 0; Q < qb; ++Q)
+                zgemm_nn(b1, b2, b1, Gtp, b1, Vb + (size_t)Q * b1 * b2, b2, X1 + (size_t)Q * b2, qb * b2);
+              /* X2[t'][m][P] = sum_n G^{k2}(t)[m][n] conj(V[P][t'][n])   (gw_block.cpp:67-69) */
               for (int P_ = 0; P_ < qb; ++P_)
                 for (int tp = 0; tp < b1; ++tp)
-                  for (int m = 0; m < b2; ++m) {
-                    cplx acc = 0;
-                    const cplx *vr = Vb + ((size_t)P_ * b1 + tp) * b2;
-                    for (int n = 0; n < b2; ++n) acc += conj(vr[n]) * Gmn[m * b2 + n];
-                    X2[((size_t)P_ * b1 + tp) * b2 + m] = acc;
-                  }
-              /* P0[Q][P] += sum_{t',m} X1[t',m][Q] X2[P][t',m]   (gw_block.cpp:72-74) */
+                  for (int n = 0; n < b2; ++n)
+                    VT[((size_t)tp * b2 + n) * qb + P_] = conj(Vb[((size_t)P_ * b1 + tp) * b2 + n]);
+              for (int tp = 0; tp < b1; ++tp)
+                zgemm_nn(b2, qb, b2, Gmn, b2, VT + (size_t)tp * b2 * qb, qb, X2 + (size_t)tp * b2 * qb, qb);
+              /* P0[Q][P] += sum_{t',m} X1[t'][Q][m] X2[t'][m][P]   (gw_block.cpp:72-74) */
               cplx *Pb = P + l->aux_off[l->aux_ptr[q] + iq];
-              int K = b1 * b2;
-              for (int Q = 0; Q < qb; ++Q)
-                for (int P_ = 0; P_ < qb; ++P_) {
-                  cplx acc = 0;
-                  const cplx *x2 = X2 + (size_t)P_ * K;
-                  for (int kk = 0; kk < K; ++kk) acc += X1[(size_t)kk * qb + Q] * x2[kk];
-                  Pb[(size_t)Q * qb + P_] += acc;
-                }
+              for (int tp = 0; tp < b1; ++tp)
+                zgemm_nn_acc(qb, qb, b2, X1 + (size_t)tp * qb * b2, b2, X2 + (size_t)tp * b2 * qb, qb, Pb, qb);
             }
           }
         }
         for (int64_t i = 0; i < qsz; ++i) P[i] *= pref;
       }
-    free(X1); free(X2);
+    free(X1); free(X2); free(VT);
   }
 }
 
@@ -474,7 +479,7 @@ void gwo_sigma(const gwo_layout *l, int ns, int nts, int nt_max, const double *G
 #pragma omp parallel num_threads(gwo_get_threads())
   {
     size_t cap = 0;
-    cplx *Y1 = NULL, *Y2 = NULL;
+    cplx *Y1 = NULL, *Y2 = NULL, *VT = NULL;
 #pragma omp for collapse(2) schedule(dynamic)
     for (int ik = 0; ik < ink; ++ik)
       for (int t = 0; t < nt_max; ++t) {
@@ -496,31 +501,26 @@ void gwo_sigma(const gwo_layout *l, int ns, int nts, int nt_max, const double *G
               const cplx *PQP = Pq + l->aux_off[l->aux_ptr[q] + iq];
               size_t need = (size_t)qb * b1 * b2;
               if (need > cap) {
-                free(Y1); free(Y2);
+                free(Y1); free(Y2); free(VT);
                 cap = need;
                 Y1 = (cplx *)malloc(sizeof(cplx) * cap);
                 Y2 = (cplx *)malloc(sizeof(cplx) * cap);
+                VT = (cplx *)malloc(sizeof(cplx) * cap);
               }
               /* Y1[Q,i][n] = sum_m V[Q,i][m] G^{k2}(t)[m][n]   (gw_block.cpp:134-136) */
               zgemm_nn(qb * b1, b2, b2, Vb, b2, Gmn, b2, Y1, b2);
               /* Y2[i,n][P] = sum_Q Y1[Q][i,n] P[Q][P]   (gw_block.cpp:139-141) */
               int K = b1 * b2;
-              for (int in = 0; in < K; ++in)
-                for (int P_ = 0; P_ < qb; ++P_) {
-                  cplx acc = 0;
-                  for (int Q = 0; Q < qb; ++Q) acc += Y1[(size_t)Q * K + in] * PQP[(size_t)Q * qb + P_];
-                  Y2[(size_t)in * qb + P_] = acc;
-                }
+              memset(Y2, 0, sizeof(cplx) * (size_t)K * qb);
+              for (int Q = 0; Q < qb; ++Q)
+                for (int in = 0; in < K; ++in) zaxpy(qb, Y1[(size_t)Q * K + in], PQP + (size_t)Q * qb, Y2 + (size_t)in * qb);
               /* Sigma[i][j] += sum_{n,P} Y2[i][n,P] conj(V[P][j][n])   (gw_block.cpp:146-150) */
-              cplx *Sb = S + l->ao_off[l->ao_ptr[k1] + i1];
-              for (int i = 0; i < b1; ++i)
-                for (int j = 0; j < b1; ++j) {
-                  cplx acc = 0;
+              for (int P_ = 0; P_ < qb; ++P_)
+                for (int j = 0; j < b1; ++j)
                   for (int n = 0; n < b2; ++n)
-                    for (int P_ = 0; P_ < qb; ++P_)
-                      acc += Y2[((size_t)i * b2 + n) * qb + P_] * conj(Vb[((size_t)P_ * b1 + j) * b2 + n]);
-                  Sb[i * b1 + j] += acc;
-                }
+                    VT[((size_t)n * qb + P_) * b1 + j] = conj(Vb[((size_t)P_ * b1 + j) * b2 + n]);
+              cplx *Sb = S + l->ao_off[l->ao_ptr[k1] + i1];
+              zgemm_nn_acc(b1, b1, b2 * qb, Y2, b2 * qb, VT, b1, Sb, b1);
             }
           }
         }
@@ -529,7 +529,7 @@ void gwo_sigma(const gwo_layout *l, int ns, int nts, int nt_max, const double *G
           for (int64_t i = 0; i < l->kao_sz[k1]; ++i) S[i] *= -1.0 / nk;
         }
       }
-    free(Y1); free(Y2);
+    free(Y1); free(Y2); free(VT);
   }
 }
 
