@@ -29,6 +29,13 @@ Outputs (committed; the GPU tests read only these):
      block packing rule (q = k2 - k1 labelling).
   4. P0 and Sigma: the C oracle vs an independent numpy einsum restatement of
      ``gw_block.cpp`` on the same block inputs.
+  5. P0 and Sigma, block vs dense: the oracle's block P0 and Sigma (on the
+     block chain: input_flat.h5, VQ_flat_0.h5) vs a restatement of the
+     reference's DENSE solver (``gw_solver::compute_full_P0_t`` /
+     ``compute_Sigma_from_P_t``, src/cpu_ref/gw.cpp:65-127) on the dense chain
+     (G from the dense Dyson on input_blk.h5, P~ from the dense W~ solve, V
+     blocks in dense arrays) -- the route of the reference's own dense-solver
+     test (test/test_cugw.cpp:250-291).
 """
 from __future__ import annotations
 
@@ -209,8 +216,47 @@ def main():
         d = max(d, float(np.abs(P[nts * o: nts * (o + sz)].reshape(nts, sz) - P_dense_flat[:, o:o + sz]).max()))
     rel["p_tilde_block_vs_dense"] = d
 
+    # 5. P0, block oracle vs the reference's DENSE algorithm (gw_solver::compute_full_P0_t,
+    #    src/cpu_ref/gw.cpp:65-100 with P0_contraction :203-216) on the dense chain: G from
+    #    the dense Dyson on input_blk.h5, V(k1, k2) the block file's blocks in dense
+    #    [NQ][nao][nao] arrays (the reference's P_flat_to_block / dense-solver test route,
+    #    test/test_cugw.cpp:250-291).
+    Vd = {(k1, k2): V_block_dense(k1, k2) for k1 in range(nk) for k2 in range(nk)}
+    pref = -1.0 / nk * (2.0 if ns == 1 else 1.0)
+    P0d = np.zeros((NT_P0, nk, naux, naux), np.complex128)
+    for q in range(nk):
+        for k1 in range(nk):
+            k2 = L.mom_cons(k1, 0, q)  # k2 = k1 + q
+            V = Vd[(k1, k2)]
+            for t in range(NT_P0):
+                for s in range(ns):
+                    P0d[t, q] += np.einsum("tp,Qpm,Ptn,mn->QP", Gd[nts - 1 - t, s, k1], V, V.conj(), Gd[t, s, k2],
+                                           optimize=True)
+    P0d *= pref
+    P0d_flat = L.P_block_to_flat(P0d)
+    d = 0.0
+    for iq in range(L.ink):
+        o, sz = L.qaux_slice_offsets_irre[iq], L.qaux_slice_sizes_irre[iq]
+        d = max(d, float(np.abs(P0[nts * o: nts * (o + sz)].reshape(nts, sz)[:NT_P0] - P0d_flat[:, o:o + sz]).max()))
+    rel["p0_block_vs_dense_gw"] = d
+
     Pf = orc.rotate_P(P)
     Sig = orc.sigma(Gf, Pf, ri.V)
+
+    # 6. Sigma, block oracle vs the dense algorithm (gw_solver::compute_Sigma_from_P_t,
+    #    gw.cpp:102-127 with Sigma_contraction :218-231) on the dense chain's P~ (Pd2).
+    Sd = np.zeros((NT_SIG, ns, nk, nao, nao), np.complex128)
+    for q in range(nk):
+        for k1 in range(nk):
+            k2 = L.mom_cons(k1, q, 0)  # k2 = k1 - q
+            V = Vd[(k1, k2)]
+            for t in range(NT_SIG):
+                for s in range(ns):
+                    Sd[t, s, k1] += np.einsum("Qim,mn,QP,Pjn->ij", V, Gd[t, s, k2], Pd2[t, q], V.conj(),
+                                              optimize=True)
+    Sd *= -1.0 / nk
+    Sd_flat = L.G_block_to_flat(Sd).reshape(NT_SIG, ns, L.flat_ao_size)
+    rel["sigma_block_vs_dense_gw"] = float(np.abs(Sig.reshape(nts, ns, L.flat_ao_size)[:NT_SIG] - Sd_flat).max())
 
     def P_full_fn(q, t, iq):
         o = nts * L.qaux_slice_offsets[q] + t * L.qaux_slice_sizes[q] + L.aux_offsets[q][iq]
@@ -233,6 +279,8 @@ def main():
     assert rel["V_spectra_block_vs_dense"] < 1e-10
     assert rel["p0_oracle_vs_numpy"] < 1e-12
     assert rel["sigma_oracle_vs_numpy"] < 1e-12
+    assert rel["p0_block_vs_dense_gw"] < 1e-10
+    assert rel["sigma_block_vs_dense_gw"] < 1e-10
 
     # ---- inputs ----
     cat = lambda xs: np.concatenate([np.asarray(x).reshape(-1) for x in xs])  # noqa: E731
@@ -249,11 +297,11 @@ def main():
     )
     # ---- golden outputs ----
     P_sel = np.concatenate([P_dense_flat[t] for t in T_PT])
-    P0_sel = np.concatenate([P0t[t] for t in range(NT_P0)])
+    P0_sel = np.concatenate([P0d_flat[t] for t in range(NT_P0)])  # the dense chain's P0
     np.savez_compressed(
         os.path.join(HERE, "lih_golden.npz"),
         G=G_dense_flat, P0_t=P0_sel, nt_p0=NT_P0, P_tilde_t=P_sel, t_pt=np.array(T_PT),
-        Sigma_t=S3[:NT_SIG].reshape(-1), nt_sigma=NT_SIG, G_after_gw=G2,
+        Sigma_t=Sd_flat.reshape(-1), nt_sigma=NT_SIG, G_after_gw=G2,  # the dense chain's Sigma
         leakage_g0=leak, leakage_g1=leak2,
         **{"rel_" + k: v for k, v in rel.items()},
     )
