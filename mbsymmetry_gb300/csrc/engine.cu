@@ -463,7 +463,6 @@ class Engine {
   int64_t oz_vcat_elems_ = 0, oz_bcat_elems_ = 0, oz_vcats_elems_ = 0, oz_z1_elems_ = 0, oz_zcat_elems_ = 0,
           oz_w_elems_ = 0, oz_u_elems_ = 0;
   std::vector<OzLaunch> oz_p0_, oz_sig_;
-  int oz_tch_p0_ = 1, oz_tch_sig_ = 1;
   std::vector<P0Contrib> pc_host_;
   std::vector<SigContrib> sc_host_;
   std::vector<Owner> sig_own_host_;
@@ -1471,16 +1470,19 @@ void oz_check(const OzDesc &d, int nrep, int64_t na, int64_t nb, int64_t nc, con
 }  // namespace
 
 void Engine::build_oz_lists() {
-  // Layouts (float-float, complex elements).  Every tau-dependent buffer is a
-  // sequence of tau slabs with one stride (z1t, zct, wct, uct elements per tau),
-  // so one repetition offset serves every row of a packed GEMM.
+  // Layouts (float-float, complex elements).  The contractions run in chunks of
+  // output blocks (P0: output blocks (q_irr, iq); Sigma: AO blocks (k_irr, i1)
+  // with their spins), each chunk over ALL tau, so the final GEMMs (P0, Sigma)
+  // get full 128-row tiles of (tau, row); a chunk's tau-dependent buffers are
+  // sequences of tau slabs with one stride (z1t, zct, wct, uct elements per
+  // tau), so one repetition offset serves every row of a packed GEMM.
   //   Z1[tau][pack][m][row]      row = (c, P, t) of the contributions sharing G2's block
   //   Zcat[tau][group][P][K]     K = (c, s, m, p) of the P0 output block (q_irr, iq)
-  //   Vcat[group][Q][K]          = V_c[Q][p][m] at the same K
-  //   W[tau][group][Q][col]      col = (c, j, n) of the P~ block group
+  //   Vcat[group][Q][K]          = V_c[Q][p][m] at the same K (all groups, once per upload)
+  //   W[tau][group][Q][col]      col = (c, j, n) of the chunk's contributions in the P~ block group
   //   U[tau][owner][j][K]        K = (c, Q, m) of the Sigma owner (k_irr, i1, s)
-  //   VcatS[owner][i][K]         = Vt_c[Q][i][m] at the same K
-  // Per-tau stages (Z1, Z, U) pack all contributions that share their
+  //   VcatS[owner][i][K]         = Vt_c[Q][i][m] at the same K (all owners, once per upload)
+  // Per-tau stages (Z1, Z, U) pack the chunk's contributions that share their
   // G-block operand (same block and spin) into one GEMM with a row table.
   const Lay &l = l_;
   const int ns = ns_, nts = nts_, half = nts / 2;
@@ -1503,7 +1505,7 @@ void Engine::build_oz_lists() {
   auto stage = [&](std::vector<OzLaunch> &v, size_t t0, int a, int b, int c) {
     auto cost = [&](const OzTask &t) { return (int64_t)t.nrep * ((ds[t.desc].K + OZ_KR - 1) / OZ_KR); };
     std::stable_sort(ts.begin() + t0, ts.end(), [&](const OzTask &x, const OzTask &y) { return cost(x) > cost(y); });
-    v.push_back({(int64_t)t0, (int64_t)(ts.size() - t0), a, b, c});
+    if (ts.size() > t0) v.push_back({(int64_t)t0, (int64_t)(ts.size() - t0), a, b, c});
   };
   // Row-table checks: every entry (plus the row's K extent and reps) inside the buffer.
   auto check_tab = [&](int64_t base, int M, int64_t klen, int64_t rep, int nrep, int64_t size, const char *what) {
@@ -1516,13 +1518,14 @@ void Engine::build_oz_lists() {
   oz_p0_.clear();
   oz_sig_.clear();
   const int64_t gsz = (int64_t)Gall_.n, psz = (int64_t)Pall_.n, ssz = (int64_t)nts * ns * l.flat_ao;
+  const double pref = -1.0 / l.nk * (ns == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
 
   // ---- P0 -------------------------------------------------------------------
   std::vector<OzPerm> pv;
-  struct PG { int64_t voff, zc; int zld; };
+  struct PG { int64_t voff; int zld; };
   std::vector<PG> pg;
   std::vector<int> zcol(pc.size() * ns), cgrp(pc.size());
-  int64_t voff = 0, zct = 0;
+  int64_t voff = 0;
   for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {
     const P0Group &g = p0_groups_[gi];
     int zld = 0;
@@ -1533,51 +1536,70 @@ void Engine::build_oz_lists() {
         zld += pc[c].b1 * pc[c].b2;
       }
     }
-    pg.push_back({voff, zct, zld});
+    pg.push_back({voff, zld});
     for (int c = g.c0; c < g.c1; ++c)
       for (int sp = 0; sp < ns; ++sp)  // Vcat[Q][zcol + m b1 + p] = V_c[Q][p][m]
         pv.push_back({pc[c].v, voff + zcol[c * ns + sp], zld, 1, pc[c].b1, g.qb, pc[c].b1, pc[c].b2, 0});
     voff += (int64_t)g.qb * zld;
-    zct += (int64_t)g.qb * zld;
   }
   oz_vcat_elems_ = voff;
-  // Z1 packs: (G2 block, spin) -> [(contribution, row position in the pack)]
-  struct PackRow { int c; int64_t pos; };
-  std::map<std::pair<int64_t, int>, std::vector<PackRow>> z1p, zp;
-  std::vector<int64_t> z1pack(pc.size() * ns), z1mp(pc.size() * ns), z1pos(pc.size() * ns);
-  for (size_t c = 0; c < pc.size(); ++c)
-    for (int sp = 0; sp < ns; ++sp) {
-      auto &v = z1p[{pc[c].gb, sp}];
-      const int64_t pos = v.empty() ? 0 : v.back().pos + (int64_t)p0_groups_[cgrp[v.back().c]].qb * pc[v.back().c].b1;
-      v.push_back({(int)c, pos});
-      zp[{pc[c].ga, sp}].push_back({(int)c, 0});
+  // chunks of output blocks: Z1 and Zcat of a chunk (all nts/2 tau) within the budget
+  const int64_t budget = std::max<int64_t>(1, tc_chunk_bytes_ / 16);  // complex float-float elements
+  std::vector<std::pair<int, int>> pchunks;
+  for (size_t g0 = 0; g0 < p0_groups_.size();) {
+    size_t g1 = g0;
+    int64_t need = 0;
+    while (g1 < p0_groups_.size()) {
+      const int64_t n = 2 * (int64_t)p0_groups_[g1].qb * pg[g1].zld * half;
+      if (g1 > g0 && need + n > budget) break;
+      need += n;
+      ++g1;
     }
-  int64_t z1t = 0;
-  for (auto &kv : z1p) {
-    const auto &v = kv.second;
-    const int64_t mp = v.back().pos + (int64_t)p0_groups_[cgrp[v.back().c]].qb * pc[v.back().c].b1;
-    const int b2 = pc[v[0].c].b2;
-    for (const PackRow &x : v) {
-      z1pack[x.c * ns + kv.first.second] = z1t;
-      z1mp[x.c * ns + kv.first.second] = mp;
-      z1pos[x.c * ns + kv.first.second] = x.pos;
-    }
-    z1t += mp * b2;
+    pchunks.push_back({(int)g0, (int)g1});
+    g0 = g1;
   }
-  const int64_t p0_tau_bytes = 16 * std::max<int64_t>(1, zct + z1t);
-  const int tp = (int)std::max<int64_t>(1, std::min<int64_t>(half, tc_chunk_bytes_ / p0_tau_bytes));
-  oz_tch_p0_ = tp;
-  oz_z1_elems_ = z1t * tp;
-  oz_zcat_elems_ = zct * tp;
-  const double pref = -1.0 / l.nk * (ns == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
-  for (int t0 = 0; t0 < half; t0 += tp) {
-    const int ntc = std::min(tp, half - t0);
+  oz_z1_elems_ = oz_zcat_elems_ = 1;
+  struct PackRow { int c; int64_t pos; };
+  for (const auto &ch : pchunks) {
+    // chunk-local per-tau layouts
+    std::vector<int64_t> zc(p0_groups_.size(), 0);
+    int64_t zct = 0;
+    for (int gi = ch.first; gi < ch.second; ++gi) {
+      zc[gi] = zct;
+      zct += (int64_t)p0_groups_[gi].qb * pg[gi].zld;
+    }
+    std::map<std::pair<int64_t, int>, std::vector<PackRow>> z1p, zp;
+    for (int gi = ch.first; gi < ch.second; ++gi)
+      for (int c = p0_groups_[gi].c0; c < p0_groups_[gi].c1; ++c)
+        for (int sp = 0; sp < ns; ++sp) {
+          auto &v = z1p[{pc[c].gb, sp}];
+          const int64_t pos =
+              v.empty() ? 0 : v.back().pos + (int64_t)p0_groups_[cgrp[v.back().c]].qb * pc[v.back().c].b1;
+          v.push_back({c, pos});
+          zp[{pc[c].ga, sp}].push_back({c, 0});
+        }
+    std::map<int, int64_t> z1pack, z1mp, z1pos;  // keyed by c * ns + s
+    int64_t z1t = 0;
+    for (auto &kv : z1p) {
+      const auto &v = kv.second;
+      const int64_t mp = v.back().pos + (int64_t)p0_groups_[cgrp[v.back().c]].qb * pc[v.back().c].b1;
+      for (const PackRow &x : v) {
+        const int k = x.c * ns + kv.first.second;
+        z1pack[k] = z1t;
+        z1mp[k] = mp;
+        z1pos[k] = x.pos;
+      }
+      z1t += mp * pc[v[0].c].b2;
+    }
+    const int64_t z1_elems = z1t * half, zcat_elems = zct * half;
+    oz_z1_elems_ = std::max(oz_z1_elems_, z1_elems);
+    oz_zcat_elems_ = std::max(oz_zcat_elems_, zcat_elems);
     size_t s0 = ts.size();
     for (auto &kv : z1p) {  // Z1[tau][m][(c,P,t)] = sum_n conj(V_c[P][t][n]) G2(tau)[m][n]
       const int sp = kv.first.second;
       const auto &v = kv.second;
       const P0Contrib &c0 = pc[v[0].c];
-      const int b2 = c0.b2;
+      const int b2 = c0.b2, k0 = v[0].c * ns + sp;
       const int64_t tab = (int64_t)rt.size();
       for (const PackRow &x : v) {
         const P0Contrib &cb = pc[x.c];
@@ -1588,17 +1610,17 @@ void Engine::build_oz_lists() {
       OzDesc d{};
       d.M = (int)(rt.size() - tab);
       d.a = {tab, 0, 0, 0};
-      d.b = {c0.gb + ((int64_t)t0 * ns + sp) * c0.sb, (int64_t)ns * c0.sb, b2, b2};
-      d.c = {z1pack[v[0].c * ns + sp], 1, 0, 1};
+      d.b = {c0.gb + (int64_t)sp * c0.sb, (int64_t)ns * c0.sb, b2, b2};
+      d.c = {z1pack[k0], 1, 0, 1};
       d.cn1 = z1t;
-      d.cn0 = (int32_t)z1mp[v[0].c * ns + sp];
+      d.cn0 = (int32_t)z1mp[k0];
       d.cnd = b2;
       d.aks = d.bks = 1;
-      d.N = ntc * b2;
+      d.N = half * b2;
       d.K = b2;
       d.flags = OZ_CONJ_A;
       check_tab(tab, d.M, b2, 0, 1, l.flat_V, "P0 stage Z1 (V rows)");
-      oz_check(d, 1, l.flat_V, gsz, oz_z1_elems_, "P0 stage Z1");
+      oz_check(d, 1, l.flat_V, gsz, z1_elems, "P0 stage Z1");
       add(d, 1, 1);
     }
     stage(oz_p0_, s0, OZB_VFF, OZB_GFF, OZB_Z1);
@@ -1620,14 +1642,13 @@ void Engine::build_oz_lists() {
         const P0Contrib &cb = pc[x.c];
         const int gi = cgrp[x.c], qb = p0_groups_[gi].qb, k = x.c * ns + sp;
         for (int P = 0; P < qb; ++P)
-          for (int m = 0; m < cb.b2; ++m)
-            rt.push_back(pg[gi].zc + (int64_t)P * pg[gi].zld + zcol[k] + (int64_t)m * b1);
+          for (int m = 0; m < cb.b2; ++m) rt.push_back(zc[gi] + (int64_t)P * pg[gi].zld + zcol[k] + (int64_t)m * b1);
       }
       OzDesc d{};
       d.M = (int)(tabc - taba);
       d.a = {taba, 0, 0, 0};
       d.ra = z1t;
-      d.b = {c0.ga + ((int64_t)(nts - 1 - t0) * ns + sp) * c0.sa, 1, 0, 1};
+      d.b = {c0.ga + ((int64_t)(nts - 1) * ns + sp) * c0.sa, 1, 0, 1};
       d.bks = b1;
       d.rb = -(int64_t)ns * c0.sa;
       d.c = {tabc, 0, 0, 0};
@@ -1637,40 +1658,43 @@ void Engine::build_oz_lists() {
       d.aks = 1;
       d.N = b1;
       d.K = b1;
-      check_tab(taba, d.M, b1, z1t, ntc, oz_z1_elems_, "P0 stage Z (Z1 rows)");
-      check_tab(tabc, d.M, b1, zct, ntc, oz_zcat_elems_, "P0 stage Z (Zcat rows)");
-      oz_check(d, ntc, oz_z1_elems_, gsz, oz_zcat_elems_, "P0 stage Z");
-      add(d, ntc, REPG);
+      check_tab(taba, d.M, b1, z1t, half, z1_elems, "P0 stage Z (Z1 rows)");
+      check_tab(tabc, d.M, b1, zct, half, zcat_elems, "P0 stage Z (Zcat rows)");
+      oz_check(d, half, z1_elems, gsz, zcat_elems, "P0 stage Z");
+      add(d, half, REPG);
     }
     stage(oz_p0_, s0, OZB_Z1, OZB_GFF, OZB_ZCAT);
     s0 = ts.size();
-    for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {  // P0[Q][P] = sum_K Zcat[(tau,P)][K] Vcat[Q][K]
+    for (int gi = ch.first; gi < ch.second; ++gi) {  // P0[Q][P] = sum_K Zcat[(tau,P)][K] Vcat[Q][K]
       const P0Group &g = p0_groups_[gi];
       if (g.c1 == g.c0) continue;
       OzDesc d{};
-      d.a = {pg[gi].zc, zct, pg[gi].zld, g.qb};
+      d.a = {zc[gi], zct, pg[gi].zld, g.qb};
       d.b = {pg[gi].voff, pg[gi].zld, 0, 1};
-      d.c = {g.pout + (int64_t)t0 * g.pstride, g.pstride, 1, g.qb};
+      d.c = {g.pout, g.pstride, 1, g.qb};
       d.cn1 = g.qb;
       d.cnd = 1;
       d.aks = d.bks = 1;
-      d.M = ntc * g.qb;
+      d.M = half * g.qb;
       d.N = g.qb;
       d.K = pg[gi].zld;
       d.flags = OZ_OUT_F64;
       d.alpha = pref;
-      oz_check(d, 1, oz_zcat_elems_, oz_vcat_elems_, psz, "P0 stage P0");
+      oz_check(d, 1, zcat_elems, oz_vcat_elems_, psz, "P0 stage P0");
       add(d, 1, 1);
     }
     stage(oz_p0_, s0, OZB_ZCAT, OZB_VCAT, OZB_P0);
   }
 
   // ---- Sigma ----------------------------------------------------------------
+  // Bcat per P~ block group, columns in contribution order (so the columns of a
+  // chunk of AO-block owners are contiguous in every group)
   std::vector<OzPerm> pb, psg;
-  struct SG { int64_t boff, wc; int ncol; };
+  struct SG { int64_t boff; int qb; };
   std::vector<SG> sg;
   std::vector<int> cgroup(sc.size(), -1), ccol(sc.size(), 0);
-  int64_t boff = 0, wct = 0;
+  std::vector<std::vector<int>> gcs;  // contributions of each group (increasing)
+  int64_t boff = 0;
   for (const auto &grp : sig_groups_) {
     const std::vector<int> &cs = grp.second;
     const int qb = sc[cs[0]].qb;
@@ -1681,70 +1705,113 @@ void Engine::build_oz_lists() {
       pb.push_back({sc[c].v, boff + (int64_t)ncol * qb, 1, (int64_t)sc[c].b2 * qb, qb, qb, sig_b1_[c], sc[c].b2, 1});
       ncol += sig_b1_[c] * sc[c].b2;
     }
-    sg.push_back({boff, wct, ncol});
+    sg.push_back({boff, qb});
+    gcs.push_back(cs);
     boff += (int64_t)ncol * qb;
-    wct += (int64_t)qb * ncol;
   }
   oz_bcat_elems_ = boff;
+  // AO-block owners (k_irr, i1): the owners of their spins share (c0, c1)
   std::vector<int> ucol(sc.size(), 0);
   std::map<std::pair<int, int>, std::pair<int64_t, int>> vs;  // (c0, c1) -> (VcatS offset, uld)
-  int64_t vsoff = 0, uct = 0;
-  std::vector<int64_t> uoff(sig_own_host_.size());
+  std::vector<std::pair<int, int>> aoo;                       // distinct (c0, c1) in owner order
+  std::map<std::pair<int, int>, int> aoidx;                   // (c0, c1) -> index in aoo
+  int64_t vsoff = 0;
   for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {
     const Owner &o = sig_own_host_[oi];
+    const auto key = std::make_pair(o.c0, o.c1);
+    if (vs.count(key)) continue;
     int uld = 0;
     for (int c = o.c0; c < o.c1; ++c) {
       ucol[c] = uld;
       uld += sc[c].qb * sc[c].b2;
     }
-    const auto key = std::make_pair(o.c0, o.c1);
-    if (!vs.count(key)) {
-      vs[key] = {vsoff, uld};
-      for (int c = o.c0; c < o.c1; ++c)
-        psg.push_back({sc[c].v, vsoff + ucol[c], sc[c].b2, uld, 1, sc[c].qb, sig_b1_[c], sc[c].b2, 0});
-      vsoff += (int64_t)o.n * uld;
-    }
-    uoff[oi] = uct;
-    uct += (int64_t)o.n * uld;
+    vs[key] = {vsoff, uld};
+    aoidx[key] = (int)aoo.size();
+    aoo.push_back(key);
+    for (int c = o.c0; c < o.c1; ++c)
+      psg.push_back({sc[c].v, vsoff + ucol[c], sc[c].b2, uld, 1, sc[c].qb, sig_b1_[c], sc[c].b2, 0});
+    vsoff += (int64_t)o.n * uld;
   }
   oz_vcats_elems_ = vsoff;
-  // U packs: (G2 block, spin) -> [(owner, contribution)]
-  std::map<std::pair<int64_t, int>, std::vector<std::pair<int, int>>> up;
-  for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {
-    const Owner &o = sig_own_host_[oi];
-    for (int c = o.c0; c < o.c1; ++c) up[{sc[c].gb, o.s}].push_back({(int)oi, c});
+  // chunks of AO-block owners: W and U of a chunk (all nts tau) within the budget
+  auto ao_need = [&](const std::pair<int, int> &key) {
+    int64_t w = 0;
+    for (int c = key.first; c < key.second; ++c) w += (int64_t)sc[c].qb * sig_b1_[c] * sc[c].b2;
+    return (1 + ns) * w * nts;
+  };
+  std::vector<std::pair<int, int>> schunks;  // ranges of aoo
+  for (size_t a0 = 0; a0 < aoo.size();) {
+    size_t a1 = a0;
+    int64_t need = 0;
+    while (a1 < aoo.size()) {
+      const int64_t n = ao_need(aoo[a1]);
+      if (a1 > a0 && need + n > budget) break;
+      need += n;
+      ++a1;
+    }
+    schunks.push_back({(int)a0, (int)a1});
+    a0 = a1;
   }
-  const int64_t sig_tau_bytes = 16 * std::max<int64_t>(1, wct + uct);
-  const int tsg = (int)std::max<int64_t>(1, std::min<int64_t>(nts, tc_chunk_bytes_ / sig_tau_bytes));
-  oz_tch_sig_ = tsg;
-  oz_w_elems_ = wct * tsg;
-  oz_u_elems_ = uct * tsg;
-  for (int t0 = 0; t0 < nts; t0 += tsg) {
-    const int ntc = std::min(tsg, nts - t0);
+  oz_w_elems_ = oz_u_elems_ = 1;
+  for (const auto &ch : schunks) {
+    const int cA = aoo[ch.first].first, cB = aoo[ch.second - 1].second;  // contributions [cA, cB)
+    // W: per group, the chunk's columns (contiguous: contributions in [cA, cB))
+    struct WG { int g, col0, ncol; int64_t wc; };
+    std::vector<WG> wg;
+    std::vector<int> wgi(sg.size(), -1);
+    int64_t wct = 0;
+    for (size_t gi = 0; gi < sg.size(); ++gi) {
+      int col0 = -1, ncol = 0;
+      for (int c : gcs[gi])
+        if (c >= cA && c < cB) {
+          if (col0 < 0) col0 = ccol[c];
+          ncol += sig_b1_[c] * sc[c].b2;
+        }
+      if (ncol == 0) continue;
+      wgi[gi] = (int)wg.size();
+      wg.push_back({(int)gi, col0, ncol, wct});
+      wct += (int64_t)sg[gi].qb * ncol;
+    }
+    // U: the chunk's owners (all spins)
+    std::vector<int64_t> uoff(sig_own_host_.size(), -1);
+    int64_t uct = 0;
+    for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {
+      const Owner &o = sig_own_host_[oi];
+      const int ai = aoidx[std::make_pair(o.c0, o.c1)];
+      if (ai < ch.first || ai >= ch.second) continue;
+      uoff[oi] = uct;
+      uct += (int64_t)o.n * vs[std::make_pair(o.c0, o.c1)].second;
+    }
+    const int64_t w_elems = std::max<int64_t>(1, wct * nts), u_elems = std::max<int64_t>(1, uct * nts);
+    oz_w_elems_ = std::max(oz_w_elems_, w_elems);
+    oz_u_elems_ = std::max(oz_u_elems_, u_elems);
     size_t s0 = ts.size();
-    {  // W[tau][Q][(c,j,n)] = sum_P op(P~(tau))[Q][P] conj(Vt_c[P][j][n])
-      size_t gi = 0;
-      for (const auto &grp : sig_groups_) {
-        const SigContrib &c0 = sc[grp.second[0]];
-        const int qb = c0.qb;
-        OzDesc d{};
-        d.a = {c0.pq + (int64_t)t0 * c0.pstride, c0.pstride, qb, qb};
-        d.b = {sg[gi].boff, qb, 0, 1};
-        d.c = {sg[gi].wc, wct, sg[gi].ncol, qb};
-        d.cn1 = 1;
-        d.cnd = 1;
-        d.aks = d.bks = 1;
-        d.M = ntc * qb;
-        d.N = sg[gi].ncol;
-        d.K = qb;
-        d.flags = c0.pconj ? OZ_CONJ_A : 0;
-        oz_check(d, 1, psz, oz_bcat_elems_, oz_w_elems_, "Sigma stage W");
-        add(d, 1, 1);
-        ++gi;
-      }
+    for (const WG &w : wg) {  // W[tau][Q][(c,j,n)] = sum_P op(P~(tau))[Q][P] conj(Vt_c[P][j][n])
+      const SigContrib &c0 = sc[gcs[w.g][0]];
+      const int qb = c0.qb;
+      OzDesc d{};
+      d.a = {c0.pq, c0.pstride, qb, qb};
+      d.b = {sg[w.g].boff + (int64_t)w.col0 * qb, qb, 0, 1};
+      d.c = {w.wc, wct, w.ncol, qb};
+      d.cn1 = 1;
+      d.cnd = 1;
+      d.aks = d.bks = 1;
+      d.M = nts * qb;
+      d.N = w.ncol;
+      d.K = qb;
+      d.flags = c0.pconj ? OZ_CONJ_A : 0;
+      oz_check(d, 1, psz, oz_bcat_elems_, w_elems, "Sigma stage W");
+      add(d, 1, 1);
     }
     stage(oz_sig_, s0, OZB_PFF, OZB_BCAT, OZB_W);
     s0 = ts.size();
+    // U packs: (G2 block, spin) -> [(owner, contribution)]
+    std::map<std::pair<int64_t, int>, std::vector<std::pair<int, int>>> up;
+    for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {
+      if (uoff[oi] < 0) continue;
+      const Owner &o = sig_own_host_[oi];
+      for (int c = o.c0; c < o.c1; ++c) up[{sc[c].gb, o.s}].push_back({(int)oi, c});
+    }
     for (auto &kv : up) {  // U[tau][j][(c,Q,m)] = sum_n W[tau][Q][(c,j,n)] G2(tau)[m][n]
       const int sp = kv.first.second;
       const auto &v = kv.second;
@@ -1753,9 +1820,10 @@ void Engine::build_oz_lists() {
       const int64_t taba = (int64_t)rt.size();
       for (const auto &x : v) {
         const int c = x.second, b1 = sig_b1_[c];
-        const SG &g = sg[cgroup[c]];
+        const WG &w = wg[wgi[cgroup[c]]];
         for (int Q = 0; Q < sc[c].qb; ++Q)
-          for (int j = 0; j < b1; ++j) rt.push_back(g.wc + (int64_t)Q * g.ncol + ccol[c] + (int64_t)j * b2);
+          for (int j = 0; j < b1; ++j)
+            rt.push_back(w.wc + (int64_t)Q * w.ncol + (ccol[c] - w.col0) + (int64_t)j * b2);
       }
       const int64_t tabc = (int64_t)rt.size();
       for (const auto &x : v) {
@@ -1769,7 +1837,7 @@ void Engine::build_oz_lists() {
       d.M = (int)(tabc - taba);
       d.a = {taba, 0, 0, 0};
       d.ra = wct;
-      d.b = {c0.gb + ((int64_t)t0 * ns + sp) * c0.sb, b2, 0, 1};
+      d.b = {c0.gb + (int64_t)sp * c0.sb, b2, 0, 1};
       d.rb = (int64_t)ns * c0.sb;
       d.c = {tabc, 0, 0, 0};
       d.rc = uct;
@@ -1778,30 +1846,31 @@ void Engine::build_oz_lists() {
       d.aks = d.bks = 1;
       d.N = b2;
       d.K = b2;
-      check_tab(taba, d.M, b2, wct, ntc, oz_w_elems_, "Sigma stage U (W rows)");
-      check_tab(tabc, d.M, b2, uct, ntc, oz_u_elems_, "Sigma stage U (U rows)");
-      oz_check(d, ntc, oz_w_elems_, gsz, oz_u_elems_, "Sigma stage U");
-      add(d, ntc, REPG);
+      check_tab(taba, d.M, b2, wct, nts, w_elems, "Sigma stage U (W rows)");
+      check_tab(tabc, d.M, b2, uct, nts, u_elems, "Sigma stage U (U rows)");
+      oz_check(d, nts, w_elems, gsz, u_elems, "Sigma stage U");
+      add(d, nts, REPG);
     }
     stage(oz_sig_, s0, OZB_W, OZB_GFF, OZB_U);
     s0 = ts.size();
     for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {  // Sigma[i][j] = sum_K U[(tau,j)][K] VcatS[i][K]
+      if (uoff[oi] < 0) continue;
       const Owner &o = sig_own_host_[oi];
       const auto &v = vs[std::make_pair(o.c0, o.c1)];
       if (v.second == 0) continue;
       OzDesc d{};
       d.a = {uoff[oi], uct, v.second, o.n};
       d.b = {v.first, v.second, 0, 1};
-      d.c = {o.out + (int64_t)t0 * o.ostride, o.ostride, 1, o.n};
+      d.c = {o.out, o.ostride, 1, o.n};
       d.cn1 = o.n;
       d.cnd = 1;
       d.aks = d.bks = 1;
-      d.M = ntc * o.n;
+      d.M = nts * o.n;
       d.N = o.n;
       d.K = v.second;
       d.flags = OZ_OUT_F64;
       d.alpha = -1.0 / l.nk;
-      oz_check(d, 1, oz_u_elems_, oz_vcats_elems_, ssz, "Sigma stage Sigma");
+      oz_check(d, 1, u_elems, oz_vcats_elems_, ssz, "Sigma stage Sigma");
       add(d, 1, 1);
     }
     stage(oz_sig_, s0, OZB_U, OZB_VCATS, OZB_SIG);

@@ -1,0 +1,127 @@
+"""The sliced (Ozaki) split-precision contractions (GWGB_PREC_OZAKI) at the
+stated bound: P0, Sigma and G within 1e-7 (absolute) of the FP64 path and of
+the FP64 oracle, the self-consistent loop's per-iteration Sigma, mu and
+correlation energy within 1e-7 of the FP64 loop, bitwise independence of the
+tau chunking and of the V storage, and bitwise reproducibility."""
+import numpy as np
+import pytest
+
+from _helpers import crystal
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+BOUND = 1e-7  # Ha, absolute: the split-precision path's stated Sigma and energy error
+
+
+def _solver(cr, tr, precision="fp64", **kw):
+    from mbsymmetry_gb300.solver import GWSolver
+    s = GWSolver(cr.layout, cr.ns, tr, precision=precision, **kw)
+    s.set_shared_Coulomb(cr.V)
+    s.set_fock(cr.F, cr.S)
+    s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+    return s
+
+
+def _solve(cr, tr, precision, G0=None):
+    s = _solver(cr, tr, precision)
+    if G0 is None:
+        s.dyson(cr.mu)
+    else:
+        s.set_G(G0)
+    G0 = s.G_tau()
+    s.solve()
+    out = (G0, s.P0_q_t_QP(), s.Selfenergy())
+    s.dyson(cr.mu)
+    out += (s.G_tau(),)
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("name,ns,physical", [("C1", 1, False), ("C1", 2, False), ("C1", 1, True),
+                                              ("C2", 1, False), ("C2", 1, True)])
+def test_sliced_within_bound_of_fp64(name, ns, physical):
+    cr, tr = crystal(name, ns=ns, physical=physical)
+    G0, P64, S64, G64 = _solve(cr, tr, "fp64")
+    _, Poz, Soz, Goz = _solve(cr, tr, "ozaki", G0)
+    e = [float(np.abs(a - b).max()) for a, b in ((Poz, P64), (Soz, S64), (Goz, G64))]
+    print(f"{name} ns={ns} physical={physical}: max|ozaki - fp64| P~ {e[0]:.2e} Sigma {e[1]:.2e} "
+          f"G {e[2]:.2e} (max|Sigma| {np.abs(S64).max():.2f})")
+    assert max(e) < BOUND
+
+
+@pytest.mark.parametrize("ns", [1, 2])
+def test_sliced_against_oracle(ns):
+    cr, tr = crystal("C1", ns=ns)
+    L = cr.layout
+    orc = Oracle(L, cr.ns, tr.nts)
+    zero = np.zeros(tr.nts * cr.ns * L.flat_ao_size, np.complex128)
+    G0, _ = orc.dyson(zero, cr.F, cr.S, tr, cr.mu)
+    G1r, Sr, *_ = orc.iteration(G0, cr.V, cr.F, cr.S, tr, cr.mu)
+    s = _solver(cr, tr, "ozaki")
+    s.set_G(G0)
+    s.iteration(cr.mu)
+    Sg, Gg = s.Selfenergy(), s.G_tau()
+    s.close()
+    assert np.abs(Sg - Sr).max() < BOUND
+    assert np.abs(Gg - G1r).max() < BOUND
+
+
+def test_sliced_sc_loop_energy_within_bound():
+    """Five self-consistent iterations (alpha = 0.5, device mu search): per
+    iteration mu and E_corr, and the final Sigma, within 1e-7 of the FP64 loop."""
+    cr, tr = crystal("C2")
+    recs, sig = {}, {}
+    for prec in ("fp64", "ozaki"):
+        s = _solver(cr, tr, prec)
+        s.set_hcore(cr.H)
+        s.dyson(cr.mu)
+        recs[prec] = s.sc_loop(5, 0.5, float(cr.layout.nao), cr.mu, step=0.05, tol=1e-10, max_evals=24)
+        sig[prec] = s.Selfenergy()
+        s.close()
+    for a, b in zip(recs["fp64"], recs["ozaki"]):
+        print(f"mu {a['mu']:.12f} {b['mu']:.12f}  e_corr {a['e_corr']:.12f} {b['e_corr']:.12f}")
+        assert abs(a["e_corr"] - b["e_corr"]) < BOUND
+        assert abs(a["mu"] - b["mu"]) < BOUND
+    assert np.abs(sig["fp64"] - sig["ozaki"]).max() < BOUND
+
+
+def test_sliced_tau_chunks_and_reruns_are_bitwise(monkeypatch):
+    """The tau-dependent intermediates hold one tau chunk at a time: one tau per
+    chunk (GWGB_TC_CHUNK_MB=1) gives bitwise the same P~ and Sigma as one
+    chunk, and a rerun on the same handle is bitwise identical."""
+    cr, tr = crystal("C2")
+    out = []
+    for env in (None, "1"):
+        if env is None:
+            monkeypatch.delenv("GWGB_TC_CHUNK_MB", raising=False)
+        else:
+            monkeypatch.setenv("GWGB_TC_CHUNK_MB", env)
+        s = _solver(cr, tr, "ozaki")
+        s.dyson(cr.mu)
+        G0 = s.G_tau()
+        for _ in range(2):
+            s.set_G(G0)
+            s.solve()
+            out.append((s.Selfenergy(), s.P0_q_t_QP(), s.stats()["kernel_launches"]))
+        s.close()
+    (s1, p1, n1), (s1b, p1b, _), (s2, p2, n2), _ = out
+    assert np.array_equal(s1, s1b) and np.array_equal(p1, p1b)
+    assert n2 > n1
+    assert np.array_equal(p1, p2) and np.array_equal(s1, s2)
+
+
+def test_sliced_used_pairs_only_storage_is_exact():
+    from mbsymmetry_gb300.crystal import CONFIGS, load_ir, make_crystal
+    from mbsymmetry_gb300.transformer import build_transforms
+    spec = CONFIGS["C1"]
+    tr = build_transforms(load_ir(spec.nts), spec.beta)
+    out = []
+    for used in (False, True):
+        cr = make_crystal(spec, used_pairs_only=used)
+        s = _solver(cr, tr, "ozaki")
+        s.dyson(cr.mu)
+        s.solve()
+        out.append((s.P0_q_t_QP(), s.Selfenergy()))
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
