@@ -286,6 +286,7 @@ class Engine {
         Gff_.alloc(Gall_.n);
         Pff_.alloc(Pall_.n);
         Vff_.alloc((size_t)l_.flat_V);
+        ozPart_.alloc((size_t)oz_part_elems_);
         oz_ready_ = false;
       }
       return;
@@ -453,12 +454,17 @@ class Engine {
   // tau-independent ones from V / Vt.
   enum OzBufId { OZB_GFF, OZB_PFF, OZB_VFF, OZB_VCAT, OZB_BCAT, OZB_VCATS, OZB_Z1, OZB_ZCAT, OZB_W, OZB_U, OZB_P0,
                  OZB_SIG };
-  struct OzLaunch { int64_t t0, n; int a, b, c; };
+  // one stage launch: tasks [t0, t0 + n); with nr > 0 the stage writes FP64 K-slice partials to
+  // ozPart_ and the ordered sums oz_red_[r0, r0 + nr) (times scale) go to buffer c afterwards
+  struct OzLaunch { int64_t t0, n; int a, b, c; int64_t r0 = 0, nr = 0; double scale = 1.0; };
   bool oz_built_ = false, oz_ready_ = false;
   DBuf<OzDesc> oz_descs_;
   DBuf<OzTask> oz_tasks_;
   DBuf<OzPerm> oz_perm_v_, oz_perm_b_, oz_perm_s_;
   DBuf<int64_t> oz_rowtab_;
+  DBuf<RedTask> oz_red_;
+  DBuf<double2> ozPart_;
+  int64_t oz_part_elems_ = 1;
   DBuf<float4> Gff_, Pff_, Vff_, ozVcat_, ozBcat_, ozVcatS_, ozZ1_, ozZcat_, ozW_, ozU_;
   int64_t oz_vcat_elems_ = 0, oz_bcat_elems_ = 0, oz_vcats_elems_ = 0, oz_z1_elems_ = 0, oz_zcat_elems_ = 0,
           oz_w_elems_ = 0, oz_u_elems_ = 0;
@@ -484,10 +490,14 @@ class Engine {
     }
   }
   void oz_run(const std::vector<OzLaunch> &ls) {
-    for (const OzLaunch &x : ls)
+    for (const OzLaunch &x : ls) {
+      void *c = x.nr ? static_cast<void *>(ozPart_.p) : const_cast<void *>(oz_ptr(x.c));
       launch_oz_gemm(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, static_cast<const float4 *>(oz_ptr(x.a)),
-                     static_cast<const float4 *>(oz_ptr(x.b)), const_cast<void *>(oz_ptr(x.c)), oz_rowtab_.p, nsm_,
-                     bad_.p + 2, st_);
+                     static_cast<const float4 *>(oz_ptr(x.b)), c, oz_rowtab_.p, nsm_, bad_.p + 2, st_);
+      if (x.nr)
+        launch_reduce_slices(oz_red_.p + x.r0, (int)x.nr, ozPart_.p,
+                             static_cast<double2 *>(const_cast<void *>(oz_ptr(x.c))), nts_, x.scale, 0, st_);
+    }
   }
   struct P0Group { int64_t pout; int32_t pstride, qb, c0, c1; };
   std::vector<P0Group> p0_groups_;                            // host: P0 output blocks
@@ -653,6 +663,7 @@ Engine::~Engine() {
   pz_tasks_.free(); vc_tasks_.free(); pk_tiles_.free(); pr_tiles_.free(); Zbuf_.free(); Vcat_.free(); Ppart_.free();
   oz_descs_.free(); oz_tasks_.free(); oz_perm_v_.free(); oz_perm_b_.free(); oz_perm_s_.free(); oz_rowtab_.free();
   for (DBuf<float4> *b : {&Gff_, &Pff_, &Vff_, &ozVcat_, &ozBcat_, &ozVcatS_, &ozZ1_, &ozZcat_, &ozW_, &ozU_}) b->free();
+  oz_red_.free(); ozPart_.free();
   for (auto *b : bufs) b->free();
   tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
   qoff_irr_.free(); qsz_irr_.free();
@@ -1507,6 +1518,53 @@ void Engine::build_oz_lists() {
     std::stable_sort(ts.begin() + t0, ts.end(), [&](const OzTask &x, const OzTask &y) { return cost(x) > cost(y); });
     if (ts.size() > t0) v.push_back({(int64_t)t0, (int64_t)(ts.size() - t0), a, b, c});
   };
+  // Final GEMMs (P0, Sigma) in K slices: each slice writes an FP64 partial block
+  // [slice][rows][cols] to ozPart_; the slices are summed in order afterwards
+  // (reduce_slices_kernel), so the result does not depend on the launch order.
+  // The slice count depends on the block alone (about two waves of CTAs for
+  // that block, at least 32 rounds of K per slice), so results do not depend on
+  // how blocks are grouped into chunks.
+  std::vector<RedTask> red;
+  struct Fin { OzDesc d; int64_t out; int32_t ostride, nt, elems; };
+  auto final_stage = [&](std::vector<OzLaunch> &v, const std::vector<Fin> &fins, int a, int b, int c, double scale,
+                         int64_t na, int64_t nb, int64_t nout, const char *what) {
+    const size_t t0 = ts.size(), r0 = red.size();
+    int64_t part = 0;
+    for (const Fin &f : fins) {
+      const int64_t tiles = (int64_t)((f.d.M + OZ_M - 1) / OZ_M) * ((f.d.N + OZ_NC - 1) / OZ_NC);
+      const int64_t want = (2 * (int64_t)std::max(1, nsm_) + tiles - 1) / tiles;
+      const int nk16 = (f.d.K + OZ_KR - 1) / OZ_KR;
+      const int nsl = (int)std::max<int64_t>(1, std::min<int64_t>(want, nk16 / 32));
+      const int per = (nk16 + nsl - 1) / nsl * OZ_KR;
+      const int64_t mn = (int64_t)f.d.M * f.d.N;
+      int used = 0;
+      for (int k0 = 0; k0 < f.d.K; k0 += per, ++used) {
+        OzDesc d = f.d;
+        d.a.base += k0;
+        d.b.base += k0;
+        d.K = std::min(per, f.d.K - k0);
+        d.c = {part + used * mn, f.elems, 1, f.d.c.d};
+        d.alpha = 1.0;
+        d.flags |= OZ_OUT_F64;
+        oz_check(d, 1, na, nb, (int64_t)1 << 62, what);
+        add(d, 1, 1);
+      }
+      red.push_back({part, f.out, f.ostride, f.elems, 0, f.nt, used, 0});
+      check_range(f.out, (int64_t)(f.nt - 1) * f.ostride + f.elems, nout, what);
+      part += used * mn;
+    }
+    oz_part_elems_ = std::max(oz_part_elems_, part);
+    std::stable_sort(ts.begin() + t0, ts.end(), [&](const OzTask &x, const OzTask &y) {
+      return (int64_t)x.nrep * ds[x.desc].K > (int64_t)y.nrep * ds[y.desc].K;
+    });
+    if (ts.size() > t0) {
+      OzLaunch l{(int64_t)t0, (int64_t)(ts.size() - t0), a, b, c};
+      l.r0 = (int64_t)r0;
+      l.nr = (int64_t)(red.size() - r0);
+      l.scale = scale;
+      v.push_back(l);
+    }
+  };
   // Row-table checks: every entry (plus the row's K extent and reps) inside the buffer.
   auto check_tab = [&](int64_t base, int M, int64_t klen, int64_t rep, int nrep, int64_t size, const char *what) {
     for (int r = 0; r < M; ++r) {
@@ -1517,6 +1575,7 @@ void Engine::build_oz_lists() {
   };
   oz_p0_.clear();
   oz_sig_.clear();
+  oz_part_elems_ = 1;
   const int64_t gsz = (int64_t)Gall_.n, psz = (int64_t)Pall_.n, ssz = (int64_t)nts * ns * l.flat_ao;
   const double pref = -1.0 / l.nk * (ns == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
 
@@ -1664,26 +1723,24 @@ void Engine::build_oz_lists() {
       add(d, half, REPG);
     }
     stage(oz_p0_, s0, OZB_Z1, OZB_GFF, OZB_ZCAT);
-    s0 = ts.size();
+    std::vector<Fin> fins;
     for (int gi = ch.first; gi < ch.second; ++gi) {  // P0[Q][P] = sum_K Zcat[(tau,P)][K] Vcat[Q][K]
       const P0Group &g = p0_groups_[gi];
       if (g.c1 == g.c0) continue;
       OzDesc d{};
       d.a = {zc[gi], zct, pg[gi].zld, g.qb};
       d.b = {pg[gi].voff, pg[gi].zld, 0, 1};
-      d.c = {g.pout, g.pstride, 1, g.qb};
+      d.c = {0, 0, 1, g.qb};  // partial [slice][(tau, P)][Q]: rows (tau, P), column Q at Q * qb
       d.cn1 = g.qb;
       d.cnd = 1;
       d.aks = d.bks = 1;
       d.M = half * g.qb;
       d.N = g.qb;
       d.K = pg[gi].zld;
-      d.flags = OZ_OUT_F64;
-      d.alpha = pref;
-      oz_check(d, 1, zcat_elems, oz_vcat_elems_, psz, "P0 stage P0");
-      add(d, 1, 1);
+      oz_check(d, 1, zcat_elems, oz_vcat_elems_, (int64_t)1 << 62, "P0 stage P0");
+      fins.push_back({d, g.pout, g.pstride, half, g.qb * g.qb});
     }
-    stage(oz_p0_, s0, OZB_ZCAT, OZB_VCAT, OZB_P0);
+    final_stage(oz_p0_, fins, OZB_ZCAT, OZB_VCAT, OZB_P0, pref, zcat_elems, oz_vcat_elems_, psz, "P0 stage P0");
   }
 
   // ---- Sigma ----------------------------------------------------------------
@@ -1852,7 +1909,7 @@ void Engine::build_oz_lists() {
       add(d, nts, REPG);
     }
     stage(oz_sig_, s0, OZB_W, OZB_GFF, OZB_U);
-    s0 = ts.size();
+    std::vector<Fin> fins;
     for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {  // Sigma[i][j] = sum_K U[(tau,j)][K] VcatS[i][K]
       if (uoff[oi] < 0) continue;
       const Owner &o = sig_own_host_[oi];
@@ -1861,19 +1918,18 @@ void Engine::build_oz_lists() {
       OzDesc d{};
       d.a = {uoff[oi], uct, v.second, o.n};
       d.b = {v.first, v.second, 0, 1};
-      d.c = {o.out, o.ostride, 1, o.n};
+      d.c = {0, 0, 1, o.n};  // partial [slice][(tau, j)][i]: rows (tau, j), column i at i * b1
       d.cn1 = o.n;
       d.cnd = 1;
       d.aks = d.bks = 1;
       d.M = nts * o.n;
       d.N = o.n;
       d.K = v.second;
-      d.flags = OZ_OUT_F64;
-      d.alpha = -1.0 / l.nk;
-      oz_check(d, 1, u_elems, oz_vcats_elems_, ssz, "Sigma stage Sigma");
-      add(d, 1, 1);
+      oz_check(d, 1, u_elems, oz_vcats_elems_, (int64_t)1 << 62, "Sigma stage Sigma");
+      fins.push_back({d, o.out, o.ostride, nts, o.n * o.n});
     }
-    stage(oz_sig_, s0, OZB_U, OZB_VCATS, OZB_SIG);
+    final_stage(oz_sig_, fins, OZB_U, OZB_VCATS, OZB_SIG, -1.0 / l.nk, u_elems, oz_vcats_elems_, ssz,
+                "Sigma stage Sigma");
   }
   for (const OzPerm &t : pv) {
     check_range(t.src, (int64_t)t.X * t.Y * t.Z, l.flat_V, "sliced Vcat source");
@@ -1892,6 +1948,8 @@ void Engine::build_oz_lists() {
   oz_descs_.upload(ds, st_);
   oz_tasks_.upload(ts, st_);
   oz_rowtab_.upload(rt.empty() ? std::vector<int64_t>(1, 0) : rt, st_);
+  for (const RedTask &r : red) check_range(r.part, (int64_t)r.nslice * r.nt * r.elems, oz_part_elems_, "sliced partials");
+  oz_red_.upload(red.empty() ? std::vector<RedTask>(1, RedTask{}) : red, st_);
   oz_perm_v_.upload(pv, st_);
   oz_perm_b_.upload(pb, st_);
   oz_perm_s_.upload(psg, st_);
