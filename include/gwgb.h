@@ -69,6 +69,10 @@ typedef struct gwgb_params {
   int32_t sw_npk_max;  /* widest W-GEMM column pack (16, 32 or 64 complex columns) */
   int32_t uv_waves;    /* U/Sigma contribution slices per tau, in units of the SM count (1..16; default 8) */
   int32_t uv_simt;     /* 1: all U/Sigma tiles on the FP32 SIMT kernels (the path for AO blocks above 64) */
+  /* Sliced path (GWGB_PREC_OZAKI): block GEMMs with at most this many output
+   * columns run on the CUDA-core float-float kernel instead of tcgen05
+   * (0: the built-in 8; -1: none; at most 1024). */
+  int32_t oz_simt_cols;
 } gwgb_params;
 
 /* Block layout: the arrays symmetry_utils_t reads from symmetry_info.h5,

@@ -36,6 +36,7 @@ class GwgbParams(ctypes.Structure):
         ("beta", c_double), ("precision", c_int32), ("device", c_int32),
         ("nt_batch", c_int32), ("flags", c_int32),
         ("uvt_smem_kb", c_int32), ("sw_npk_max", c_int32), ("uv_waves", c_int32), ("uv_simt", c_int32),
+        ("oz_simt_cols", c_int32),
     ]
 
 

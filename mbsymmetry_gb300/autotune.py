@@ -1,4 +1,15 @@
-"""Empirical tile-shape tuning of the tcgen05 Sigma path for one workload.
+"""Empirical tuning of the contraction kernels for one workload.
+
+Sliced path (precision "ozaki"): every P0 / Sigma stage is a list of block
+GEMMs whose output width N is set by an irrep block size (AO block for the
+G products and the final Sigma GEMM, aux block for the final P0 GEMM).  A
+tcgen05 round stages 128 rows x 16 complex K whatever N is, so narrow blocks
+run faster on the CUDA-core float-float kernel.  gwgb_params.oz_simt_cols is
+the width class boundary: blocks with N <= oz_simt_cols go to the CUDA cores.
+OZAKI_CANDIDATES spans the classes (none, N <= 4, 8, 16, 32), scored on the
+whole iteration (the boundary moves work in both contractions).
+
+Split FP32-class paths (tf32x3 / bf16x3):
 
 The engine picks tile shapes per irrep-block size class by rule (tau per
 U/Sigma tile from 128 / k1_b and the shared-memory budget, aux rows per chunk
@@ -32,6 +43,14 @@ DEFAULT_CANDIDATES = (
     {"uvt_smem_kb": 110, "sw_npk_max": 32, "uv_waves": 8},
 )
 
+OZAKI_CANDIDATES = (
+    {"oz_simt_cols": 0},    # the built-in boundary (8)
+    {"oz_simt_cols": -1},   # every block GEMM on tcgen05
+    {"oz_simt_cols": 4},
+    {"oz_simt_cols": 16},
+    {"oz_simt_cols": 32},
+)
+
 
 def _device_key(device: int) -> str:
     """Library version plus the GPU's name, SM count and shared memory per block:
@@ -62,18 +81,23 @@ def fingerprint(layout, nts: int, precision: str, device: int = 0) -> str:
     return h.hexdigest()[:16]
 
 
-def autotune(layout, ns, transforms, V, F, S, mu, G=None, precision="tf32x3", candidates=DEFAULT_CANDIDATES,
+def autotune(layout, ns, transforms, V, F, S, mu, G=None, precision="tf32x3", candidates=None,
              warmup=1, reps=2, cache=None, device=0):
     """Time each candidate on this workload; return {"best": settings, "trials": [...]}.
 
     G: the Green's function to iterate from (default: Dyson of Sigma = 0 at mu).
-    The metric is the Sigma stage (the stage the settings shape) of `reps`
-    iterations after `warmup`; each trial also records the whole iteration.
+    candidates: default OZAKI_CANDIDATES for "ozaki", else DEFAULT_CANDIDATES.
+    The metric is the whole iteration for "ozaki" and the Sigma stage (the
+    stage the settings shape) otherwise, median of `reps` iterations after
+    `warmup`; each trial records both.
     With ``cache`` (a JSON file path) an earlier result for the same
     fingerprint is returned without timing, and new results are added.
     Each candidate is a full handle with V in device memory, built and closed
     in turn: the device needs room for one such handle besides any the caller
     holds (at C5 scale, 180 GB, tune before creating the working handle)."""
+    if candidates is None:
+        candidates = OZAKI_CANDIDATES if precision == "ozaki" else DEFAULT_CANDIDATES
+    metric = "iteration_ms" if precision == "ozaki" else "sigma_ms"
     key = fingerprint(layout, transforms.nts, precision, device)
     store = {}
     if cache and os.path.exists(cache):
@@ -105,8 +129,8 @@ def autotune(layout, ns, transforms, V, F, S, mu, G=None, precision="tf32x3", ca
                            "iteration_ms": float(np.median(tot))})
         finally:
             s.close()
-    best = min(trials, key=lambda t: t["sigma_ms"])
-    out = {"fingerprint": key, "precision": precision, "best": best["settings"], "trials": trials}
+    best = min(trials, key=lambda t: t[metric])
+    out = {"fingerprint": key, "precision": precision, "metric": metric, "best": best["settings"], "trials": trials}
     if cache:
         store[key] = out
         with open(cache, "w") as f:

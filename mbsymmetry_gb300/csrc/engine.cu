@@ -456,7 +456,15 @@ class Engine {
                  OZB_SIG };
   // one stage launch: tasks [t0, t0 + n); with nr > 0 the stage writes FP64 K-slice partials to
   // ozPart_ and the ordered sums oz_red_[r0, r0 + nr) (times scale) go to buffer c afterwards
-  struct OzLaunch { int64_t t0, n; int a, b, c; int64_t r0 = 0, nr = 0; double scale = 1.0; };
+  // simt: the CUDA-core float-float kernel; part: C is ozPart_ (K-slice partials)
+  struct OzLaunch {
+    int64_t t0, n;
+    int a, b, c;
+    bool simt = false, part = false;
+    int64_t r0 = 0, nr = 0;
+    double scale = 1.0;
+  };
+  int oz_simt_n_ = 8;  // block GEMMs with at most this many output columns run on the CUDA cores
   bool oz_built_ = false, oz_ready_ = false;
   DBuf<OzDesc> oz_descs_;
   DBuf<OzTask> oz_tasks_;
@@ -491,9 +499,12 @@ class Engine {
   }
   void oz_run(const std::vector<OzLaunch> &ls) {
     for (const OzLaunch &x : ls) {
-      void *c = x.nr ? static_cast<void *>(ozPart_.p) : const_cast<void *>(oz_ptr(x.c));
-      launch_oz_gemm(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, static_cast<const float4 *>(oz_ptr(x.a)),
-                     static_cast<const float4 *>(oz_ptr(x.b)), c, oz_rowtab_.p, nsm_, bad_.p + 2, st_);
+      void *c = x.part ? static_cast<void *>(ozPart_.p) : const_cast<void *>(oz_ptr(x.c));
+      const float4 *a = static_cast<const float4 *>(oz_ptr(x.a)), *b = static_cast<const float4 *>(oz_ptr(x.b));
+      if (x.simt)
+        launch_oz_simt(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, a, b, c, oz_rowtab_.p, st_);
+      else
+        launch_oz_gemm(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, a, b, c, oz_rowtab_.p, nsm_, bad_.p + 2, st_);
       if (x.nr)
         launch_reduce_slices(oz_red_.p + x.r0, (int)x.nr, ozPart_.p,
                              static_cast<double2 *>(const_cast<void *>(oz_ptr(x.c))), nts_, x.scale, 0, st_);
@@ -585,6 +596,8 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
                "sw_npk_max must be 0, 16, 32 or 64");
   GWGB_REQUIRE(p.uv_waves >= 0 && p.uv_waves <= 16, GWGB_E_INVALID, "uv_waves must be in [0, 16]");
   GWGB_REQUIRE(p.uv_simt == 0 || p.uv_simt == 1, GWGB_E_INVALID, "uv_simt must be 0 or 1");
+  GWGB_REQUIRE(p.oz_simt_cols >= -1 && p.oz_simt_cols <= 1024, GWGB_E_INVALID, "oz_simt_cols must be in [-1, 1024]");
+  oz_simt_n_ = p.oz_simt_cols == 0 ? 8 : std::max(0, p.oz_simt_cols);
   tune_uvt_kb_ = p.uvt_smem_kb;
   tune_simt_ = p.uv_simt;
   if (p.sw_npk_max) tune_npk_ = p.sw_npk_max;
@@ -1503,20 +1516,46 @@ void Engine::build_oz_lists() {
   std::vector<OzTask> ts;
   std::vector<int64_t> rt;  // row table
   constexpr int REPG = 8;   // tau per task in the per-tau stages (Z, U)
-  auto add = [&](const OzDesc &d, int nrep, int repg) {
+  // narrow[id]: descriptor id runs on the CUDA-core kernel.  The choice uses a
+  // width that does not depend on the chunking (width < 0: d.N), so chunked and
+  // unchunked runs use the same arithmetic for every output element.
+  std::vector<char> narrow_d;
+  auto add = [&](const OzDesc &d, int nrep, int repg, int width = -1) {
     const int id = (int)ds.size();
     ds.push_back(d);
+    narrow_d.push_back((width < 0 ? d.N : width) <= oz_simt_n_);
     const int mtn = (d.M + OZ_M - 1) / OZ_M, ntn = (d.N + OZ_NC - 1) / OZ_NC;
     GWGB_REQUIRE(mtn < 65536 && ntn < 65536, GWGB_E_UNSUPPORTED, "sliced GEMM too large");
     for (int r0 = 0; r0 < nrep; r0 += repg)
       for (int mt = 0; mt < mtn; ++mt)
         for (int nt = 0; nt < ntn; ++nt) ts.push_back({id, r0, std::min(repg, nrep - r0), (mt << 16) | nt});
   };
-  // tasks of one stage (appended since t0): heaviest first, then one launch
-  auto stage = [&](std::vector<OzLaunch> &v, size_t t0, int a, int b, int c) {
-    auto cost = [&](const OzTask &t) { return (int64_t)t.nrep * ((ds[t.desc].K + OZ_KR - 1) / OZ_KR); };
-    std::stable_sort(ts.begin() + t0, ts.end(), [&](const OzTask &x, const OzTask &y) { return cost(x) > cost(y); });
-    if (ts.size() > t0) v.push_back({(int64_t)t0, (int64_t)(ts.size() - t0), a, b, c});
+  // tasks of one stage (appended since t0): the tensor-core tasks, then the
+  // narrow ones (at most oz_simt_n_ output columns) for the CUDA-core kernel,
+  // each heaviest first; one launch per kind.  The last launch carries `last`.
+  auto narrow = [&](const OzTask &t) { return narrow_d[t.desc] != 0; };
+  auto stage = [&](std::vector<OzLaunch> &v, size_t t0, int a, int b, int c, bool part = false,
+                   const OzLaunch *last = nullptr) {
+    auto cost = [&](const OzTask &t) { return (int64_t)t.nrep * ds[t.desc].K; };
+    std::stable_sort(ts.begin() + t0, ts.end(), [&](const OzTask &x, const OzTask &y) {
+      const bool nx = narrow(x), ny = narrow(y);
+      return nx != ny ? ny : cost(x) > cost(y);
+    });
+    const size_t t1 = std::find_if(ts.begin() + t0, ts.end(), narrow) - ts.begin();
+    const size_t n0 = v.size();
+    for (int k = 0; k < 2; ++k) {
+      const size_t lo = k ? t1 : t0, hi = k ? ts.size() : t1;
+      if (hi == lo) continue;
+      OzLaunch l{(int64_t)lo, (int64_t)(hi - lo), a, b, c};
+      l.simt = k == 1;
+      l.part = part;
+      v.push_back(l);
+    }
+    if (last && v.size() > n0) {
+      v.back().r0 = last->r0;
+      v.back().nr = last->nr;
+      v.back().scale = last->scale;
+    }
   };
   // Final GEMMs (P0, Sigma) in K slices: each slice writes an FP64 partial block
   // [slice][rows][cols] to ozPart_; the slices are summed in order afterwards
@@ -1554,16 +1593,11 @@ void Engine::build_oz_lists() {
       part += used * mn;
     }
     oz_part_elems_ = std::max(oz_part_elems_, part);
-    std::stable_sort(ts.begin() + t0, ts.end(), [&](const OzTask &x, const OzTask &y) {
-      return (int64_t)x.nrep * ds[x.desc].K > (int64_t)y.nrep * ds[y.desc].K;
-    });
-    if (ts.size() > t0) {
-      OzLaunch l{(int64_t)t0, (int64_t)(ts.size() - t0), a, b, c};
-      l.r0 = (int64_t)r0;
-      l.nr = (int64_t)(red.size() - r0);
-      l.scale = scale;
-      v.push_back(l);
-    }
+    OzLaunch red_info{0, 0, a, b, c};
+    red_info.r0 = (int64_t)r0;
+    red_info.nr = (int64_t)(red.size() - r0);
+    red_info.scale = scale;
+    stage(v, t0, a, b, c, true, &red_info);
   };
   // Row-table checks: every entry (plus the row's K extent and reps) inside the buffer.
   auto check_tab = [&](int64_t base, int M, int64_t klen, int64_t rep, int nrep, int64_t size, const char *what) {
@@ -1858,7 +1892,9 @@ void Engine::build_oz_lists() {
       d.K = qb;
       d.flags = c0.pconj ? OZ_CONJ_A : 0;
       oz_check(d, 1, psz, oz_bcat_elems_, w_elems, "Sigma stage W");
-      add(d, 1, 1);
+      int gcols = 0;  // the group's full width (every chunk routes its part the same way)
+      for (int c : gcs[w.g]) gcols += sig_b1_[c] * sc[c].b2;
+      add(d, 1, 1, gcols);
     }
     stage(oz_sig_, s0, OZB_PFF, OZB_BCAT, OZB_W);
     s0 = ts.size();

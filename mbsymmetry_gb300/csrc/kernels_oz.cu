@@ -463,6 +463,80 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   if (warp == 0) tc::tmem_dealloc(tm, OZ_TMEM_WS);
 }
 
+// (h, l) += (a + al)(b + bl) without renormalising (the a_l b_l term, below
+// 2^-48 of the product, is dropped): the product's rounding error comes from an
+// FMA (exact), the sum's from a two-sum; both go to the low word.
+__device__ __forceinline__ void ff_mac(float &h, float &l, float a, float al, float b, float bl) {
+  const float p = a * b;
+  float e = fmaf(a, b, -p);
+  e = fmaf(a, bl, e);
+  e = fmaf(al, b, e);
+  const float s = h + p;
+  const float bb = s - h;
+  l += ((h - (s - bb)) + (p - bb)) + e;
+  h = s;
+}
+
+// Narrow block GEMMs (few output columns) on the CUDA cores in float-float:
+// the same descriptors and tasks as oz_gemm_kernel (one CTA per task, one
+// thread per row of the 128-row tile, four output columns at a time), for
+// shapes where a tensor-core round would stage 128 x 16 slices for a handful
+// of columns.  Every operand keeps its float-float value (no slicing), so the
+// result carries about 46 bits.  B is read with addresses uniform across the
+// warp (broadcast loads).
+__global__ void __launch_bounds__(OZ_M) oz_simt_kernel(const OzDesc *__restrict__ descs,
+                                                       const OzTask *__restrict__ tasks, const float4 *__restrict__ Ag,
+                                                       const float4 *__restrict__ Bg, void *__restrict__ Cg,
+                                                       const int64_t *__restrict__ rowtab) {
+  const OzTask tk = tasks[blockIdx.x];
+  const OzDesc dg = descs[tk.desc];
+  const int mt = tk.mtnt >> 16, nt = tk.mtnt & 0xffff;
+  const int Mt = min(OZ_M, dg.M - mt * OZ_M), Nt = min(OZ_NC, dg.N - nt * OZ_NC);
+  const int r = threadIdx.x;
+  if (r >= Mt) return;
+  const int64_t arow0 = row_off(dg.a, mt * OZ_M + r, rowtab), crow0 = row_off(dg.c, mt * OZ_M + r, rowtab);
+  const float sa = (dg.flags & OZ_CONJ_A) ? -1.f : 1.f, sb = (dg.flags & OZ_CONJ_B) ? -1.f : 1.f;
+  const bool f64 = dg.flags & OZ_OUT_F64;
+  for (int rr = 0; rr < tk.nrep; ++rr) {
+    const int rep = tk.rep0 + rr;
+    const float4 *arow = Ag + arow0 + (int64_t)rep * dg.ra;
+    const int64_t co = crow0 + (int64_t)rep * dg.rc;
+    for (int n0 = 0; n0 < Nt; n0 += 4) {
+      const int nc = min(4, Nt - n0);
+      const float4 *bp[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c)  // columns past the tile re-read column n0 (results unused)
+        bp[c] = Bg + row_off(dg.b, nt * OZ_NC + n0 + (c < nc ? c : 0), rowtab) + (int64_t)rep * dg.rb;
+      float acc[4][4];  // per column: re (h, l), im (h, l)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[c][0] = acc[c][1] = acc[c][2] = acc[c][3] = 0.f;
+      for (int k = 0; k < dg.K; ++k) {
+        const float4 a = __ldg(arow + (int64_t)k * dg.aks);
+        const float ai = sa * a.y, ail = sa * a.w;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const float4 b = __ldg(bp[c] + (int64_t)k * dg.bks);
+          const float bi = sb * b.y, bil = sb * b.w;
+          ff_mac(acc[c][0], acc[c][1], a.x, a.z, b.x, b.z);    // re += ar br
+          ff_mac(acc[c][0], acc[c][1], -ai, -ail, bi, bil);    //     - ai bi
+          ff_mac(acc[c][2], acc[c][3], a.x, a.z, bi, bil);     // im += ar bi
+          ff_mac(acc[c][2], acc[c][3], ai, ail, b.x, b.z);     //     + ai br
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (c < nc) {
+          const int n = nt * OZ_NC + n0 + c;
+          const int nq = n / dg.cnd, nr = n - nq * dg.cnd;
+          const float rh = acc[c][0] + acc[c][1], ih = acc[c][2] + acc[c][3];
+          const float rl = acc[c][1] - (rh - acc[c][0]), il = acc[c][3] - (ih - acc[c][2]);
+          oz_store(Cg, co + nq * dg.cn1 + (int64_t)nr * dg.cn0, f64, dg.alpha, rh, ih, rl, il);
+        }
+      }
+    }
+  }
+}
+
 __global__ void to_ffc_kernel(const double2 *__restrict__ x, float4 *__restrict__ y, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double2 v = x[i];
@@ -496,6 +570,13 @@ void launch_oz_gemm(const OzDesc *descs, const OzTask *tasks, int ntasks, const 
   if (ntasks == 0) return;
   const int grid = std::min(ntasks, std::max(1, nsm));
   oz_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM_WS, st>>>(descs, tasks, ntasks, A, B, C, rowtab, err);
+  GWGB_CUDA(cudaGetLastError());
+}
+
+void launch_oz_simt(const OzDesc *descs, const OzTask *tasks, int ntasks, const float4 *A, const float4 *B, void *C,
+                    const int64_t *rowtab, cudaStream_t st) {
+  if (ntasks == 0) return;
+  oz_simt_kernel<<<ntasks, OZ_M, 0, st>>>(descs, tasks, A, B, C, rowtab);
   GWGB_CUDA(cudaGetLastError());
 }
 

@@ -74,6 +74,11 @@ void set_oz_kernel_attributes();
 void launch_oz_gemm(const OzDesc *descs, const OzTask *tasks, int ntasks, const float4 *A, const float4 *B, void *C,
                     const int64_t *rowtab, int nsm, int *err, cudaStream_t st);
 
+// The same tasks on the CUDA cores in float-float arithmetic (one CTA per task):
+// for block GEMMs with few output columns.
+void launch_oz_simt(const OzDesc *descs, const OzTask *tasks, int ntasks, const float4 *A, const float4 *B, void *C,
+                    const int64_t *rowtab, cudaStream_t st);
+
 // y[i] = float-float(x[i]) for n complex elements.
 void launch_to_ffc(const double2 *x, float4 *y, int64_t n, cudaStream_t st);
 

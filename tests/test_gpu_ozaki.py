@@ -23,8 +23,8 @@ def _solver(cr, tr, precision="fp64", **kw):
     return s
 
 
-def _solve(cr, tr, precision, G0=None):
-    s = _solver(cr, tr, precision)
+def _solve(cr, tr, precision, G0=None, tune=None):
+    s = _solver(cr, tr, precision, tune=tune)
     if G0 is None:
         s.dyson(cr.mu)
     else:
@@ -125,3 +125,20 @@ def test_sliced_used_pairs_only_storage_is_exact():
         out.append((s.P0_q_t_QP(), s.Selfenergy()))
         s.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("name,ns", [("C1", 2), ("C2", 1)])
+def test_narrow_blocks_on_cuda_cores_within_bound(name, ns):
+    """Block GEMMs routed by output width: all on tcgen05 (oz_simt_cols=-1),
+    the built-in boundary, and every block of up to 32 columns on the CUDA-core
+    float-float kernel each stay within 1e-7 of FP64, and within 1e-8 of each other."""
+    cr, tr = crystal(name, ns=ns)
+    G0, P64, S64, _ = _solve(cr, tr, "fp64")
+    res = {}
+    for cols in (-1, 0, 32):
+        _, P, S, G = _solve(cr, tr, "ozaki", G0, tune={"oz_simt_cols": cols})
+        e = (float(np.abs(P - P64).max()), float(np.abs(S - S64).max()))
+        print(f"{name} ns={ns} oz_simt_cols={cols}: P~ {e[0]:.2e} Sigma {e[1]:.2e}")
+        assert max(e) < BOUND
+        res[cols] = S
+    assert np.abs(res[-1] - res[32]).max() < 1e-8 and np.abs(res[0] - res[32]).max() < 1e-8

@@ -62,8 +62,11 @@ def test_c2_sigma_acceptance():
 
 @pytest.mark.parametrize("name,kind", [("C1", "tf32x3"), ("C2", "tf32x3"), ("C1", "bf16x3"), ("C2", "bf16x3")])
 def test_mixed_sigma_error(name, kind):
-    """Split tensor-core contractions (TF32x3: 3 products of 2 TF32 planes;
-    BF16x3: 6 products of 3 BF16 planes) against the FP64 path on the same input."""
+    """FP32-class split tensor-core contractions (TF32x3: 3 products of 2 TF32
+    planes; BF16x3: 6 products of 3 BF16 planes) against the FP64 path on the
+    same input.  These paths carry about 24 bits and make no 1e-7 Ha claim
+    (the sliced path does: tests/test_gpu_ozaki.py); the bound here is their
+    FP32-class error, 1e-5 relative to max|Sigma|."""
     from mbsymmetry_gb300.solver import GWSolver
     cr, tr = crystal(name)
     L = cr.layout
