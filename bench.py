@@ -4,7 +4,11 @@ Workload: the C2 crystal (Fm-3m, 3x3x3 k mesh = 27 k / 4 irreducible,
 nao=26, naux=120, nts=100, beta=100, ns=1, V stored for all 729 k pairs),
 synthetic seeded data (see mbsymmetry_gb300/crystal.py).  One step = one GW
 iteration P0 -> P~ (W~ solve) -> Sigma -> Dyson with all tau <-> i omega
-transforms, FP64 (the drop-in path), replayed as one CUDA graph.
+transforms, replayed as one CUDA graph, with the P0 and Sigma contractions on
+the sliced split-precision path (BF16 fixed-point slices on tcgen05, Sigma
+within 1e-7 Ha of FP64: the error is measured and reported in the line); the
+FP64 drop-in, the FP32-class split paths, a C4 mixed-vs-FP64 block and the
+self-consistent loop are reported beside it.
 
   value  device time of the iteration (CUDA events recorded on the engine's
          stream), inputs resident in HBM, L2 flushed before every iteration.
@@ -40,7 +44,10 @@ WORKLOADS = {
             "on the Fm-3m 3x3x3 mesh (27 k)"),
 }
 WORKLOAD = WORKLOADS[CONFIG]
-METRIC = "s/GW iteration (FP64 drop-in, P0 -> W~ -> Sigma -> Dyson)"
+METRIC = "s/GW iteration + tensor TFLOP/s: mixed vs FP64 GPU at Sigma err<=1e-7 Ha; CPU ref"
+# dram__bytes_read.sum + dram__bytes_write.sum summed over one iteration's launches of
+# each sliced-path GEMM kernel on C2, from one ncu capture of `bench.py --profile`.
+OZ_TRAFFIC = {"oz_gemm_kernel": 8.629e9, "oz_simt_kernel": 21.484e9}
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -74,7 +81,7 @@ class ClockSampler:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -178,11 +185,165 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "precision": "fp64"},
+        "config": {"workload": WORKLOAD}, "precision": "fp64 (CPU restatement)",
         "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def _peaks(dev):
+    """Roofline denominators measured in this run (peaks/peaks.cu) and the driver's file."""
+    import ctypes
+    probe = ctypes.CDLL(os.path.join(ROOT, "peaks", "libgwgb_peaks.so"))
+    for fn in ("gwgb_probe_fp64_tflops", "gwgb_probe_dmma_tflops"):
+        getattr(probe, fn).restype = ctypes.c_double
+        getattr(probe, fn).argtypes = [ctypes.c_int]
+    probe.gwgb_probe_tc_tflops.restype = ctypes.c_double
+    probe.gwgb_probe_tc_tflops.argtypes = [ctypes.c_int, ctypes.c_int]
+    probe.gwgb_probe_fp32_tflops.restype = ctypes.c_double
+    probe.gwgb_probe_fp32_tflops.argtypes = [ctypes.c_int]
+    pk = _load_peaks()
+    return {"hbm_gbs": pk.get("hbm_gbs"), "bf16_tflops_cublas": pk.get("bf16_tflops"),
+            "fp64_fma_tflops": probe.gwgb_probe_fp64_tflops(dev), "fp64_dmma_tflops": probe.gwgb_probe_dmma_tflops(dev),
+            "fp32_fma_tflops": probe.gwgb_probe_fp32_tflops(dev),
+            "tcgen05_tf32_tflops": probe.gwgb_probe_tc_tflops(dev, 0),
+            "tcgen05_bf16_tflops": probe.gwgb_probe_tc_tflops(dev, 1)}
+
+
+STAGE_KEYS = ("rotate_G_ms", "p0_ms", "pq_ms", "sigma_ms", "dyson_ms", "transform_ms", "solve_ms")
+PREC_LABEL = {
+    "ozaki": ("bf16 x4 fixed-point slices per operand row (Ozaki scheme) on tcgen05 kind::f16, 10 products, "
+              "exact FP32 partial sums, float-float accumulation and intermediates; FP64 W~ solve, Dyson, "
+              "transforms, mu search, energies"),
+    "fp64": "complex128 contractions on CUDA cores (the drop-in)",
+    "tf32x3": ("tf32x3 (tcgen05 kind::tf32, 2 planes, 3 products, FP32 accumulate within an aux block or "
+               "aux-row chunk, FP64 across): FP32-class error, no 1e-7 claim"),
+    "bf16x3": ("bf16x3 (tcgen05 kind::f16, 3 BF16 planes, 6 products, FP32 accumulate within an aux block or "
+               "aux-row chunk, FP64 across): FP32-class error, no 1e-7 claim"),
+}
+
+
+def _timed(s, G0, mu, prec, steps, warmup, flush, sync):
+    """Device time of `steps` graph-launched iterations from G0 (L2 flushed before each)."""
+    s.single_prec_run(prec != "fp64", prec)
+    for _ in range(warmup):
+        s.set_G(G0)
+        s.iteration(mu)
+    times, stg = [], {}
+    for _ in range(steps):
+        s.set_G(G0)
+        flush.zero_()
+        sync()
+        s.iteration(mu)
+        st = s.stats()
+        times.append(st["total_ms"])
+        for k in STAGE_KEYS:
+            stg[k] = stg.get(k, 0.0) + st[k] / steps
+    return float(np.mean(times)), stg, st
+
+
+def _launch_profile(s, G0, mu, steps):
+    """Per-launch CUDA-event times of the sliced path (gwgb_set_launch_timing)
+    over `steps` iterations from G0, summed per kernel and per stage (per
+    iteration).  A separate pass after the headline timing: the events add a
+    few microseconds per launch."""
+    s.launch_timing(True)
+    s.set_G(G0)
+    s.iteration(mu)  # captures the graph with the event records
+    kern, stage = {}, {}
+    for _ in range(steps):
+        s.set_G(G0)
+        s.iteration(mu)
+        for x in s.launch_stats():
+            if not x["ran"]:
+                continue
+            k = kern.setdefault(x["kernel"], {"ms": 0.0, "flops": 0.0, "mma_flops": 0.0, "bytes": 0.0, "launches": 0})
+            g = stage.setdefault(x["stage"], {"ms": 0.0, "flops": 0.0})
+            for d in (k, g):
+                d["ms"] += x["ms"] / steps
+                d["flops"] += x["flops"] / steps
+            k["mma_flops"] += x["mma_flops"] / steps
+            k["bytes"] += x["bytes"] / steps
+            k["launches"] += 1
+    s.launch_timing(False)
+    for k in kern.values():
+        k["launches"] //= steps
+    return kern, stage
+
+
+def _kernel_roofline(kern, peaks, traffic):
+    """Roofline of the sliced path's dominant kernel (largest summed launch time)."""
+    name = max(kern, key=lambda n: kern[n]["ms"])
+    k = kern[name]
+    t = k["ms"] * 1e-3
+    if name == "oz_gemm_kernel":
+        peak = peaks["tcgen05_bf16_tflops"]
+        alg = k["flops"] / t / 1e12
+        exe = k["mma_flops"] / t / 1e12
+        return {"bound": "tensor", "kernel": name, "achieved": alg, "peak": peak, "unit": "TFLOP/s",
+                "frac": alg / peak, "executed_tflops": exe, "frac_executed": exe / peak,
+                "peak_source": "tcgen05 kind::f16 (BF16) rate measured in this run (peaks/peaks.cu), of measured",
+                "achieved_note": "algorithmic complex FLOPs (8 M N K per block GEMM) of its launches / their summed "
+                                 "CUDA-event time; executed = BF16 MMA FLOPs issued (10 slice products, real "
+                                 "embedding, 128-row tiles, N and K padded to the MMA shape)",
+                "launches_per_step": k["launches"], "ms_per_step": k["ms"], "traffic": traffic.get(name),
+                "traffic_unit": "bytes per step, all launches of the kernel (ncu)"}
+    if name == "oz_simt_kernel":
+        peak = peaks["fp32_fma_tflops"]
+        alg = k["flops"] / t / 1e12
+        ins = k["mma_flops"] / t / 1e12  # FP32 instructions (48 per complex MAC) per second, in T/s
+        return {"bound": "fp32 (CUDA-core float-float)", "kernel": name, "achieved": alg, "peak": peak,
+                "unit": "TFLOP/s", "frac": alg / peak, "fp32_instr_per_s_T": ins,
+                "frac_fp32_issue": 2.0 * ins / peak,
+                "peak_source": "FP32 FMA rate measured in this run (peaks/peaks.cu, 2 flops per FMA), of measured",
+                "achieved_note": "algorithmic complex FLOPs / summed launch time; each complex MAC costs 48 FP32 "
+                                 "instructions in float-float, so frac_fp32_issue = instructions / FMA issue rate",
+                "launches_per_step": k["launches"], "ms_per_step": k["ms"], "traffic": traffic.get(name),
+                "traffic_unit": "bytes per step, all launches of the kernel (ncu)"}
+    gbs = k["bytes"] / t / 1e9
+    return {"bound": "hbm", "kernel": name, "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None, "traffic": traffic.get(name)}
+
+
+def _c4_block(dev, warmup):
+    """Mixed vs FP64 on the uneven-block crystal C4 (P6_3mc-like hexagonal 4x4x3,
+    nao=72, naux=350, nts=120, beta=200; blocks 2-30): one timed iteration each
+    after warm-up, Sigma and G error of the sliced path against FP64."""
+    from mbsymmetry_gb300.crystal import CONFIGS, load_ir, make_crystal
+    from mbsymmetry_gb300.solver import GWSolver
+    from mbsymmetry_gb300.transformer import build_transforms
+    spec = CONFIGS["C4"]
+    cr = make_crystal(spec)
+    tr = build_transforms(load_ir(spec.nts), spec.beta)
+    s = GWSolver(cr.layout, cr.ns, tr, device=dev)
+    s.set_shared_Coulomb(cr.V)
+    s.set_fock(cr.F, cr.S)
+    s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
+    s.dyson(cr.mu)
+    G0 = s.G_tau()
+    out, res = {"workload": "C4: hexagonal 4x4x3 k mesh (48 k, 8 irreducible), nao=72, naux=350, nts=120, "
+                            "beta=200, irrep blocks 2-30, V for all k pairs"}, {}
+    for prec in ("fp64", "ozaki"):
+        s.single_prec_run(prec != "fp64", prec)
+        for _ in range(1 + (prec != "fp64") * max(0, min(warmup, 1))):
+            s.set_G(G0)
+            s.iteration(cr.mu)
+        st = s.stats()
+        res[prec] = (s.Selfenergy(), s.G_tau())
+        out[prec] = {"s_per_iteration": st["total_ms"] / 1e3, "p0_s": st["p0_ms"] / 1e3,
+                     "sigma_s": st["sigma_ms"] / 1e3,
+                     "contraction_tflops_alg": {k: st[f"{k}_flops"] / (st[f"{k}_ms"] * 1e-3) / 1e12
+                                                for k in ("p0", "sigma")}}
+    kern, stage = _launch_profile(s, G0, cr.mu, 1)
+    out["ozaki"]["kernels"] = kern
+    out["ozaki"]["stages_ms"] = {k: v["ms"] for k, v in stage.items()}
+    s.close()
+    out["speedup"] = out["fp64"]["s_per_iteration"] / out["ozaki"]["s_per_iteration"]
+    out["sigma_max_abs_err"] = float(np.abs(res["ozaki"][0] - res["fp64"][0]).max())
+    out["G_max_abs_err"] = float(np.abs(res["ozaki"][1] - res["fp64"][1]).max())
+    out["sigma_max_abs"] = float(np.abs(res["fp64"][0]).max())
+    return out
 
 
 def run_gpu(args):
@@ -205,32 +366,27 @@ def run_gpu(args):
     s.dyson(cr.mu)                          # G0: the input of every timed iteration
     G0 = s.G_tau()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    sync = torch.cuda.synchronize
 
-    barrier = reps.barrier
+    clocks = ClockSampler(dev)
+    with clocks:  # clocks sampled over both timed regions (FP64, then the headline)
+        # ---- FP64 drop-in (the accuracy reference of the split paths) -------
+        ms64, st64, s64 = _timed(s, G0, cr.mu, "fp64", args.steps, args.warmup, flush, sync)
+        sig64, g64 = s.Selfenergy(), s.G_tau()
 
-    for _ in range(args.warmup):
-        s.set_G(G0)
-        s.iteration(cr.mu)
-    stage_tot = {}
-    times = []
-    with ClockSampler(dev) as clocks:
-        barrier()
-        for _ in range(args.steps):
-            s.set_G(G0)                     # same input each step (not timed)
-            flush.zero_()                   # L2 flush between timed iterations
-            torch.cuda.synchronize()
-            s.iteration(cr.mu)              # events inside the engine's graph
-            st = s.stats()
-            times.append(st["total_ms"])
-            for k in ("rotate_G_ms", "p0_ms", "pq_ms", "rotate_P_ms", "sigma_ms", "dyson_ms", "transform_ms",
-                      "solve_ms"):
-                stage_tot[k] = stage_tot.get(k, 0.0) + st[k]
-        barrier()
+        # ---- headline: the sliced split-precision path -----------------------
+        s.single_prec_run(True, "ozaki")
+        for _ in range(args.warmup):
+            s.set_G(G0)
+            s.iteration(cr.mu)
+        reps.barrier()
+        ms, stages, st = _timed(s, G0, cr.mu, "ozaki", args.steps, 0, flush, sync)
+        reps.barrier()
     launches = int(st["kernel_launches"]) * args.steps
-    ms = reps.max_over_ranks(float(np.mean(times)))
-    stages = {k: v / args.steps for k, v in stage_tot.items()}
+    ms = reps.max_over_ranks(ms)
+    sig_oz, g_oz = s.Selfenergy(), s.G_tau()
 
-    # ---- e2e through the C ABI with pinned host buffers ------------------
+    # ---- e2e through the C ABI with pinned host buffers (sliced path) -------
     g_host = torch.from_numpy(G0.view(np.float64)).pin_memory()
     sig_host = torch.empty(2 * s.g_size, dtype=torch.float64).pin_memory()
     g_out = torch.empty(2 * s.g_size, dtype=torch.float64).pin_memory()
@@ -241,91 +397,61 @@ def run_gpu(args):
         _abi.check(lib.gwgb_set_G(h, vp(g_host.data_ptr())))
         _abi.check(lib.gwgb_iteration(h, cr.mu))
     e2e = []
-    barrier()
+    reps.barrier()
     for _ in range(args.steps):
         flush.zero_()
-        torch.cuda.synchronize()
+        sync()
         t0 = time.perf_counter()
         _abi.check(lib.gwgb_set_G(h, vp(g_host.data_ptr())))
         _abi.check(lib.gwgb_iteration(h, cr.mu))
         _abi.check(lib.gwgb_get_sigma(h, vp(sig_host.data_ptr())))
         _abi.check(lib.gwgb_get_G(h, vp(g_out.data_ptr())))
         e2e.append(time.perf_counter() - t0)
-    barrier()
+    reps.barrier()
     e2e_s = reps.max_over_ranks(float(np.mean(e2e)))
     gbytes = s.g_size * 16
 
-    # ---- roofline of the dominant kernel ---------------------------------
-    peaks = _load_peaks()
-    probe = ctypes.CDLL(os.path.join(ROOT, "peaks", "libgwgb_peaks.so"))
-    for fn in ("gwgb_probe_fp64_tflops", "gwgb_probe_dmma_tflops"):
-        getattr(probe, fn).restype = ctypes.c_double
-        getattr(probe, fn).argtypes = [ctypes.c_int]
-    probe.gwgb_probe_tc_tflops.restype = ctypes.c_double
-    probe.gwgb_probe_tc_tflops.argtypes = [ctypes.c_int, ctypes.c_int]
-    fp64_peak = probe.gwgb_probe_fp64_tflops(dev)
-    dmma_peak = probe.gwgb_probe_dmma_tflops(dev)
-    tf32_peak = probe.gwgb_probe_tc_tflops(dev, 0)
-    bf16_tc_peak = probe.gwgb_probe_tc_tflops(dev, 1)
-    dom = "sigma" if stages["sigma_ms"] >= stages["p0_ms"] else "p0"
-    flops = st[f"{dom}_flops"]
-    dom_ms = stages[f"{dom}_ms"]
-    achieved = flops / (dom_ms * 1e-3) / 1e12
-    # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the same
-    # kernel on this workload from one ncu capture; the kernels are FP64-pipe bound.
-    traffic = {"sigma": 0.0703e9, "p0": 0.0563e9}[dom]
-    roofline = {"bound": "tensor", "kernel": f"{dom}_fp64_kernel", "achieved": achieved, "peak": fp64_peak,
-                "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": traffic,
-                "traffic_unit": "bytes per launch (ncu)",
-                "peak_source": "FP64 FMA microbenchmark measured in this run (MEASURED_PEAKS.json has no FP64 "
-                               "figure); contraction FLOPs = 8MNK per complex GEMM of the block layout",
-                "flop_alg_per_launch": flops, "kernel_ms": dom_ms}
+    # ---- rooflines ------------------------------------------------------------
+    peaks = _peaks(dev)
+    fp64_peak = peaks["fp64_fma_tflops"]
+    kern, lstages = _launch_profile(s, G0, cr.mu, args.steps)
+    roofline = _kernel_roofline(kern, peaks, OZ_TRAFFIC)
+    roofline["kernels"] = kern
+    roofline["stages_ms"] = {k: v["ms"] for k, v in lstages.items()}
+    dom64 = "sigma" if st64["sigma_ms"] >= st64["p0_ms"] else "p0"
+    a64 = s64[f"{dom64}_flops"] / (st64[f"{dom64}_ms"] * 1e-3) / 1e12
+    fp64 = {"precision": PREC_LABEL["fp64"], "s_per_iteration": ms64 / 1e3, "stages_ms": st64,
+            "contraction_tflops": {k: s64[f"{k}_flops"] / (st64[f"{k}_ms"] * 1e-3) / 1e12 for k in ("p0", "sigma")},
+            "roofline": {"bound": "fp64 (CUDA-core FMA)", "kernel": f"{dom64}_fp64_kernel", "achieved": a64,
+                         "peak": fp64_peak, "unit": "TFLOP/s", "frac": a64 / fp64_peak if fp64_peak > 0 else None,
+                         "traffic": {"sigma": 0.0703e9, "p0": 0.0563e9}[dom64],
+                         "traffic_unit": "bytes per launch (ncu)",
+                         "note": "FP64 FMA on CUDA cores: the FP64 tensor path (DMMA) measures slower on this "
+                                 "GPU (peaks.fp64_dmma_tflops)"},
+            "transforms": {"ms": st64["transform_ms"], "bytes_alg": s64["transform_bytes"],
+                           "achieved_gbs": s64["transform_bytes"] / (st64["transform_ms"] * 1e-3) / 1e9,
+                           "flops_alg": s64["transform_flops"],
+                           "frac_fp64": s64["transform_flops"] / (st64["transform_ms"] * 1e-3) / 1e12 / fp64_peak
+                                        if fp64_peak > 0 else None},
+            "solves": {"ms": st64["solve_ms"], "gflops": s64["solve_flops"] / (st64["solve_ms"] * 1e-3) / 1e9}}
 
-    # ---- split tensor-core precisions on the same input ---------------------
-    sig64 = s.Selfenergy()
-    g64 = s.G_tau()
+    # ---- FP32-class split precisions on the same input ----------------------
+    def run_split(kind):
+        m, stg, stk = _timed(s, G0, cr.mu, kind, args.steps, args.warmup, flush, sync)
+        return {"precision": PREC_LABEL[kind], "s_per_iteration": m / 1e3, "speedup_vs_fp64": ms64 / m,
+                "sigma_max_abs_err_vs_fp64": float(np.abs(s.Selfenergy() - sig64).max()),
+                "G_max_abs_err_vs_fp64": float(np.abs(s.G_tau() - g64).max()), "stages_ms": stg}
 
-    def run_mixed(kind, label):
-        s.single_prec_run(True, kind)
-        for _ in range(args.warmup):
-            s.set_G(G0)
-            s.iteration(cr.mu)
-        mtimes, mstage = [], {}
-        for _ in range(args.steps):
-            s.set_G(G0)
-            flush.zero_()
-            torch.cuda.synchronize()
-            s.iteration(cr.mu)
-            stm = s.stats()
-            mtimes.append(stm["total_ms"])
-            for k in ("p0_ms", "sigma_ms", "pq_ms", "rotate_P_ms", "dyson_ms"):
-                mstage[k] = mstage.get(k, 0.0) + stm[k] / args.steps
-        sig32 = s.Selfenergy()
-        g32 = s.G_tau()
-        s.single_prec_run(False)
-        return {"precision": label,
-                "s_per_iteration": float(np.mean(mtimes)) / 1e3,
-                "speedup_vs_fp64": ms / float(np.mean(mtimes)),
-                "sigma_max_abs_err_vs_fp64": float(np.abs(sig32 - sig64).max()),
-                "sigma_max_abs": float(np.abs(sig64).max()),
-                "G_max_abs_err_vs_fp64": float(np.abs(g32 - g64).max()),
-                "stages_ms": mstage,
-                "contraction_tflops_alg": {"p0": stm["p0_flops"] / (mstage["p0_ms"] * 1e-3) / 1e12,
-                                           "sigma": stm["sigma_flops"] / (mstage["sigma_ms"] * 1e-3) / 1e12}}
+    split_tf32 = run_split("tf32x3")
+    split_bf16 = run_split("bf16x3")
+    s.single_prec_run(False)
 
-    mixed = run_mixed("tf32x3", "tf32x3 (tcgen05 kind::tf32, 2 planes, 3 products, FP32 accumulate within an aux "
-                                "block or aux-row chunk, FP64 across)")
-    mixed_bf16 = run_mixed("bf16x3", "bf16x3 (tcgen05 kind::f16, 3 BF16 planes, 6 products, FP32 accumulate within "
-                                     "an aux block or aux-row chunk, FP64 across)")
-
-    # ---- tile-shape autotuner (mbsymmetry_gb300/autotune.py) on this workload ---
+    # ---- autotuner (mbsymmetry_gb300/autotune.py): the sliced path's width-class
+    # boundary between tcgen05 and the CUDA-core kernel, on this workload
     from mbsymmetry_gb300 import autotune as _autotune
-    tune = _autotune.autotune(L, cr.ns, tr, cr.V, cr.F, cr.S, cr.mu, G=G0, precision="tf32x3", reps=2)
+    tune = _autotune.autotune(L, cr.ns, tr, cr.V, cr.F, cr.S, cr.mu, G=G0, precision="ozaki", reps=2)
 
     # ---- the reference's cuBLAS call sequence on this GPU (measurement only) --
-    # G rotation + per-pair strided-batched ZGEMM chains of P0 and Sigma, 16
-    # streams, 4 tau per batch (the reference's nqkpt streams and test nt_batch);
-    # P0 from G0, Sigma from G0 and the FP64 P~ of the same solve.
     s.set_G(G0)
     s.solve()
     s.refproxy(nt_batch=4, nstreams=16)  # warm-up: cuBLAS handle and kernel loading
@@ -338,70 +464,64 @@ def run_gpu(args):
              "nt_batch": 4, "streams": 16, "p0_s": px["p0_ms"] / 1e3, "sigma_s": px["sigma_ms"] / 1e3,
              "contractions_s": px_s, "gemm_calls": int(px["gemm_calls"]), "other_calls": int(px["other_calls"]),
              "sigma_max_abs_diff_vs_fp64_kernels": float(np.abs(sig_px - sig64).max()),
-             "speedup_fp64_kernels": px_s / ((stages["p0_ms"] + stages["sigma_ms"]) / 1e3),
-             "speedup_tf32x3_kernels": px_s / ((mixed["stages_ms"]["p0_ms"] + mixed["stages_ms"]["sigma_ms"]) / 1e3)}
+             "speedup_fp64_kernels": px_s / ((st64["p0_ms"] + st64["sigma_ms"]) / 1e3),
+             "speedup_sliced_kernels": px_s / ((stages["p0_ms"] + stages["sigma_ms"]) / 1e3)}
 
     # ---- self-consistent loop: 10 graph-launched iterations, alpha = 0.5 ----
     # Each iteration: GW Sigma, linear mixing, device-side mu search (half
-    # filling, N = nao), Dyson, energies.  FP64 throughout, and TF32x3 with the
-    # last iteration in FP64; the final Sigma / energy of the two are compared.
+    # filling, N = nao), Dyson, energies.  FP64 and the sliced path; per
+    # iteration mu and E_corr and the final Sigma are compared.
     zeros = np.zeros(s.g_size, np.complex128)
     sc = {"iterations": 10, "alpha": 0.5, "n_electrons": float(L.nao),
           "note": "graph launches back to back (no L2 flush between iterations)"}
     finals = {}
-    for label, prec, final in (("fp64", "fp64", False), ("tf32x3_final_fp64", "tf32x3", True)):
-        s.single_prec_run(prec != "fp64", "tf32x3")
+    for prec in ("fp64", "ozaki"):
+        s.single_prec_run(prec != "fp64", prec)
         s.set_G(G0)
         s.set_Selfenergy(zeros)
-        recs = s.sc_loop(10, 0.5, float(L.nao), cr.mu, step=0.05, tol=1e-10, max_evals=24, final_fp64=final)
+        recs = s.sc_loop(10, 0.5, float(L.nao), cr.mu, step=0.05, tol=1e-10, max_evals=24)
         stl = s.stats()
-        finals[label] = (s.Selfenergy(), recs[-1])
-        sc[label] = {"s_per_iteration": stl["total_ms"] / 1e3, "mu": [r["mu"] for r in recs],
-                     "e_corr": [r["e_corr"] for r in recs], "mu_evals": [r["mu_evals"] for r in recs],
-                     "n_final": recs[-1]["n_electrons"], "leakage_final": recs[-1]["leakage"]}
+        finals[prec] = (s.Selfenergy(), recs)
+        sc[prec] = {"s_per_iteration": stl["total_ms"] / 1e3, "mu": [r["mu"] for r in recs],
+                    "e_corr": [r["e_corr"] for r in recs], "mu_evals": [r["mu_evals"] for r in recs],
+                    "n_final": recs[-1]["n_electrons"], "leakage_final": recs[-1]["leakage"]}
     s.single_prec_run(False)
-    sc["final_sigma_max_abs_diff"] = float(np.abs(finals["fp64"][0] - finals["tf32x3_final_fp64"][0]).max())
-    sc["final_e_corr_diff"] = abs(finals["fp64"][1]["e_corr"] - finals["tf32x3_final_fp64"][1]["e_corr"])
-    sc["speedup"] = sc["fp64"]["s_per_iteration"] / sc["tf32x3_final_fp64"]["s_per_iteration"]
+    sc["per_iteration_e_corr_abs_diff"] = [abs(a["e_corr"] - b["e_corr"])
+                                           for a, b in zip(finals["fp64"][1], finals["ozaki"][1])]
+    sc["per_iteration_mu_abs_diff"] = [abs(a["mu"] - b["mu"]) for a, b in zip(finals["fp64"][1], finals["ozaki"][1])]
+    sc["final_sigma_max_abs_diff"] = float(np.abs(finals["fp64"][0] - finals["ozaki"][0]).max())
+    sc["speedup"] = sc["fp64"]["s_per_iteration"] / sc["ozaki"]["s_per_iteration"]
+    s.close()
+    c4 = None if args.no_c4 or world > 1 else _c4_block(dev, args.warmup)
 
     line = {
         "metric": METRIC, "value": reps.seconds_per_iteration(ms), "unit": "s", "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "precision": "fp64", "l2": "flushed (256 MiB write) before each step",
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x4 slices (c128 in/out, fp64 solves)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD},
+        "precision": "ozaki: " + PREC_LABEL["ozaki"], "l2": "flushed (256 MiB write) before each step",
+        "parallelism": "replicas" if world > 1 else "1 GPU",
+        "sigma_max_abs_err_vs_fp64": float(np.abs(sig_oz - sig64).max()),
+        "G_max_abs_err_vs_fp64": float(np.abs(g_oz - g64).max()),
+        "sigma_max_abs": float(np.abs(sig64).max()),
+        "speedup_vs_fp64": ms64 / ms,
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": gbytes, "d2h_bytes_per_step": 2 * gbytes},
         "gpu_launches": launches,
         "stages_ms": stages,
-        "contraction_tflops": {"p0": st["p0_flops"] / (stages["p0_ms"] * 1e-3) / 1e12,
-                               "sigma": st["sigma_flops"] / (stages["sigma_ms"] * 1e-3) / 1e12},
+        "contraction_tflops_alg": {k: st[f"{k}_flops"] / (stages[f"{k}_ms"] * 1e-3) / 1e12 for k in ("p0", "sigma")},
         "roofline": roofline,
-        # the four tau <-> omega transforms of an iteration (HBM-bound) and the block solves
-        # (FP64 latency-bound, no roofline claim), from events inside the iteration's graph
-        # (bound: FP64 FMA, about 25 flop per byte at n ~ 100; the HBM figure is given too)
-        "transforms": {"ms": stages["transform_ms"], "bytes_alg": st["transform_bytes"],
-                       "achieved_gbs": st["transform_bytes"] / (stages["transform_ms"] * 1e-3) / 1e9,
-                       "peak_gbs": peaks.get("hbm_gbs"),
-                       "frac_hbm": (st["transform_bytes"] / (stages["transform_ms"] * 1e-3) / 1e9 / peaks["hbm_gbs"])
-                                   if peaks.get("hbm_gbs") else None,
-                       "flops_alg": st["transform_flops"], "bound": "fp64",
-                       "achieved_tflops": st["transform_flops"] / (stages["transform_ms"] * 1e-3) / 1e12,
-                       "frac_fp64": st["transform_flops"] / (stages["transform_ms"] * 1e-3) / 1e12 / fp64_peak
-                                    if fp64_peak > 0 else None},
-        "solves": {"ms": stages["solve_ms"], "flops": st["solve_flops"],
-                   "gflops": st["solve_flops"] / (stages["solve_ms"] * 1e-3) / 1e9},
         "clocks": clocks.summary(),
-        "mixed": mixed,
-        "mixed_bf16x3": mixed_bf16,
+        "fp64": fp64,
+        "split_tf32x3": split_tf32,
+        "split_bf16x3": split_bf16,
+        "c4_mixed_vs_fp64": c4,
         "reference_gpu_proxy": proxy,
-        "autotune": {"best": tune["best"], "default": _autotune.DEFAULT_CANDIDATES[0],
-                     "trials": tune["trials"]},
+        "autotune": {"precision": "ozaki", "metric": tune["metric"], "best": tune["best"],
+                     "default": _autotune.OZAKI_CANDIDATES[0], "trials": tune["trials"]},
         "sc_loop": sc,
-        "peaks": {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops"),
-                  "fp64_tflops_measured": fp64_peak},
+        "peaks": peaks,
     }
-    s.close()
     if reps.reports and world == 1 and not args.no_cpu_baseline:  # rank 0 at N = 1 only
         ref = _cpu_reference(cr, tr, 1, with_numpy=True)
         line["cpu_baseline"] = {"value": ref["value"], "unit": "s", "cores": ref["cores"], "kind": "port",
@@ -413,9 +533,10 @@ def run_gpu(args):
 
 
 def run_profile(args):
-    """One FP64 and one TF32x3 iteration of the workload, then (C2) two FP64
-    self-consistent iterations: the command that ncu captures (a plain run of
-    it must exit 0 first)."""
+    """One FP64 and one sliced-path iteration of the workload (each after one
+    warm-up iteration): the command that ncu captures (a plain run of it must
+    exit 0 first).  The sliced path's six oz_gemm_kernel launches of the second
+    iteration are the stages Z1, Z, P0, W, U, Sigma in that order."""
     import torch
     from mbsymmetry_gb300.solver import GWSolver
     torch.cuda.set_device(0)
@@ -426,19 +547,15 @@ def run_profile(args):
     s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
     s.dyson(cr.mu)
     G0 = s.G_tau()
-    s.iteration(cr.mu)
-    s.single_prec_run(True, "tf32x3")
     s.set_G(G0)
     s.iteration(cr.mu)
-    st = s.stats()
-    if CONFIG == "C2":  # the SC loop only on the benchmark workload
-        s.single_prec_run(False)
+    s.single_prec_run(True, "ozaki")
+    for _ in range(2):
         s.set_G(G0)
-        s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
-        s.sc_loop(2, 0.5, float(cr.layout.nao), cr.mu, step=0.05, tol=1e-10, max_evals=24)
+        s.iteration(cr.mu)
+    st = s.stats()
     s.close()
-    print(f"profile run: {CONFIG}, one FP64 and one TF32x3 iteration (last {st['total_ms']:.2f} ms), "
-          "then two FP64 self-consistent iterations")
+    print(f"profile run: {CONFIG}, one FP64 and two sliced-path iterations (last {st['total_ms']:.2f} ms)")
 
 
 def main():
@@ -448,11 +565,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c4", action="store_true", help="skip the C4 mixed-vs-FP64 block")
     ap.add_argument("--config", default="C2", choices=sorted(WORKLOADS),
                     help="workload (C2 is the benchmark; C3 is for profiling and manual runs)")
     ap.add_argument("--profile", action="store_true",
-                    help="one FP64 and one TF32x3 iteration and two self-consistent iterations only "
-                         "(the command for ncu captures)")
+                    help="one FP64 and two sliced-path iterations only (the command for ncu captures)")
     args = ap.parse_args()
     global CONFIG, WORKLOAD
     CONFIG, WORKLOAD = args.config, WORKLOADS[args.config]

@@ -64,6 +64,17 @@ class GwgbStats(ctypes.Structure):
     ]
 
 
+class GwgbLaunchStat(ctypes.Structure):
+    _fields_ = [
+        ("stage", c_int32), ("kernel", c_int32), ("tasks", c_int32), ("ran", c_int32),
+        ("ms", c_double), ("flops", c_double), ("mma_flops", c_double), ("bytes", c_double),
+    ]
+
+
+LAUNCH_STAGES = ("Z1", "Z", "P0", "W", "U", "Sigma")
+LAUNCH_KERNELS = ("oz_gemm_kernel", "oz_simt_kernel", "reduce_slices_kernel")
+
+
 class GwgbProxyStats(ctypes.Structure):
     _fields_ = [("p0_ms", c_double), ("sigma_ms", c_double), ("gemm_calls", c_int64), ("other_calls", c_int64)]
 
@@ -109,6 +120,8 @@ SIGNATURES = {
     "gwgb_dyson": (c_int32, [c_void_p, c_double]),
     "gwgb_iteration": (c_int32, [c_void_p, c_double]),
     "gwgb_get_stats": (c_int32, [c_void_p, POINTER(GwgbStats)]),
+    "gwgb_set_launch_timing": (c_int32, [c_void_p, c_int32]),
+    "gwgb_get_launch_stats": (c_int32, [c_void_p, POINTER(GwgbLaunchStat), c_int32, POINTER(c_int32)]),
     "gwgb_synchronize": (c_int32, [c_void_p]),
     "gwgb_refproxy_run": (c_int32, [c_void_p, c_int32, c_int32, POINTER(GwgbProxyStats)]),
     "gwgb_refproxy_get": (c_int32, [c_void_p, c_void_p, c_void_p]),

@@ -463,7 +463,76 @@ class Engine {
     bool simt = false, part = false;
     int64_t r0 = 0, nr = 0;
     double scale = 1.0;
+    int stage = 0;            // gwgb_launch_stat.stage
+    double flops = 0, ops = 0, red_bytes = 0;
+    int red_ny = 1;           // CTAs per reduced block
   };
+  // per-launch profile (gwgb_set_launch_timing): records [0, n_p0) P0, then Sigma
+  bool lt_on_ = false, lt_ran_p0_ = false, lt_ran_sig_ = false;
+  std::vector<cudaEvent_t> lt_ev_;
+  std::vector<gwgb_launch_stat> lt_info_;
+  int lt_n_p0_ = 0;
+  void rec_ev(cudaEvent_t e) {
+    if (capturing_)
+      GWGB_CUDA(cudaEventRecordWithFlags(e, st_, cudaEventRecordExternal));
+    else
+      GWGB_CUDA(cudaEventRecord(e, st_));
+  }
+  void lt_build() {  // one entry per GEMM launch and per reduction, in launch order
+    lt_info_.clear();
+    for (int l = 0; l < 2; ++l) {
+      for (const OzLaunch &x : l ? oz_sig_ : oz_p0_) {
+        gwgb_launch_stat g{};
+        g.stage = x.stage;
+        g.kernel = x.simt ? 1 : 0;
+        g.tasks = (int32_t)x.n;
+        g.flops = x.flops;
+        g.mma_flops = x.ops;
+        lt_info_.push_back(g);
+        if (x.nr) {
+          gwgb_launch_stat r{};
+          r.stage = x.stage;
+          r.kernel = 2;
+          r.tasks = (int32_t)x.nr;
+          r.bytes = x.red_bytes;
+          lt_info_.push_back(r);
+        }
+      }
+      if (l == 0) lt_n_p0_ = (int)lt_info_.size();
+    }
+  }
+  void lt_free() {
+    for (cudaEvent_t e : lt_ev_) cudaEventDestroy(e);
+    lt_ev_.clear();
+  }
+
+ public:
+  void set_launch_timing(int on) {
+    GWGB_REQUIRE(on == 0 || on == 1, GWGB_E_INVALID, "launch timing must be 0 or 1");
+    if ((on != 0) == lt_on_) return;
+    drop_graphs();  // the captured graph holds (or lacks) the event records
+    lt_on_ = on != 0;
+    lt_ran_p0_ = lt_ran_sig_ = false;
+  }
+  void launch_stats(gwgb_launch_stat *out, int max, int *n) {
+    GWGB_REQUIRE(n && (out || max == 0) && max >= 0, GWGB_E_INVALID, "bad launch-stats arguments");
+    *n = (int)lt_info_.size();
+    GWGB_CUDA(cudaStreamSynchronize(st_));
+    for (int i = 0; i < std::min(max, (int)lt_info_.size()); ++i) {
+      gwgb_launch_stat g = lt_info_[i];
+      const bool ran = lt_on_ && (i < lt_n_p0_ ? lt_ran_p0_ : lt_ran_sig_) && (int)lt_ev_.size() > 2 * i + 1;
+      g.ran = ran ? 1 : 0;
+      g.ms = 0;
+      if (ran) {
+        float ms = 0;
+        GWGB_CUDA(cudaEventElapsedTime(&ms, lt_ev_[2 * i], lt_ev_[2 * i + 1]));
+        g.ms = ms;
+      }
+      out[i] = g;
+    }
+  }
+
+ private:
   int oz_simt_n_ = 8;  // block GEMMs with at most this many output columns run on the CUDA cores
   bool oz_built_ = false, oz_ready_ = false;
   DBuf<OzDesc> oz_descs_;
@@ -497,17 +566,31 @@ class Engine {
       default: return Sig_.p;
     }
   }
-  void oz_run(const std::vector<OzLaunch> &ls) {
+  // rec: first profile record of this list (P0: 0, Sigma: lt_n_p0_)
+  void oz_run(const std::vector<OzLaunch> &ls, int rec) {
+    if (lt_on_ && lt_ev_.size() < 2 * lt_info_.size()) {
+      const size_t n0 = lt_ev_.size();
+      lt_ev_.resize(2 * lt_info_.size());
+      for (size_t i = n0; i < lt_ev_.size(); ++i) GWGB_CUDA(cudaEventCreate(&lt_ev_[i]));
+    }
     for (const OzLaunch &x : ls) {
       void *c = x.part ? static_cast<void *>(ozPart_.p) : const_cast<void *>(oz_ptr(x.c));
       const float4 *a = static_cast<const float4 *>(oz_ptr(x.a)), *b = static_cast<const float4 *>(oz_ptr(x.b));
+      if (lt_on_) rec_ev(lt_ev_[2 * rec]);
       if (x.simt)
         launch_oz_simt(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, a, b, c, oz_rowtab_.p, st_);
       else
         launch_oz_gemm(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, a, b, c, oz_rowtab_.p, nsm_, bad_.p + 2, st_);
-      if (x.nr)
+      if (lt_on_) rec_ev(lt_ev_[2 * rec + 1]);
+      ++rec;
+      if (x.nr) {
+        if (lt_on_) rec_ev(lt_ev_[2 * rec]);
         launch_reduce_slices(oz_red_.p + x.r0, (int)x.nr, ozPart_.p,
-                             static_cast<double2 *>(const_cast<void *>(oz_ptr(x.c))), nts_, x.scale, 0, st_);
+                             static_cast<double2 *>(const_cast<void *>(oz_ptr(x.c))), nts_, x.scale, 0, st_,
+                             x.red_ny);
+        if (lt_on_) rec_ev(lt_ev_[2 * rec + 1]);
+        ++rec;
+      }
     }
   }
   struct P0Group { int64_t pout; int32_t pstride, qb, c0, c1; };
@@ -667,6 +750,7 @@ Engine::~Engine() {
   drop_graphs();
   for (auto &e : ev_) if (e) cudaEventDestroy(e);
   for (auto &e : sc_ev_) if (e) cudaEventDestroy(e);
+  lt_free();
   Wg_.free(); Gb_.free(); Sold_.free(); Hc_.free(); Me_.free(); Hm_.free();
   mus_.free(); recs_.free(); counter_.free(); tr_tasks_.free(); slab_e_.free();
   if (mu_host_) cudaFreeHost(mu_host_);
@@ -1534,6 +1618,7 @@ void Engine::build_oz_lists() {
   // narrow ones (at most oz_simt_n_ output columns) for the CUDA-core kernel,
   // each heaviest first; one launch per kind.  The last launch carries `last`.
   auto narrow = [&](const OzTask &t) { return narrow_d[t.desc] != 0; };
+  int cur_stage = 0;  // gwgb_launch_stat.stage of the launches being built
   auto stage = [&](std::vector<OzLaunch> &v, size_t t0, int a, int b, int c, bool part = false,
                    const OzLaunch *last = nullptr) {
     auto cost = [&](const OzTask &t) { return (int64_t)t.nrep * ds[t.desc].K; };
@@ -1549,12 +1634,28 @@ void Engine::build_oz_lists() {
       OzLaunch l{(int64_t)lo, (int64_t)(hi - lo), a, b, c};
       l.simt = k == 1;
       l.part = part;
+      l.stage = cur_stage;
+      for (size_t t = lo; t < hi; ++t) {  // algorithmic FLOPs; tcgen05 MMA FLOPs or FP32 instructions
+        const OzTask &tk = ts[t];
+        const OzDesc &d = ds[tk.desc];
+        const int Mt = std::min(OZ_M, d.M - (tk.mtnt >> 16) * OZ_M), Nt = std::min(OZ_NC, d.N - (tk.mtnt & 0xffff) * OZ_NC);
+        const double cmac = (double)Mt * Nt * d.K * tk.nrep;
+        l.flops += 8.0 * cmac;
+        if (l.simt) {
+          l.ops += 48.0 * cmac;
+        } else {
+          const int ksteps = (d.K / OZ_KR) * 2 + ((d.K % OZ_KR) + 7) / 8;  // MMA K steps of 8 complex
+          l.ops += 10.0 * 2.0 * OZ_M * (16.0 * ((Nt + 7) / 8)) * 16.0 * ksteps * tk.nrep;
+        }
+      }
       v.push_back(l);
     }
     if (last && v.size() > n0) {
       v.back().r0 = last->r0;
       v.back().nr = last->nr;
       v.back().scale = last->scale;
+      v.back().red_bytes = last->red_bytes;
+      v.back().red_ny = last->red_ny;
     }
   };
   // Final GEMMs (P0, Sigma) in K slices: each slice writes an FP64 partial block
@@ -1597,6 +1698,15 @@ void Engine::build_oz_lists() {
     red_info.r0 = (int64_t)r0;
     red_info.nr = (int64_t)(red.size() - r0);
     red_info.scale = scale;
+    int64_t maxn = 1;
+    for (size_t r = r0; r < red.size(); ++r) {  // partials read, output written
+      red_info.red_bytes += 16.0 * red[r].nt * red[r].elems * (red[r].nslice + 1);
+      maxn = std::max<int64_t>(maxn, (int64_t)red[r].nt * red[r].elems);
+    }
+    // enough CTAs for about four waves of 256-thread blocks, none with under 1024 elements
+    const int64_t nblk = std::max<int64_t>(1, (int64_t)(red.size() - r0));
+    const int64_t want = (4 * 8 * (int64_t)std::max(1, nsm_) + nblk - 1) / nblk;
+    red_info.red_ny = (int)std::max<int64_t>(1, std::min<int64_t>({want, (maxn + 1023) / 1024, 4096}));
     stage(v, t0, a, b, c, true, &red_info);
   };
   // Row-table checks: every entry (plus the row's K extent and reps) inside the buffer.
@@ -1716,6 +1826,7 @@ void Engine::build_oz_lists() {
       oz_check(d, 1, l.flat_V, gsz, z1_elems, "P0 stage Z1");
       add(d, 1, 1);
     }
+    cur_stage = 0;
     stage(oz_p0_, s0, OZB_VFF, OZB_GFF, OZB_Z1);
     s0 = ts.size();
     for (auto &kv : zp) {  // Zcat[tau][P][K = (c,s,m,p)] = sum_t G1(beta-tau)[t][p] Z1[tau][m][(c,P,t)]
@@ -1756,6 +1867,7 @@ void Engine::build_oz_lists() {
       oz_check(d, half, z1_elems, gsz, zcat_elems, "P0 stage Z");
       add(d, half, REPG);
     }
+    cur_stage = 1;
     stage(oz_p0_, s0, OZB_Z1, OZB_GFF, OZB_ZCAT);
     std::vector<Fin> fins;
     for (int gi = ch.first; gi < ch.second; ++gi) {  // P0[Q][P] = sum_K Zcat[(tau,P)][K] Vcat[Q][K]
@@ -1774,6 +1886,7 @@ void Engine::build_oz_lists() {
       oz_check(d, 1, zcat_elems, oz_vcat_elems_, (int64_t)1 << 62, "P0 stage P0");
       fins.push_back({d, g.pout, g.pstride, half, g.qb * g.qb});
     }
+    cur_stage = 2;
     final_stage(oz_p0_, fins, OZB_ZCAT, OZB_VCAT, OZB_P0, pref, zcat_elems, oz_vcat_elems_, psz, "P0 stage P0");
   }
 
@@ -1896,6 +2009,7 @@ void Engine::build_oz_lists() {
       for (int c : gcs[w.g]) gcols += sig_b1_[c] * sc[c].b2;
       add(d, 1, 1, gcols);
     }
+    cur_stage = 3;
     stage(oz_sig_, s0, OZB_PFF, OZB_BCAT, OZB_W);
     s0 = ts.size();
     // U packs: (G2 block, spin) -> [(owner, contribution)]
@@ -1944,6 +2058,7 @@ void Engine::build_oz_lists() {
       oz_check(d, nts, w_elems, gsz, u_elems, "Sigma stage U");
       add(d, nts, REPG);
     }
+    cur_stage = 4;
     stage(oz_sig_, s0, OZB_W, OZB_GFF, OZB_U);
     std::vector<Fin> fins;
     for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {  // Sigma[i][j] = sum_K U[(tau,j)][K] VcatS[i][K]
@@ -1964,6 +2079,7 @@ void Engine::build_oz_lists() {
       oz_check(d, 1, u_elems, oz_vcats_elems_, (int64_t)1 << 62, "Sigma stage Sigma");
       fins.push_back({d, o.out, o.ostride, nts, o.n * o.n});
     }
+    cur_stage = 5;
     final_stage(oz_sig_, fins, OZB_U, OZB_VCATS, OZB_SIG, -1.0 / l.nk, u_elems, oz_vcats_elems_, ssz,
                 "Sigma stage Sigma");
   }
@@ -1990,6 +2106,7 @@ void Engine::build_oz_lists() {
   oz_perm_b_.upload(pb, st_);
   oz_perm_s_.upload(psg, st_);
   GWGB_CUDA(cudaStreamSynchronize(st_));
+  lt_build();
   oz_built_ = true;
 }
 
@@ -2093,7 +2210,8 @@ void Engine::k_p0(int mirror) {
     GWGB_REQUIRE(oz_ready_, GWGB_E_STATE, "sliced-precision operands not prepared");
     launch_to_ffc(Gall_.p, Gff_.p, (int64_t)Gall_.n, st_);
     GWGB_CUDA(cudaMemsetAsync(Pall_.p, 0, Pall_.n * sizeof(double2), st_));  // blocks without contributions
-    oz_run(oz_p0_);
+    oz_run(oz_p0_, 0);
+    lt_ran_p0_ = lt_on_;
     if (mirror) launch_mirror(Pall_.p, qoff_irr_.p, qsz_irr_.p, l_.ink, nts_, st_);
   } else if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE((Zbuf_.p || !zbuf_elems_) && vcat_ready_, GWGB_E_STATE, "mixed-precision operands not prepared");
@@ -2126,7 +2244,8 @@ void Engine::k_sigma() {
     launch_to_ffc(Gall_.p, Gff_.p, (int64_t)Gall_.n, st_);
     launch_to_ffc(Pall_.p, Pff_.p, (int64_t)Pall_.n, st_);
     GWGB_CUDA(cudaMemsetAsync(Sig_.p, 0, Sig_.n * sizeof(double2), st_));  // blocks without contributions
-    oz_run(oz_sig_);
+    oz_run(oz_sig_, lt_n_p0_);
+    lt_ran_sig_ = lt_on_;
   } else if (prec_ != GWGB_PREC_FP64) {  // tcgen05 split contractions
     GWGB_REQUIRE(Wbuf_.p || !wbuf_elems_, GWGB_E_STATE, "mixed-precision work buffer missing");
     for (const SigChunk &ch : sig_chunks_) {
@@ -2696,6 +2815,9 @@ GWGB_FORWARD(gwgb_dyson, (gwgb_handle h, double mu), e.dyson(mu))
 GWGB_FORWARD(gwgb_iteration, (gwgb_handle h, double mu), e.iteration(mu))
 GWGB_FORWARD(gwgb_get_stats, (gwgb_handle h, gwgb_stats *out), GWGB_REQUIRE(out, GWGB_E_INVALID, "NULL stats"); e.stats(out))
 GWGB_FORWARD(gwgb_synchronize, (gwgb_handle h), e.synchronize())
+GWGB_FORWARD(gwgb_set_launch_timing, (gwgb_handle h, int32_t on), e.set_launch_timing(on))
+GWGB_FORWARD(gwgb_get_launch_stats, (gwgb_handle h, gwgb_launch_stat *out, int32_t max, int32_t *n),
+             e.launch_stats(out, max, n))
 GWGB_FORWARD(gwgb_test_raise_status, (gwgb_handle h, int32_t which), e.test_raise_status(which))
 
 int gwgb_test_wait_timeout(int32_t device, int32_t polls) {

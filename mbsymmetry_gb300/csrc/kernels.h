@@ -34,8 +34,9 @@ void launch_sigma_fp64(const SigTile *tiles, int ntiles, int maxo, const SigCont
                        const double2 *V, const double2 *G, const double2 *P, double2 *Part, int ns,
                        int smem_bytes, cudaStream_t st);
 
+// ny: CTAs per task (each takes every ny-th 256-element stretch of the block)
 void launch_reduce_slices(const RedTask *tasks, int ntasks, const double2 *part, double2 *out, int nts,
-                          double scale, int mirror, cudaStream_t st);
+                          double scale, int mirror, cudaStream_t st, int ny = 1);
 
 void launch_rotate(const RotTask *tasks, int ntasks, int nbatch, int smem_bytes, const double2 *src,
                    const double2 *O, double2 *dst, cudaStream_t st);

@@ -218,7 +218,7 @@ __global__ void reduce_slices_kernel(const RedTask *__restrict__ tasks, const do
                                      double2 *__restrict__ out, int nts, double scale, int mirror) {
   const RedTask tk = tasks[blockIdx.x];
   const int n = tk.nt * tk.elems;
-  for (int o = threadIdx.x; o < n; o += blockDim.x) {
+  for (int o = blockIdx.y * blockDim.x + threadIdx.x; o < n; o += gridDim.y * blockDim.x) {
     double2 a = part[tk.part + o];
     for (int sl = 1; sl < tk.nslice; ++sl) a = cadd(a, part[tk.part + (int64_t)sl * n + o]);
     const int it = o / tk.elems, e = o - it * tk.elems;
@@ -749,9 +749,10 @@ void launch_hartree(const HcTask *ct, int nct, const HcItem *ci, const HjTask *j
 }
 
 void launch_reduce_slices(const RedTask *tasks, int ntasks, const double2 *part, double2 *out, int nts,
-                          double scale, int mirror, cudaStream_t st) {
+                          double scale, int mirror, cudaStream_t st, int ny) {
   if (ntasks == 0) return;
-  reduce_slices_kernel<<<ntasks, 256, 0, st>>>(tasks, part, out, nts, scale, mirror);
+  reduce_slices_kernel<<<dim3(ntasks, std::max(1, std::min(ny, 65535))), 256, 0, st>>>(tasks, part, out, nts, scale,
+                                                                                       mirror);
   GWGB_CUDA(cudaGetLastError());
 }
 

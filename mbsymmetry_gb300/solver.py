@@ -275,5 +275,25 @@ class GWSolver:
         _abi.check(self.lib.gwgb_get_stats(self.h, ctypes.byref(s)))
         return {name: getattr(s, name) for name, _ in _abi.GwgbStats._fields_}
 
+    def launch_timing(self, on: bool = True):
+        """Bracket every sliced-path GEMM / reduction launch with CUDA events
+        (gwgb_set_launch_timing); read them with launch_stats()."""
+        _abi.check(self.lib.gwgb_set_launch_timing(self.h, 1 if on else 0))
+
+    def launch_stats(self) -> list:
+        """One dict per sliced-path launch of the last solve / iteration:
+        stage, kernel, tasks, ran, ms, flops, mma_flops, bytes."""
+        n = ctypes.c_int32()
+        _abi.check(self.lib.gwgb_get_launch_stats(self.h, None, 0, ctypes.byref(n)))
+        arr = (_abi.GwgbLaunchStat * max(1, n.value))()
+        _abi.check(self.lib.gwgb_get_launch_stats(self.h, arr, n.value, ctypes.byref(n)))
+        out = []
+        for x in arr[:n.value]:
+            d = {name: getattr(x, name) for name, _ in _abi.GwgbLaunchStat._fields_}
+            d["stage"] = _abi.LAUNCH_STAGES[x.stage]
+            d["kernel"] = _abi.LAUNCH_KERNELS[x.kernel]
+            out.append(d)
+        return out
+
     def name(self) -> str:
         return "GB300 GW solver"

@@ -1,5 +1,5 @@
 // Throughput probes for the roofline denominators that MEASURED_PEAKS.json
-// does not hold: the FP64 FMA rate (CUDA cores), the FP64 tensor rate
+// does not hold: the FP64 and FP32 FMA rates (CUDA cores), the FP64 tensor rate
 // (mma.sync f64, "DMMA"), and the tcgen05 rates of kind::tf32 and kind::f16
 // with BF16 operands.  Measurement code for bench.py; not part of the engine
 // or its C ABI.  Every wait on the tensor core is bounded.
@@ -18,6 +18,20 @@ __global__ void dfma_loop(double *out, int iters, double b, double c) {
     a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+__global__ void ffma_loop(float *out, int iters, float b, float c) {
+  float a[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) a[j] = threadIdx.x * 1e-3f + j;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) a[j] = fmaf(a[j], b, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) s += a[j];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
 // Warp-level FP64 tensor MMA (m8n8k4, 512 flop per instruction), four
@@ -127,6 +141,23 @@ extern "C" double gwgb_probe_fp64_tflops(int dev) {
   cudaFree(out);
   if (err != cudaSuccess) return -1.0;
   return 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3) / 1e12;
+}
+
+// Best-of-5 FP32 FMA throughput (CUDA cores) in TFLOP/s (2 flops per FMA);
+// negative on a CUDA error.
+extern "C" double gwgb_probe_fp32_tflops(int dev) {
+  if (cudaSetDevice(dev) != cudaSuccess) return -1.0;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 1 << 14;
+  float *out = nullptr;
+  if (cudaMalloc(&out, sizeof(float) * blocks * threads) != cudaSuccess) return -1.0;
+  ffma_loop<<<blocks, threads>>>(out, 64, 0.9999999f, 1e-6f);
+  const float ms = best_ms([&] { ffma_loop<<<blocks, threads>>>(out, iters, 0.9999999f, 1e-6f); }, 5);
+  cudaError_t err = cudaGetLastError();
+  cudaFree(out);
+  if (err != cudaSuccess) return -1.0;
+  return 2.0 * 16.0 * (double)iters * blocks * threads / (ms * 1e-3) / 1e12;
 }
 
 // Best-of-5 FP64 tensor-core (mma.sync f64) throughput in TFLOP/s.

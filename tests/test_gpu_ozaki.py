@@ -142,3 +142,31 @@ def test_narrow_blocks_on_cuda_cores_within_bound(name, ns):
         assert max(e) < BOUND
         res[cols] = S
     assert np.abs(res[-1] - res[32]).max() < 1e-8 and np.abs(res[0] - res[32]).max() < 1e-8
+
+
+def test_launch_profile_covers_every_launch_and_changes_nothing():
+    """gwgb_set_launch_timing: one entry per GEMM / reduction launch of the
+    sliced P0 and Sigma stages, all run, their summed times within the stage
+    times, and the results bitwise the same as without the events."""
+    cr, tr = crystal("C2")
+    s = _solver(cr, tr, "ozaki")
+    s.dyson(cr.mu)
+    G0 = s.G_tau()
+    s.set_G(G0)
+    s.iteration(cr.mu)
+    ref = s.Selfenergy()
+    s.launch_timing(True)
+    for _ in range(2):
+        s.set_G(G0)
+        s.iteration(cr.mu)
+    st, ls = s.stats(), s.launch_stats()
+    S = s.Selfenergy()
+    s.close()
+    assert np.array_equal(S, ref)
+    assert ls and all(x["ran"] and x["ms"] > 0 for x in ls)
+    assert {x["stage"] for x in ls} == {"Z1", "Z", "P0", "W", "U", "Sigma"}
+    p0 = sum(x["ms"] for x in ls if x["stage"] in ("Z1", "Z", "P0"))
+    sig = sum(x["ms"] for x in ls if x["stage"] in ("W", "U", "Sigma"))
+    print(f"P0 launches {p0:.2f} of {st['p0_ms']:.2f} ms, Sigma launches {sig:.2f} of {st['sigma_ms']:.2f} ms")
+    assert p0 <= st["p0_ms"] * 1.02 + 0.05 and sig <= st["sigma_ms"] * 1.02 + 0.05
+    assert p0 > 0.5 * st["p0_ms"] and sig > 0.5 * st["sigma_ms"]
