@@ -502,6 +502,7 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD},
         "precision": "ozaki: " + PREC_LABEL["ozaki"], "l2": "flushed (256 MiB write) before each step",
         "parallelism": "replicas" if world > 1 else "1 GPU",
+        "replica_iterations_per_s": reps.replica_throughput(ms) if world > 1 else None,
         "sigma_max_abs_err_vs_fp64": float(np.abs(sig_oz - sig64).max()),
         "G_max_abs_err_vs_fp64": float(np.abs(g_oz - g64).max()),
         "sigma_max_abs": float(np.abs(sig64).max()),
