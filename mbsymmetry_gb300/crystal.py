@@ -27,6 +27,23 @@ numbers:
   S = I; H = F.
 * orep / auxrep: a random unitary per block for every non-representative k.
 * mu: half filling of the G0 bands (nel = nao per spin-summed cell).
+
+``symmetric=True`` (fcc) builds data that are exactly consistent with the
+group, so that a calculation on the irreducible k points with rotations and
+one on every k point of the mesh give the same P0, P~ and Sigma (the
+reference's iBZ-vs-full-BZ checks, ``SymmetryMBPT/test/test_cugw.cpp:306-436``):
+
+* gauge 0: V0(k1, k2) is the same on every orbit of pairs under the point
+  group (g k1, g k2), with V0(k2, k1)_{Q,j,i} = conj(V0(k1, k2)_{Q,i,j}) on
+  the swapped orbit (averaged over the stabiliser when a group operation
+  swaps the pair), and F0(k) is the same on every star;
+* every k and q gets a basis change, a random unitary per irrep block
+  (W_k for AO, X_q for aux; the identity at the representatives, and
+  X_{-q} = conj(X_q) so that the Hermitian pair relation survives);
+* the data are the gauge-0 data in those bases, V^Q(k1, k2) =
+  sum_Q' X_q[Q, Q'] W_k1 V0^Q'(k1, k2) W_k2^H and F(k) = W_k F0 W_k^H, and
+  the rotations are orep(k) = W_k, auxrep(q) = X_q: a representation of the
+  group in which every datum transforms covariantly.
 """
 from __future__ import annotations
 
@@ -198,8 +215,65 @@ def _rand_unitary(rng, n):
     return q * (np.diag(r) / np.abs(np.diag(r)))[None, :]
 
 
+def _symmetric_V(spec, layout, kmesh, ops, Wk, Xq, sigma, V):
+    """Group-consistent V (module docstring): gauge-0 blocks per orbit of pairs
+    under the point group and the swap, then the per-k / per-q bases."""
+    nk = layout.nk
+    perm = np.array([[_find(wrap_1stbz(M @ kmesh[k]), kmesh) for k in range(nk)] for M in ops])
+    src = {}  # pair -> (representative pair, swapped)
+    sym = {}  # representative -> some operation swaps it onto itself
+    for k1 in range(nk):
+        for k2 in range(nk):
+            if (k1, k2) in src:
+                continue
+            r = (k1, k2)
+            sym[r] = False
+            for g in range(len(ops)):
+                a, b = int(perm[g][k1]), int(perm[g][k2])
+                src.setdefault((a, b), (r, False))
+            for g in range(len(ops)):
+                a, b = int(perm[g][k2]), int(perm[g][k1])
+                if (a, b) == r:
+                    sym[r] = True
+                src.setdefault((a, b), (r, True))
+
+    def blocks_of(k1, k2):
+        p = k1 * nk + k2
+        return p, {tuple(int(x) for x in t): i for i, t in enumerate(layout.tensor_irreps[p])}
+
+    V0 = {}
+    for r in sym:  # representatives in pair order (deterministic streams)
+        k1, k2 = r
+        p, idx = blocks_of(k1, k2)
+        q = layout.pair_q(k1, k2)
+        vrng = np.random.default_rng((spec.seed + 29, p))
+        blk = {}
+        for t in layout.tensor_irreps[p]:
+            iq, i1, i2 = (int(x) for x in t)
+            qb, b1, b2 = layout.aux_sizes[q][iq], layout.ao_sizes[k1][i1], layout.ao_sizes[k2][i2]
+            blk[(iq, i1, i2)] = sigma * (vrng.normal(size=(qb, b1, b2)) + 1j * vrng.normal(size=(qb, b1, b2))) / np.sqrt(2)
+        if sym[r]:  # an operation maps (k2, k1) onto (k1, k2): V0 equals its swapped conjugate
+            blk = {t: 0.5 * (x + blk[(t[0], t[2], t[1])].transpose(0, 2, 1).conj()) for t, x in blk.items()}
+        V0[r] = blk
+    for (k1, k2), (r, sw) in src.items():
+        p, _ = blocks_of(k1, k2)
+        q = layout.pair_q(k1, k2)
+        base = layout.kpair_slice_offsets[p]
+        for b, t in enumerate(layout.tensor_irreps[p]):
+            iq, i1, i2 = (int(x) for x in t)
+            x0 = V0[r][(iq, i2, i1)].transpose(0, 2, 1).conj() if sw else V0[r][(iq, i1, i2)]
+            x = np.einsum("QR,ij,Rjl,ml->Qim", Xq[q][iq], Wk[k1][i1], x0, Wk[k2][i2].conj(), optimize=True)
+            o = base + layout.tensor_offsets[p][b]
+            V[o:o + x.size] = x.ravel()
+
+
+def _gauge(rng, sizes):
+    """A random unitary per irrep block (the block-diagonal basis change of one k)."""
+    return [_rand_unitary(rng, int(b)) for b in sizes]
+
+
 def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool = False,
-                 with_V: bool = True, physical: bool = False) -> Crystal:
+                 with_V: bool = True, physical: bool = False, symmetric: bool = False) -> Crystal:
     """Build the crystal.  ``rotate=False`` keeps every k point (ink = nk,
     identity rotations), the reference's no-symmetry mode.
 
@@ -214,7 +288,13 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
     representative k (:mod:`symmetry`: d blocks of size m per irrep of
     dimension d and multiplicity m, for spec.atoms atoms with s/p/d shells)
     instead of drawing them in the spec's ranges; block labels and the V
-    selection rule stay the labelled ones."""
+    selection rule stay the labelled ones.  ``symmetric=True`` builds
+    group-consistent data (module docstring); the same V, and F in the same
+    bases, with ``rotate`` True or False."""
+    if symmetric and spec.lattice != "fcc":
+        raise ValueError("symmetric crystals are built for the fcc (O_h, with inversion) lattice")
+    if symmetric and used_pairs_only:
+        raise ValueError("symmetric crystals store V for every pair")
     rng = np.random.default_rng(spec.seed)
     ops, inversion = _fcc_ops() if spec.lattice == "fcc" else _hex_ops()
     kmesh = _kmesh(spec.mesh)
@@ -315,16 +395,35 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
 
     # rotations: random unitary per block for non-representatives
     orep_blocks, orep_irreps, auxrep_blocks, auxrep_irreps = [], [], [], []
+    Wk, Xq = None, None
+    if symmetric:  # the basis changes of every k / q (identity at the representatives)
+        grng = np.random.default_rng(spec.seed + 23)
+        is_rep = np.zeros(nk, dtype=bool)
+        is_rep[reps] = True
+        Wk = [[np.eye(b) for b in ao_sizes[k]] if is_rep[k] else _gauge(grng, ao_sizes[k]) for k in range(nk)]
+        Xq = [None] * nk
+        for q in range(nk):
+            if Xq[q] is not None:
+                continue
+            mq = int(minus[q])
+            if is_rep[q] or is_rep[mq] or mq == q:
+                Xq[q] = [np.eye(b) for b in aux_sizes[q]]
+                Xq[mq] = [np.eye(b) for b in aux_sizes[mq]]
+            else:
+                Xq[q] = _gauge(grng, aux_sizes[q])
+                Xq[mq] = [x.conj() for x in Xq[q]]
     for k in range(nk):
         rep_k = (idx[cidx[k]] == cidx[k])
         osz = ao_sizes[k]
         asz = aux_sizes[k]
         orep_irreps.append(np.stack([np.arange(len(osz)), np.arange(len(osz))], 1))
         auxrep_irreps.append(np.stack([np.arange(len(asz)), np.arange(len(asz))], 1))
-        for b in osz:
-            orep_blocks.append((np.eye(b) if rep_k else _rand_unitary(rng, b)).ravel())
-        for b in asz:
-            auxrep_blocks.append((np.eye(b) if rep_k else _rand_unitary(rng, b)).ravel())
+        for i, b in enumerate(osz):
+            u = np.eye(b) if rep_k else (Wk[k][i] if symmetric else _rand_unitary(rng, b))
+            orep_blocks.append(u.ravel())
+        for i, b in enumerate(asz):
+            u = np.eye(b) if rep_k else (Xq[k][i] if symmetric else _rand_unitary(rng, b))
+            auxrep_blocks.append(u.ravel())
     layout = BlockLayout(nk=nk, kmesh=kmesh, ao_sizes=ao_sizes, aux_sizes=aux_sizes, tensor_irreps=ti,
                          irre_list=irre_list, index=idx, irre_index=irre_index, conj_index=cidx,
                          orep=np.concatenate(orep_blocks).astype(np.complex128), orep_irreps=orep_irreps,
@@ -333,7 +432,9 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
     # --- V with the Hermitian pair relation V(k2,k1)_{Q,j,i} = conj(V(k1,k2)_{Q,i,j})
     V = np.zeros(layout.flat_V_size if with_V else 0, dtype=np.complex128)
     sigma = spec.v_scale / np.sqrt(spec.nao)
-    for k1 in (range(nk) if with_V else ()):
+    if symmetric and with_V:
+        _symmetric_V(spec, layout, kmesh, ops, Wk, Xq, sigma, V)
+    for k1 in (range(nk) if with_V and not symmetric else ()):
         for k2 in range(k1, nk):
             p = k1 * nk + k2
             pr = k2 * nk + k1
@@ -367,12 +468,25 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
     S = np.zeros((ns, fa), np.complex128)
     frng = np.random.default_rng(spec.seed + 11)
     eigs = []
+    F0 = {}  # symmetric: F0 per star (gauge 0), drawn in representative order
+    if symmetric:
+        for st_, r in enumerate(reps):
+            blocks = []
+            for s_ in ao_sizes[r]:
+                x = frng.uniform(-1, 1, size=(s_, s_)) + 1j * frng.uniform(-1, 1, size=(s_, s_))
+                blocks.append(0.5 * (x + x.conj().T) * 0.6 + np.diag(frng.normal(0.0, 0.5, size=s_)))
+            F0[st_] = blocks
     for ik, k in enumerate(layout.irre_list):
         w = star_size[star_of[k]] if rotate else 1
         for b, s_ in enumerate(ao_sizes[k]):
             o = layout.kao_slice_offsets_irre[ik] + layout.ao_offsets[k][b]
-            x = frng.uniform(-1, 1, size=(s_, s_)) + 1j * frng.uniform(-1, 1, size=(s_, s_))
-            h = 0.5 * (x + x.conj().T) * 0.6 + np.diag(frng.normal(0.0, 0.5, size=s_))
+            if symmetric:
+                u = Wk[k][b]
+                h = u @ F0[star_of[k]][b] @ u.conj().T
+                h = 0.5 * (h + h.conj().T)
+            else:
+                x = frng.uniform(-1, 1, size=(s_, s_)) + 1j * frng.uniform(-1, 1, size=(s_, s_))
+                h = 0.5 * (x + x.conj().T) * 0.6 + np.diag(frng.normal(0.0, 0.5, size=s_))
             for sp in range(ns):
                 F[sp, o:o + s_ * s_] = h.ravel()
                 S[sp, o:o + s_ * s_] = np.eye(s_).ravel()
