@@ -65,8 +65,9 @@ class gb300_gw_solver {
     ++iter_;
   }
   virtual void get_iter(int &iter) { iter = iter_; }
+  // the split-precision path with the 1e-7 Ha bound (GWGB_PREC_OZAKI)
   virtual void single_prec_run(bool run_sp) {
-    check(gwgb_set_precision(h_, run_sp ? GWGB_PREC_TF32X3 : GWGB_PREC_FP64));
+    check(gwgb_set_precision(h_, run_sp ? GWGB_PREC_OZAKI : GWGB_PREC_FP64));
   }
   virtual void set_shared_Coulomb() {
     if (!V_) throw std::runtime_error("gb300_gw_solver: no Coulomb integrals were given");

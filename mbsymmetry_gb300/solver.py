@@ -85,7 +85,9 @@ class GWSolver:
         S = np.ascontiguousarray(S, dtype=np.complex128)
         _abi.check(self.lib.gwgb_set_fock(self.h, _ptr(F), _ptr(S)))
 
-    def single_prec_run(self, run_sp: bool, kind: str = "tf32x3"):
+    def single_prec_run(self, run_sp: bool, kind: str = "ozaki"):
+        """Split-precision contractions on (``kind``: "ozaki", the path with the
+        1e-7 Ha bound, or the FP32-class "tf32x3" / "bf16x3") or off (FP64)."""
         _abi.check(self.lib.gwgb_set_precision(self.h, _abi.PREC_NAMES[kind if run_sp else "fp64"]))
 
     # -- G / Sigma / P host <-> device ----------------------------------------
