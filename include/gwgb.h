@@ -247,14 +247,15 @@ int gwgb_synchronize(gwgb_handle h);
  * Switching it re-captures the iteration graph. */
 typedef struct gwgb_launch_stat {
   int32_t stage;    /* 0 Z1 (V G2), 1 Z (G1 Z1), 2 P0 (final), 3 W (P~ V), 4 U (W G2), 5 Sigma (final) */
-  int32_t kernel;   /* 0 oz_gemm_kernel (tcgen05), 1 oz_simt_kernel (CUDA cores), 2 reduce_slices_kernel */
+  int32_t kernel;   /* 0 oz_gemm_kernel (tcgen05), 1 oz_simt_kernel (CUDA cores), 2 reduce_slices_kernel,
+                       3 oz_perm_kernel (a chunk's copy of V blocks into a concatenated operand) */
   int32_t tasks;    /* CTA work items (kernels 0, 1) or reduced blocks (kernel 2) */
   int32_t ran;      /* 1 when the launch ran in the last solve / iteration */
   double ms;        /* CUDA-event time of the launch */
   double flops;     /* algorithmic: 8 M N K per complex block GEMM (0 for reductions) */
   double mma_flops; /* kernel 0: BF16 MMA FLOPs issued (128-row tiles, N and K padded to the MMA shape,
                        10 slice products, real embedding); kernel 1: FP32 instructions (48 per complex MAC) */
-  double bytes;     /* kernel 2: partials read + output written */
+  double bytes;     /* kernels 2, 3: bytes read + written */
 } gwgb_launch_stat;
 
 int gwgb_set_launch_timing(gwgb_handle h, int32_t on);

@@ -72,7 +72,7 @@ class GwgbLaunchStat(ctypes.Structure):
 
 
 LAUNCH_STAGES = ("Z1", "Z", "P0", "W", "U", "Sigma")
-LAUNCH_KERNELS = ("oz_gemm_kernel", "oz_simt_kernel", "reduce_slices_kernel")
+LAUNCH_KERNELS = ("oz_gemm_kernel", "oz_simt_kernel", "reduce_slices_kernel", "oz_perm_kernel")
 
 
 class GwgbProxyStats(ctypes.Structure):

@@ -276,6 +276,24 @@ class Engine {
     if (prec_ == GWGB_PREC_OZAKI) {
       if (!oz_built_) build_oz_lists();
       if (!ozVcat_.p) {
+        {  // the sliced path's buffers must fit the free memory: say which take it otherwise
+          const std::pair<const char *, int64_t> need[] = {
+              {"Z1", oz_z1_elems_ * 16}, {"Zcat", oz_zcat_elems_ * 16}, {"W", oz_w_elems_ * 16},
+              {"U", oz_u_elems_ * 16}, {"Vcat", oz_vcat_elems_ * 16}, {"Bcat", oz_bcat_elems_ * 16},
+              {"VcatS", oz_vcats_elems_ * 16}, {"V blocks", oz_vz_elems_ * 16}, {"partials", oz_part_elems_ * 16},
+              {"G, P~ copies", (int64_t)(Gall_.n + Pall_.n) * 16}};
+          int64_t tot = 0;
+          std::string msg;
+          for (const auto &x : need) {
+            tot += x.second;
+            msg += std::string(" ") + x.first + " " + std::to_string(x.second >> 20) + " MB";
+          }
+          size_t free_b = 0, total_b = 0;
+          GWGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+          GWGB_REQUIRE(tot + (256ll << 20) <= (int64_t)free_b, GWGB_E_UNSUPPORTED,
+                       "sliced-precision buffers need " + std::to_string(tot >> 20) + " MB (" + msg + " ), " +
+                           std::to_string(free_b >> 20) + " MB free");
+        }
         ozVcat_.alloc((size_t)oz_vcat_elems_);
         ozBcat_.alloc((size_t)oz_bcat_elems_);
         ozVcatS_.alloc((size_t)oz_vcats_elems_);
@@ -283,9 +301,9 @@ class Engine {
         ozZcat_.alloc((size_t)oz_zcat_elems_);
         ozW_.alloc((size_t)oz_w_elems_);
         ozU_.alloc((size_t)oz_u_elems_);
+        ozVz_.alloc((size_t)oz_vz_elems_);
         Gff_.alloc(Gall_.n);
         Pff_.alloc(Pall_.n);
-        Vff_.alloc((size_t)l_.flat_V);
         ozPart_.alloc((size_t)oz_part_elems_);
         oz_ready_ = false;
       }
@@ -433,10 +451,10 @@ class Engine {
       built = true;
     }
     if (prec_ == GWGB_PREC_OZAKI && !oz_ready_) {
-      launch_to_ffc(V_.p, Vff_.p, (int64_t)l_.flat_V, st_);
-      launch_oz_perm(oz_perm_v_.p, (int)oz_perm_v_.n, V_.p, ozVcat_.p, st_);
-      launch_oz_perm(oz_perm_b_.p, (int)oz_perm_b_.n, Vt_.p, ozBcat_.p, st_);
-      launch_oz_perm(oz_perm_s_.p, (int)oz_perm_s_.n, Vt_.p, ozVcatS_.p, st_);
+      // tau-independent operands of contractions that run in one chunk: built once per upload
+      for (const OzLaunch &x : oz_static_)
+        launch_oz_perm(oz_perm_.p + x.t0, (int)x.n, static_cast<const double2 *>(oz_ptr(x.a)),
+                       static_cast<float4 *>(const_cast<void *>(oz_ptr(x.c))), st_);
       oz_ready_ = true;
       built = true;
     }
@@ -452,8 +470,10 @@ class Engine {
   // Sliced (Ozaki) path: descriptors and tasks of the six GEMM stages per tau
   // chunk, the float-float operand buffers and the copies that build the
   // tau-independent ones from V / Vt.
-  enum OzBufId { OZB_GFF, OZB_PFF, OZB_VFF, OZB_VCAT, OZB_BCAT, OZB_VCATS, OZB_Z1, OZB_ZCAT, OZB_W, OZB_U, OZB_P0,
-                 OZB_SIG };
+  // OZB_G, OZB_P: float-float copies of G and P~ (per iteration); OZB_V, OZB_VT: the
+  // FP64 V and pre-rotated V (sources of the operand builds); OZB_VZ: a chunk's V blocks
+  enum OzBufId { OZB_G, OZB_P, OZB_V, OZB_VT, OZB_VZ, OZB_VCAT, OZB_BCAT, OZB_VCATS, OZB_Z1, OZB_ZCAT, OZB_W, OZB_U,
+                 OZB_P0, OZB_SIG };
   // one stage launch: tasks [t0, t0 + n); with nr > 0 the stage writes FP64 K-slice partials to
   // ozPart_ and the ordered sums oz_red_[r0, r0 + nr) (times scale) go to buffer c afterwards
   // simt: the CUDA-core float-float kernel; part: C is ozPart_ (K-slice partials)
@@ -461,6 +481,7 @@ class Engine {
     int64_t t0, n;
     int a, b, c;
     bool simt = false, part = false;
+    bool perm = false;        // an operand build: oz_perm_[t0, t0 + n) from buffer a into buffer c
     int64_t r0 = 0, nr = 0;
     double scale = 1.0;
     int stage = 0;            // gwgb_launch_stat.stage
@@ -484,12 +505,13 @@ class Engine {
       for (const OzLaunch &x : l ? oz_sig_ : oz_p0_) {
         gwgb_launch_stat g{};
         g.stage = x.stage;
-        g.kernel = x.simt ? 1 : 0;
+        g.kernel = x.perm ? 3 : x.simt ? 1 : 0;
         g.tasks = (int32_t)x.n;
         g.flops = x.flops;
         g.mma_flops = x.ops;
+        g.bytes = x.red_bytes;
         lt_info_.push_back(g);
-        if (x.nr) {
+        if (x.nr && !x.perm) {
           gwgb_launch_stat r{};
           r.stage = x.stage;
           r.kernel = 2;
@@ -537,12 +559,16 @@ class Engine {
   bool oz_built_ = false, oz_ready_ = false;
   DBuf<OzDesc> oz_descs_;
   DBuf<OzTask> oz_tasks_;
-  DBuf<OzPerm> oz_perm_v_, oz_perm_b_, oz_perm_s_;
   DBuf<int64_t> oz_rowtab_;
   DBuf<RedTask> oz_red_;
   DBuf<double2> ozPart_;
   int64_t oz_part_elems_ = 1;
-  DBuf<float4> Gff_, Pff_, Vff_, ozVcat_, ozBcat_, ozVcatS_, ozZ1_, ozZcat_, ozW_, ozU_;
+  DBuf<float4> Gff_, Pff_, ozVz_, ozVcat_, ozBcat_, ozVcatS_, ozZ1_, ozZcat_, ozW_, ozU_;
+  int64_t oz_vz_elems_ = 1;
+  // operand builds (copies of V / Vt blocks into chunk-local Vcat, Bcat, VcatS):
+  // in the launch lists per chunk, or in oz_static_ when a contraction has one chunk
+  DBuf<OzPerm> oz_perm_;
+  std::vector<OzLaunch> oz_static_;
   int64_t oz_vcat_elems_ = 0, oz_bcat_elems_ = 0, oz_vcats_elems_ = 0, oz_z1_elems_ = 0, oz_zcat_elems_ = 0,
           oz_w_elems_ = 0, oz_u_elems_ = 0;
   std::vector<OzLaunch> oz_p0_, oz_sig_;
@@ -552,9 +578,11 @@ class Engine {
   void build_oz_lists();
   const void *oz_ptr(int id) const {
     switch (id) {
-      case OZB_GFF: return Gff_.p;
-      case OZB_PFF: return Pff_.p;
-      case OZB_VFF: return Vff_.p;
+      case OZB_G: return Gff_.p;
+      case OZB_P: return Pff_.p;
+      case OZB_V: return V_.p;
+      case OZB_VT: return Vt_.p;
+      case OZB_VZ: return ozVz_.p;
       case OZB_VCAT: return ozVcat_.p;
       case OZB_BCAT: return ozBcat_.p;
       case OZB_VCATS: return ozVcatS_.p;
@@ -575,12 +603,15 @@ class Engine {
     }
     for (const OzLaunch &x : ls) {
       void *c = x.part ? static_cast<void *>(ozPart_.p) : const_cast<void *>(oz_ptr(x.c));
-      const float4 *a = static_cast<const float4 *>(oz_ptr(x.a)), *b = static_cast<const float4 *>(oz_ptr(x.b));
+      const void *a = oz_ptr(x.a), *b = oz_ptr(x.b);
+      const float4 *af = static_cast<const float4 *>(a), *bf = static_cast<const float4 *>(b);
       if (lt_on_) rec_ev(lt_ev_[2 * rec]);
-      if (x.simt)
-        launch_oz_simt(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, a, b, c, oz_rowtab_.p, st_);
+      if (x.perm)
+        launch_oz_perm(oz_perm_.p + x.t0, (int)x.n, static_cast<const double2 *>(a), static_cast<float4 *>(c), st_);
+      else if (x.simt)
+        launch_oz_simt(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, af, bf, c, oz_rowtab_.p, st_);
       else
-        launch_oz_gemm(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, a, b, c, oz_rowtab_.p, nsm_, bad_.p + 2, st_);
+        launch_oz_gemm(oz_descs_.p, oz_tasks_.p + x.t0, (int)x.n, af, bf, c, oz_rowtab_.p, nsm_, bad_.p + 2, st_);
       if (lt_on_) rec_ev(lt_ev_[2 * rec + 1]);
       ++rec;
       if (x.nr) {
@@ -758,8 +789,8 @@ Engine::~Engine() {
                            &Tnt_, &Ttn_, &TntBF_, &TtnFB_};
   sw_tiles_.free(); bc_tasks_.free(); sig_wref_.free(); Wbuf_.free(); Bcat_.free(); uv_red_.free();
   pz_tasks_.free(); vc_tasks_.free(); pk_tiles_.free(); pr_tiles_.free(); Zbuf_.free(); Vcat_.free(); Ppart_.free();
-  oz_descs_.free(); oz_tasks_.free(); oz_perm_v_.free(); oz_perm_b_.free(); oz_perm_s_.free(); oz_rowtab_.free();
-  for (DBuf<float4> *b : {&Gff_, &Pff_, &Vff_, &ozVcat_, &ozBcat_, &ozVcatS_, &ozZ1_, &ozZcat_, &ozW_, &ozU_}) b->free();
+  oz_descs_.free(); oz_tasks_.free(); oz_perm_.free(); oz_rowtab_.free();
+  for (DBuf<float4> *b : {&Gff_, &Pff_, &ozVz_, &ozVcat_, &ozBcat_, &ozVcatS_, &ozZ1_, &ozZcat_, &ozW_, &ozU_}) b->free();
   oz_red_.free(); ozPart_.free();
   for (auto *b : bufs) b->free();
   tct_f_.free(); tct_l_.free(); mu_dev_.free(); ws_.free(); bad_.free(); leak_.free();
@@ -1665,13 +1696,14 @@ void Engine::build_oz_lists() {
   // that block, at least 32 rounds of K per slice), so results do not depend on
   // how blocks are grouped into chunks.
   std::vector<RedTask> red;
-  struct Fin { OzDesc d; int64_t out; int32_t ostride, nt, elems; };
+  // mfull: rows of the block over all tau (the slice count must not depend on the tau chunking)
+  struct Fin { OzDesc d; int64_t out; int32_t ostride, nt, elems, mfull; };
   auto final_stage = [&](std::vector<OzLaunch> &v, const std::vector<Fin> &fins, int a, int b, int c, double scale,
                          int64_t na, int64_t nb, int64_t nout, const char *what) {
     const size_t t0 = ts.size(), r0 = red.size();
     int64_t part = 0;
     for (const Fin &f : fins) {
-      const int64_t tiles = (int64_t)((f.d.M + OZ_M - 1) / OZ_M) * ((f.d.N + OZ_NC - 1) / OZ_NC);
+      const int64_t tiles = (int64_t)((f.mfull + OZ_M - 1) / OZ_M) * ((f.d.N + OZ_NC - 1) / OZ_NC);
       const int64_t want = (2 * (int64_t)std::max(1, nsm_) + tiles - 1) / tiles;
       const int nk16 = (f.d.K + OZ_KR - 1) / OZ_KR;
       const int nsl = (int)std::max<int64_t>(1, std::min<int64_t>(want, nk16 / 32));
@@ -1724,11 +1756,21 @@ void Engine::build_oz_lists() {
   const double pref = -1.0 / l.nk * (ns == 1 ? 2.0 : 1.0);  // cugw_qkpt_block.cu:210, cugw_solver_block.cpp:303
 
   // ---- P0 -------------------------------------------------------------------
-  std::vector<OzPerm> pv;
-  struct PG { int64_t voff; int zld; };
+  // Operand builds (copies of V / Vt blocks): one launch per chunk and buffer, or
+  // a launch in oz_static_ (once per upload) when the contraction has one chunk.
+  std::vector<OzPerm> perms;
+  oz_static_.clear();
+  auto perm_launch = [&](std::vector<OzLaunch> &v, size_t p0, int src, int dst, bool once) {
+    if (perms.size() == p0) return;
+    OzLaunch l{(int64_t)p0, (int64_t)(perms.size() - p0), src, src, dst};
+    l.perm = true;
+    l.stage = cur_stage;
+    for (size_t t = p0; t < perms.size(); ++t) l.red_bytes += 32.0 * perms[t].X * perms[t].Y * perms[t].Z;
+    (once ? oz_static_ : v).push_back(l);
+  };
+  struct PG { int64_t voff; int zld; };  // Vcat offset (chunk-local) and row length of a P0 group
   std::vector<PG> pg;
   std::vector<int> zcol(pc.size() * ns), cgrp(pc.size());
-  int64_t voff = 0;
   for (size_t gi = 0; gi < p0_groups_.size(); ++gi) {
     const P0Group &g = p0_groups_[gi];
     int zld = 0;
@@ -1739,31 +1781,83 @@ void Engine::build_oz_lists() {
         zld += pc[c].b1 * pc[c].b2;
       }
     }
-    pg.push_back({voff, zld});
-    for (int c = g.c0; c < g.c1; ++c)
-      for (int sp = 0; sp < ns; ++sp)  // Vcat[Q][zcol + m b1 + p] = V_c[Q][p][m]
-        pv.push_back({pc[c].v, voff + zcol[c * ns + sp], zld, 1, pc[c].b1, g.qb, pc[c].b1, pc[c].b2, 0});
-    voff += (int64_t)g.qb * zld;
+    pg.push_back({0, zld});
   }
-  oz_vcat_elems_ = voff;
-  // chunks of output blocks: Z1 and Zcat of a chunk (all nts/2 tau) within the budget
-  const int64_t budget = std::max<int64_t>(1, tc_chunk_bytes_ / 16);  // complex float-float elements
-  std::vector<std::pair<int, int>> pchunks;
-  for (size_t g0 = 0; g0 < p0_groups_.size();) {
-    size_t g1 = g0;
-    int64_t need = 0;
-    while (g1 < p0_groups_.size()) {
-      const int64_t n = 2 * (int64_t)p0_groups_[g1].qb * pg[g1].zld * half;
-      if (g1 > g0 && need + n > budget) break;
-      need += n;
-      ++g1;
+  // chunks of output blocks: Z1, Zcat, Vcat and V blocks of a chunk (all nts/2 tau) within
+  // the budget.  Every buffer of a stage is sized to its largest chunk and the P0 and
+  // Sigma buffers coexist, so the budget is a twelfth of the memory free now (after
+  // V), at most the handle's chunk size (GWGB_TC_CHUNK_MB) and at least 64 MB.
+  int64_t budget;  // complex float-float elements
+  {
+    size_t free_b = 0, total_b = 0;
+    GWGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const int64_t by_free = std::max<int64_t>(64ll << 20, (int64_t)(free_b / 12));
+    budget = std::max<int64_t>(1, std::min<int64_t>(tc_chunk_bytes_, by_free) / 16);
+  }
+  // A group whose own need is above the budget gets chunks of its own over tau ranges.
+  struct Chunk { int first, second, t0, t1; };  // output blocks [first, second), tau [t0, t1)
+  std::vector<Chunk> pchunks;
+  {
+    auto need = [&](size_t g, int nt) {  // Z1 and Zcat per tau, Vcat and V blocks once
+      return (2 * (int64_t)nt + 2) * p0_groups_[g].qb * pg[g].zld;
+    };
+    for (size_t g0 = 0; g0 < p0_groups_.size();) {
+      if (need(g0, half) > budget) {
+        const int64_t per = 2 * (int64_t)p0_groups_[g0].qb * pg[g0].zld;
+        const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(half, (budget - per) / per));
+        for (int t0 = 0; t0 < half; t0 += nt) pchunks.push_back({(int)g0, (int)g0 + 1, t0, std::min(half, t0 + nt)});
+        ++g0;
+        continue;
+      }
+      size_t g1 = g0;
+      int64_t tot = 0;
+      while (g1 < p0_groups_.size() && need(g1, half) <= budget && (g1 == g0 || tot + need(g1, half) <= budget))
+        tot += need(g1++, half);
+      pchunks.push_back({(int)g0, (int)g1, 0, half});
+      g0 = g1;
     }
-    pchunks.push_back({(int)g0, (int)g1});
-    g0 = g1;
   }
-  oz_z1_elems_ = oz_zcat_elems_ = 1;
+  oz_z1_elems_ = oz_zcat_elems_ = oz_vcat_elems_ = oz_vz_elems_ = 1;
   struct PackRow { int c; int64_t pos; };
   for (const auto &ch : pchunks) {
+    const int t0 = ch.t0, ntc = ch.t1 - ch.t0;  // the chunk's tau range
+    {  // Vcat of the chunk's groups: Vcat[Q][zcol + m b1 + p] = V_c[Q][p][m]
+      const size_t p0 = perms.size();
+      int64_t voff = 0;
+      for (int gi = ch.first; gi < ch.second; ++gi) {
+        const P0Group &g = p0_groups_[gi];
+        pg[gi].voff = voff;
+        for (int c = g.c0; c < g.c1; ++c)
+          for (int sp = 0; sp < ns; ++sp)
+            perms.push_back({pc[c].v, voff + zcol[c * ns + sp], pg[gi].zld, 1, pc[c].b1, g.qb, pc[c].b1, pc[c].b2, 0});
+        voff += (int64_t)g.qb * pg[gi].zld;
+      }
+      oz_vcat_elems_ = std::max(oz_vcat_elems_, voff);
+      for (size_t t = p0; t < perms.size(); ++t) {
+        const OzPerm &x = perms[t];
+        check_range(x.src, (int64_t)x.X * x.Y * x.Z, l.flat_V, "sliced Vcat source");
+        check_range(x.dst, (x.X - 1) * x.dx + (x.Y - 1) * x.dy + (x.Z - 1) * x.dz + 1, voff, "sliced Vcat");
+      }
+      cur_stage = 2;
+      perm_launch(oz_p0_, p0, OZB_V, OZB_VCAT, pchunks.size() == 1);
+    }
+    std::vector<int64_t> vz(pc.size(), -1);  // the chunk's V blocks in float-float (the Z1 stage's A rows)
+    int64_t vz_elems = 0;
+    {
+      const size_t p0 = perms.size();
+      int64_t &off = vz_elems;
+      for (int gi = ch.first; gi < ch.second; ++gi)
+        for (int c = p0_groups_[gi].c0; c < p0_groups_[gi].c1; ++c) {
+          const int qb = p0_groups_[gi].qb, b1 = pc[c].b1, b2 = pc[c].b2;
+          vz[c] = off;
+          perms.push_back({pc[c].v, off, (int64_t)b1 * b2, b2, 1, qb, b1, b2, 0});
+          check_range(pc[c].v, (int64_t)qb * b1 * b2, l.flat_V, "sliced V block source");
+          off += (int64_t)qb * b1 * b2;
+        }
+      oz_vz_elems_ = std::max(oz_vz_elems_, off);
+      cur_stage = 0;
+      perm_launch(oz_p0_, p0, OZB_V, OZB_VZ, pchunks.size() == 1);
+    }
     // chunk-local per-tau layouts
     std::vector<int64_t> zc(p0_groups_.size(), 0);
     int64_t zct = 0;
@@ -1794,7 +1888,7 @@ void Engine::build_oz_lists() {
       }
       z1t += mp * pc[v[0].c].b2;
     }
-    const int64_t z1_elems = z1t * half, zcat_elems = zct * half;
+    const int64_t z1_elems = z1t * ntc, zcat_elems = zct * ntc;
     oz_z1_elems_ = std::max(oz_z1_elems_, z1_elems);
     oz_zcat_elems_ = std::max(oz_zcat_elems_, zcat_elems);
     size_t s0 = ts.size();
@@ -1808,26 +1902,26 @@ void Engine::build_oz_lists() {
         const P0Contrib &cb = pc[x.c];
         const int qb = p0_groups_[cgrp[x.c]].qb;
         for (int P = 0; P < qb; ++P)
-          for (int t = 0; t < cb.b1; ++t) rt.push_back(cb.v + ((int64_t)P * cb.b1 + t) * b2);
+          for (int t = 0; t < cb.b1; ++t) rt.push_back(vz[x.c] + ((int64_t)P * cb.b1 + t) * b2);
       }
       OzDesc d{};
       d.M = (int)(rt.size() - tab);
       d.a = {tab, 0, 0, 0};
-      d.b = {c0.gb + (int64_t)sp * c0.sb, (int64_t)ns * c0.sb, b2, b2};
+      d.b = {c0.gb + ((int64_t)t0 * ns + sp) * c0.sb, (int64_t)ns * c0.sb, b2, b2};  // G2(tau) rows (tau, m)
       d.c = {z1pack[k0], 1, 0, 1};
       d.cn1 = z1t;
       d.cn0 = (int32_t)z1mp[k0];
       d.cnd = b2;
       d.aks = d.bks = 1;
-      d.N = half * b2;
+      d.N = ntc * b2;
       d.K = b2;
       d.flags = OZ_CONJ_A;
-      check_tab(tab, d.M, b2, 0, 1, l.flat_V, "P0 stage Z1 (V rows)");
-      oz_check(d, 1, l.flat_V, gsz, z1_elems, "P0 stage Z1");
-      add(d, 1, 1);
+      check_tab(tab, d.M, b2, 0, 1, vz_elems, "P0 stage Z1 (V rows)");
+      oz_check(d, 1, vz_elems, gsz, z1_elems, "P0 stage Z1");
+      add(d, 1, 1, half * b2);  // routed by the width over all tau (every tau chunk the same way)
     }
     cur_stage = 0;
-    stage(oz_p0_, s0, OZB_VFF, OZB_GFF, OZB_Z1);
+    stage(oz_p0_, s0, OZB_VZ, OZB_G, OZB_Z1);
     s0 = ts.size();
     for (auto &kv : zp) {  // Zcat[tau][P][K = (c,s,m,p)] = sum_t G1(beta-tau)[t][p] Z1[tau][m][(c,P,t)]
       const int sp = kv.first.second;
@@ -1852,7 +1946,7 @@ void Engine::build_oz_lists() {
       d.M = (int)(tabc - taba);
       d.a = {taba, 0, 0, 0};
       d.ra = z1t;
-      d.b = {c0.ga + ((int64_t)(nts - 1) * ns + sp) * c0.sa, 1, 0, 1};
+      d.b = {c0.ga + ((int64_t)(nts - 1 - t0) * ns + sp) * c0.sa, 1, 0, 1};  // G1(beta - tau)
       d.bks = b1;
       d.rb = -(int64_t)ns * c0.sa;
       d.c = {tabc, 0, 0, 0};
@@ -1862,13 +1956,13 @@ void Engine::build_oz_lists() {
       d.aks = 1;
       d.N = b1;
       d.K = b1;
-      check_tab(taba, d.M, b1, z1t, half, z1_elems, "P0 stage Z (Z1 rows)");
-      check_tab(tabc, d.M, b1, zct, half, zcat_elems, "P0 stage Z (Zcat rows)");
-      oz_check(d, half, z1_elems, gsz, zcat_elems, "P0 stage Z");
-      add(d, half, REPG);
+      check_tab(taba, d.M, b1, z1t, ntc, z1_elems, "P0 stage Z (Z1 rows)");
+      check_tab(tabc, d.M, b1, zct, ntc, zcat_elems, "P0 stage Z (Zcat rows)");
+      oz_check(d, ntc, z1_elems, gsz, zcat_elems, "P0 stage Z");
+      add(d, ntc, REPG);
     }
     cur_stage = 1;
-    stage(oz_p0_, s0, OZB_Z1, OZB_GFF, OZB_ZCAT);
+    stage(oz_p0_, s0, OZB_Z1, OZB_G, OZB_ZCAT);
     std::vector<Fin> fins;
     for (int gi = ch.first; gi < ch.second; ++gi) {  // P0[Q][P] = sum_K Zcat[(tau,P)][K] Vcat[Q][K]
       const P0Group &g = p0_groups_[gi];
@@ -1880,11 +1974,11 @@ void Engine::build_oz_lists() {
       d.cn1 = g.qb;
       d.cnd = 1;
       d.aks = d.bks = 1;
-      d.M = half * g.qb;
+      d.M = ntc * g.qb;
       d.N = g.qb;
       d.K = pg[gi].zld;
       oz_check(d, 1, zcat_elems, oz_vcat_elems_, (int64_t)1 << 62, "P0 stage P0");
-      fins.push_back({d, g.pout, g.pstride, half, g.qb * g.qb});
+      fins.push_back({d, g.pout + (int64_t)t0 * g.pstride, g.pstride, ntc, g.qb * g.qb, half * g.qb});
     }
     cur_stage = 2;
     final_stage(oz_p0_, fins, OZB_ZCAT, OZB_VCAT, OZB_P0, pref, zcat_elems, oz_vcat_elems_, psz, "P0 stage P0");
@@ -1892,13 +1986,11 @@ void Engine::build_oz_lists() {
 
   // ---- Sigma ----------------------------------------------------------------
   // Bcat per P~ block group, columns in contribution order (so the columns of a
-  // chunk of AO-block owners are contiguous in every group)
-  std::vector<OzPerm> pb, psg;
-  struct SG { int64_t boff; int qb; };
+  // chunk of AO-block owners are contiguous in every group); chunk-local copies
+  struct SG { int qb, ncol; };
   std::vector<SG> sg;
   std::vector<int> cgroup(sc.size(), -1), ccol(sc.size(), 0);
   std::vector<std::vector<int>> gcs;  // contributions of each group (increasing)
-  int64_t boff = 0;
   for (const auto &grp : sig_groups_) {
     const std::vector<int> &cs = grp.second;
     const int qb = sc[cs[0]].qb;
@@ -1906,64 +1998,70 @@ void Engine::build_oz_lists() {
     for (int c : cs) {
       cgroup[c] = (int)sg.size();
       ccol[c] = ncol;
-      pb.push_back({sc[c].v, boff + (int64_t)ncol * qb, 1, (int64_t)sc[c].b2 * qb, qb, qb, sig_b1_[c], sc[c].b2, 1});
       ncol += sig_b1_[c] * sc[c].b2;
     }
-    sg.push_back({boff, qb});
+    sg.push_back({qb, ncol});
     gcs.push_back(cs);
-    boff += (int64_t)ncol * qb;
   }
-  oz_bcat_elems_ = boff;
   // AO-block owners (k_irr, i1): the owners of their spins share (c0, c1)
   std::vector<int> ucol(sc.size(), 0);
-  std::map<std::pair<int, int>, std::pair<int64_t, int>> vs;  // (c0, c1) -> (VcatS offset, uld)
-  std::vector<std::pair<int, int>> aoo;                       // distinct (c0, c1) in owner order
-  std::map<std::pair<int, int>, int> aoidx;                   // (c0, c1) -> index in aoo
-  int64_t vsoff = 0;
+  std::map<std::pair<int, int>, int> uldk;  // (c0, c1) -> row length of U and VcatS
+  std::vector<std::pair<int, int>> aoo;     // distinct (c0, c1) in owner order
+  std::map<std::pair<int, int>, int> aoidx; // (c0, c1) -> index in aoo
+  std::map<std::pair<int, int>, int> aon;   // (c0, c1) -> block size (rows of VcatS)
   for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {
     const Owner &o = sig_own_host_[oi];
     const auto key = std::make_pair(o.c0, o.c1);
-    if (vs.count(key)) continue;
+    if (uldk.count(key)) continue;
     int uld = 0;
     for (int c = o.c0; c < o.c1; ++c) {
       ucol[c] = uld;
       uld += sc[c].qb * sc[c].b2;
     }
-    vs[key] = {vsoff, uld};
+    uldk[key] = uld;
+    aon[key] = o.n;
     aoidx[key] = (int)aoo.size();
     aoo.push_back(key);
-    for (int c = o.c0; c < o.c1; ++c)
-      psg.push_back({sc[c].v, vsoff + ucol[c], sc[c].b2, uld, 1, sc[c].qb, sig_b1_[c], sc[c].b2, 0});
-    vsoff += (int64_t)o.n * uld;
   }
-  oz_vcats_elems_ = vsoff;
-  // chunks of AO-block owners: W and U of a chunk (all nts tau) within the budget
-  auto ao_need = [&](const std::pair<int, int> &key) {
+  // chunks of AO-block owners: W and U of a chunk (all nts tau) and its Bcat and
+  // VcatS within the budget
+  // An owner whose own need is above the budget gets chunks of its own over tau ranges.
+  auto ao_w = [&](const std::pair<int, int> &key) {
     int64_t w = 0;
     for (int c = key.first; c < key.second; ++c) w += (int64_t)sc[c].qb * sig_b1_[c] * sc[c].b2;
-    return (1 + ns) * w * nts;
+    return w;
   };
-  std::vector<std::pair<int, int>> schunks;  // ranges of aoo
+  auto ao_need = [&](const std::pair<int, int> &key, int nt) {  // W and U per tau, Bcat and VcatS once
+    const int64_t w = ao_w(key);
+    return (1 + ns) * w * nt + w + (int64_t)aon[key] * uldk[key];
+  };
+  std::vector<Chunk> schunks;  // ranges of aoo, tau ranges
   for (size_t a0 = 0; a0 < aoo.size();) {
-    size_t a1 = a0;
-    int64_t need = 0;
-    while (a1 < aoo.size()) {
-      const int64_t n = ao_need(aoo[a1]);
-      if (a1 > a0 && need + n > budget) break;
-      need += n;
-      ++a1;
+    if (ao_need(aoo[a0], nts) > budget) {
+      const int64_t per = (1 + ns) * ao_w(aoo[a0]), fixed = ao_need(aoo[a0], 0);
+      const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(nts, (budget - fixed) / per));
+      for (int t0 = 0; t0 < nts; t0 += nt) schunks.push_back({(int)a0, (int)a0 + 1, t0, std::min(nts, t0 + nt)});
+      ++a0;
+      continue;
     }
-    schunks.push_back({(int)a0, (int)a1});
+    size_t a1 = a0;
+    int64_t tot = 0;
+    while (a1 < aoo.size() && ao_need(aoo[a1], nts) <= budget && (a1 == a0 || tot + ao_need(aoo[a1], nts) <= budget))
+      tot += ao_need(aoo[a1++], nts);
+    schunks.push_back({(int)a0, (int)a1, 0, nts});
     a0 = a1;
   }
-  oz_w_elems_ = oz_u_elems_ = 1;
+  oz_w_elems_ = oz_u_elems_ = oz_bcat_elems_ = oz_vcats_elems_ = 1;
   for (const auto &ch : schunks) {
+    const int t0 = ch.t0, ntc = ch.t1 - ch.t0;                           // the chunk's tau range
     const int cA = aoo[ch.first].first, cB = aoo[ch.second - 1].second;  // contributions [cA, cB)
-    // W: per group, the chunk's columns (contiguous: contributions in [cA, cB))
-    struct WG { int g, col0, ncol; int64_t wc; };
+    // W: per group, the chunk's columns (contiguous: contributions in [cA, cB)); the
+    // chunk's Bcat holds those columns, group after group: Bcat[col][P] = conj(Vt_c[P][j][n])
+    struct WG { int g, col0, ncol; int64_t wc, boff; };
     std::vector<WG> wg;
     std::vector<int> wgi(sg.size(), -1);
-    int64_t wct = 0;
+    int64_t wct = 0, boff = 0;
+    const size_t pb0 = perms.size();
     for (size_t gi = 0; gi < sg.size(); ++gi) {
       int col0 = -1, ncol = 0;
       for (int c : gcs[gi])
@@ -1972,10 +2070,44 @@ void Engine::build_oz_lists() {
           ncol += sig_b1_[c] * sc[c].b2;
         }
       if (ncol == 0) continue;
+      const int qb = sg[gi].qb;
+      for (int c : gcs[gi])
+        if (c >= cA && c < cB)
+          perms.push_back({sc[c].v, boff + (int64_t)(ccol[c] - col0) * qb, 1, (int64_t)sc[c].b2 * qb, qb, qb,
+                           sig_b1_[c], sc[c].b2, 1});
       wgi[gi] = (int)wg.size();
-      wg.push_back({(int)gi, col0, ncol, wct});
-      wct += (int64_t)sg[gi].qb * ncol;
+      wg.push_back({(int)gi, col0, ncol, wct, boff});
+      wct += (int64_t)qb * ncol;
+      boff += (int64_t)qb * ncol;
     }
+    oz_bcat_elems_ = std::max(oz_bcat_elems_, boff);
+    for (size_t t = pb0; t < perms.size(); ++t) {
+      const OzPerm &x = perms[t];
+      check_range(x.src, (int64_t)x.X * x.Y * x.Z, (int64_t)Vt_.n, "sliced Bcat source");
+      check_range(x.dst, (x.X - 1) * x.dx + (x.Y - 1) * x.dy + (x.Z - 1) * x.dz + 1, boff, "sliced Bcat");
+    }
+    cur_stage = 3;
+    perm_launch(oz_sig_, pb0, OZB_VT, OZB_BCAT, schunks.size() == 1);
+    // VcatS of the chunk's owner blocks: VcatS[i][ucol + Q b2 + n] = Vt_c[Q][i][n]
+    const size_t ps0 = perms.size();
+    std::map<std::pair<int, int>, std::pair<int64_t, int>> vs;  // (c0, c1) -> (VcatS offset, uld)
+    int64_t vsoff = 0;
+    for (int ai = ch.first; ai < ch.second; ++ai) {
+      const auto key = aoo[ai];
+      const int uld = uldk[key];
+      vs[key] = {vsoff, uld};
+      for (int c = key.first; c < key.second; ++c)
+        perms.push_back({sc[c].v, vsoff + ucol[c], sc[c].b2, uld, 1, sc[c].qb, sig_b1_[c], sc[c].b2, 0});
+      vsoff += (int64_t)aon[key] * uld;
+    }
+    oz_vcats_elems_ = std::max(oz_vcats_elems_, vsoff);
+    for (size_t t = ps0; t < perms.size(); ++t) {
+      const OzPerm &x = perms[t];
+      check_range(x.src, (int64_t)x.X * x.Y * x.Z, (int64_t)Vt_.n, "sliced VcatS source");
+      check_range(x.dst, (x.X - 1) * x.dx + (x.Y - 1) * x.dy + (x.Z - 1) * x.dz + 1, vsoff, "sliced VcatS");
+    }
+    cur_stage = 5;
+    perm_launch(oz_sig_, ps0, OZB_VT, OZB_VCATS, schunks.size() == 1);
     // U: the chunk's owners (all spins)
     std::vector<int64_t> uoff(sig_own_host_.size(), -1);
     int64_t uct = 0;
@@ -1986,7 +2118,7 @@ void Engine::build_oz_lists() {
       uoff[oi] = uct;
       uct += (int64_t)o.n * vs[std::make_pair(o.c0, o.c1)].second;
     }
-    const int64_t w_elems = std::max<int64_t>(1, wct * nts), u_elems = std::max<int64_t>(1, uct * nts);
+    const int64_t w_elems = std::max<int64_t>(1, wct * ntc), u_elems = std::max<int64_t>(1, uct * ntc);
     oz_w_elems_ = std::max(oz_w_elems_, w_elems);
     oz_u_elems_ = std::max(oz_u_elems_, u_elems);
     size_t s0 = ts.size();
@@ -1994,23 +2126,21 @@ void Engine::build_oz_lists() {
       const SigContrib &c0 = sc[gcs[w.g][0]];
       const int qb = c0.qb;
       OzDesc d{};
-      d.a = {c0.pq, c0.pstride, qb, qb};
-      d.b = {sg[w.g].boff + (int64_t)w.col0 * qb, qb, 0, 1};
+      d.a = {c0.pq + (int64_t)t0 * c0.pstride, c0.pstride, qb, qb};  // P~ rows (tau, Q) of the tau range
+      d.b = {w.boff, qb, 0, 1};  // the chunk's Bcat columns of this group
       d.c = {w.wc, wct, w.ncol, qb};
       d.cn1 = 1;
       d.cnd = 1;
       d.aks = d.bks = 1;
-      d.M = nts * qb;
+      d.M = ntc * qb;
       d.N = w.ncol;
       d.K = qb;
       d.flags = c0.pconj ? OZ_CONJ_A : 0;
       oz_check(d, 1, psz, oz_bcat_elems_, w_elems, "Sigma stage W");
-      int gcols = 0;  // the group's full width (every chunk routes its part the same way)
-      for (int c : gcs[w.g]) gcols += sig_b1_[c] * sc[c].b2;
-      add(d, 1, 1, gcols);
+      add(d, 1, 1, sg[w.g].ncol);  // routed by the group's full width (every chunk the same way)
     }
     cur_stage = 3;
-    stage(oz_sig_, s0, OZB_PFF, OZB_BCAT, OZB_W);
+    stage(oz_sig_, s0, OZB_P, OZB_BCAT, OZB_W);
     s0 = ts.size();
     // U packs: (G2 block, spin) -> [(owner, contribution)]
     std::map<std::pair<int64_t, int>, std::vector<std::pair<int, int>>> up;
@@ -2044,7 +2174,7 @@ void Engine::build_oz_lists() {
       d.M = (int)(tabc - taba);
       d.a = {taba, 0, 0, 0};
       d.ra = wct;
-      d.b = {c0.gb + (int64_t)sp * c0.sb, b2, 0, 1};
+      d.b = {c0.gb + ((int64_t)t0 * ns + sp) * c0.sb, b2, 0, 1};  // G2(tau), tau from t0
       d.rb = (int64_t)ns * c0.sb;
       d.c = {tabc, 0, 0, 0};
       d.rc = uct;
@@ -2053,13 +2183,13 @@ void Engine::build_oz_lists() {
       d.aks = d.bks = 1;
       d.N = b2;
       d.K = b2;
-      check_tab(taba, d.M, b2, wct, nts, w_elems, "Sigma stage U (W rows)");
-      check_tab(tabc, d.M, b2, uct, nts, u_elems, "Sigma stage U (U rows)");
-      oz_check(d, nts, w_elems, gsz, u_elems, "Sigma stage U");
-      add(d, nts, REPG);
+      check_tab(taba, d.M, b2, wct, ntc, w_elems, "Sigma stage U (W rows)");
+      check_tab(tabc, d.M, b2, uct, ntc, u_elems, "Sigma stage U (U rows)");
+      oz_check(d, ntc, w_elems, gsz, u_elems, "Sigma stage U");
+      add(d, ntc, REPG);
     }
     cur_stage = 4;
-    stage(oz_sig_, s0, OZB_W, OZB_GFF, OZB_U);
+    stage(oz_sig_, s0, OZB_W, OZB_G, OZB_U);
     std::vector<Fin> fins;
     for (size_t oi = 0; oi < sig_own_host_.size(); ++oi) {  // Sigma[i][j] = sum_K U[(tau,j)][K] VcatS[i][K]
       if (uoff[oi] < 0) continue;
@@ -2073,38 +2203,34 @@ void Engine::build_oz_lists() {
       d.cn1 = o.n;
       d.cnd = 1;
       d.aks = d.bks = 1;
-      d.M = nts * o.n;
+      d.M = ntc * o.n;
       d.N = o.n;
       d.K = v.second;
       oz_check(d, 1, u_elems, oz_vcats_elems_, (int64_t)1 << 62, "Sigma stage Sigma");
-      fins.push_back({d, o.out, o.ostride, nts, o.n * o.n});
+      fins.push_back({d, o.out + (int64_t)t0 * o.ostride, o.ostride, ntc, o.n * o.n, nts * o.n});
     }
     cur_stage = 5;
     final_stage(oz_sig_, fins, OZB_U, OZB_VCATS, OZB_SIG, -1.0 / l.nk, u_elems, oz_vcats_elems_, ssz,
                 "Sigma stage Sigma");
   }
-  for (const OzPerm &t : pv) {
-    check_range(t.src, (int64_t)t.X * t.Y * t.Z, l.flat_V, "sliced Vcat source");
-    check_range(t.dst, (t.X - 1) * t.dx + (t.Y - 1) * t.dy + (t.Z - 1) * t.dz + 1, oz_vcat_elems_, "sliced Vcat");
-  }
-  for (const OzPerm &t : pb) {
-    check_range(t.src, (int64_t)t.X * t.Y * t.Z, (int64_t)Vt_.n, "sliced Bcat source");
-    check_range(t.dst, (t.X - 1) * t.dx + (t.Y - 1) * t.dy + (t.Z - 1) * t.dz + 1, oz_bcat_elems_, "sliced Bcat");
-  }
-  for (const OzPerm &t : psg) {
-    check_range(t.src, (int64_t)t.X * t.Y * t.Z, (int64_t)Vt_.n, "sliced Sigma Vcat source");
-    check_range(t.dst, (t.X - 1) * t.dx + (t.Y - 1) * t.dy + (t.Z - 1) * t.dz + 1, oz_vcats_elems_,
-                "sliced Sigma Vcat");
-  }
   GWGB_REQUIRE(ts.size() < (size_t)INT32_MAX, GWGB_E_UNSUPPORTED, "too many sliced GEMM tasks");
+  {
+    const int64_t lists = (int64_t)(ds.size() * sizeof(OzDesc) + ts.size() * sizeof(OzTask) + rt.size() * 8 +
+                                    perms.size() * sizeof(OzPerm) + red.size() * sizeof(RedTask));
+    size_t free_b = 0, total_b = 0;
+    GWGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    GWGB_REQUIRE(lists + (256ll << 20) <= (int64_t)free_b, GWGB_E_UNSUPPORTED,
+                 "sliced-precision work lists need " + std::to_string(lists >> 20) + " MB (row tables " +
+                     std::to_string((rt.size() * 8) >> 20) + " MB, tasks " +
+                     std::to_string((ts.size() * sizeof(OzTask)) >> 20) + " MB), " + std::to_string(free_b >> 20) +
+                     " MB free");
+  }
   oz_descs_.upload(ds, st_);
   oz_tasks_.upload(ts, st_);
   oz_rowtab_.upload(rt.empty() ? std::vector<int64_t>(1, 0) : rt, st_);
   for (const RedTask &r : red) check_range(r.part, (int64_t)r.nslice * r.nt * r.elems, oz_part_elems_, "sliced partials");
   oz_red_.upload(red.empty() ? std::vector<RedTask>(1, RedTask{}) : red, st_);
-  oz_perm_v_.upload(pv, st_);
-  oz_perm_b_.upload(pb, st_);
-  oz_perm_s_.upload(psg, st_);
+  oz_perm_.upload(perms.empty() ? std::vector<OzPerm>(1, OzPerm{}) : perms, st_);
   GWGB_CUDA(cudaStreamSynchronize(st_));
   lt_build();
   oz_built_ = true;
