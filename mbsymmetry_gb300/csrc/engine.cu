@@ -509,7 +509,7 @@ class Engine {
         g.tasks = (int32_t)x.n;
         g.flops = x.flops;
         g.mma_flops = x.ops;
-        g.bytes = x.red_bytes;
+        g.bytes = x.perm ? x.red_bytes : 0.0;
         lt_info_.push_back(g);
         if (x.nr && !x.perm) {
           gwgb_launch_stat r{};
@@ -1794,6 +1794,22 @@ void Engine::build_oz_lists() {
     const int64_t by_free = std::max<int64_t>(64ll << 20, (int64_t)(free_b / 12));
     budget = std::max<int64_t>(1, std::min<int64_t>(tc_chunk_bytes_, by_free) / 16);
   }
+  // The concatenated operands of every chunk are kept (built once per upload) when
+  // together they take at most a quarter of the free memory; otherwise each chunk
+  // builds its own in the launch list.
+  bool persist;
+  {
+    int64_t tot = 0;
+    for (size_t gi = 0; gi < p0_groups_.size(); ++gi) tot += 2 * (int64_t)p0_groups_[gi].qb * pg[gi].zld;
+    for (const SigContrib &x : sc) tot += 2 * (int64_t)x.qb * x.b2 * 64;  // Bcat + VcatS, AO blocks <= 64
+    size_t free_b = 0, total_b = 0;
+    GWGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    persist = tot * 16 <= (int64_t)(free_b / 4);
+  }
+  int64_t vcat_base = 0, vz_base = 0, bcat_base = 0, vcats_base = 0;  // persistent: each chunk's offset
+  // persistent: where a block's operand copy already is (tau chunks of one block share it)
+  std::vector<int64_t> vcat_at(p0_groups_.size(), -1), vz_at(pc.size(), -1);
+  std::map<std::pair<int, int>, int64_t> bcat_at, vcats_at;
   // A group whose own need is above the budget gets chunks of its own over tau ranges.
   struct Chunk { int first, second, t0, t1; };  // output blocks [first, second), tau [t0, t1)
   std::vector<Chunk> pchunks;
@@ -1823,10 +1839,15 @@ void Engine::build_oz_lists() {
     const int t0 = ch.t0, ntc = ch.t1 - ch.t0;  // the chunk's tau range
     {  // Vcat of the chunk's groups: Vcat[Q][zcol + m b1 + p] = V_c[Q][p][m]
       const size_t p0 = perms.size();
-      int64_t voff = 0;
+      int64_t voff = persist ? vcat_base : 0;
       for (int gi = ch.first; gi < ch.second; ++gi) {
         const P0Group &g = p0_groups_[gi];
+        if (persist && vcat_at[gi] >= 0) {
+          pg[gi].voff = vcat_at[gi];
+          continue;
+        }
         pg[gi].voff = voff;
+        vcat_at[gi] = voff;
         for (int c = g.c0; c < g.c1; ++c)
           for (int sp = 0; sp < ns; ++sp)
             perms.push_back({pc[c].v, voff + zcol[c * ns + sp], pg[gi].zld, 1, pc[c].b1, g.qb, pc[c].b1, pc[c].b2, 0});
@@ -1838,25 +1859,31 @@ void Engine::build_oz_lists() {
         check_range(x.src, (int64_t)x.X * x.Y * x.Z, l.flat_V, "sliced Vcat source");
         check_range(x.dst, (x.X - 1) * x.dx + (x.Y - 1) * x.dy + (x.Z - 1) * x.dz + 1, voff, "sliced Vcat");
       }
+      if (persist) vcat_base = voff;
       cur_stage = 2;
-      perm_launch(oz_p0_, p0, OZB_V, OZB_VCAT, pchunks.size() == 1);
+      perm_launch(oz_p0_, p0, OZB_V, OZB_VCAT, persist || pchunks.size() == 1);
     }
     std::vector<int64_t> vz(pc.size(), -1);  // the chunk's V blocks in float-float (the Z1 stage's A rows)
-    int64_t vz_elems = 0;
+    int64_t vz_elems = persist ? vz_base : 0;
     {
       const size_t p0 = perms.size();
       int64_t &off = vz_elems;
       for (int gi = ch.first; gi < ch.second; ++gi)
         for (int c = p0_groups_[gi].c0; c < p0_groups_[gi].c1; ++c) {
           const int qb = p0_groups_[gi].qb, b1 = pc[c].b1, b2 = pc[c].b2;
-          vz[c] = off;
+          if (persist && vz_at[c] >= 0) {
+            vz[c] = vz_at[c];
+            continue;
+          }
+          vz[c] = vz_at[c] = off;
           perms.push_back({pc[c].v, off, (int64_t)b1 * b2, b2, 1, qb, b1, b2, 0});
           check_range(pc[c].v, (int64_t)qb * b1 * b2, l.flat_V, "sliced V block source");
           off += (int64_t)qb * b1 * b2;
         }
       oz_vz_elems_ = std::max(oz_vz_elems_, off);
+      if (persist) vz_base = off;
       cur_stage = 0;
-      perm_launch(oz_p0_, p0, OZB_V, OZB_VZ, pchunks.size() == 1);
+      perm_launch(oz_p0_, p0, OZB_V, OZB_VZ, persist || pchunks.size() == 1);
     }
     // chunk-local per-tau layouts
     std::vector<int64_t> zc(p0_groups_.size(), 0);
@@ -2060,7 +2087,7 @@ void Engine::build_oz_lists() {
     struct WG { int g, col0, ncol; int64_t wc, boff; };
     std::vector<WG> wg;
     std::vector<int> wgi(sg.size(), -1);
-    int64_t wct = 0, boff = 0;
+    int64_t wct = 0, boff = persist ? bcat_base : 0;
     const size_t pb0 = perms.size();
     for (size_t gi = 0; gi < sg.size(); ++gi) {
       int col0 = -1, ncol = 0;
@@ -2071,14 +2098,21 @@ void Engine::build_oz_lists() {
         }
       if (ncol == 0) continue;
       const int qb = sg[gi].qb;
-      for (int c : gcs[gi])
-        if (c >= cA && c < cB)
-          perms.push_back({sc[c].v, boff + (int64_t)(ccol[c] - col0) * qb, 1, (int64_t)sc[c].b2 * qb, qb, qb,
-                           sig_b1_[c], sc[c].b2, 1});
+      int64_t at = boff;
+      auto hit = bcat_at.find({(int)gi, cA});
+      if (persist && hit != bcat_at.end()) {
+        at = hit->second;
+      } else {
+        for (int c : gcs[gi])
+          if (c >= cA && c < cB)
+            perms.push_back({sc[c].v, boff + (int64_t)(ccol[c] - col0) * qb, 1, (int64_t)sc[c].b2 * qb, qb, qb,
+                             sig_b1_[c], sc[c].b2, 1});
+        bcat_at[{(int)gi, cA}] = boff;
+        boff += (int64_t)qb * ncol;
+      }
       wgi[gi] = (int)wg.size();
-      wg.push_back({(int)gi, col0, ncol, wct, boff});
+      wg.push_back({(int)gi, col0, ncol, wct, at});
       wct += (int64_t)qb * ncol;
-      boff += (int64_t)qb * ncol;
     }
     oz_bcat_elems_ = std::max(oz_bcat_elems_, boff);
     for (size_t t = pb0; t < perms.size(); ++t) {
@@ -2086,16 +2120,23 @@ void Engine::build_oz_lists() {
       check_range(x.src, (int64_t)x.X * x.Y * x.Z, (int64_t)Vt_.n, "sliced Bcat source");
       check_range(x.dst, (x.X - 1) * x.dx + (x.Y - 1) * x.dy + (x.Z - 1) * x.dz + 1, boff, "sliced Bcat");
     }
+    if (persist) bcat_base = boff;
     cur_stage = 3;
-    perm_launch(oz_sig_, pb0, OZB_VT, OZB_BCAT, schunks.size() == 1);
+    perm_launch(oz_sig_, pb0, OZB_VT, OZB_BCAT, persist || schunks.size() == 1);
     // VcatS of the chunk's owner blocks: VcatS[i][ucol + Q b2 + n] = Vt_c[Q][i][n]
     const size_t ps0 = perms.size();
     std::map<std::pair<int, int>, std::pair<int64_t, int>> vs;  // (c0, c1) -> (VcatS offset, uld)
-    int64_t vsoff = 0;
+    int64_t vsoff = persist ? vcats_base : 0;
     for (int ai = ch.first; ai < ch.second; ++ai) {
       const auto key = aoo[ai];
       const int uld = uldk[key];
+      auto hit = vcats_at.find(key);
+      if (persist && hit != vcats_at.end()) {
+        vs[key] = {hit->second, uld};
+        continue;
+      }
       vs[key] = {vsoff, uld};
+      vcats_at[key] = vsoff;
       for (int c = key.first; c < key.second; ++c)
         perms.push_back({sc[c].v, vsoff + ucol[c], sc[c].b2, uld, 1, sc[c].qb, sig_b1_[c], sc[c].b2, 0});
       vsoff += (int64_t)aon[key] * uld;
@@ -2106,8 +2147,9 @@ void Engine::build_oz_lists() {
       check_range(x.src, (int64_t)x.X * x.Y * x.Z, (int64_t)Vt_.n, "sliced VcatS source");
       check_range(x.dst, (x.X - 1) * x.dx + (x.Y - 1) * x.dy + (x.Z - 1) * x.dz + 1, vsoff, "sliced VcatS");
     }
+    if (persist) vcats_base = vsoff;
     cur_stage = 5;
-    perm_launch(oz_sig_, ps0, OZB_VT, OZB_VCATS, schunks.size() == 1);
+    perm_launch(oz_sig_, ps0, OZB_VT, OZB_VCATS, persist || schunks.size() == 1);
     // U: the chunk's owners (all spins)
     std::vector<int64_t> uoff(sig_own_host_.size(), -1);
     int64_t uct = 0;
