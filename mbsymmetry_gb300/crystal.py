@@ -287,8 +287,9 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
     AO and aux block sizes of every star from the O_h irreps at its
     representative k (:mod:`symmetry`: d blocks of size m per irrep of
     dimension d and multiplicity m, for spec.atoms atoms with s/p/d shells)
-    instead of drawing them in the spec's ranges; block labels and the V
-    selection rule stay the labelled ones.  ``symmetric=True`` builds
+    instead of drawing them in the spec's ranges (hex: from P6_3mc on the four
+    wurtzite sites, with its projective representations); block labels and
+    the V selection rule stay the labelled ones.  ``symmetric=True`` builds
     group-consistent data (module docstring); the same V, and F in the same
     bases, with ``rotate`` True or False."""
     if symmetric and spec.lattice != "fcc":
@@ -312,14 +313,17 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
     ao_sizes_star, ao_labels_star, aux_sizes_star, aux_labels_star = {}, {}, {}, {}
     phys = None
     if physical:
-        if spec.lattice != "fcc":
-            raise ValueError("physical block sizes are built for the fcc (O_h) crystals only")
         from . import symmetry
-        Bt = np.linalg.inv(0.5 * np.array([[0, 1, 1], [1, 0, 1], [1, 1, 0]], dtype=float))
-        ops_c = symmetry.oh_operations()
-        bao, baux = symmetry.fcc_basis(spec.nao, spec.atoms), symmetry.fcc_basis(spec.naux, spec.atoms)
-        phys = {s: (np.array(symmetry.block_sizes(Bt @ kmesh[k], bao, ops_c)),
-                    np.array(symmetry.block_sizes(Bt @ kmesh[k], baux, ops_c))) for s, k in enumerate(reps)}
+        if spec.lattice == "fcc":
+            Bt = np.linalg.inv(0.5 * np.array([[0, 1, 1], [1, 0, 1], [1, 1, 0]], dtype=float))
+            ops_c = symmetry.oh_operations()
+            bao, baux = symmetry.fcc_basis(spec.nao, spec.atoms), symmetry.fcc_basis(spec.naux, spec.atoms)
+            phys = {s: (np.array(symmetry.block_sizes(Bt @ kmesh[k], bao, ops_c)),
+                        np.array(symmetry.block_sizes(Bt @ kmesh[k], baux, ops_c))) for s, k in enumerate(reps)}
+        else:  # wurtzite, P6_3mc: projective representations at the zone boundary
+            bao, baux = symmetry.wurtzite_basis(spec.nao), symmetry.wurtzite_basis(spec.naux)
+            phys = {s: (np.array(symmetry.sg_block_sizes(kmesh[k], bao)),
+                        np.array(symmetry.sg_block_sizes(kmesh[k], baux))) for s, k in enumerate(reps)}
     for s, k in enumerate(reps):
         g = little[s]
         shrink = 1.0 / np.sqrt(max(1.0, g / 2.0))

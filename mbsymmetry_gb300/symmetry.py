@@ -1,5 +1,6 @@
 """Irrep block sizes from the space group: the physical counterpart of the
-labelled-block generator in crystal.py, for symmorphic cubic crystals.
+labelled-block generator in crystal.py, for the symmorphic cubic crystals
+(O_h) and the non-symmorphic wurtzite structure (P6_3mc).
 
 SymmetryAdaptation (the reference's offline tool,
 ``SymmetryAdaptation/src/dirac_character.cpp:7-126``,
@@ -21,8 +22,18 @@ for the Fm-3m point group O_h on an FCC lattice:
 
 An irrep Gamma of dimension d with multiplicity m contributes d blocks of
 size m (the rows of Gamma), which is how the flat layout lists them.
-Non-symmorphic groups (P6_3mc) would need projective representations at the
-zone boundary and are not covered.
+
+Non-symmorphic groups (P6_3mc, the wurtzite structure of config C4): the
+operations are {R | t} with fractional translations t (the 6_3 screw axis and
+the c glides), and on Bloch sums at k the operations of the little group form
+a projective representation of the little co-group (the factor system
+exp(-i k . (R_g t_h + t_g - t_gh)) is non-trivial at the zone boundary, where
+every irrep of P6_3mc at A is two-dimensional).  ``projective_content``
+decomposes any unitary (projective) representation without classes: the
+average over the group of D(h) A D(h)^H for a random A in the span of the D(g)
+is central, its eigenspaces are the isotypic components, and the average of
+D(h) X D(h)^H for a random Hermitian X acts on a component as I_d x M_m, so its
+eigenvalues there come in m distinct values of multiplicity d.
 """
 from __future__ import annotations
 
@@ -215,3 +226,127 @@ def fcc_basis(count: int, atoms: int) -> Basis:
         return Basis(np.array([[0, 0, 0], [0.5, 0.5, 0.5], [0.25, 0.25, 0.25], [0.75, 0.75, 0.75]]),
                      [shells_for(a), shells_for(r - a), shells_for(c), shells_for(c)])
     raise ValueError("2 or 4 atoms")
+
+
+# --------------------------------------------------------------------------- #
+# non-symmorphic: P6_3mc (wurtzite)
+# --------------------------------------------------------------------------- #
+HEX_C = 1.633  # ideal c/a
+HEX_A = np.array([[1.0, -0.5, 0.0], [0.0, np.sqrt(3.0) / 2.0, 0.0], [0.0, 0.0, HEX_C]])  # columns: a1, a2, a3
+
+# The 12 operations of P6_3mc (International Tables No. 186) as coordinate
+# triplets in the hexagonal setting, with the translation along c (in units of
+# c): the 6_3 and 2_1 screw rotations and one class of mirrors carry c/2 (c
+# glides), in the origin where the wurtzite sites are (1/3, 2/3, z) and
+# (2/3, 1/3, z + 1/2) (Wyckoff 2b); tests check that every operation maps
+# the structure onto itself.
+_P63MC = [("x", "y", "z", 0.0), ("-y", "x-y", "z", 0.0), ("-x+y", "-x", "z", 0.0), ("-x", "-y", "z", 0.5),
+          ("y", "-x+y", "z", 0.5), ("x-y", "x", "z", 0.5), ("y", "x", "z", 0.5), ("x-y", "-y", "z", 0.5),
+          ("-x", "-x+y", "z", 0.5), ("-y", "-x", "z", 0.0), ("-x+y", "y", "z", 0.0), ("x", "x-y", "z", 0.0)]
+
+
+def _triplet_row(expr: str) -> np.ndarray:
+    row, sign = np.zeros(3, dtype=int), 1
+    for ch in expr:
+        if ch in "+-":
+            sign = 1 if ch == "+" else -1
+        else:
+            row["xyz".index(ch)] += sign
+            sign = 1
+    return row
+
+
+def p63mc_operations() -> List[Tuple[np.ndarray, np.ndarray]]:
+    """(M, t): x -> M x + t on fractional coordinates of the hexagonal lattice."""
+    return [(np.array([_triplet_row(a), _triplet_row(b), _triplet_row(c)]), np.array([0.0, 0.0, tz]))
+            for a, b, c, tz in _P63MC]
+
+
+def wurtzite_basis(count: int, u: float = 0.375) -> Basis:
+    """`count` functions on the four wurtzite sites (fractional coordinates): species
+    A at (1/3, 2/3, 0) and (2/3, 1/3, 1/2), species B at the same raised by u c;
+    the two sites of a species share a shell list (B gets the smaller half)."""
+    a = (count + 1) // 2
+    a -= a % 2 if (count - a) % 2 else 0
+    half_a, half_b = a // 2, (count - a) // 2
+    if 2 * half_a + 2 * half_b != count:
+        half_a = (count - 2 * (count // 4)) // 2
+        half_b = count // 4
+    pos = np.array([[1 / 3, 2 / 3, 0.0], [2 / 3, 1 / 3, 0.5], [1 / 3, 2 / 3, u], [2 / 3, 1 / 3, 0.5 + u]])
+    sa, sb = shells_for(half_a), shells_for(half_b)
+    return Basis(pos, [sa, sa, sb, sb])
+
+
+def sg_little_group(k_frac: np.ndarray, ops) -> list:
+    """Space-group operations whose rotation maps k (reduced reciprocal coordinates)
+    onto itself modulo a reciprocal lattice vector."""
+    out = []
+    for M, t in ops:
+        d = np.linalg.inv(M).T @ k_frac - k_frac
+        if np.allclose(d, np.round(d), atol=1e-9):
+            out.append((M, t))
+    return out
+
+
+def sg_bloch_representation(k_frac: np.ndarray, M: np.ndarray, t: np.ndarray, basis: Basis,
+                            A: np.ndarray = HEX_A) -> np.ndarray:
+    """D({M|t}) on the Bloch sums at k (reduced reciprocal coordinates; positions and
+    t fractional): atom a goes to M tau_a + t = tau_b + T, phase exp(-2 pi i (M k) . T),
+    shells rotated by the Cartesian R = A M A^-1."""
+    n = basis.size
+    D = np.zeros((n, n), dtype=complex)
+    offs = np.cumsum([0] + [sum(2 * l + 1 for l in sh) for sh in basis.shells])
+    R = A @ M @ np.linalg.inv(A)
+    kR = np.linalg.inv(M).T @ k_frac
+    pos = np.asarray(basis.positions, dtype=float)
+    for a in range(len(pos)):
+        ra = M @ pos[a] + t
+        b = next(b for b in range(len(pos)) if np.allclose(ra - pos[b], np.round(ra - pos[b]), atol=1e-9))
+        if list(basis.shells[a]) != list(basis.shells[b]):
+            raise ValueError("an operation maps atoms with different shells onto each other")
+        T = np.round(ra - pos[b])
+        phase = np.exp(-2j * np.pi * kR @ T)
+        oa, ob = offs[a], offs[b]
+        for l in basis.shells[a]:
+            w = 2 * l + 1
+            D[ob:ob + w, oa:oa + w] = phase * shell_matrix(l, R)
+            oa += w
+            ob += w
+    return D
+
+
+def projective_content(Ds: List[np.ndarray], seed: int = 0) -> List[Tuple[int, int]]:
+    """[(irrep dimension d, multiplicity m)] of a unitary, possibly projective,
+    representation given by its matrices on the (little) group."""
+    rng = np.random.default_rng(seed)
+    G = len(Ds)
+    n = Ds[0].shape[0]
+    A = sum((rng.standard_normal() + 1j * rng.standard_normal()) * D for D in Ds)
+    C = sum(D @ A @ D.conj().T for D in Ds) / G
+    X = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    X = X + X.conj().T
+    Y = sum(D @ X @ D.conj().T for D in Ds) / G
+    w, V = np.linalg.eig(C)
+    scale = max(1.0, np.abs(w).max())
+    out, used = [], np.zeros(n, dtype=bool)
+    for i in range(n):
+        if used[i]:
+            continue
+        grp = np.where(~used & (np.abs(w - w[i]) < 1e-7 * scale))[0]
+        used[grp] = True
+        Q, _ = np.linalg.qr(V[:, grp])
+        y = np.sort(np.linalg.eigvalsh(Q.conj().T @ Y @ Q))
+        ys = max(1.0, np.abs(y).max())
+        m = 1 + int(np.sum(np.diff(y) > 1e-7 * ys))
+        if len(grp) % m:
+            raise RuntimeError("inconsistent isotypic component")
+        out.append((len(grp) // m, m))
+    return sorted(out)
+
+
+def sg_block_sizes(k_frac: np.ndarray, basis: Basis, ops=None, A: np.ndarray = HEX_A) -> List[int]:
+    """Block sizes at k from the space group (default P6_3mc): d blocks of size m per irrep."""
+    ops = p63mc_operations() if ops is None else ops
+    G = sg_little_group(np.asarray(k_frac, dtype=float), ops)
+    Ds = [sg_bloch_representation(np.asarray(k_frac, dtype=float), M, t, basis, A) for M, t in G]
+    return [m for d, m in projective_content(Ds) for _ in range(d)]
