@@ -274,7 +274,13 @@ class Engine {
     if (prec != prec_) drop_graphs();  // the captured graphs hold the old kernels
     prec_ = prec;
     if (prec_ == GWGB_PREC_OZAKI) {
-      if (!oz_built_) build_oz_lists();
+      if (!oz_built_) {  // the largest chunks whose buffers fit: budget 1/4, 1/8, ... of the free memory
+        oz_div_ = 4;
+        while (!build_oz_lists()) {
+          GWGB_REQUIRE(oz_div_ < 256, GWGB_E_UNSUPPORTED, "the sliced-precision buffers do not fit the device memory");
+          oz_div_ *= 2;
+        }
+      }
       if (!ozVcat_.p) {
         {  // the sliced path's buffers must fit the free memory: say which take it otherwise
           const std::pair<const char *, int64_t> need[] = {
@@ -575,7 +581,11 @@ class Engine {
   std::vector<P0Contrib> pc_host_;
   std::vector<SigContrib> sc_host_;
   std::vector<Owner> sig_own_host_;
-  void build_oz_lists();
+  // Builds the lists with a chunk budget of 1/oz_div_ of the free memory; false
+  // (nothing uploaded) when the buffers would take more than 85% of it.
+  bool build_oz_lists();
+  int oz_div_ = 4;
+  bool tc_chunk_env_ = false;  // GWGB_TC_CHUNK_MB given: it caps the sliced path's chunks too
   const void *oz_ptr(int id) const {
     switch (id) {
       case OZB_G: return Gff_.p;
@@ -745,6 +755,7 @@ Engine::Engine(const gwgb_params &p, const gwgb_layout &L) {
     const long long mb = std::atoll(e);
     GWGB_REQUIRE(mb >= 1, GWGB_E_INVALID, "GWGB_TC_CHUNK_MB must be a positive integer");
     tc_chunk_bytes_ = (int64_t)mb << 20;
+    tc_chunk_env_ = true;
   }
   build_work_lists();
   if (p.precision != GWGB_PREC_FP64) set_precision(p.precision);
@@ -1608,19 +1619,20 @@ void oz_check(const OzDesc &d, int nrep, int64_t na, int64_t nb, int64_t nc, con
 
 }  // namespace
 
-void Engine::build_oz_lists() {
+bool Engine::build_oz_lists() {
   // Layouts (float-float, complex elements).  The contractions run in chunks of
   // output blocks (P0: output blocks (q_irr, iq); Sigma: AO blocks (k_irr, i1)
-  // with their spins), each chunk over ALL tau, so the final GEMMs (P0, Sigma)
-  // get full 128-row tiles of (tau, row); a chunk's tau-dependent buffers are
+  // with their spins), each chunk over all tau (a block whose own buffers exceed
+  // the budget: over tau ranges), so the final GEMMs (P0, Sigma) get full
+  // 128-row tiles of (tau, row); a chunk's tau-dependent buffers are
   // sequences of tau slabs with one stride (z1t, zct, wct, uct elements per
   // tau), so one repetition offset serves every row of a packed GEMM.
   //   Z1[tau][pack][m][row]      row = (c, P, t) of the contributions sharing G2's block
   //   Zcat[tau][group][P][K]     K = (c, s, m, p) of the P0 output block (q_irr, iq)
-  //   Vcat[group][Q][K]          = V_c[Q][p][m] at the same K (all groups, once per upload)
+  //   Vcat[group][Q][K]          = V_c[Q][p][m] at the same K (per chunk, or all chunks once per upload)
   //   W[tau][group][Q][col]      col = (c, j, n) of the chunk's contributions in the P~ block group
   //   U[tau][owner][j][K]        K = (c, Q, m) of the Sigma owner (k_irr, i1, s)
-  //   VcatS[owner][i][K]         = Vt_c[Q][i][m] at the same K (all owners, once per upload)
+  //   VcatS[owner][i][K]         = Vt_c[Q][i][m] at the same K (per chunk, or all chunks once per upload)
   // Per-tau stages (Z1, Z, U) pack the chunk's contributions that share their
   // G-block operand (same block and spin) into one GEMM with a row table.
   const Lay &l = l_;
@@ -1784,15 +1796,15 @@ void Engine::build_oz_lists() {
     pg.push_back({0, zld});
   }
   // chunks of output blocks: Z1, Zcat, Vcat and V blocks of a chunk (all nts/2 tau) within
-  // the budget.  Every buffer of a stage is sized to its largest chunk and the P0 and
-  // Sigma buffers coexist, so the budget is a twelfth of the memory free now (after
-  // V), at most the handle's chunk size (GWGB_TC_CHUNK_MB) and at least 64 MB.
+  // the budget: 1/oz_div_ of the memory free now (after V), at most GWGB_TC_CHUNK_MB
+  // when that is given, at least 64 MB.  Every buffer is sized to its largest chunk and
+  // the P0 and Sigma buffers coexist; the caller halves the budget until they fit.
   int64_t budget;  // complex float-float elements
   {
     size_t free_b = 0, total_b = 0;
     GWGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const int64_t by_free = std::max<int64_t>(64ll << 20, (int64_t)(free_b / 12));
-    budget = std::max<int64_t>(1, std::min<int64_t>(tc_chunk_bytes_, by_free) / 16);
+    const int64_t by_free = std::max<int64_t>(64ll << 20, (int64_t)(free_b / oz_div_));
+    budget = std::max<int64_t>(1, (tc_chunk_env_ ? std::min<int64_t>(tc_chunk_bytes_, by_free) : by_free) / 16);
   }
   // The concatenated operands of every chunk are kept (built once per upload) when
   // together they take at most a quarter of the free memory; otherwise each chunk
@@ -2256,6 +2268,15 @@ void Engine::build_oz_lists() {
                 "Sigma stage Sigma");
   }
   GWGB_REQUIRE(ts.size() < (size_t)INT32_MAX, GWGB_E_UNSUPPORTED, "too many sliced GEMM tasks");
+  {  // buffers and lists within 85% of the free memory, or a smaller budget
+    const int64_t bufs = 16 * (oz_z1_elems_ + oz_zcat_elems_ + oz_w_elems_ + oz_u_elems_ + oz_vcat_elems_ +
+                               oz_bcat_elems_ + oz_vcats_elems_ + oz_vz_elems_ + oz_part_elems_ +
+                               (int64_t)(Gall_.n + Pall_.n)) +
+                         (int64_t)(ds.size() * sizeof(OzDesc) + ts.size() * sizeof(OzTask) + rt.size() * 8);
+    size_t free_b = 0, total_b = 0;
+    GWGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (bufs > (int64_t)(0.85 * (double)free_b) && oz_div_ < 256) return false;
+  }
   {
     const int64_t lists = (int64_t)(ds.size() * sizeof(OzDesc) + ts.size() * sizeof(OzTask) + rt.size() * 8 +
                                     perms.size() * sizeof(OzPerm) + red.size() * sizeof(RedTask));
@@ -2276,6 +2297,7 @@ void Engine::build_oz_lists() {
   GWGB_CUDA(cudaStreamSynchronize(st_));
   lt_build();
   oz_built_ = true;
+  return true;
 }
 
 // ---------------------------------------------------------------------------
