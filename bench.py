@@ -418,6 +418,9 @@ def run_gpu(args):
     roofline = _kernel_roofline(kern, peaks, OZ_TRAFFIC)
     roofline["kernels"] = kern
     roofline["stages_ms"] = {k: v["ms"] for k, v in lstages.items()}
+    # the same figures for every sliced-path kernel (the tcgen05 one beside the dominant one)
+    roofline["per_kernel"] = {n: {k: v for k, v in _kernel_roofline({n: kern[n]}, peaks, OZ_TRAFFIC).items()
+                                  if k not in ("achieved_note", "peak_source")} for n in kern}
     dom64 = "sigma" if st64["sigma_ms"] >= st64["p0_ms"] else "p0"
     a64 = s64[f"{dom64}_flops"] / (st64[f"{dom64}_ms"] * 1e-3) / 1e12
     fp64 = {"precision": PREC_LABEL["fp64"], "s_per_iteration": ms64 / 1e3, "stages_ms": st64,
