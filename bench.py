@@ -7,8 +7,8 @@ iteration P0 -> P~ (W~ solve) -> Sigma -> Dyson with all tau <-> i omega
 transforms, replayed as one CUDA graph, with the P0 and Sigma contractions on
 the sliced split-precision path (BF16 fixed-point slices on tcgen05, Sigma
 within 1e-7 Ha of FP64: the error is measured and reported in the line); the
-FP64 drop-in, the FP32-class split paths, a C4 mixed-vs-FP64 block and the
-self-consistent loop are reported beside it.
+FP64 drop-in, the FP32-class split paths, C3 and C4 mixed-vs-FP64 blocks and
+the self-consistent loop are reported beside it.
 
   value  device time of the iteration (CUDA events recorded on the engine's
          stream), inputs resident in HBM, L2 flushed before every iteration.
@@ -306,14 +306,21 @@ def _kernel_roofline(kern, peaks, traffic):
             "frac": gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None, "traffic": traffic.get(name)}
 
 
-def _c4_block(dev, warmup):
-    """Mixed vs FP64 on the uneven-block crystal C4 (P6_3mc-like hexagonal 4x4x3,
-    nao=72, naux=350, nts=120, beta=200; blocks 2-30): one timed iteration each
+CONFIG_BLOCKS = {
+    "C3": "C3 (the mixed-precision config): Fm-3m 4x4x4 k mesh (64 k, 8 irreducible), nao=52, naux=250, nts=120, "
+          "beta=100, irrep blocks 2-16 (AO) / 4-64 (aux), V for all k pairs (12.2 GB)",
+    "C4": "C4: hexagonal 4x4x3 k mesh (48 k, 8 irreducible), nao=72, naux=350, nts=120, beta=200, irrep blocks "
+          "2-30, V for all k pairs",
+}
+
+
+def _config_block(name, dev, warmup):
+    """Mixed vs FP64 on a larger crystal (C3, C4): one timed iteration each
     after warm-up, Sigma and G error of the sliced path against FP64."""
     from mbsymmetry_gb300.crystal import CONFIGS, load_ir, make_crystal
     from mbsymmetry_gb300.solver import GWSolver
     from mbsymmetry_gb300.transformer import build_transforms
-    spec = CONFIGS["C4"]
+    spec = CONFIGS[name]
     cr = make_crystal(spec)
     tr = build_transforms(load_ir(spec.nts), spec.beta)
     s = GWSolver(cr.layout, cr.ns, tr, device=dev)
@@ -322,8 +329,7 @@ def _c4_block(dev, warmup):
     s.set_Selfenergy(np.zeros(s.g_size, np.complex128))
     s.dyson(cr.mu)
     G0 = s.G_tau()
-    out, res = {"workload": "C4: hexagonal 4x4x3 k mesh (48 k, 8 irreducible), nao=72, naux=350, nts=120, "
-                            "beta=200, irrep blocks 2-30, V for all k pairs"}, {}
+    out, res = {"workload": CONFIG_BLOCKS[name]}, {}
     for prec in ("fp64", "ozaki"):
         s.single_prec_run(prec != "fp64", prec)
         for _ in range(1 + (prec != "fp64") * max(0, min(warmup, 1))):
@@ -495,7 +501,7 @@ def run_gpu(args):
     sc["final_sigma_max_abs_diff"] = float(np.abs(finals["fp64"][0] - finals["ozaki"][0]).max())
     sc["speedup"] = sc["fp64"]["s_per_iteration"] / sc["ozaki"]["s_per_iteration"]
     s.close()
-    c4 = None if args.no_c4 or world > 1 else _c4_block(dev, args.warmup)
+    big = {} if args.no_c4 or world > 1 else {n: _config_block(n, dev, args.warmup) for n in ("C3", "C4")}
 
     line = {
         "metric": METRIC, "value": reps.seconds_per_iteration(ms), "unit": "s", "n_gpus": world,
@@ -519,7 +525,8 @@ def run_gpu(args):
         "fp64": fp64,
         "split_tf32x3": split_tf32,
         "split_bf16x3": split_bf16,
-        "c4_mixed_vs_fp64": c4,
+        "c3_mixed_vs_fp64": big.get("C3"),
+        "c4_mixed_vs_fp64": big.get("C4"),
         "reference_gpu_proxy": proxy,
         "autotune": {"precision": "ozaki", "metric": tune["metric"], "best": tune["best"],
                      "default": _autotune.OZAKI_CANDIDATES[0], "trials": tune["trials"]},
@@ -569,7 +576,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-c4", action="store_true", help="skip the C4 mixed-vs-FP64 block")
+    ap.add_argument("--no-c4", action="store_true", help="skip the C3 and C4 mixed-vs-FP64 blocks")
     ap.add_argument("--config", default="C2", choices=sorted(WORKLOADS),
                     help="workload (C2 is the benchmark; C3 is for profiling and manual runs)")
     ap.add_argument("--profile", action="store_true",
