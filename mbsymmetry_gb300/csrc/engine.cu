@@ -2951,7 +2951,9 @@ static int on_handle(gwgb_handle h, F &&f) {
 
 extern "C" {
 
-const char *gwgb_version(void) { return "gwgb 0.4 (sm_103a; FP64, TF32x3 and BF16x3 contraction paths)"; }
+const char *gwgb_version(void) {
+  return "gwgb 0.5 (sm_103a; FP64, sliced BF16 (Ozaki), TF32x3 and BF16x3 contraction paths)";
+}
 
 const char *gwgb_last_error(void) { return gwgb::g_last_error.c_str(); }
 
