@@ -217,6 +217,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     return false;
   };
   auto aborted = [&]() { return *(volatile int *)&abort_flag != 0; };
+  // Every stop decision is taken by the whole warp (the tcgen05 loads, the
+  // shuffles and the warp barrier of the staging loop need all 32 lanes): a
+  // warp stops when any lane saw the abort flag or a wait that ran out.  Each
+  // lane's wait is bounded, so the votes end, and a timed-out wait can never
+  // leave part of a warp waiting for lanes that left the loop.
+  auto warp_aborted = [&]() { return __any_sync(0xffffffffu, aborted()); };
+  auto warp_ok = [&](bool ok) { return __all_sync(0xffffffffu, ok); };
 
   if (warp >= 8) {
     // ------------------------------ producers (and the MMA issuer) ------------------------------
@@ -241,10 +248,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const float4 *arow = Ag + arow0 + (int64_t)rep * dg.ra;
         const float4 *brow = Bg + brow0 + (int64_t)rep * dg.rb;
         for (int k0 = 0; k0 < dg.K; k0 += OZ_KR, ++i) {
-          if (aborted()) { stop = true; break; }
+          if (warp_aborted()) { stop = true; break; }
           const int b = i & 1, e = i & 3;
-          if (i >= 2 && !bwait(&empty[b], ((i >> 1) - 1) & 1)) { stop = true; break; }
-          if (i >= 4 && !bwait(&efree[e], ((i >> 2) - 1) & 1)) { stop = true; break; }
+          if (i >= 2 && !warp_ok(bwait(&empty[b], ((i >> 1) - 1) & 1))) { stop = true; break; }
+          if (i >= 4 && !warp_ok(bwait(&efree[e], ((i >> 2) - 1) & 1))) { stop = true; break; }
           const int kn = min(OZ_KR, dg.K - k0);
           const int nks = (kn + 7) >> 3;  // MMA K steps this round (8 complex each)
           const int kw = 4 * nks;         // complex K per thread of an A row (4 or 8)
@@ -261,7 +268,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             }
             amax[b][ah][ar] = m;
             tc::mbar_arrive(&mx[b]);  // both halves' maxima posted (bounded wait, no named barrier)
-            if (!bwait(&mx[b], (i >> 1) & 1)) { stop = true; break; }
+            if (!warp_ok(bwait(&mx[b], (i >> 1) & 1))) { stop = true; break; }
             const int ea = oz_exponent(fmaxf(amax[b][0][ar], amax[b][1][ar]));
             const float f = oz_pow2(7 - ea);
 #pragma unroll
@@ -397,9 +404,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       for (int rr = 0; rr < tk.nrep && !stop; ++rr) {
         const int64_t co = crow0 + (int64_t)(tk.rep0 + rr) * dg.rc;
         for (int k0 = 0; k0 < dg.K; k0 += OZ_KR, ++i) {
-          if (aborted()) { stop = true; break; }
+          if (warp_aborted()) { stop = true; break; }
           const int a = i & 1, e = i & 3;
-          if (!bwait(&done[a], (i >> 1) & 1) || !bwait(&eready[e], (i >> 2) & 1)) { stop = true; break; }
+          if (!warp_ok(bwait(&done[a], (i >> 1) & 1) && bwait(&eready[e], (i >> 2) & 1))) { stop = true; break; }
           tc::fence_after_sync();
           const bool first = k0 == 0, lastr = k0 + OZ_KR >= dg.K;
           const int ea = ea_s[e][r];
