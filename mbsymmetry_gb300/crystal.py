@@ -495,19 +495,24 @@ def make_crystal(spec: CrystalSpec, rotate: bool = True, used_pairs_only: bool =
                 F[sp, o:o + s_ * s_] = h.ravel()
                 S[sp, o:o + s_ * s_] = np.eye(s_).ravel()
             eigs.extend([(e, w) for e in np.linalg.eigvalsh(h)])
-    # half filling: nao * nk / 2 states per spin
-    eigs.sort()
-    target = spec.nao * nk / 2.0
+    mu = half_filling_mu(eigs, spec.nao, nk)
+    return Crystal(spec=spec, layout=layout, V=V, F=F, S=S, H=F.copy(), mu=float(mu),
+                   star_sizes=np.array([star_size[star_of[k]] for k in layout.irre_list]))
+
+
+def half_filling_mu(eigs, nao: int, nk: int) -> float:
+    """Chemical potential midway between the last filled and the first empty
+    band energy at half filling (nao * nk / 2 states per spin); eigs: (energy,
+    weight of its k point) over the stored k points."""
+    eigs = sorted(eigs)
+    target = nao * nk / 2.0
     acc = 0.0
-    mu = eigs[-1][0]
     for i, (e, w) in enumerate(eigs):
         acc += w
         if acc >= target:
             nxt = eigs[i + 1][0] if i + 1 < len(eigs) else e + 1.0
-            mu = 0.5 * (e + nxt)
-            break
-    return Crystal(spec=spec, layout=layout, V=V, F=F, S=S, H=F.copy(), mu=float(mu),
-                   star_sizes=np.array([star_size[star_of[k]] for k in layout.irre_list]))
+            return 0.5 * (e + nxt)
+    return eigs[-1][0]
 
 
 def load_ir(nts: int):
