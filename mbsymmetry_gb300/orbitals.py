@@ -45,9 +45,13 @@ rock-salt or the 4-atom basis of ``symmetry.fcc_basis``):
   central in O_h, conj(Y(q_r)) and D(I) Y(q_r) diagonalise the same matrix,
   so -q is reached from q_r by g I and auxrep stays block-diagonal; at
   self-conjugate q the basis is real.
-* selection rule: the V blocks that vanish by symmetry in these bases (at
-  rounding level, many orders of magnitude below every other block) are
-  left out of the pair's block list; the rest are stored.
+* selection rule: a block of V(k1, k2) is stored unless the group forbids it,
+  i.e. unless it vanishes for a generic tensor averaged over the pair's
+  magnetic stabiliser (the operations that fix k1 and k2, and time reversal
+  after I h, which real orbitals make a symmetry: V(-k1, -k2) =
+  conj(V(k1, k2))).  The data vanish on every forbidden block to rounding;
+  a few allowed blocks can vanish too (the (Q|ij) = (Q|ji) symmetry of real
+  orbitals, which the rule does not use) and are stored as zeros.
 
 A crystal built with ``rotate=True`` (irreducible k, rotations) and one with
 ``rotate=False`` (every k, identity rotations) hold the same V and F in the
@@ -268,6 +272,8 @@ class _Generator:
         self.minus = np.array([_find(wrap_1stbz(-self.kmesh[k]), self.kmesh) for k in range(self.nk)])
         self.op_of = np.array([self._first_op(self.index[k], k) for k in range(self.nk)])
         self.inv_op = next(i for i, R in enumerate(self.ops) if np.array_equal(R, -np.eye(3, dtype=int)))
+        self._dcache = {}
+        self.perm = np.array([[_find(wrap_1stbz(M @ k), self.kmesh) for k in self.kmesh] for M in self.ops_red])
         self.ao = symmetry.fcc_basis(spec.nao, spec.atoms)
         self.aux = symmetry.fcc_basis(spec.naux, spec.atoms)
         self.species = atom_species(self.ao, self.ops)
@@ -289,8 +295,14 @@ class _Generator:
         return [g for g, M in enumerate(self.ops_red)
                 if _find(wrap_1stbz(M @ self.kmesh[k]), self.kmesh) == k]
 
-    def D(self, g: int, k: int, basis: symmetry.Basis, R: np.ndarray = None) -> np.ndarray:
-        return symmetry.bloch_representation(self.kcart(k), self.ops[g] if R is None else R, basis)
+    def D(self, g: int, k: int, basis: symmetry.Basis, inverted: bool = False) -> np.ndarray:
+        """Representation on the Bloch sums at k of operation g, or of g I with
+        ``inverted`` (cached per operation, k and basis)."""
+        key = (g, k, id(basis), inverted)
+        if key not in self._dcache:
+            R = self.ops[g] @ self.ops[self.inv_op] if inverted else self.ops[g]
+            self._dcache[key] = symmetry.bloch_representation(self.kcart(k), R, basis)
+        return self._dcache[key]
 
     def adapted_basis(self, k: int, basis: symmetry.Basis) -> Tuple[np.ndarray, List[int]]:
         """Eigenvectors of sum_h c_h (D(h) + D(h)^H) over the little group of k,
@@ -406,6 +418,29 @@ class _Generator:
                                 V[:, xq[3]:xq[3] + nq, xi[3]:xi[3] + ni, xj[3]:xj[3] + nj] += blk
         return V
 
+    # -- the selection rule -------------------------------------------------- #
+    def selection_rule(self, p: int, adapted, rng) -> np.ndarray:
+        """A generic V(k1, k2) invariant under the pair's magnetic stabiliser, in
+        the adapted bases (normalised to max 1): the operations h that fix k1
+        and k2 act as V -> (D_aux(h, p) x D(h, k1) x conj D(h, k2)) V, and time
+        reversal after I h (which takes the pair to (-k1, -k2); real orbitals
+        give V(-k1, -k2) = conj(V(k1, k2))) as V -> conj(T_Ih V).  Its zero
+        blocks are the blocks the group forbids."""
+        nk = self.nk
+        k1, k2 = divmod(p, nk)
+        kq = _find(wrap_1stbz(self.kmesh[k2] - self.kmesh[k1]), self.kmesh)
+        H = [g for g in range(len(self.ops)) if self.perm[g][k1] == k1 and self.perm[g][k2] == k2]
+        X = rng.normal(size=(self.spec.naux, self.spec.nao, self.spec.nao)) \
+            + 1j * rng.normal(size=(self.spec.naux, self.spec.nao, self.spec.nao))
+        acc = np.zeros_like(X)
+        for h in H:
+            for anti in (False, True):
+                T = np.matmul(np.matmul(self.D(h, k1, self.ao, anti), np.tensordot(self.D(h, kq, self.aux, anti), X, 1)),
+                              self.D(h, k2, self.ao, anti).conj().T)
+                acc += T.conj() if anti else T
+        out = adapted(p, acc)
+        return out / np.abs(out).max()
+
     # -- bases and rotations ------------------------------------------------ #
     def bases(self, rng):
         """AO bases U[k], aux bases Y[q] (full matrices), block sizes per k / q,
@@ -451,7 +486,7 @@ class _Generator:
                 assert self.index[mq] == qr and Y[mq] is None
                 Y[mq] = Y[q].conj()
                 aux_sizes[mq] = list(sz)
-                Dm = self.D(g, qr, self.aux, R=self.ops[g] @ self.ops[self.inv_op])
+                Dm = self.D(g, qr, self.aux, inverted=True)
                 auxrep[mq] = Y[mq].conj().T @ Dm @ Yr
         return U, Y, ao_sizes, aux_sizes, orep, auxrep
 
@@ -504,35 +539,40 @@ def make_orbital_crystal(spec: CrystalSpec, rotate: bool = True, model: OrbitalM
     U, Y, ao_sizes, aux_sizes, orep_full, auxrep_full = gen.bases(np.random.default_rng(model.seed + spec.seed + 1))
     off = {"F": 0.0, "orep": 0.0, "auxrep": 0.0}
 
-    # V in the adapted bases; blocks that vanish by symmetry are left out
+    # V in the adapted bases; the blocks that the group forbids are left out
     layout0 = BlockLayout(nk=nk, kmesh=gen.kmesh, ao_sizes=ao_sizes, aux_sizes=aux_sizes,
                           tensor_irreps=[np.zeros((0, 3), int)] * (nk * nk),
                           irre_list=np.arange(nk), index=np.arange(nk), irre_index=np.arange(nk),
                           conj_index=np.arange(nk))
-    Vsa = np.empty_like(V_ao)
-    for p in range(nk * nk):
+
+    def adapted(p, X):
+        """conj(Y(q))^T x conj(U(k1))^T x U(k2)^T applied to V(k1, k2)[Q', i', j']."""
         k1, k2 = divmod(p, nk)
-        q = layout0.pair_q(k1, k2)
-        x = np.tensordot(Y[q].conj(), V_ao[p], axes=([0], [0]))          # Q, i', j'
-        x = np.einsum("Qab,ai->Qib", x, U[k1].conj(), optimize=True)
-        Vsa[p] = np.einsum("Qib,bj->Qij", x, U[k2], optimize=True)
+        x = np.tensordot(Y[layout0.pair_q(k1, k2)].conj().T, X, 1)
+        return np.matmul(np.matmul(U[k1].conj().T, x), U[k2])
+
+    Vsa = np.stack([adapted(p, V_ao[p]) for p in range(nk * nk)])
     vmax = float(np.abs(Vsa).max())
     norms, ti = {}, []
     ao_off = [np.concatenate([[0], np.cumsum(s)]).astype(int) for s in ao_sizes]
     aux_off = [np.concatenate([[0], np.cumsum(s)]).astype(int) for s in aux_sizes]
+    off["V_forbidden"] = 0.0
     for p in range(nk * nk):
         k1, k2 = divmod(p, nk)
         q = layout0.pair_q(k1, k2)
+        allowed = gen.selection_rule(p, adapted, np.random.default_rng((model.seed, p)))
         blocks = []
         for iq in range(len(aux_sizes[q])):
             for i1 in range(len(ao_sizes[k1])):
                 for i2 in range(len(ao_sizes[k2])):
-                    b = Vsa[p, aux_off[q][iq]:aux_off[q][iq + 1], ao_off[k1][i1]:ao_off[k1][i1 + 1],
-                            ao_off[k2][i2]:ao_off[k2][i2 + 1]]
-                    n = float(np.abs(b).max()) / vmax
+                    sl = (slice(aux_off[q][iq], aux_off[q][iq + 1]), slice(ao_off[k1][i1], ao_off[k1][i1 + 1]),
+                          slice(ao_off[k2][i2], ao_off[k2][i2 + 1]))
+                    n = float(np.abs(Vsa[p][sl]).max()) / vmax
                     norms[(p, iq, i1, i2)] = n
-                    if n > 1e-10:
+                    if np.abs(allowed[sl]).max() > 1e-12:
                         blocks.append((iq, i1, i2))
+                    else:
+                        off["V_forbidden"] = max(off["V_forbidden"], n)
         ti.append(np.array(blocks, dtype=np.int32).reshape(-1, 3))
 
     # rotations (block-diagonal) and the stored k points

@@ -107,17 +107,20 @@ def test_adapted_blocks_match_the_dirac_character_decomposition(gen):
 
 def test_block_structure_in_the_adapted_bases(c1):
     """F, orep and auxrep are block-diagonal; the aux basis at -q is the
-    conjugate of the one at q; the V blocks split into symmetry zeros and the
-    rest with a wide gap, and some blocks are zero."""
-    assert max(c1.off_block.values()) < 1e-13
+    conjugate of the one at q; the data vanish on every block the group
+    forbids, and on C1 every allowed block is non-zero (the rule and the data
+    agree block for block)."""
+    assert max(c1.off_block[k] for k in ("F", "orep", "auxrep")) < 1e-13
+    assert c1.off_block["V_forbidden"] < 1e-13
     L = c1.layout
     minus = [L.mom_cons(0, q, 0) for q in range(L.nk)]   # -q
     for q in range(L.nk):
         assert np.abs(c1.Y[minus[q]] - c1.Y[q].conj()).max() < 1e-14
-    n = np.array(list(c1.V_block_norms.values()))
-    zero, kept = n[n < 1e-10], n[n >= 1e-10]
-    assert len(zero) > 0.05 * len(n)
-    assert zero.max() < 1e-13 and kept.min() > 1e-9
+    stored = {(p, *(int(x) for x in b)) for p in range(L.nk * L.nk) for b in L.tensor_irreps[p]}
+    n = c1.V_block_norms
+    assert len(stored) < 0.95 * len(n)
+    assert min(n[b] for b in stored) > 1e-9
+    assert max(v for b, v in n.items() if b not in stored) < 1e-13
 
 
 def _characters(gen, k, basis, cols):
@@ -165,11 +168,14 @@ def _chain(cr, tr):
     return Gf, Pf, orc.sigma(Gf, Pf, cr.V)
 
 
-@pytest.mark.parametrize("ns", [1, 2])
-def test_irreducible_and_full_mesh_agree(ns):
+@pytest.mark.parametrize("ns,change", [(1, {}), (2, {}), (1, {"mesh": (2, 2, 2)}),
+                                       (1, {"atoms": 4, "nao": 16, "naux": 40})])
+def test_irreducible_and_full_mesh_agree(ns, change):
     """Orbital crystal on the irreducible k with the group's rotations and on
-    every k without: G, P~ (every q) and Sigma (irreducible k) agree."""
-    spec = dataclasses.replace(CONFIGS["C1"], ns=ns)
+    every k without: G, P~ (every q) and Sigma (irreducible k) agree.  C1's
+    3x3x3 mesh, the 2x2x2 mesh (every point self-conjugate: real aux bases),
+    and the 4-atom basis (an atom pair exchanged by the group)."""
+    spec = dataclasses.replace(CONFIGS["C1"], ns=ns, **change)
     tr = build_transforms(load_ir(spec.nts), spec.beta)
     cr = O.make_orbital_crystal(spec, rotate=True)
     cf = O.make_orbital_crystal(spec, rotate=False)
