@@ -220,7 +220,6 @@ def shell_norm(alpha: float, l: int) -> float:
 class _Shells:
     """Per-function bookkeeping of a basis: atom, shell (l, index on the atom), offsets."""
     basis: symmetry.Basis
-    species: np.ndarray
     shells: List[Tuple[int, int, int, int]] = field(default_factory=list)  # (atom, shell index, l, offset)
 
     def __post_init__(self):
@@ -327,8 +326,8 @@ class _Generator:
     # -- parameters -------------------------------------------------------- #
     def shell_parameters(self):
         m, rng = self.model, self.par_rng
-        ao_sh = _Shells(self.ao, self.species)
-        aux_sh = _Shells(self.aux, self.species)
+        ao_sh = _Shells(self.ao)
+        aux_sh = _Shells(self.aux)
         keys_ao = sorted({(int(self.species[a]), s) for (a, s, _, _) in ao_sh.shells})
         keys_aux = sorted({(int(self.species[a]), s) for (a, s, _, _) in aux_sh.shells})
         onsite = {k: rng.normal(0.0, m.onsite) for k in keys_ao}

@@ -4,6 +4,7 @@ reference-input loader unchanged (on-disk format compatibility)."""
 import os
 
 import numpy as np
+import pytest
 
 from _helpers import GOLDEN, crystal, lih
 from mbsymmetry_gb300 import h5write
@@ -47,8 +48,14 @@ def test_export_reference_block_dir_lih(tmp_path):
     assert np.allclose(ri.onebody.S, d["S"], rtol=0, atol=1e-14)
 
 
-def test_export_reference_block_dir_crystal(tmp_path):
-    cr, _ = crystal("C1", rotate=False)
+@pytest.mark.parametrize("kind", ["labelled", "orbital"])
+def test_export_reference_block_dir_crystal(tmp_path, kind):
+    if kind == "labelled":
+        cr, _ = crystal("C1", rotate=False)
+    else:   # Slater-Koster / Gaussian-orbital data with the group's selection rule
+        from mbsymmetry_gb300.crystal import CONFIGS
+        from mbsymmetry_gb300.orbitals import make_orbital_crystal
+        cr = make_orbital_crystal(CONFIGS["C1"], rotate=False)
     out = str(tmp_path / "block")
     h5write.export_reference_inputs(out, cr.layout, cr.V, cr.F, cr.S, cr.H, cr.ns)
     ri = load_reference_inputs(out)
