@@ -161,24 +161,67 @@ class IRBasis:
             out[c:c + 4096] = self.uhat(n[c:c + 4096], l + 1)[:, l]
         return out
 
-    def matsubara_sampling(self) -> np.ndarray:
+    def matsubara_sampling(self, symmetric: bool = True) -> np.ndarray:
         """``size`` Matsubara indices chosen greedily for a well-conditioned
-        sampling matrix: column-pivoted QR of [u_l(i nu_n)] over a candidate
-        set (every |n| < 2000, then a geometric grid up to 50 Lambda)."""
+        sampling matrix over a candidate set (every |n| < 2000, then a
+        geometric grid up to 50 Lambda).
+
+        symmetric (the default): the set is closed under nu -> -nu, as
+        sparse-ir's sampling and the reference's own grid (``1e3_72.h5``)
+        are: pairs (nu, -nu) are taken greedily by the residual norm of
+        [Re u_l(i nu), Im u_l(i nu)] (u_l(-i nu) = conj(u_l(i nu)) for real
+        u_l), with nu = 0 first for an odd bosonic size.  Time reversal then
+        maps the sampled frequencies onto themselves, which keeps
+        P~(-q) = conj(P~(q)) exact through the nonlinear W~ step.
+        symmetric=False: column-pivoted QR of the complex rows (an
+        unsymmetric set)."""
         import scipy.linalg
         L = self.size
         nmax = int(max(4000, 50 * self.lam))
         pos = np.unique(np.concatenate([np.arange(0, 2000),
                                         np.round(np.geomspace(2000, nmax, 3000)).astype(np.int64)]))
-        if self.stat == "F":
-            cand = np.concatenate([-pos[::-1] - 1, pos])
-        else:
-            cand = np.unique(np.concatenate([-pos[::-1], pos]))
-        M = np.empty((len(cand), L), dtype=np.complex128)
-        for c in range(0, len(cand), 4096):
-            M[c:c + 4096] = self.uhat(cand[c:c + 4096], L)
-        _, _, piv = scipy.linalg.qr(M.T, pivoting=True, mode="economic")
-        return np.sort(cand[piv[:L]])
+        if not symmetric:
+            if self.stat == "F":
+                cand = np.concatenate([-pos[::-1] - 1, pos])
+            else:
+                cand = np.unique(np.concatenate([-pos[::-1], pos]))
+            M = np.empty((len(cand), L), dtype=np.complex128)
+            for c in range(0, len(cand), 4096):
+                M[c:c + 4096] = self.uhat(cand[c:c + 4096], L)
+            _, _, piv = scipy.linalg.qr(M.T, pivoting=True, mode="economic")
+            return np.sort(cand[piv[:L]])
+        M = np.empty((len(pos), L), dtype=np.complex128)
+        for c in range(0, len(pos), 4096):
+            M[c:c + 4096] = self.uhat(pos[c:c + 4096], L)
+        R = np.stack([M.real, M.imag], axis=1)          # (candidate, re/im, l): residual rows
+
+        def take(i, rows):
+            for r in rows:                               # Gram-Schmidt of the chosen rows out of every residual
+                v = R[i, r].copy()
+                nv = np.linalg.norm(v)
+                if nv > 0:
+                    v /= nv
+                    R[...] -= np.einsum("crl,l->cr", R, v)[:, :, None] * v[None, None, :]
+            R[i] = 0.0
+
+        if self.stat == "F" and L % 2:
+            raise ValueError("a symmetric fermionic sampling set has an even size")
+        chosen = []
+        i0 = int(np.nonzero(pos == 0)[0][0])
+        if self.stat == "B" and L % 2 == 1:              # nu = 0 (a real row) completes an odd size
+            take(i0, (0,))
+            chosen.append(i0)
+        elif self.stat == "B":
+            R[i0] = 0.0                                  # nu = 0 has no partner
+        pairs = []
+        while len(pairs) < L // 2:
+            i = int(np.argmax(np.einsum("crl,crl->c", R, R)))
+            take(i, (0, 1))
+            pairs.append(i)
+        n = pos[np.array(pairs, dtype=np.int64)]
+        neg = -n - 1 if self.stat == "F" else -n
+        n = np.concatenate([n, pos[np.array(chosen, dtype=np.int64)]])
+        return np.sort(np.unique(np.concatenate([n, neg])))
 
 
 def find_lambda(size: int, eps: float = 1e-13, lo: float = 10.0, hi: float = 1e9) -> float:

@@ -50,3 +50,15 @@ def test_committed_grids_round_trip(nts, beta, tol):
     assert tr.nts == nts and tr.nw == nts - 2 and tr.nw_b == nts - 3
     assert np.linalg.cond(ir["fermi/uxl"]) < 1e4
     assert _single_pole_error(tr) < tol
+
+
+@pytest.mark.parametrize("nts", [62, 100, 120, 150])
+def test_committed_grids_sample_symmetrically(nts):
+    """Matsubara sampling closed under nu -> -nu, like the reference's own grid
+    (and sparse-ir's): time reversal maps the sampled frequencies onto
+    themselves."""
+    ir = load_ir(nts)
+    wf, wb = ir["fermi/wsample"].ravel(), ir["bose/wsample"].ravel()
+    assert set(wf.tolist()) == set((-wf - 1).tolist()) and set(wb.tolist()) == set((-wb).tolist())
+    ref = lih()["ir"]
+    assert set(ref["fermi/wsample"].ravel().tolist()) == set((-ref["fermi/wsample"].ravel() - 1).tolist())
