@@ -7,7 +7,10 @@ SymmetryAdaptation's block diagonalisation
 ``SymmetryAdaptation/src/dirac_character.cpp:7-126``,
 ``SymmetryAdaptation/src/space_group_rep.cpp``).  Neither runs here; this
 module builds inputs of the same kind for an FCC crystal (O_h; the 2-atom
-rock-salt or the 4-atom basis of ``symmetry.fcc_basis``):
+rock-salt or the 4-atom basis of ``symmetry.fcc_basis``) and for wurtzite
+(P6_3mc, ``symmetry.wurtzite_basis``: non-symmorphic, projective
+representations at the zone boundary, no inversion).  Both are handled as
+space groups, operations (M, t) on fractional coordinates:
 
 * orbitals: s/p/d shells on the atoms; real solid harmonics (1; x, y, z;
   r.Q_n.r for the orthonormal traceless Q_n of ``symmetry``) times Gaussians.
@@ -41,10 +44,17 @@ rock-salt or the 4-atom basis of ``symmetry.fcc_basis``):
 * aux bases: the same construction, and the basis at -q is the complex
   conjugate of the one at q (the pairing that the P0 loop, which reads
   V(k, k + q), and the Sigma loop, which reads V(k, k - q), assume when
-  they use the same aux blocks for both).  With real c_h and inversion
-  central in O_h, conj(Y(q_r)) and D(I) Y(q_r) diagonalise the same matrix,
-  so -q is reached from q_r by g I and auxrep stays block-diagonal; at
-  self-conjugate q the basis is real.
+  they use the same aux blocks for both).  Where an operation u takes k_r
+  to -k_r, the matrix diagonalised is B + D(u)^H conj(B) D(u) with B the
+  sum above, so that conj(Y(k_r)) and D(u) Y(k_r) span the same eigenspaces
+  in the same order: -q is then reached from q_r by g u and auxrep stays
+  block-diagonal.  At self-conjugate q the basis is real.  Rows that time
+  reversal glues together (the A-L-H face of wurtzite) end up in one block.
+* time reversal: where the point group lacks the operation (wurtzite), k =
+  -k' joins the star of k' through time reversal (``conj_index``); its bases
+  are conj(U(k')), conj(Y(k')) and the rotation path conjugates G and P~
+  there (F(-k) = conj(F(k)) and V(-k1, -k2) = conj(V(k1, k2)) for real
+  orbitals).
 * selection rule: a block of V(k1, k2) is stored unless the group forbids it,
   i.e. unless it vanishes for a generic tensor averaged over the pair's
   magnetic stabiliser (the operations that fix k1 and k2, and time reversal
@@ -78,7 +88,8 @@ from .layout import BlockLayout, wrap_1stbz
 @dataclass
 class OrbitalModel:
     """Length scales and parameter ranges of the tight-binding model (bohr, Ha)."""
-    a_lat: float = 7.0                       # conventional cubic lattice constant
+    a_lat: float = 7.0                       # conventional cubic lattice constant (fcc)
+    a_lat_hex: float = 6.1                   # in-plane lattice constant (hexagonal; c = 1.633 a)
     ao_exponents: Tuple[float, float] = (0.3, 1.2)
     aux_exponents: Tuple[float, float] = (0.3, 3.0)
     onsite: float = 0.4                      # onsite energies ~ N(0, onsite)
@@ -231,88 +242,118 @@ class _Shells:
 
 
 def atom_species(basis: symmetry.Basis, ops) -> np.ndarray:
-    """Orbit index of every atom under the point group (atoms of an orbit share parameters)."""
+    """Orbit index of every atom under the space group ((M, t) on fractional
+    coordinates); atoms of an orbit share shells and parameters."""
     pos = np.asarray(basis.positions, dtype=float)
     sp = -np.ones(len(pos), dtype=int)
     n = 0
     for a in range(len(pos)):
         if sp[a] >= 0:
             continue
-        for R in ops:
-            ra = R @ pos[a]
+        for M, t in ops:
+            ra = M @ pos[a] + t
             for b in range(len(pos)):
-                if sp[b] < 0 and symmetry._is_lattice(ra - pos[b]):
+                d = ra - pos[b]
+                if sp[b] < 0 and np.allclose(d, np.round(d), atol=1e-9):
                     sp[b] = n
         n += 1
     return sp
 
 
-def _lattice_vectors(rmax: float) -> Tuple[np.ndarray, np.ndarray]:
-    """Integer coordinates n and cubic-coordinate vectors L = FCC_A n with |L| <= rmax (a = 1)."""
-    m = int(np.ceil(2 * rmax)) + 2
+def _lattice_vectors(A: np.ndarray, rmax: float) -> Tuple[np.ndarray, np.ndarray]:
+    """Integer coordinates n and vectors L = A n (columns of A: primitive
+    vectors) with |L| <= rmax."""
+    m = int(np.ceil(rmax * np.linalg.norm(np.linalg.inv(A), 2))) + 2
     rng = np.arange(-m, m + 1)
     n = np.array(list(itertools.product(rng, rng, rng)))
-    L = n @ symmetry.FCC_A.T
+    L = n @ A.T
     keep = np.linalg.norm(L, axis=1) <= rmax + 1e-9
     return n[keep], L[keep]
 
 
+def _fractional(basis: symmetry.Basis, A: np.ndarray) -> symmetry.Basis:
+    return symmetry.Basis(np.linalg.solve(A, np.asarray(basis.positions, dtype=float).T).T, basis.shells)
+
+
 class _Generator:
+    """The crystal's space group in one form for both lattices: operations
+    (M, t) on fractional coordinates (O_h on the FCC primitive vectors with
+    t = 0; P6_3mc with its screw and glide translations), k in reduced
+    reciprocal coordinates transforming as inv(M)^T k, and the representation
+    on Bloch sums from ``symmetry.sg_bloch_representation``."""
+
     def __init__(self, spec: CrystalSpec, model: OrbitalModel):
-        if spec.lattice != "fcc":
-            raise ValueError("orbital crystals are built for the fcc (O_h) lattice")
         self.spec, self.model = spec, model
-        self.ops_red, _ = _fcc_ops()                       # reduced reciprocal coordinates
-        self.ops = symmetry.oh_operations()                # Cartesian, same order
+        if spec.lattice == "fcc":
+            self.A = symmetry.FCC_A
+            Ainv = np.linalg.inv(self.A)
+            self.ops = [(np.round(Ainv @ R @ self.A).astype(int), np.zeros(3)) for R in symmetry.oh_operations()]
+            self.ao = _fractional(symmetry.fcc_basis(spec.nao, spec.atoms), self.A)
+            self.aux = _fractional(symmetry.fcc_basis(spec.naux, spec.atoms), self.A)
+            self.a_lat = model.a_lat
+        elif spec.lattice == "hex":
+            self.A = symmetry.HEX_A
+            self.ops = symmetry.p63mc_operations()
+            self.ao, self.aux = symmetry.wurtzite_basis(spec.nao), symmetry.wurtzite_basis(spec.naux)
+            self.a_lat = model.a_lat_hex
+        else:
+            raise ValueError(f"unknown lattice {spec.lattice!r}")
+        self.ops_k = [np.round(np.linalg.inv(M).T).astype(int) for M, _ in self.ops]
         self.kmesh = _kmesh(spec.mesh)
-        self.nk = len(self.kmesh)
-        self.Bt = np.linalg.inv(symmetry.FCC_A.T)          # k_cart = Bt @ k_frac (units of 2 pi / a)
-        self.reps, self.star_of, self.index, self.conj_index = _stars(self.kmesh, self.ops_red, True)
-        self.minus = np.array([_find(wrap_1stbz(-self.kmesh[k]), self.kmesh) for k in range(self.nk)])
-        self.op_of = np.array([self._first_op(self.index[k], k) for k in range(self.nk)])
-        self.inv_op = next(i for i, R in enumerate(self.ops) if np.array_equal(R, -np.eye(3, dtype=int)))
+        self.nk = nk = len(self.kmesh)
+        inversion = any(np.array_equal(K, -np.eye(3, dtype=int)) for K in self.ops_k)
+        self.inv_op = next((g for g, K in enumerate(self.ops_k) if np.array_equal(K, -np.eye(3, dtype=int))), None)
+        self.reps, self.star_of, self.index, self.conj_index = _stars(self.kmesh, self.ops_k, inversion)
+        self.minus = np.array([_find(wrap_1stbz(-self.kmesh[k]), self.kmesh) for k in range(nk)])
+        self.perm = np.array([[_find(wrap_1stbz(K @ k), self.kmesh) for k in self.kmesh] for K in self.ops_k])
+        # the operation taking each point-group-reached k from its representative
+        self.op_of = np.array([next(g for g in range(len(self.ops)) if self.perm[g][self.index[k]] == k)
+                               if self.conj_index[k] == k else -1 for k in range(nk)])
+        # per representative: an operation taking k_r to -k_r (inversion first), if the point group has one
+        self.minus_op = {}
+        for kr in self.reps:
+            cands = [g for g in range(len(self.ops)) if self.perm[g][kr] == self.minus[kr]]
+            self.minus_op[kr] = (self.inv_op if self.inv_op in cands else cands[0]) if cands else None
         self._dcache = {}
-        self.perm = np.array([[_find(wrap_1stbz(M @ k), self.kmesh) for k in self.kmesh] for M in self.ops_red])
-        self.ao = symmetry.fcc_basis(spec.nao, spec.atoms)
-        self.aux = symmetry.fcc_basis(spec.naux, spec.atoms)
         self.species = atom_species(self.ao, self.ops)
         rng = np.random.default_rng(model.seed + spec.seed)
         self.coef = rng.uniform(0.5, 1.5, size=len(self.ops))  # c_h, one per group operation
         self.par_rng = rng
 
     # -- group helpers ----------------------------------------------------- #
-    def _first_op(self, kr: int, k: int) -> int:
-        for g, M in enumerate(self.ops_red):
-            if _find(wrap_1stbz(M @ self.kmesh[kr]), self.kmesh) == k:
-                return g
-        raise RuntimeError("k is not in the star of its representative")
-
-    def kcart(self, k: int) -> np.ndarray:
-        return self.Bt @ self.kmesh[k]
-
     def little_group(self, k: int) -> List[int]:
-        return [g for g, M in enumerate(self.ops_red)
-                if _find(wrap_1stbz(M @ self.kmesh[k]), self.kmesh) == k]
+        return [g for g in range(len(self.ops)) if self.perm[g][k] == k]
 
-    def D(self, g: int, k: int, basis: symmetry.Basis, inverted: bool = False) -> np.ndarray:
-        """Representation on the Bloch sums at k of operation g, or of g I with
-        ``inverted`` (cached per operation, k and basis)."""
-        key = (g, k, id(basis), inverted)
+    def D(self, g: int, k: int, basis: symmetry.Basis, then: int = None) -> np.ndarray:
+        """Representation on the Bloch sums at k of operation g, or of the
+        product g u when ``then`` = u (u applied first); cached per operation,
+        k and basis."""
+        key = (g, k, id(basis), then)
         if key not in self._dcache:
-            R = self.ops[g] @ self.ops[self.inv_op] if inverted else self.ops[g]
-            self._dcache[key] = symmetry.bloch_representation(self.kcart(k), R, basis)
+            M, t = self.ops[g]
+            if then is not None:
+                Mu, tu = self.ops[then]
+                M, t = M @ Mu, M @ tu + t
+            self._dcache[key] = symmetry.sg_bloch_representation(self.kmesh[k], M, t, basis, self.A)
         return self._dcache[key]
 
     def adapted_basis(self, k: int, basis: symmetry.Basis) -> Tuple[np.ndarray, List[int]]:
-        """Eigenvectors of sum_h c_h (D(h) + D(h)^H) over the little group of k,
-        grouped by eigenvalue: (U, block sizes)."""
-        A = sum(self.coef[h] * (Dh + Dh.conj().T) for h in self.little_group(k)
+        """Eigenvectors of A = B + Theta(B), B = sum_h c_h (D(h) + D(h)^H) over
+        the little group of k, grouped by eigenvalue: (U, block sizes).
+        Theta(B) = D(u)^H conj(B) D(u) for an operation u taking k to -k (B
+        alone when there is none) makes conj(U) and D(u) U span the same
+        eigenspaces in the same order, which the aux bases at q and -q need."""
+        B = sum(self.coef[h] * (Dh + Dh.conj().T) for h in self.little_group(k)
                 for Dh in [self.D(h, k, basis)])
-        if self.minus[k] == k:           # self-conjugate: the representation is real
-            assert np.abs(A.imag).max() < 1e-10
-            w, U = np.linalg.eigh(A.real)
+        u = self.minus_op.get(k)
+        if u is not None:
+            Du = self.D(u, k, basis)
+            B = B + Du.conj().T @ B.conj() @ Du
+        if self.minus[k] == k:           # self-conjugate: a real matrix, real eigenvectors
+            assert np.abs(B.imag).max() < 1e-10
+            w, U = np.linalg.eigh(B.real)
         else:
-            w, U = np.linalg.eigh(A)
+            w, U = np.linalg.eigh(B)
         scale = max(1.0, np.abs(w).max())
         sizes, i = [], 0
         while i < len(w):
@@ -340,13 +381,22 @@ class _Generator:
                 hop[(ki, kj)] = mag * rng.choice([-1.0, 1.0], size=3)
         return ao_sh, aux_sh, onsite, ao_exp, aux_exp, hop
 
+    def _cart(self, basis: symmetry.Basis) -> np.ndarray:
+        """Atom positions in Cartesian coordinates (units of the lattice constant)."""
+        return np.asarray(basis.positions, dtype=float) @ self.A.T
+
+    def nearest_neighbour(self) -> float:
+        pos = self._cart(self.ao)
+        _, L = _lattice_vectors(self.A, 2.0)
+        d = np.linalg.norm(pos[None, :, None, :] + L[None, None, :, :] - pos[:, None, None, :], axis=-1)
+        return float(d[d > 1e-9].min()) * self.a_lat
+
     # -- F(k) in the orbital Bloch basis ----------------------------------- #
     def fock_ao(self, ao_sh, onsite, hop) -> np.ndarray:
         m, nao = self.model, self.spec.nao
-        pos = np.asarray(self.ao.positions, dtype=float)
-        nvec, Lvec = _lattice_vectors(m.hop_cutoff + 1.0)
-        d_nn = m.a_lat / 2.0
-        F = np.zeros((self.nk, nao, nao), dtype=np.complex128)
+        pos = self._cart(self.ao)
+        nvec, Lvec = _lattice_vectors(self.A, m.hop_cutoff + 2.0)
+        d_nn = self.nearest_neighbour()
         phase = np.exp(2j * np.pi * (self.kmesh @ nvec.T))     # (nk, nL)
         blocks = np.zeros((len(nvec), nao, nao))
         for (ai, si, li, oi) in ao_sh.shells:
@@ -358,9 +408,9 @@ class _Generator:
                 else:
                     v = hop[(kj, ki)] * (-1.0) ** (li + lj)
                 for n in range(len(nvec)):
-                    d = (pos[aj] + Lvec[n] - pos[ai]) * m.a_lat
+                    d = (pos[aj] + Lvec[n] - pos[ai]) * self.a_lat
                     r = np.linalg.norm(d)
-                    if r < 1e-9 or r > m.hop_cutoff * m.a_lat + 1e-9:
+                    if r < 1e-9 or r > m.hop_cutoff * self.a_lat + 1e-9:
                         continue
                     blocks[n, oi:oi + 2 * li + 1, oj:oj + 2 * lj + 1] = sk_block(
                         li, lj, v * np.exp(-(r - d_nn) / m.decay), d)
@@ -375,9 +425,8 @@ class _Generator:
         m, nk = self.model, self.nk
         naux, nao = self.spec.naux, self.spec.nao
         rc = m.v_cutoff
-        pos_ao = np.asarray(self.ao.positions, dtype=float)
-        pos_aux = np.asarray(self.aux.positions, dtype=float)
-        nvec, Lvec = _lattice_vectors(rc + 2.0)
+        pos_ao, pos_aux = self._cart(self.ao), self._cart(self.aux)
+        nvec, Lvec = _lattice_vectors(self.A, rc + 2.0)
         natom = len(pos_ao)
         k1 = np.repeat(np.arange(nk), nk)
         k2 = np.tile(np.arange(nk), nk)
@@ -401,8 +450,8 @@ class _Generator:
                     gq, gj = gq.ravel(), gj.ravel()
                     ok = np.linalg.norm(cq[gq] - cj[gj], axis=1) <= rc + 1e-9
                     gq, gj = gq[ok], gj[ok]
-                    AQ, AJ = cq[gq] * m.a_lat, cj[gj] * m.a_lat
-                    AI = np.broadcast_to(A_i * m.a_lat, AQ.shape)
+                    AQ, AJ = cq[gq] * self.a_lat, cj[gj] * self.a_lat
+                    AI = np.broadcast_to(A_i * self.a_lat, AQ.shape)
                     ph = np.exp(2j * np.pi * (-(kf2 - kf1) @ nvec[gq].T + kf2 @ nvec[gj].T))  # (pairs, conf)
                     for xq in aux_by_atom[aq]:
                         eq = aux_exp[(int(self.species[aq]), xq[1])]
@@ -421,29 +470,32 @@ class _Generator:
     def selection_rule(self, p: int, adapted, rng) -> np.ndarray:
         """A generic V(k1, k2) invariant under the pair's magnetic stabiliser, in
         the adapted bases (normalised to max 1): the operations h that fix k1
-        and k2 act as V -> (D_aux(h, p) x D(h, k1) x conj D(h, k2)) V, and time
-        reversal after I h (which takes the pair to (-k1, -k2); real orbitals
-        give V(-k1, -k2) = conj(V(k1, k2))) as V -> conj(T_Ih V).  Its zero
-        blocks are the blocks the group forbids."""
-        nk = self.nk
-        k1, k2 = divmod(p, nk)
+        and k2 act as V -> (D_aux(h, p) x D(h, k1) x conj D(h, k2)) V = T_h V,
+        and time reversal after an operation g that takes the pair to
+        (-k1, -k2) (real orbitals give V(-k1, -k2) = conj(V(k1, k2))) as
+        V -> conj(T_g V).  Its zero blocks are the blocks the group forbids."""
+        k1, k2 = divmod(p, self.nk)
         kq = _find(wrap_1stbz(self.kmesh[k2] - self.kmesh[k1]), self.kmesh)
-        H = [g for g in range(len(self.ops)) if self.perm[g][k1] == k1 and self.perm[g][k2] == k2]
+        ng = len(self.ops)
+        unitary = [g for g in range(ng) if self.perm[g][k1] == k1 and self.perm[g][k2] == k2]
+        anti = [g for g in range(ng) if self.perm[g][k1] == self.minus[k1] and self.perm[g][k2] == self.minus[k2]]
         X = rng.normal(size=(self.spec.naux, self.spec.nao, self.spec.nao)) \
             + 1j * rng.normal(size=(self.spec.naux, self.spec.nao, self.spec.nao))
         acc = np.zeros_like(X)
-        for h in H:
-            for anti in (False, True):
-                T = np.matmul(np.matmul(self.D(h, k1, self.ao, anti), np.tensordot(self.D(h, kq, self.aux, anti), X, 1)),
-                              self.D(h, k2, self.ao, anti).conj().T)
-                acc += T.conj() if anti else T
+        for g, conj in [(g, False) for g in unitary] + [(g, True) for g in anti]:
+            T = np.matmul(np.matmul(self.D(g, k1, self.ao), np.tensordot(self.D(g, kq, self.aux), X, 1)),
+                          self.D(g, k2, self.ao).conj().T)
+            acc += T.conj() if conj else T
         out = adapted(p, acc)
         return out / np.abs(out).max()
 
     # -- bases and rotations ------------------------------------------------ #
     def bases(self, rng):
         """AO bases U[k], aux bases Y[q] (full matrices), block sizes per k / q,
-        and the full rotation matrices orep[k] = U[k]^H D U[k_r], auxrep[q]."""
+        and the full rotation matrices orep[k] = U[k]^H D U[k_r], auxrep[q].
+        A k that time reversal brings into the star (conj_index[k] = k' != k,
+        k = -k') takes conj(U[k']) and the rotation of k': the rotation path
+        conjugates G and P~ there."""
         nk = self.nk
         U, Y, ao_sizes, aux_sizes = [None] * nk, [None] * nk, [None] * nk, [None] * nk
         orep, auxrep = [None] * nk, [None] * nk
@@ -460,7 +512,9 @@ class _Generator:
                     blocks.append(_rand_unitary(rng, b))
             return _block_diag(blocks)
 
-        for k in range(nk):
+        by_group = [k for k in range(nk) if self.conj_index[k] == k]
+        by_tr = [k for k in range(nk) if self.conj_index[k] != k]
+        for k in by_group:
             kr = int(self.index[k])
             Ur, sz = rep_ao[kr]
             Dg = self.D(int(self.op_of[k]), kr, self.ao)
@@ -468,25 +522,27 @@ class _Generator:
             U[k] = Dg @ Ur @ W
             ao_sizes[k] = list(sz)
             orep[k] = U[k].conj().T @ Dg @ Ur
-        for q in range(nk):
+        for q in by_group:
             if Y[q] is not None:
                 continue
             qr = int(self.index[q])
             Yr, sz = rep_aux[qr]
             g = int(self.op_of[q])
             Dg = self.D(g, qr, self.aux)
-            selfconj = self.minus[q] == q
-            W = np.eye(len(Yr), dtype=np.complex128) if q == qr else gauge(sz, selfconj)
+            W = np.eye(len(Yr), dtype=np.complex128) if q == qr else gauge(sz, self.minus[q] == q)
             Y[q] = Dg @ Yr @ W
             aux_sizes[q] = list(sz)
             auxrep[q] = Y[q].conj().T @ Dg @ Yr
             mq = int(self.minus[q])
-            if mq != q:
-                assert self.index[mq] == qr and Y[mq] is None
+            if mq != q and self.conj_index[mq] == mq:   # -q in the star by the group: g u takes q_r there
+                assert self.index[mq] == qr and Y[mq] is None and self.minus_op[qr] is not None
                 Y[mq] = Y[q].conj()
                 aux_sizes[mq] = list(sz)
-                Dm = self.D(g, qr, self.aux, inverted=True)
-                auxrep[mq] = Y[mq].conj().T @ Dm @ Yr
+                auxrep[mq] = Y[mq].conj().T @ self.D(g, qr, self.aux, then=self.minus_op[qr]) @ Yr
+        for k in by_tr:
+            c = int(self.conj_index[k])
+            U[k], ao_sizes[k], orep[k] = U[c].conj(), list(ao_sizes[c]), orep[c]
+            Y[k], aux_sizes[k], auxrep[k] = Y[c].conj(), list(aux_sizes[c]), auxrep[c]
         return U, Y, ao_sizes, aux_sizes, orep, auxrep
 
 
@@ -578,8 +634,8 @@ def make_orbital_crystal(spec: CrystalSpec, rotate: bool = True, model: OrbitalM
     if rotate:
         irre_list = np.array(gen.reps)
         pos = {int(k): i for i, k in enumerate(irre_list)}
-        irre_index = np.array([pos[int(gen.index[k])] for k in range(nk)])
-        idx = gen.index.copy()
+        irre_index = np.array([pos[int(gen.index[gen.conj_index[k]])] for k in range(nk)])
+        idx, cidx = gen.index.copy(), gen.conj_index.copy()
         orep_b, orep_i, auxrep_b, auxrep_i = [], [], [], []
         for k in range(nk):
             ob, e = _diag_blocks(orep_full[k], ao_sizes[k])
@@ -593,10 +649,10 @@ def make_orbital_crystal(spec: CrystalSpec, rotate: bool = True, model: OrbitalM
         reps_kw = dict(orep=np.concatenate(orep_b), orep_irreps=orep_i,
                        auxrep=np.concatenate(auxrep_b), auxrep_irreps=auxrep_i)
     else:
-        irre_list, irre_index, idx = np.arange(nk), np.arange(nk), np.arange(nk)
+        irre_list, irre_index, idx, cidx = np.arange(nk), np.arange(nk), np.arange(nk), np.arange(nk)
         reps_kw = {}
     layout = BlockLayout(nk=nk, kmesh=gen.kmesh, ao_sizes=ao_sizes, aux_sizes=aux_sizes, tensor_irreps=ti,
-                         irre_list=irre_list, index=idx, irre_index=irre_index, conj_index=np.arange(nk),
+                         irre_list=irre_list, index=idx, irre_index=irre_index, conj_index=cidx,
                          **reps_kw)
 
     # flat V, scaled to the spec's entry size

@@ -72,7 +72,7 @@ def test_fock_is_hermitian_and_covariant(c1, gen):
     assert np.abs(F - F.conj().transpose(0, 2, 1)).max() < 1e-14
     for k in range(gen.nk):
         for g in range(0, 48, 5):
-            gk = O._find(O.wrap_1stbz(gen.ops_red[g] @ gen.kmesh[k]), gen.kmesh)
+            gk = gen.perm[g][k]
             D = gen.D(g, k, gen.ao)
             assert np.abs(D @ F[k] @ D.conj().T - F[gk]).max() < 1e-13
 
@@ -90,7 +90,7 @@ def test_coulomb_pair_relation_and_covariance(c1, gen):
     for _ in range(12):
         k1, k2, g = int(rng.integers(nk)), int(rng.integers(nk)), int(rng.integers(48))
         p = c1.layout.pair_q(k1, k2)
-        img = lambda k: O._find(O.wrap_1stbz(gen.ops_red[g] @ gen.kmesh[k]), gen.kmesh)  # noqa: E731
+        img = lambda k: gen.perm[g][k]  # noqa: E731
         Dq, D1, D2 = gen.D(g, p, gen.aux), gen.D(g, k1, gen.ao), gen.D(g, k2, gen.ao)
         want = np.einsum("QR,ia,jb,Rab->Qij", Dq, D1, D2.conj(), V[k1 * nk + k2], optimize=True)
         assert np.abs(want - V[img(k1) * nk + img(k2)]).max() < 1e-12 * np.abs(V).max()
@@ -99,10 +99,13 @@ def test_coulomb_pair_relation_and_covariance(c1, gen):
 def test_adapted_blocks_match_the_dirac_character_decomposition(gen):
     """Eigen-clusters of the seeded group-algebra element = d blocks of size m
     per irrep, as the class-sum method finds them."""
+    spec = CONFIGS["C1"]
+    ao, aux = S.fcc_basis(spec.nao, spec.atoms), S.fcc_basis(spec.naux, spec.atoms)   # cubic coordinates
+    Bt = np.linalg.inv(S.FCC_A.T)
     for kr in gen.reps:
-        kc = gen.kcart(kr)
-        assert sorted(gen.adapted_basis(kr, gen.ao)[1]) == sorted(S.block_sizes(kc, gen.ao))
-        assert sorted(gen.adapted_basis(kr, gen.aux)[1]) == sorted(S.block_sizes(kc, gen.aux))
+        kc = Bt @ gen.kmesh[kr]
+        assert sorted(gen.adapted_basis(kr, gen.ao)[1]) == sorted(S.block_sizes(kc, ao))
+        assert sorted(gen.adapted_basis(kr, gen.aux)[1]) == sorted(S.block_sizes(kc, aux))
 
 
 def test_block_structure_in_the_adapted_bases(c1):
@@ -210,3 +213,85 @@ def test_a_wrong_rotation_breaks_the_relation():
     _, Pr, _ = _chain(cr, tr)
     _, Pf, _ = _chain(cf, tr)
     assert np.abs(Pr - Pf).max() > 1e-6
+
+
+# --------------------------------------------------------------------------- #
+# wurtzite (P6_3mc: screw axis and glides, projective representations at the
+# zone boundary, no inversion: time reversal brings -k into the stars)
+# --------------------------------------------------------------------------- #
+def _wurtzite(mesh):
+    return dataclasses.replace(CONFIGS["C4"], name="wurtzite", mesh=mesh, nao=16, naux=40, nts=62, beta=50.0)
+
+
+@pytest.fixture(scope="module")
+def wz():
+    spec = _wurtzite((3, 3, 2))
+    return (O.make_orbital_crystal(spec, rotate=True, keep_ao_data=True), O._Generator(spec, O.OrbitalModel()))
+
+
+def test_wurtzite_data_are_covariant(wz):
+    """F(g k) = D F(k) D^H and V(g k1, g k2) = (D_aux x D x conj D) V(k1, k2)
+    for the 12 space-group operations (the screws and glides carry their
+    c/2 translations into the Bloch phases), the Hermitian pair relation, and
+    block-diagonal F and rotations in the adapted bases."""
+    cr, gen = wz
+    F, V, nk = cr.F_ao, cr.V_ao, gen.nk
+    assert np.abs(F - F.conj().transpose(0, 2, 1)).max() < 1e-14
+    for k in range(nk):
+        for g in range(len(gen.ops)):
+            D = gen.D(g, k, gen.ao)
+            assert np.abs(D @ F[k] @ D.conj().T - F[gen.perm[g][k]]).max() < 1e-13
+    for k1 in range(nk):
+        for k2 in range(nk):
+            a, b = V[k1 * nk + k2], V[k2 * nk + k1]
+            assert np.abs(b - a.transpose(0, 2, 1).conj()).max() < 1e-13 * np.abs(V).max()
+    rng = np.random.default_rng(5)
+    for _ in range(12):
+        k1, k2, g = int(rng.integers(nk)), int(rng.integers(nk)), int(rng.integers(len(gen.ops)))
+        p = cr.layout.pair_q(k1, k2)
+        want = np.einsum("QR,ia,jb,Rab->Qij", gen.D(g, p, gen.aux), gen.D(g, k1, gen.ao), gen.D(g, k2, gen.ao).conj(),
+                         V[k1 * nk + k2], optimize=True)
+        assert np.abs(want - V[gen.perm[g][k1] * nk + gen.perm[g][k2]]).max() < 1e-12 * np.abs(V).max()
+    assert max(cr.off_block.values()) < 1e-13
+
+
+def test_wurtzite_blocks_and_time_reversal_sticking(wz):
+    """Block sizes at every representative: the projective-representation
+    content (d blocks of size m per irrep, symmetry.sg_block_sizes), except
+    where time reversal glues the rows of each irrep pair together (on the
+    A-L-H face kz = 1/2, where the screw's factor system makes every irrep
+    two-dimensional): there the blocks are those sizes merged in pairs."""
+    cr, gen = wz
+    L = cr.layout
+    merged_points = 0
+    for kr in gen.reps:
+        for basis, sizes in ((gen.ao, L.ao_sizes[kr]), (gen.aux, L.aux_sizes[kr])):
+            theirs, mine = sorted(S.sg_block_sizes(gen.kmesh[kr], basis)), sorted(int(x) for x in sizes)
+            if mine != theirs:
+                assert abs(gen.kmesh[kr][2] - 0.5) < 1e-12
+                pairs = sorted(2 * x for x in theirs[::2])
+                assert theirs[::2] == theirs[1::2] and mine == pairs
+                merged_points += 1
+    assert merged_points > 0
+
+
+@pytest.mark.parametrize("mesh,bound", [((3, 3, 2), 1e-12), ((2, 2, 3), 1e-10)])
+def test_wurtzite_irreducible_and_full_mesh_agree(mesh, bound):
+    """iBZ with the space group's rotations against the full mesh.  On the
+    2x2x3 mesh time reversal brings kz = 2/3 into the stars of kz = 1/3: G
+    and P~ are conjugated there (the rotation path's conj_index), which is
+    exact because the committed grids sample +/- Matsubara pairs."""
+    spec = _wurtzite(mesh)
+    tr = build_transforms(load_ir(spec.nts), spec.beta)
+    cr = O.make_orbital_crystal(spec, rotate=True)
+    cf = O.make_orbital_crystal(spec, rotate=False)
+    if mesh[2] == 3:
+        assert np.any(cr.layout.conj_index != np.arange(cr.layout.nk))
+    Gr, Pr, Sr = _chain(cr, tr)
+    Gf, Pf, Sf = _chain(cf, tr)
+    Lr, Lf, nts, ns = cr.layout, cf.layout, tr.nts, cr.ns
+    Sr, Sf = Sr.reshape(nts, ns, -1), Sf.reshape(nts, ns, -1)
+    d = max(float(np.abs(Sr[:, :, Lr.kao_slice_offsets_irre[ik]:][:, :, :Lr.kao_slice_sizes[k]]
+                         - Sf[:, :, Lf.kao_slice_offsets_irre[k]:][:, :, :Lr.kao_slice_sizes[k]]).max())
+            for ik, k in enumerate(Lr.irre_list))
+    assert np.abs(Gr - Gf).max() < bound and np.abs(Pr - Pf).max() < bound and d < bound
