@@ -275,6 +275,25 @@ def test_wurtzite_blocks_and_time_reversal_sticking(wz):
     assert merged_points > 0
 
 
+def test_wurtzite_selection_rule_at_gamma_follows_the_irreps(wz):
+    """At (Gamma, Gamma) every index transforms under C6v: a block whose
+    irreps' character product has no invariant is zero in the data."""
+    cr, gen = wz
+    L = cr.layout
+    aux_off = np.concatenate([[0], np.cumsum(L.aux_sizes[0])])
+    ao_off = np.concatenate([[0], np.cumsum(L.ao_sizes[0])])
+    chi_q = [_characters(gen, 0, gen.aux, cr.Y[0][:, aux_off[i]:aux_off[i + 1]]) for i in range(len(aux_off) - 1)]
+    chi_a = [_characters(gen, 0, gen.ao, cr.U[0][:, ao_off[i]:ao_off[i + 1]]) for i in range(len(ao_off) - 1)]
+    forbidden = 0
+    for iq, cq in enumerate(chi_q):
+        for i1, ca in enumerate(chi_a):
+            for i2, cb in enumerate(chi_a):
+                if abs(np.mean(cq * ca * cb.conj())) < 1e-9:
+                    forbidden += 1
+                    assert cr.V_block_norms[(0, iq, i1, i2)] < 1e-13
+    assert forbidden > 0
+
+
 @pytest.mark.parametrize("mesh,bound", [((3, 3, 2), 1e-12), ((2, 2, 3), 1e-10)])
 def test_wurtzite_irreducible_and_full_mesh_agree(mesh, bound):
     """iBZ with the space group's rotations against the full mesh.  On the
