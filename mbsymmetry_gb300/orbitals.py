@@ -578,13 +578,36 @@ class OrbitalCrystal(Crystal):
     V_ao: np.ndarray = None
     V_block_norms: Dict = None     # (pair, iq, i1, i2) -> max |V| of every candidate block
     off_block: Dict = None         # largest off-block entries of F, orep, auxrep in the adapted bases
+    p0_transports: Dict = None     # (k, q_irr) -> (k_r or -k_r - 1, q', A): see vstore.p0_from_stored_pairs
+
+
+def p0_transports(gen: _Generator, Y, irre_list) -> Dict:
+    """For every k of the mesh and irreducible q: the stored pair (k_r, q')
+    and the aux transport A with c(k, q) = A c(k_r, q') A^H, where k = g k_r
+    (g the operation that brings k into its star), q' = g^-1 q and
+    A = Y(q)^H D_aux(g, q') Y(q').  A time-reversal partner k = -k'' uses
+    c(k, q) = conj(c(k'', -q)) and is returned as (-k_r - 1, q', conj(A))."""
+    inv_perm = np.argsort(gen.perm, axis=1)          # inv_perm[g][q] = g^-1 q
+    out = {}
+    for q in (int(x) for x in irre_list):
+        for k in range(gen.nk):
+            tr = gen.conj_index[k] != k
+            kk, qq = (int(gen.minus[k]), int(gen.minus[q])) if tr else (k, q)
+            g = int(gen.op_of[kk])
+            qp = int(inv_perm[g][qq])
+            A = Y[qq].conj().T @ gen.D(g, qp, gen.aux) @ Y[qp]
+            kr = int(gen.index[kk])
+            out[(k, q)] = (-kr - 1, qp, A.conj()) if tr else (kr, qp, A)
+    return out
 
 
 def make_orbital_crystal(spec: CrystalSpec, rotate: bool = True, model: OrbitalModel = None,
-                         keep_ao_data: bool = False) -> OrbitalCrystal:
+                         keep_ao_data: bool = False, transports: bool = False) -> OrbitalCrystal:
     """Build the crystal (module docstring).  ``rotate=False`` stores every k
     point with identity rotations (same bases, V and F as ``rotate=True``).
-    ``keep_ao_data`` keeps F and V in the orbital Bloch bases for checks."""
+    ``keep_ao_data`` keeps F and V in the orbital Bloch bases for checks;
+    ``transports`` (with ``rotate``) adds the aux transports that P0 needs to
+    read only the pairs with an irreducible first k (``vstore``)."""
     model = OrbitalModel() if model is None else model
     gen = _Generator(spec, model)
     nk = gen.nk
@@ -689,5 +712,6 @@ def make_orbital_crystal(spec: CrystalSpec, rotate: bool = True, model: OrbitalM
     mu = half_filling_mu(eigs, spec.nao, nk)
     return OrbitalCrystal(spec=spec, layout=layout, V=V, F=F, S=S, H=F.copy(), mu=float(mu),
                           star_sizes=np.array([star_size[gen.star_of[k]] for k in layout.irre_list]),
+                          p0_transports=p0_transports(gen, Y, layout.irre_list) if transports and rotate else None,
                           U=U, Y=Y, F_ao=F_ao if keep_ao_data else None,
                           V_ao=V_ao * scale if keep_ao_data else None, V_block_norms=norms, off_block=off)
