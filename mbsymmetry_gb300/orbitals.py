@@ -77,7 +77,7 @@ from typing import Dict, List, Tuple
 import numpy as np
 
 from . import symmetry
-from .crystal import Crystal, CrystalSpec, _fcc_ops, _find, _kmesh, _rand_unitary, _stars, half_filling_mu
+from .crystal import Crystal, CrystalSpec, _find, _kmesh, _rand_unitary, _stars, half_filling_mu
 from .layout import BlockLayout, wrap_1stbz
 
 # --------------------------------------------------------------------------- #
