@@ -15,6 +15,7 @@ from oracle import Oracle
 
 CASES = {
     "fcc-C1": (CONFIGS["C1"], 1e-13),
+    "fcc-C1-ns2": (dataclasses.replace(CONFIGS["C1"], ns=2), 1e-13),
     # time reversal brings kz = 2/3 into the stars: c(-k, q) = conj(c(k, -q))
     "wurtzite-2x2x3": (dataclasses.replace(CONFIGS["C4"], name="wurtzite", mesh=(2, 2, 3), nao=16, naux=40,
                                            nts=62, beta=50.0), 1e-11),
