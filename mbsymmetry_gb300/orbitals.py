@@ -19,9 +19,11 @@ space groups, operations (M, t) on fractional coordinates:
 * F(k)_ij = sum_L exp(2 pi i k.L) E_ij(tau_j + L - tau_i) + onsite energies:
   Slater-Koster two-centre hoppings.  E(d) = D(R_d) E0(|d|) D(R_d)^T with
   R_d a rotation taking z onto d and E0 the bond-frame matrix, diagonal in
-  the sigma / pi / delta channels (seeded strengths decaying as
-  exp(-(|d| - d_nn) / lambda)); the strength of the ordered shell pair (j, i)
-  is (-1)^(l_i + l_j) times that of (i, j), which makes F Hermitian.  S = I.
+  the sigma / pi / delta channels; by default nearest-neighbour bonds only,
+  strengths U(-1, 1) Ha and onsite energies N(0, 0.5) Ha (further shells,
+  when asked for, decay as exp(-(|d| - d_nn) / lambda)); the strength of
+  the ordered shell pair (j, i) is (-1)^(l_i + l_j) times that of (i, j),
+  which makes F Hermitian.  S = I.
 * V^Q_ij(k1, k2) = sum_{L_Q, L_j} exp(2 pi i (-p.L_Q + k2.L_j))
   (Q, tau_Q + L_Q | i, tau_i | j, tau_j + L_j), p = k2 - k1 (the q that
   labels the pair's aux blocks): Bloch sums of three-centre overlaps of
@@ -92,10 +94,10 @@ class OrbitalModel:
     a_lat_hex: float = 6.1                   # in-plane lattice constant (hexagonal; c = 1.633 a)
     ao_exponents: Tuple[float, float] = (0.3, 1.2)
     aux_exponents: Tuple[float, float] = (0.3, 3.0)
-    onsite: float = 0.4                      # onsite energies ~ N(0, onsite)
-    hopping: Tuple[float, float] = (0.05, 0.3)  # |bond-frame strength| at the nearest-neighbour distance
-    decay: float = 1.5                       # lambda of exp(-(d - d_nn) / lambda)
-    hop_cutoff: float = 1.0                  # hoppings up to this many a_lat
+    onsite: float = 0.5                      # onsite energies ~ N(0, onsite)
+    hopping: float = 1.0                     # bond-frame strengths ~ U(-hopping, hopping) at d_nn
+    decay: float = 1.5                       # lambda of exp(-(d - d_nn) / lambda) beyond the first shell
+    neighbour_shells: int = 1                # hoppings over this many neighbour distances
     v_cutoff: float = 1.2                    # three-centre pair distances up to this many a_lat
     seed: int = 20260201
 
@@ -377,26 +379,34 @@ class _Generator:
         hop = {}
         for i, ki in enumerate(keys_ao):
             for kj in keys_ao[i:]:
-                mag = rng.uniform(*m.hopping, size=3)
-                hop[(ki, kj)] = mag * rng.choice([-1.0, 1.0], size=3)
+                hop[(ki, kj)] = rng.uniform(-m.hopping, m.hopping, size=3)
         return ao_sh, aux_sh, onsite, ao_exp, aux_exp, hop
 
     def _cart(self, basis: symmetry.Basis) -> np.ndarray:
         """Atom positions in Cartesian coordinates (units of the lattice constant)."""
         return np.asarray(basis.positions, dtype=float) @ self.A.T
 
-    def nearest_neighbour(self) -> float:
+    def neighbour_distances(self, n: int) -> np.ndarray:
+        """The n smallest distinct interatomic distances (bohr)."""
         pos = self._cart(self.ao)
-        _, L = _lattice_vectors(self.A, 2.0)
+        _, L = _lattice_vectors(self.A, 3.0)
         d = np.linalg.norm(pos[None, :, None, :] + L[None, None, :, :] - pos[:, None, None, :], axis=-1)
-        return float(d[d > 1e-9].min()) * self.a_lat
+        d = np.sort(d[d > 1e-9].ravel())
+        shells = [d[0]]
+        for x in d[1:]:
+            if x > shells[-1] * (1 + 1e-6):
+                shells.append(x)
+            if len(shells) == n:
+                break
+        return np.array(shells[:n]) * self.a_lat
 
     # -- F(k) in the orbital Bloch basis ----------------------------------- #
     def fock_ao(self, ao_sh, onsite, hop) -> np.ndarray:
         m, nao = self.model, self.spec.nao
         pos = self._cart(self.ao)
-        nvec, Lvec = _lattice_vectors(self.A, m.hop_cutoff + 2.0)
-        d_nn = self.nearest_neighbour()
+        shells = self.neighbour_distances(m.neighbour_shells)
+        d_nn, cutoff = shells[0], shells[-1] * (1 + 1e-6)
+        nvec, Lvec = _lattice_vectors(self.A, cutoff / self.a_lat + 2.0)
         phase = np.exp(2j * np.pi * (self.kmesh @ nvec.T))     # (nk, nL)
         blocks = np.zeros((len(nvec), nao, nao))
         for (ai, si, li, oi) in ao_sh.shells:
@@ -410,7 +420,7 @@ class _Generator:
                 for n in range(len(nvec)):
                     d = (pos[aj] + Lvec[n] - pos[ai]) * self.a_lat
                     r = np.linalg.norm(d)
-                    if r < 1e-9 or r > m.hop_cutoff * self.a_lat + 1e-9:
+                    if r < 1e-9 or r > cutoff:
                         continue
                     blocks[n, oi:oi + 2 * li + 1, oj:oj + 2 * lj + 1] = sk_block(
                         li, lj, v * np.exp(-(r - d_nn) / m.decay), d)
