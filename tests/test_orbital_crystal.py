@@ -314,3 +314,28 @@ def test_wurtzite_irreducible_and_full_mesh_agree(mesh, bound):
                          - Sf[:, :, Lf.kao_slice_offsets_irre[k]:][:, :, :Lr.kao_slice_sizes[k]]).max())
             for ik, k in enumerate(Lr.irre_list))
     assert np.abs(Gr - Gf).max() < bound and np.abs(Pr - Pf).max() < bound and d < bound
+
+
+def test_static_and_dynamic_polarisability_is_negative_semidefinite():
+    """For a Hermitian F, G0 and V in any bases, P0(q, i Omega) = -(2/nk) sum V
+    chi V^H with chi <= 0: every block at every sampled bosonic frequency is
+    negative semidefinite (up to the transform's Hermitian-part residue), so
+    the W~ solve's A = I - (P0 + P0^H)/2 is >= I.  Checks the oracle's P0
+    sign, prefactor and tau -> i Omega transform on physical data."""
+    spec = CONFIGS["C1"]
+    tr = build_transforms(load_ir(spec.nts), spec.beta)
+    cr = O.make_orbital_crystal(spec)
+    L, nts, ns = cr.layout, tr.nts, cr.ns
+    orc = Oracle(L, ns, nts)
+    G, _ = orc.dyson(np.zeros(nts * ns * L.flat_ao_size, np.complex128), cr.F, cr.S, tr, cr.mu)
+    P0 = orc.mirror_P0(orc.p0(orc.rotate_G(G), cr.V))
+    worst, scale = -np.inf, 0.0
+    for iq, q in enumerate(L.irre_list):
+        qs = L.qaux_slice_sizes[q]
+        Pw = tr.Tnt_BF @ P0[nts * L.qaux_slice_offsets_irre[iq]:][:nts * qs].reshape(nts, qs)[1:-1]
+        for b, sz in enumerate(L.aux_sizes[q]):
+            o = L.aux_offsets[q][b]
+            for blk in Pw[:, o:o + sz * sz].reshape(-1, sz, sz):
+                e = np.linalg.eigvalsh(0.5 * (blk + blk.conj().T))
+                worst, scale = max(worst, e.max()), max(scale, -e.min())
+    assert scale > 1.0 and worst < 1e-9 * scale
