@@ -339,3 +339,19 @@ def test_static_and_dynamic_polarisability_is_negative_semidefinite():
                 e = np.linalg.eigvalsh(0.5 * (blk + blk.conj().T))
                 worst, scale = max(worst, e.max()), max(scale, -e.min())
     assert scale > 1.0 and worst < 1e-9 * scale
+
+
+def test_orbital_crystal_is_an_insulator_with_negative_correlation_energy():
+    """Half filling puts mu in a gap of the Slater-Koster bands (N(G0) = nao
+    to 1e-9), and the Galitskii-Migdal correlation energy of the first GW
+    Sigma is negative."""
+    from mbsymmetry_gb300.transformer import gm_matrix
+    spec = CONFIGS["C1"]
+    tr = build_transforms(load_ir(spec.nts), spec.beta)
+    cr = O.make_orbital_crystal(spec)
+    L = cr.layout
+    orc = Oracle(L, cr.ns, tr.nts)
+    G, _ = orc.dyson(np.zeros(tr.nts * cr.ns * L.flat_ao_size, np.complex128), cr.F, cr.S, tr, cr.mu)
+    Sigma, _, _ = orc.gw_sigma(G, cr.V, tr)
+    e_corr, _, n = orc.energy(Sigma, G, cr.F, cr.S, gm_matrix(tr))
+    assert abs(n - spec.nao) < 1e-9 and e_corr < 0
