@@ -639,7 +639,13 @@ def make_orbital_crystal(spec: CrystalSpec, rotate: bool = True, model: OrbitalM
         x = np.tensordot(Y[layout0.pair_q(k1, k2)].conj().T, X, 1)
         return np.matmul(np.matmul(U[k1].conj().T, x), U[k2])
 
-    Vsa = np.stack([adapted(p, V_ao[p]) for p in range(nk * nk)])
+    if keep_ao_data:
+        Vsa = np.stack([adapted(p, V_ao[p]) for p in range(nk * nk)])
+    else:                                   # in place: one copy of the largest array
+        Vsa = V_ao
+        for p in range(nk * nk):
+            Vsa[p] = adapted(p, V_ao[p])
+        V_ao = None
     vmax = float(np.abs(Vsa).max())
     norms, ti = {}, []
     ao_off = [np.concatenate([[0], np.cumsum(s)]).astype(int) for s in ao_sizes]
