@@ -85,15 +85,30 @@ def _dense_G(layout: BlockLayout, G_full: np.ndarray, ns: int, nts: int, k: int)
     return out
 
 
+def _contribution(V: np.ndarray, G1: np.ndarray, G2: np.ndarray, nts: int, ns: int, nt_max: int) -> np.ndarray:
+    """c[tau]_QP = sum_s sum G1(beta - tau)_{t'p} V^Q_{pm} G2(tau)_{mn} conj(V^P_{t'n})
+    (the oracle's loop body, gw_block.cpp:57-74) for dense V (naux, n1, n2)."""
+    c = np.zeros((nt_max, V.shape[0], V.shape[0]), np.complex128)
+    for t in range(nt_max):
+        for s in range(ns):
+            X1 = np.einsum("tp,Qpm->Qtm", G1[nts - 1 - t, s], V, optimize=True)
+            X2 = np.einsum("mn,Ptn->Ptm", G2[t, s], V.conj(), optimize=True)
+            c[t] += np.einsum("Qtm,Ptm->QP", X1, X2, optimize=True)
+    return c
+
+
 def p0_from_stored_pairs(layout: BlockLayout, ns: int, nts: int, G_full: np.ndarray, Vc: np.ndarray,
                          offs: Dict[int, int], transports: Dict[Tuple[int, int], Tuple[int, int, np.ndarray]],
-                         nt_max: int = None) -> Tuple[np.ndarray, float]:
+                         nt_max: int = None, rotate_v: bool = False) -> Tuple[np.ndarray, float]:
     """P0 at the irreducible q for tau < nt_max, in the oracle's layout
     ([ink][nts][qslice]), reading only stored pairs.  transports[(k, q)] =
     (k_r, q', A) for every k of the mesh and irreducible q (the time-reversal
     partners -k map to (k_r, q', A) of k with conjugation, flagged by a
-    negative k_r - 1).  Also returns the largest entry of P0 outside its
-    diagonal blocks (zero by symmetry)."""
+    negative k_r - 1).  rotate_v: apply A to the stored block's aux index
+    (A V, once per (k, q), tau-independent) and contract that, instead of
+    rotating the contribution (A c A^H for every tau); the same P0.  Also
+    returns the largest entry of P0 outside its diagonal blocks (zero by
+    symmetry)."""
     nk = layout.nk
     nt_max = nts // 2 if nt_max is None else nt_max
     pref = -1.0 / nk * (2.0 if ns == 1 else 1.0)
@@ -114,18 +129,16 @@ def p0_from_stored_pairs(layout: BlockLayout, ns: int, nts: int, G_full: np.ndar
             kr, qp, A = transports[(k, q)]
             conj = kr < 0
             kr = -kr - 1 if conj else kr
+            k2 = layout.mom_cons(kr, 0, qp)                        # k_r + q'
+            if rotate_v:                                           # c(A V) = A c(V) A^H
+                V = _dense_pair(layout, Vc, offs, kr, k2)
+                Ar = A.conj() if conj else A                       # A of the partner -k (see above)
+                c = _contribution(np.tensordot(Ar, V, 1), G(kr), G(k2), nts, ns, nt_max)
+                acc += c.conj() if conj else c
+                continue
             key = (kr, qp)
             if key not in cache:
-                k2 = layout.mom_cons(kr, 0, qp)                    # k_r + q'
-                V = _dense_pair(layout, Vc, offs, kr, k2)
-                G1, G2 = G(kr), G(k2)
-                c = np.zeros((nt_max, V.shape[0], V.shape[0]), np.complex128)
-                for t in range(nt_max):
-                    for s in range(ns):
-                        X1 = np.einsum("tp,Qpm->Qtm", G1[nts - 1 - t, s], V, optimize=True)
-                        X2 = np.einsum("mn,Ptn->Ptm", G2[t, s], V.conj(), optimize=True)
-                        c[t] += np.einsum("Qtm,Ptm->QP", X1, X2, optimize=True)
-                cache[key] = c
+                cache[key] = _contribution(_dense_pair(layout, Vc, offs, kr, k2), G(kr), G(k2), nts, ns, nt_max)
             c = cache[key].conj() if conj else cache[key]
             acc += A[None] @ c @ A.conj().T[None]
         acc *= pref

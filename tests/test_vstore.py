@@ -35,13 +35,15 @@ def test_p0_from_pairs_with_an_irreducible_first_k(case):
     Vc, offs = vstore.compress(L, cr.V)
     assert set(offs) == {k1 * L.nk + k2 for k1 in L.irre_list for k2 in range(L.nk)}
     assert Vc.size < 0.35 * cr.V.size
-    P0s, off_block = vstore.p0_from_stored_pairs(L, ns, nts, Gf, Vc, offs, cr.p0_transports)
     nt_max = nts // 2
-    d = 0.0
-    for iq, q in enumerate(L.irre_list):
-        base, qs = nts * L.qaux_slice_offsets_irre[iq], L.qaux_slice_sizes[q]
-        d = max(d, float(np.abs(P0[base:base + nt_max * qs] - P0s[base:base + nt_max * qs]).max()))
-    assert d < bound and off_block < 1e-13 and np.abs(P0).max() > 0.5
+    for rotate_v in (False, True):   # rotate each contribution, or the stored V block once per (k, q)
+        P0s, off_block = vstore.p0_from_stored_pairs(L, ns, nts, Gf, Vc, offs, cr.p0_transports,
+                                                     rotate_v=rotate_v)
+        d = 0.0
+        for iq, q in enumerate(L.irre_list):
+            base, qs = nts * L.qaux_slice_offsets_irre[iq], L.qaux_slice_sizes[q]
+            d = max(d, float(np.abs(P0[base:base + nt_max * qs] - P0s[base:base + nt_max * qs]).max()))
+        assert d < bound and off_block < 1e-13 and np.abs(P0).max() > 0.5
 
 
 def test_unstored_pairs_are_never_read():
