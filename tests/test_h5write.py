@@ -48,14 +48,17 @@ def test_export_reference_block_dir_lih(tmp_path):
     assert np.allclose(ri.onebody.S, d["S"], rtol=0, atol=1e-14)
 
 
-@pytest.mark.parametrize("kind", ["labelled", "orbital"])
+@pytest.mark.parametrize("kind", ["labelled", "orbital", "orbital-wurtzite"])
 def test_export_reference_block_dir_crystal(tmp_path, kind):
     if kind == "labelled":
         cr, _ = crystal("C1", rotate=False)
     else:   # Slater-Koster / Gaussian-orbital data with the group's selection rule
+        import dataclasses
         from mbsymmetry_gb300.crystal import CONFIGS
         from mbsymmetry_gb300.orbitals import make_orbital_crystal
-        cr = make_orbital_crystal(CONFIGS["C1"], rotate=False)
+        spec = CONFIGS["C1"] if kind == "orbital" else dataclasses.replace(
+            CONFIGS["C4"], name="wurtzite", mesh=(2, 2, 3), nao=16, naux=40, nts=62, beta=50.0)
+        cr = make_orbital_crystal(spec, rotate=False)
     out = str(tmp_path / "block")
     h5write.export_reference_inputs(out, cr.layout, cr.V, cr.F, cr.S, cr.H, cr.ns)
     ri = load_reference_inputs(out)
