@@ -32,9 +32,10 @@ def _ptr(a: np.ndarray):
 class GWSolver:
     def __init__(self, layout: BlockLayout, ns: int, transforms: IRTransforms,
                  precision: str = "fp64", device: int = 0, tune: dict = None):
-        """tune: optional tile-shape settings of the tcgen05 Sigma path
-        (uvt_smem_kb, sw_npk_max, uv_waves; see gwgb_params), e.g. the
-        "best" entry returned by autotune.autotune()."""
+        """tune: optional gwgb_params settings chosen by autotune.autotune()
+        (its "best" entry): oz_simt_cols, the width-class boundary of the
+        sliced path, or the tile settings of the FP32-class tcgen05 Sigma
+        path (uvt_smem_kb, sw_npk_max, uv_waves)."""
         self.lib = _abi.load()
         self.layout = layout
         self.ns = ns
